@@ -1,0 +1,144 @@
+"""ctypes mirror of the plain-C structs in include/ampe_gb300.h.
+
+The field order and types must match the header exactly; the test suite
+checks ``ctypes.sizeof`` against the library's own ``sizeof`` report.
+"""
+import ctypes as C
+
+AMPE_OK = 0
+AMPE_ERR_INVALID = -1
+AMPE_ERR_CUDA = -2
+AMPE_ERR_NOT_CONVERGED = -3
+AMPE_ERR_NO_DEVICE = -4
+
+FLUX_SIMPLE, FLUX_ISOTROPIC, FLUX_ANISOTROPIC = 0, 1, 2
+THERMO_DILUTE, THERMO_CALPHAD = 0, 1
+TEMP_CONSTANT, TEMP_GRADIENT, TEMP_FIELD = 0, 1, 2
+MAX_TSEG = 6
+
+
+class GTerm(C.Structure):
+    """ampe_gterm_t: piecewise pure-species Gibbs energy G(T)."""
+
+    _fields_ = [("nseg", C.c_int), ("tc", C.c_double * (MAX_TSEG + 1))] + [
+        (k, C.c_double * MAX_TSEG)
+        for k in ("a", "b", "c", "d2", "d3", "d4", "d7", "dm1", "dm9")
+    ]
+
+
+class Model(C.Structure):
+    """ampe_model_t."""
+
+    _fields_ = [
+        ("dim", C.c_int),
+        ("n", C.c_int * 3),
+        ("ng", C.c_int),
+        ("dx", C.c_double * 3),
+        ("flux_type", C.c_int),
+        ("epsilon_phi", C.c_double),
+        ("aniso_eps", C.c_double),
+        ("aniso_k", C.c_int),
+        ("qlen", C.c_int),
+        ("phase_well_scale", C.c_double),
+        ("phase_mobility", C.c_double),
+        ("well_type", C.c_char),
+        ("energy_interp", C.c_char),
+        ("conc_interp", C.c_char),
+        ("diff_interp", C.c_char),
+        ("avg_type", C.c_char),
+        ("orient_interp1", C.c_char),
+        ("orient_interp2", C.c_char),
+        ("pad0", C.c_char),
+        ("with_orient", C.c_int),
+        ("misorientation_factor", C.c_double),
+        ("epsilon_q", C.c_double),
+        ("conc_mobility", C.c_double),
+        ("D_liquid", C.c_double),
+        ("Q_liquid", C.c_double),
+        ("D_solid", C.c_double),
+        ("Q_solid", C.c_double),
+        ("thermo", C.c_int),
+        ("inv_molar_volume", C.c_double * 2),
+        ("dilute_Tm", C.c_double),
+        ("dilute_m", C.c_double),
+        ("dilute_k", C.c_double),
+        ("g", (GTerm * 2) * 2),
+        ("L", ((C.c_double * 2) * 4) * 2),
+        ("newton_max_its", C.c_int),
+        ("newton_tol", C.c_double),
+        ("temp_mode", C.c_int),
+        ("T0", C.c_double),
+        ("gradT", C.c_double),
+    ]
+
+    def cells(self):
+        return self.n[0] * self.n[1] * (self.n[2] if self.dim == 3 else 1)
+
+    def ghost_shape(self):
+        """numpy shape (z, y, x) of a ghosted cell field."""
+        g = self.ng
+        gz = g if self.dim == 3 else 0
+        nz = self.n[2] if self.dim == 3 else 1
+        return (nz + 2 * gz, self.n[1] + 2 * g, self.n[0] + 2 * g)
+
+    def interior_shape(self):
+        nz = self.n[2] if self.dim == 3 else 1
+        return (nz, self.n[1], self.n[0])
+
+    def face_shapes(self):
+        nz = self.n[2] if self.dim == 3 else 1
+        nx, ny = self.n[0], self.n[1]
+        s = [(nz, ny, nx + 1), (nz, ny + 1, nx)]
+        s.append((nz + 1, ny, nx) if self.dim == 3 else (1, 1, 1))
+        return s
+
+
+class StepParams(C.Structure):
+    """ampe_step_params_t."""
+
+    _fields_ = [
+        ("dt", C.c_double),
+        ("max_order", C.c_int),
+        ("atol", C.c_double),
+        ("rtol", C.c_double),
+        ("max_newton", C.c_int),
+        ("newton_coef", C.c_double),
+        ("max_krylov", C.c_int),
+        ("lin_coef", C.c_double),
+        ("precond", C.c_int),
+        ("fac_max_cycles", C.c_int),
+        ("rb_sweeps", C.c_int),
+        ("rb_tol", C.c_double),
+        ("mg_levels", C.c_int),
+        ("mg_pre", C.c_int),
+        ("mg_post", C.c_int),
+        ("mg_coarse_sweeps", C.c_int),
+        ("precision", C.c_int),
+        ("surrogate", C.c_int),
+        ("max_retries", C.c_int),
+    ]
+
+
+class StepStats(C.Structure):
+    """ampe_step_stats_t."""
+
+    _fields_ = [
+        (k, C.c_longlong)
+        for k in (
+            "steps",
+            "newton_iters",
+            "gmres_iters",
+            "rhs_evals",
+            "precond_solves",
+            "precond_setups",
+            "fac_cycles",
+            "newton_fail",
+            "kks_iters",
+            "kks_fallback",
+            "kks_fail",
+            "step_retries",
+        )
+    ] + [("t", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}

@@ -1,0 +1,220 @@
+// FAC operator kernels: red-black Gauss-Seidel colour update, residual and
+// the phase operator's C coefficient (EllipticFACOps / PhaseFACOps,
+// 3d/ellipticfacops.m4:16-575).  Operator  A u = C u + M div(D grad u);
+// cell arrays ghosted (width g.ng), face D arrays ghost-free.
+// Templated on the arithmetic type R so that the mixed-precision
+// preconditioner runs the same code in FP32.
+#include "common.cuh"
+#include "fac.cuh"
+
+namespace ampe {
+
+template <class R>
+__device__ __forceinline__ R face_d(const FacOp<R>& op, const Grid& g,
+                                    int dir, int i, int j, int k)
+{
+   if (!op.D0) return op.dc;
+   if (dir == 0) return op.D0[g.fx(i, j, k)];
+   if (dir == 1) return op.D1[g.fy(i, j, k)];
+   return op.D2[g.fz(i, j, k)];
+}
+
+// r = f - A u at (i,j,k) and 1/(M sum D/h^2 - C) (expression order of
+// efo_rbgswithfluxmaxvardcvarsf3d, 3d/ellipticfacops.m4:153-172)
+template <class R>
+__device__ __forceinline__ R cell_residual(const FacOp<R>& op, const Grid& g,
+                                           const R* f, const R* u, int i,
+                                           int j, int k, R* dudr)
+{
+   const long long c = g.c(i, j, k);
+   const R uc = u[c];
+   R div = R(0), dsum = R(0);
+#pragma unroll
+   for (int d = 0; d < 3; d++) {
+      if (d >= g.dim) break;
+      const int ei = d == 0, ej = d == 1, ek = d == 2;
+      const R dxi = op.dxi[d];
+      const R Dm = face_d(op, g, d, i, j, k);
+      const R Dp = face_d(op, g, d, i + ei, j + ej, k + ek);
+      const R fm = dxi * Dm * (uc - u[g.c(i - ei, j - ej, k - ek)]);
+      const R fp = dxi * Dp * (u[g.c(i + ei, j + ej, k + ek)] - uc);
+      div += dxi * (fp - fm);
+      dsum += dxi * dxi * (Dp + Dm);
+   }
+   const R M = op.M ? op.M[c] : op.mc;
+   const R C = op.C ? op.C[c] : op.cc;
+   if (dudr) *dudr = R(1) / (M * dsum - C);
+   return f[c] - M * div - C * uc;
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double* a, double v)
+{
+   atomicMax((unsigned long long*)a, (unsigned long long)__double_as_longlong(v));
+}
+
+template <class R>
+__global__ void k_rbgs_color(FacOp<R> op, Grid g, const R* f, R* u,
+                             int offset, double* maxres)
+{
+   // one thread per cell of the colour: i = 2*ih + parity(j,k)
+   const int nh = (g.n0 + 1) / 2;
+   const long long tot = (long long)nh * g.n1 * g.n2;
+   double mres = 0.0;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < tot; t += (long long)gridDim.x * blockDim.x) {
+      const int ih = (int)(t % nh);
+      const int j = (int)((t / nh) % g.n1);
+      const int k = (int)(t / ((long long)nh * g.n1));
+      const int i = 2 * ih + ((j + k + offset) & 1);
+      if (i >= g.n0) continue;
+      R dudr;
+      const R r = cell_residual(op, g, f, u, i, j, k, &dudr);
+      u[g.c(i, j, k)] += -r * dudr;
+      mres = fmax(mres, (double)fabs(r));
+   }
+   if (maxres) {
+      for (int o = 16; o > 0; o >>= 1)
+         mres = fmax(mres, __shfl_xor_sync(0xffffffffu, mres, o));
+      if ((threadIdx.x & 31) == 0) atomic_max_nonneg(maxres, mres);
+   }
+}
+
+template <class R>
+__global__ void k_residual(FacOp<R> op, Grid g, const R* f, const R* u,
+                           R* res)
+{
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      res[g.c(i, j, k)] = cell_residual(op, g, f, u, i, j, k, (R*)nullptr);
+   }
+}
+
+template <class R>
+__global__ void k_phase_set_c(Grid g, const double* phi, double gamma,
+                              double mobility, double well_scale, char wt,
+                              R* ccell)
+{
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long c = g.c(i, j, k);
+      const double g2 = second_deriv_well_func(phi[c], wt);
+      const double gm = gamma * mobility;
+      ccell[c] = (R)(1.0 + gm * well_scale * g2);
+   }
+}
+
+static unsigned nblocks(long long n)
+{
+   long long b = (n + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   return (unsigned)(b < 1 ? 1 : b);
+}
+
+template <class R>
+int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
+               int offset, double* maxres, cudaStream_t s)
+{
+   const long long tot = (long long)((g.n0 + 1) / 2) * g.n1 * g.n2;
+   k_rbgs_color<R><<<nblocks(tot), 256, 0, s>>>(op, g, f, u, offset, maxres);
+   return launch_status();
+}
+
+template <class R>
+int residual(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
+             R* res, cudaStream_t s)
+{
+   k_residual<R><<<nblocks(g.cells()), 256, 0, s>>>(op, g, f, u, res);
+   return launch_status();
+}
+
+template <class R>
+int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
+                double gamma, R* ccell, cudaStream_t s)
+{
+   k_phase_set_c<R><<<nblocks(g.cells()), 256, 0, s>>>(
+       g, phi, gamma, m.phase_mobility, m.phase_well_scale, m.well_type,
+       ccell);
+   return launch_status();
+}
+
+template int rbgs_color<double>(const FacOp<double>&, const Grid&,
+                                const double*, double*, int, double*,
+                                cudaStream_t);
+template int rbgs_color<float>(const FacOp<float>&, const Grid&, const float*,
+                               float*, int, double*, cudaStream_t);
+template int residual<double>(const FacOp<double>&, const Grid&, const double*,
+                              const double*, double*, cudaStream_t);
+template int residual<float>(const FacOp<float>&, const Grid&, const float*,
+                             const float*, float*, cudaStream_t);
+template int phase_set_c<double>(const ampe_model_t&, const Grid&,
+                                 const double*, double, double*, cudaStream_t);
+template int phase_set_c<float>(const ampe_model_t&, const Grid&,
+                                const double*, double, float*, cudaStream_t);
+
+}  // namespace ampe
+
+using namespace ampe;
+
+static FacOp<double> make_op(const ampe_model_t* m, const double* d0,
+                             const double* d1, const double* d2, double dc,
+                             const double* cc, double cconst, const double* mm,
+                             double mconst)
+{
+   FacOp<double> op;
+   op.D0 = d0;
+   op.D1 = d1;
+   op.D2 = d2;
+   op.dc = dc;
+   op.C = cc;
+   op.cc = cconst;
+   op.M = mm;
+   op.mc = mconst;
+   for (int d = 0; d < 3; d++) op.dxi[d] = d < m->dim ? 1.0 / m->dx[d] : 0.0;
+   return op;
+}
+
+extern "C" {
+
+int ampe_efo_rbgs(const ampe_model_t* m, const double* dface0,
+                  const double* dface1, const double* dface2, double d_const,
+                  const double* ccell, double c_const, const double* mcell,
+                  double m_const, const double* rhs, double* u, int offset,
+                  double* maxres, void* stream)
+{
+   if (check_model(m) || !rhs || !u || (offset != 0 && offset != 1))
+      return AMPE_ERR_INVALID;
+   if (dface0 && (!dface1 || (m->dim == 3 && !dface2))) return AMPE_ERR_INVALID;
+   FacOp<double> op = make_op(m, dface0, dface1, dface2, d_const, ccell,
+                              c_const, mcell, m_const);
+   return rbgs_color(op, make_grid(*m), rhs, u, offset, maxres,
+                     (cudaStream_t)stream);
+}
+
+int ampe_efo_residual(const ampe_model_t* m, const double* dface0,
+                      const double* dface1, const double* dface2,
+                      double d_const, const double* ccell, double c_const,
+                      const double* mcell, double m_const, const double* rhs,
+                      const double* u, double* res, void* stream)
+{
+   if (check_model(m) || !rhs || !u || !res) return AMPE_ERR_INVALID;
+   if (dface0 && (!dface1 || (m->dim == 3 && !dface2))) return AMPE_ERR_INVALID;
+   FacOp<double> op = make_op(m, dface0, dface1, dface2, d_const, ccell,
+                              c_const, mcell, m_const);
+   return residual(op, make_grid(*m), rhs, u, res, (cudaStream_t)stream);
+}
+
+int ampe_phase_fac_set_c(const ampe_model_t* m, const double* phi,
+                         double gamma, double* ccell, void* stream)
+{
+   if (check_model(m) || !phi || !ccell) return AMPE_ERR_INVALID;
+   return phase_set_c(*m, make_grid(*m), phi, gamma, ccell,
+                      (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,34 @@
+// FAC operator descriptor shared by fac.cu and the stepper.
+#pragma once
+
+#include "common.cuh"
+
+namespace ampe {
+
+// A u = C u + M div(D grad u); null pointers select the constants.
+template <class R>
+struct FacOp {
+   const R* D0 = nullptr;
+   const R* D1 = nullptr;
+   const R* D2 = nullptr;
+   R dc = 0;
+   const R* C = nullptr;
+   R cc = 0;
+   const R* M = nullptr;
+   R mc = 0;
+   R dxi[3] = {0, 0, 0};
+};
+
+template <class R>
+int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
+               int offset, double* maxres, cudaStream_t s);
+template <class R>
+int residual(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
+             R* res, cudaStream_t s);
+template <class R>
+int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
+                double gamma, R* ccell, cudaStream_t s);
+
+int fill_ghosts(const Grid& g, double* f, cudaStream_t s);
+
+}  // namespace ampe

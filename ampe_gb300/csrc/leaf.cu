@@ -1,0 +1,417 @@
+// Leaf kernels of libampe_gb300: one CUDA kernel per reference Fortran /
+// C++ routine that the C-ABI replaces (see include/ampe_gb300.h for the
+// reference file:line of each).  They keep the reference's data layout
+// (ghosted cell arrays, ghost-free side arrays) so that a SAMRAI adapter can
+// hand them patch data directly.  The fused hot-path kernels live in
+// fused.cu; these are the drop-in / parity surface.
+#include <cstdio>
+
+#include "common.cuh"
+#include "phase_flux.cuh"
+
+namespace ampe {
+
+long long g_launches = 0;
+
+int check_model(const ampe_model_t* m)
+{
+   if (!m) return AMPE_ERR_INVALID;
+   if (m->dim != 2 && m->dim != 3) return AMPE_ERR_INVALID;
+   if (m->ng < 1) return AMPE_ERR_INVALID;
+   const int nd = m->dim;
+   for (int d = 0; d < nd; d++)
+      if (m->n[d] < 2 * m->ng || m->dx[d] <= 0.0) return AMPE_ERR_INVALID;
+   if (m->dim == 2 && m->n[2] != 1) return AMPE_ERR_INVALID;
+   if (m->flux_type == AMPE_FLUX_ISOTROPIC && m->dim == 3)
+      return AMPE_ERR_INVALID;  // 3d/quatrhs.m4:90-92 stops: no 3D variant
+   return AMPE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// periodic ghost fill
+// ---------------------------------------------------------------------------
+__global__ void k_fill_ghosts(Grid g, double* f)
+{
+   const long long n = g.cells();
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+        t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const bool edge = i < g.ng || i >= g.n0 - g.ng || j < g.ng ||
+                        j >= g.n1 - g.ng ||
+                        (g.dim == 3 && (k < g.ng || k >= g.n2 - g.ng));
+      if (!edge) continue;
+      const double v = f[g.c(i, j, k)];
+      for_each_image(g, i, j, k, [&](long long idx) { f[idx] = v; });
+   }
+}
+
+int fill_ghosts(const Grid& g, double* f, cudaStream_t s)
+{
+   k_fill_ghosts<<<grid_for(g.cells(), 256), 256, 0, s>>>(g, f);
+   return launch_status();
+}
+
+// ---------------------------------------------------------------------------
+// phase fluxes
+// ---------------------------------------------------------------------------
+__global__ void k_phase_flux(ampe_model_t m, Grid g, const double* ph,
+                             const double* quat, double* f0, double* f1,
+                             double* f2)
+{
+   const long long qs = g.cells_ghost();
+   auto P = [&](int a, int b, int c) { return ph[g.c(a, b, c)]; };
+   auto Q = [&](int comp, int a, int b, int c) {
+      return quat[comp * qs + g.c(a, b, c)];
+   };
+   const long long nx = g.nfx(), ny = g.nfy();
+   const long long nz = g.dim == 3 ? g.nfz() : 0;
+   const long long tot = nx + ny + nz;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < tot; t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      long long r = t;
+      if (r < nx) {
+         dir = 0;
+         i = (int)(r % (g.n0 + 1));
+         j = (int)((r / (g.n0 + 1)) % g.n1);
+         k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
+      } else if ((r -= nx) < ny) {
+         dir = 1;
+         i = (int)(r % g.n0);
+         j = (int)((r / g.n0) % (g.n1 + 1));
+         k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
+      } else {
+         r -= ny;
+         dir = 2;
+         i = (int)(r % g.n0);
+         j = (int)((r / g.n0) % g.n1);
+         k = (int)(r / ((long long)g.n0 * g.n1));
+      }
+      const double v = phase_face_flux(m, g.dim, dir, i, j, k, P, Q);
+      if (dir == 0) f0[g.fx(i, j, k)] = v;
+      if (dir == 1) f1[g.fy(i, j, k)] = v;
+      if (dir == 2) f2[g.fz(i, j, k)] = v;
+   }
+}
+
+// ---------------------------------------------------------------------------
+// computerhspbg, driving force, composition kernels
+// ---------------------------------------------------------------------------
+__global__ void k_computerhspbg(ampe_model_t m, Grid g, const double* f0,
+                                const double* f1, const double* f2,
+                                const double* temp, const double* phi,
+                                const double* ogm, double* rhs)
+{
+   const double dxi = 1.0 / m.dx[0], dyi = 1.0 / m.dx[1];
+   const double dzi = g.dim == 3 ? 1.0 / m.dx[2] : 0.0;
+   const double eq2 = 0.5 * m.epsilon_q * m.epsilon_q;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      double d = (f0[g.fx(i + 1, j, k)] - f0[g.fx(i, j, k)]) * dxi +
+                 (f1[g.fy(i, j + 1, k)] - f1[g.fy(i, j, k)]) * dyi;
+      if (g.dim == 3) d = d + (f2[g.fz(i, j, k + 1)] - f2[g.fz(i, j, k)]) * dzi;
+      const double p = phi[g.c(i, j, k)];
+      double r = d - m.phase_well_scale * deriv_well_func(p, m.well_type);
+      if (m.with_orient) {
+         const double p1 = deriv_interp_func(p, m.orient_interp1);
+         const double p2 = deriv_interp_func(p, m.orient_interp2);
+         const double gm = ogm[t];
+         const double T = temperature_at(m, g, temp, i, j, k);
+         r = r - m.misorientation_factor * T * p1 * gm - p2 * eq2 * gm * gm;
+      }
+      rhs[t] = r;
+   }
+}
+
+__global__ void k_add_driving_force(ampe_model_t m, Grid g,
+                                    const double* temp, const double* phi,
+                                    const double* cl, const double* cs,
+                                    double* rhs)
+{
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long ci = g.c(i, j, k);
+      const ThermoCoef th = thermo_coef(m, temperature_at(m, g, temp, i, j, k));
+      const double a = cl[ci], b = cs[ci];
+      const double fl = free_energy_of(th, a, 0) * m.inv_molar_volume[0];
+      const double fa = free_energy_of(th, b, 1) * m.inv_molar_volume[1];
+      const double mu = dfdc_of(th, b, 1) * m.inv_molar_volume[1];
+      const double hp = deriv_interp_func(phi[ci], m.energy_interp);
+      rhs[t] += hp * ((fl - fa) - mu * (a - b));
+   }
+}
+
+// per-cell KKS solve over the ghost box (reference loop bounds)
+__global__ void k_phase_conc_ghostbox(ampe_model_t m, Grid g,
+                                      const double* temp, const double* phi,
+                                      const double* conc, const double* clr,
+                                      const double* csr, double* cl,
+                                      double* cs, unsigned long long* counters)
+{
+   const int ex = g.n0 + 2 * g.ng, ey = g.n1 + 2 * g.ng;
+   const long long tot = g.cells_ghost();
+   unsigned long long its = 0, fails = 0;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < tot; t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % ex) - g.ng;
+      const int j = (int)((t / ex) % ey) - g.ng;
+      const int k = (int)(t / ((long long)ex * ey)) - g.gz;
+      const long long ci = g.c(i, j, k);
+      const ThermoCoef th = thermo_coef(m, temperature_at(m, g, temp, i, j, k));
+      const double h = interp_func(phi[ci], m.conc_interp);
+      double x[2] = {clr[ci], csr[ci]};
+      const int it = kks_newton(th, h, conc[ci], x, m.newton_max_its,
+                                m.newton_tol);
+      if (it < 0) {
+         fails++;
+         its += m.newton_max_its;
+      } else {
+         its += it;
+      }
+      cl[ci] = x[0];
+      cs[ci] = x[1];
+   }
+   if (counters) {
+      atomicAdd(&counters[0], its);
+      atomicAdd(&counters[1], fails);
+   }
+}
+
+__global__ void k_conc_diffusion(ampe_model_t m, Grid g, const double* phi,
+                                 const double* temp, double* dl0, double* dl1,
+                                 double* dl2, double* ds0, double* ds1,
+                                 double* ds2)
+{
+   const double qlR = m.Q_liquid / kGasR, qsR = m.Q_solid / kGasR;
+   const long long nx = g.nfx(), ny = g.nfy();
+   const long long nz = g.dim == 3 ? g.nfz() : 0;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < nx + ny + nz; t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      long long r = t;
+      if (r < nx) {
+         dir = 0;
+         i = (int)(r % (g.n0 + 1));
+         j = (int)((r / (g.n0 + 1)) % g.n1);
+         k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
+      } else if ((r -= nx) < ny) {
+         dir = 1;
+         i = (int)(r % g.n0);
+         j = (int)((r / g.n0) % (g.n1 + 1));
+         k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
+      } else {
+         r -= ny;
+         dir = 2;
+         i = (int)(r % g.n0);
+         j = (int)((r / g.n0) % g.n1);
+         k = (int)(r / ((long long)g.n0 * g.n1));
+      }
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const double vphi = average_func(phi[g.c(i - ei, j - ej, k - ek)],
+                                       phi[g.c(i, j, k)], m.avg_type);
+      const double hphi = interp_func(vphi, m.diff_interp);
+      const double invT = 2.0 / (temperature_at(m, g, temp, i - ei, j - ej, k - ek) +
+                                 temperature_at(m, g, temp, i, j, k));
+      const double dlq = m.D_liquid * exp(-qlR * invT);
+      const double dsq = m.D_solid * exp(-qsR * invT);
+      if (dir == 0) {
+         dl0[g.fx(i, j, k)] = (1.0 - hphi) * dlq;
+         ds0[g.fx(i, j, k)] = hphi * dsq;
+      } else if (dir == 1) {
+         dl1[g.fy(i, j, k)] = (1.0 - hphi) * dlq;
+         ds1[g.fy(i, j, k)] = hphi * dsq;
+      } else {
+         dl2[g.fz(i, j, k)] = (1.0 - hphi) * dlq;
+         ds2[g.fz(i, j, k)] = hphi * dsq;
+      }
+   }
+}
+
+__global__ void k_add_flux(ampe_model_t m, Grid g, const double* u,
+                           const double* d0, const double* d1,
+                           const double* d2, double* f0, double* f1,
+                           double* f2)
+{
+   const long long nx = g.nfx(), ny = g.nfy();
+   const long long nz = g.dim == 3 ? g.nfz() : 0;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < nx + ny + nz; t += (long long)gridDim.x * blockDim.x) {
+      long long r = t;
+      if (r < nx) {
+         const int i = (int)(r % (g.n0 + 1));
+         const int j = (int)((r / (g.n0 + 1)) % g.n1);
+         const int k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
+         f0[r] = f0[r] + (1.0 / m.dx[0]) * d0[r] *
+                             (u[g.c(i, j, k)] - u[g.c(i - 1, j, k)]);
+      } else if ((r -= nx) < ny) {
+         const int i = (int)(r % g.n0);
+         const int j = (int)((r / g.n0) % (g.n1 + 1));
+         const int k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
+         f1[r] = f1[r] + (1.0 / m.dx[1]) * d1[r] *
+                             (u[g.c(i, j, k)] - u[g.c(i, j - 1, k)]);
+      } else {
+         r -= ny;
+         const int i = (int)(r % g.n0);
+         const int j = (int)((r / g.n0) % g.n1);
+         const int k = (int)(r / ((long long)g.n0 * g.n1));
+         f2[r] = f2[r] + (1.0 / m.dx[2]) * d2[r] *
+                             (u[g.c(i, j, k)] - u[g.c(i, j, k - 1)]);
+      }
+   }
+}
+
+__global__ void k_rhs_conc(ampe_model_t m, Grid g, const double* f0,
+                           const double* f1, const double* f2, double* rhs)
+{
+   const double dxi = 1.0 / m.dx[0], dyi = 1.0 / m.dx[1];
+   const double dzi = g.dim == 3 ? 1.0 / m.dx[2] : 0.0;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      double s = dxi * (f0[g.fx(i + 1, j, k)] - f0[g.fx(i, j, k)]) +
+                 dyi * (f1[g.fy(i, j + 1, k)] - f1[g.fy(i, j, k)]);
+      if (g.dim == 3) s = s + dzi * (f2[g.fz(i, j, k + 1)] - f2[g.fz(i, j, k)]);
+      rhs[t] = m.conc_mobility * s;
+   }
+}
+
+}  // namespace ampe
+
+using namespace ampe;
+
+static cudaStream_t S(void* s) { return (cudaStream_t)s; }
+static unsigned blocks_for(long long n)
+{
+   long long b = (n + 255) / 256;
+   if (b > 152 * 64) b = 152 * 64;
+   return (unsigned)(b < 1 ? 1 : b);
+}
+
+extern "C" {
+
+const char* ampe_version(void) { return "ampe_gb300 1.0 (sm_103a)"; }
+
+int ampe_device_count(void)
+{
+   int n = 0;
+   if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+   return n;
+}
+
+int ampe_fill_ghosts(const ampe_model_t* m, double* field, void* stream)
+{
+   if (check_model(m) || !field) return AMPE_ERR_INVALID;
+   return fill_ghosts(make_grid(*m), field, S(stream));
+}
+
+int ampe_phase_flux(const ampe_model_t* m, const double* phase,
+                    const double* quat, double* flux0, double* flux1,
+                    double* flux2, void* stream)
+{
+   if (check_model(m) || !phase || !flux0 || !flux1) return AMPE_ERR_INVALID;
+   if (m->dim == 3 && !flux2) return AMPE_ERR_INVALID;
+   if (m->flux_type == AMPE_FLUX_ANISOTROPIC && !quat) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   k_phase_flux<<<blocks_for(tot), 256, 0, S(stream)>>>(*m, g, phase, quat,
+                                                        flux0, flux1, flux2);
+   return launch_status();
+}
+
+int ampe_computerhspbg(const ampe_model_t* m, const double* flux0,
+                       const double* flux1, const double* flux2,
+                       const double* temp, const double* phi,
+                       const double* ogm, double* rhs, void* stream)
+{
+   if (check_model(m) || !flux0 || !flux1 || !phi || !rhs)
+      return AMPE_ERR_INVALID;
+   if (m->with_orient && !ogm) return AMPE_ERR_INVALID;
+   if (m->temp_mode == AMPE_TEMP_FIELD && m->with_orient && !temp)
+      return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   k_computerhspbg<<<blocks_for(g.cells()), 256, 0, S(stream)>>>(
+       *m, g, flux0, flux1, flux2, temp, phi, ogm, rhs);
+   return launch_status();
+}
+
+int ampe_add_driving_force(const ampe_model_t* m, const double* temp,
+                           const double* phi, const double* cl,
+                           const double* cs, double* rhs, void* stream)
+{
+   if (check_model(m) || !phi || !cl || !cs || !rhs) return AMPE_ERR_INVALID;
+   if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   k_add_driving_force<<<blocks_for(g.cells()), 256, 0, S(stream)>>>(
+       *m, g, temp, phi, cl, cs, rhs);
+   return launch_status();
+}
+
+int ampe_phase_concentrations(const ampe_model_t* m, const double* temp,
+                              const double* phi, const double* conc,
+                              const double* cl_ref, const double* cs_ref,
+                              double* cl, double* cs,
+                              unsigned long long* counters, void* stream)
+{
+   if (check_model(m) || !phi || !conc || !cl_ref || !cs_ref || !cl || !cs)
+      return AMPE_ERR_INVALID;
+   if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
+   if (m->newton_max_its < 1) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   k_phase_conc_ghostbox<<<blocks_for(g.cells_ghost()), 256, 0, S(stream)>>>(
+       *m, g, temp, phi, conc, cl_ref, cs_ref, cl, cs, counters);
+   return launch_status();
+}
+
+int ampe_conc_diffusion(const ampe_model_t* m, const double* phi,
+                        const double* temp, double* dl0, double* dl1,
+                        double* dl2, double* ds0, double* ds1, double* ds2,
+                        void* stream)
+{
+   if (check_model(m) || !phi || !dl0 || !dl1 || !ds0 || !ds1)
+      return AMPE_ERR_INVALID;
+   if (m->dim == 3 && (!dl2 || !ds2)) return AMPE_ERR_INVALID;
+   if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   k_conc_diffusion<<<blocks_for(tot), 256, 0, S(stream)>>>(
+       *m, g, phi, temp, dl0, dl1, dl2, ds0, ds1, ds2);
+   return launch_status();
+}
+
+int ampe_add_flux(const ampe_model_t* m, const double* u, const double* d0,
+                  const double* d1, const double* d2, double* flux0,
+                  double* flux1, double* flux2, void* stream)
+{
+   if (check_model(m) || !u || !d0 || !d1 || !flux0 || !flux1)
+      return AMPE_ERR_INVALID;
+   if (m->dim == 3 && (!d2 || !flux2)) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   k_add_flux<<<blocks_for(tot), 256, 0, S(stream)>>>(*m, g, u, d0, d1, d2,
+                                                      flux0, flux1, flux2);
+   return launch_status();
+}
+
+int ampe_computerhsconcentration(const ampe_model_t* m, const double* flux0,
+                                 const double* flux1, const double* flux2,
+                                 double* rhs, void* stream)
+{
+   if (check_model(m) || !flux0 || !flux1 || !rhs) return AMPE_ERR_INVALID;
+   if (m->dim == 3 && !flux2) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   k_rhs_conc<<<blocks_for(g.cells()), 256, 0, S(stream)>>>(*m, g, flux0,
+                                                            flux1, flux2, rhs);
+   return launch_status();
+}
+
+}  // extern "C"

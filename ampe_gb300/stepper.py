@@ -1,0 +1,89 @@
+"""Python front end of the C-ABI implicit stepper.
+
+Mirrors how QuatModel drives QuatIntegrator (QuatModel.cc:2318 ->
+QuatIntegrator::Advance, QuatIntegrator.cc:2096): set the state, advance a
+number of accepted steps of a fixed size, read the state back.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._native import check, lib
+
+
+def _ptr(a):
+    """Raw pointer of a contiguous numpy array or CUDA tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"] or a.dtype != np.float64:
+            raise ValueError("need a C-contiguous float64 array")
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+class ImplicitStepper:
+    """One uniform periodic level, phi + c, on the current CUDA device."""
+
+    def __init__(self, model, params):
+        self.model = model
+        self.params = params
+        h = C.c_void_p()
+        check(lib.ampe_stepper_create(C.byref(model), C.byref(params), C.byref(h)),
+              "ampe_stepper_create")
+        self._h = h
+        self.n = model.cells()
+
+    def close(self):
+        if self._h:
+            lib.ampe_stepper_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, phi, conc, cl=None, cs=None, temp=None):
+        host = isinstance(phi, np.ndarray)
+        arrs = [phi, conc, cl, cs, temp]
+        if host:
+            arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                    for a in arrs]
+        self._keep = arrs
+        check(lib.ampe_stepper_set_state(self._h, *[_ptr(a) for a in arrs],
+                                         1 if host else 0),
+              "ampe_stepper_set_state")
+
+    def get_state(self):
+        phi = np.empty(self.n)
+        c = np.empty(self.n)
+        cl = np.empty(self.n)
+        cs = np.empty(self.n)
+        check(lib.ampe_stepper_get_state(self._h, _ptr(phi), _ptr(c), _ptr(cl),
+                                         _ptr(cs), 1), "ampe_stepper_get_state")
+        shp = self.model.interior_shape()
+        return phi.reshape(shp), c.reshape(shp), cl.reshape(shp), cs.reshape(shp)
+
+    def get_state_device(self, phi, conc):
+        check(lib.ampe_stepper_get_state(self._h, _ptr(phi), _ptr(conc), None,
+                                         None, 0), "ampe_stepper_get_state")
+
+    def eval_rhs(self):
+        fp = np.empty(self.n)
+        fc = np.empty(self.n)
+        check(lib.ampe_stepper_eval_rhs(self._h, _ptr(fp), _ptr(fc), 1),
+              "ampe_stepper_eval_rhs")
+        shp = self.model.interior_shape()
+        return fp.reshape(shp), fc.reshape(shp)
+
+    def advance(self, nsteps):
+        st = abi.StepStats()
+        check(lib.ampe_stepper_advance(self._h, int(nsteps), C.byref(st)),
+              "ampe_stepper_advance")
+        return st.as_dict()
+
+    def kernel_launches(self):
+        return lib.ampe_stepper_kernel_launches(self._h)

@@ -1,0 +1,327 @@
+#!/usr/bin/env python
+"""Implicit-step throughput of the phi + c CALPHAD level on GB300.
+
+Workload (default): one uniform periodic 256^3 level, phi + binary c, CALPHAD
+regular solution with two Redlich-Kister coefficients per phase, T_run plus a
+50 K gradient along x, simple 7-point phase flux, EBS composition flux; BDF
+Newton-GMRES(5) steps of dt = 0.1 with the multigrid-preconditioned FAC
+blocks.  A "step" is one accepted implicit step of the whole level.
+
+metric: implicit-step cell-updates/s = cells x accepted steps / time.
+  value : device time (CUDA events on the stepper's stream), state resident.
+  e2e   : wall time through the public C-ABI with the state handed in from
+          pinned host memory and read back every step.
+Runs on N GPUs as N independent replicas (the level is not sharded).
+
+--impl reference: the CPU restatement of the reference path (the oracle in
+oracle/, all host threads) on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "implicit-step cell-updates/s, mixed+surrogate vs plain FP64, at ≤1e-6 rel L2 err"
+UNIT = "cell-updates/s"
+# algorithmic bytes per cell and launch of the per-cell KKS Newton kernel:
+# read phi, c, cL_ref, cS_ref (4 x 8 B), write cL, cS, dF (3 x 8 B)
+KKS_BYTES_PER_CELL = 56
+RHS_BYTES_PER_CELL = 56  # read phi, phi_lag, cL, cS, dF; write phi', c'
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--path", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precond", type=int, default=2)
+    ap.add_argument("--cpu-n", type=int, default=48)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def aggregate(local_ms, local_cell_updates, group=None):
+    """Max time over ranks and summed work (replicas): returns (ms, updates)."""
+    import torch
+    import torch.distributed as dist
+
+    if group is None and not (dist.is_available() and dist.is_initialized()):
+        return local_ms, local_cell_updates
+    t = torch.tensor([local_ms], dtype=torch.float64)
+    w = torch.tensor([float(local_cell_updates)], dtype=torch.float64)
+    backend = dist.get_backend(group)
+    if backend == "nccl":
+        t, w = t.cuda(), w.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM, group=group)
+    return float(t.item()), float(w.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.th.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def workload(n, seed=3):
+    from ampe_gb300 import configs, initial
+
+    m = configs.calphad3d(n, seed=seed, T_run=1500.0)
+    phi, c = initial.calphad3d_state(n, seed=seed, nseeds=max(2, (n // 32) ** 3 // 2),
+                                     radius=max(4.0, n / 20.0))
+    return m, phi, c
+
+
+def step_params(args, path):
+    from ampe_gb300 import configs
+
+    return configs.step_params(dt=0.1, precond=args.precond, mg_levels=5,
+                               precision=1 if path == "mixed" else 0)
+
+
+def cpu_baseline(args, threads=None):
+    """The oracle on a bounded sample (cpu_n^3 level, same physics)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle as O
+
+    n = args.cpu_n
+    m, phi, c = workload(n)
+    p = step_params(args, "fp64")
+    s = O.OracleStepper(m, p)
+    s.set_state(phi, c)
+    s.advance(1)  # warm-up (first-touch, BDF1 start)
+    steps = 2
+    t0 = time.perf_counter()
+    rc, st = s.advance(steps)
+    dt = time.perf_counter() - t0
+    cores = threads or os.cpu_count()
+    return {"value": n ** 3 * steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d^3 level, %d implicit steps (after 1 warm-up), oracle/ C++ FP64" % (n, steps)}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle as O
+
+    n = args.cpu_n
+    m, phi, c = workload(n)
+    p = step_params(args, "fp64")
+    s = O.OracleStepper(m, p)
+    s.set_state(phi, c)
+    s.advance(max(1, args.warmup))
+    t0 = time.perf_counter()
+    rc, st = s.advance(args.steps)
+    dt = time.perf_counter() - t0
+    v = n ** 3 * args.steps / dt
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "phi+c CALPHAD implicit step, bounded CPU sample %d^3" % n,
+                   "sample_of": "%d^3" % args.n},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d^3 level, %d implicit steps, oracle/ C++ FP64 (reference "
+                                   "sources unbuildable here: no SAMRAI/SUNDIALS/hypre/Thermo4PFM)"
+                                   % (n, args.steps)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from ampe_gb300 import _native
+    from ampe_gb300.stepper import ImplicitStepper
+
+    L = _native.lib
+    m, phi, c = workload(args.n)
+    N = m.cells()
+    path = args.path
+    p = step_params(args, path)
+    g = ImplicitStepper(m, p)
+    g.set_state(phi, c)
+    g.advance(args.warmup)
+    stream = torch.cuda.ExternalStream(L.ampe_stepper_stream(g._h))
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    L.ampe_stepper_profile(g._h, 1)
+    launches0 = L.ampe_stepper_kernel_launches(g._h)
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    st = g.advance(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks.stop()
+    if ws > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = L.ampe_stepper_kernel_launches(g._h) - launches0
+    kt = {}
+    for kind, name in ((0, "kks_newton"), (1, "rhs_fused")):
+        tot, cnt = C.c_double(), C.c_longlong()
+        L.ampe_stepper_kernel_time(g._h, kind, C.byref(tot), C.byref(cnt))
+        kt[name] = (tot.value, cnt.value)
+    L.ampe_stepper_profile(g._h, 0)
+    ms_max, updates = aggregate(ms, N * st["steps"] if False else N * args.steps)
+    value = updates / (ms_max / 1e3)
+
+    # end to end through the C-ABI, state from pinned host memory each step
+    e2e = None
+    if not args.no_e2e:
+        hp = torch.empty(N, dtype=torch.float64).pin_memory()
+        hc = torch.empty(N, dtype=torch.float64).pin_memory()
+        L.ampe_stepper_get_state(g._h, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()),
+                                 None, None, 1)
+        ke = max(2, min(args.steps, 6))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            L.ampe_stepper_load_y(g._h, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), 1)
+            g.advance(1)
+            L.ampe_stepper_get_state(g._h, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()),
+                                     None, None, 1)
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        _, upd_e = aggregate(te * 1e3, N * ke)
+        te_max, _ = aggregate(te * 1e3, 0)
+        e2e = {"value": upd_e / (te_max / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": 2 * N * 8, "d2h_bytes_per_step": 2 * N * 8,
+               "steps": ke}
+
+    pk, pk_kind = peaks()
+    tot, cnt = kt["kks_newton"]
+    avg_ms = tot / max(cnt, 1)
+    kks_bytes = KKS_BYTES_PER_CELL * N
+    achieved = kks_bytes / (avg_ms / 1e3) / 1e9 if cnt else None
+    roof = {"bound": "hbm", "kernel": "k_kks_interior", "achieved": achieved,
+            "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s",
+            "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
+            "algorithmic_bytes_per_launch": kks_bytes, "avg_launch_ms": avg_ms,
+            "launches": cnt, "share_of_step": tot / ms if ms else None}
+    rtot, rcnt = kt["rhs_fused"]
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if path == "fp64" else "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": "phi+c CALPHAD implicit step %d^3 (dt=0.1, BDF<=2, "
+                               "Newton-GMRES(5), MG-preconditioned FAC blocks)" % args.n,
+                   "path": path, "cells": N, "l2": "inputs larger than L2 (state 2 x %d MB)" %
+                   (N * 8 // 2 ** 20), "parallelism": "replicas" if ws > 1 else "single"},
+        "roofline": roof,
+        "kernels": {"kks_newton_ms": tot, "kks_launches": cnt, "rhs_fused_ms": rtot,
+                    "rhs_launches": rcnt},
+        "stats": st,
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "e2e": e2e,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,294 @@
+/*
+ * ampe_gb300.h -- C-ABI of the GB300 implicit-step library (libampe_gb300.so).
+ *
+ * The library implements, for ONE uniform patch level on ONE GPU, the
+ * per-level implicit step of AMPE's QuatModel with phase phi, binary
+ * composition c and (optionally) a quaternion orientation field:
+ *   - the phase right-hand side (PhaseFluxStrategy fluxes + COMPUTERHSPBG +
+ *     FreeEnergyStrategy::addDrivingForce),
+ *   - the per-cell KKS phase-concentration Newton solve
+ *     (PhaseConcentrationsStrategy::computePhaseConcentrationsOnPatch),
+ *   - the composition right-hand side (EBSCompositionRHSStrategy fluxes with
+ *     temperature dependent diffusion),
+ *   - the Phase/Conc FAC operators (red-black Gauss-Seidel smoother,
+ *     residual, within-level restrict/prolong),
+ *   - a BDF Newton-GMRES stepper that plays the role of CVODE.
+ *
+ * Conventions shared by every entry point:
+ *   - every array pointer is a DEVICE pointer unless the name says "host";
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default);
+ *   - a cell field is stored like a SAMRAI CellData<double> of depth 1 over
+ *     its ghost box: x fastest, ghost width `ng` on both sides of every
+ *     active direction (no z ghosts in 2D); strides sx=1, sy=n0+2ng,
+ *     sz=(n0+2ng)*(n1+2ng);
+ *   - a side (face) field with normal d is stored like a SAMRAI SideData with
+ *     ghost width 0: extent n_d+1 along d, n_e along the others, x fastest;
+ *   - return value: 0 success, <0 error (AMPE_ERR_*), >0 a count of cells
+ *     or cycles that did not converge (never an abort).
+ * Nothing here allocates device memory except ampe_stepper_create.
+ */
+#ifndef AMPE_GB300_H
+#define AMPE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMPE_OK 0
+#define AMPE_ERR_INVALID (-1)
+#define AMPE_ERR_CUDA (-2)
+#define AMPE_ERR_NOT_CONVERGED (-3)
+#define AMPE_ERR_NO_DEVICE (-4)
+
+/* phase flux discretisations (PhaseFluxStrategyFactory.h:12-40) */
+#define AMPE_FLUX_SIMPLE 0      /* gradient_flux, quatrhs.m4 */
+#define AMPE_FLUX_ISOTROPIC 1   /* compute_flux_isotropic, 2d/quatrhs.m4:106 */
+#define AMPE_FLUX_ANISOTROPIC 2 /* anisotropic_gradient_flux 2d:154 / 3d:180 */
+
+/* free-energy models (FreeEnergyStrategyFactory.h:46-250) */
+#define AMPE_THERMO_DILUTE 0  /* KKSdiluteBinary */
+#define AMPE_THERMO_CALPHAD 1 /* CALPHADFreeEnergyStrategyBinary */
+
+/* temperature sources */
+#define AMPE_TEMP_CONSTANT 0 /* T = T0 everywhere */
+#define AMPE_TEMP_GRADIENT 1 /* T = T0 + gradT * (i + 0.5) * dx[0], analytic */
+#define AMPE_TEMP_FIELD 2    /* T read from a cell field */
+
+#define AMPE_MAX_TSEG 6
+
+/* Pure-species Gibbs energy G(T) in J/mol, piecewise in T
+ * (thermodynamic_data/calphadAuNi.dat:1-49):
+ *   G = a + b T + c T ln T + d2 T^2 + d3 T^3 + d4 T^4 + d7 T^7
+ *       + dm1 / T + dm9 / T^9   on [tc[s], tc[s+1]). */
+typedef struct ampe_gterm {
+   int nseg;
+   double tc[AMPE_MAX_TSEG + 1];
+   double a[AMPE_MAX_TSEG], b[AMPE_MAX_TSEG], c[AMPE_MAX_TSEG];
+   double d2[AMPE_MAX_TSEG], d3[AMPE_MAX_TSEG], d4[AMPE_MAX_TSEG];
+   double d7[AMPE_MAX_TSEG], dm1[AMPE_MAX_TSEG], dm9[AMPE_MAX_TSEG];
+} ampe_gterm_t;
+
+typedef struct ampe_model {
+   /* ---- grid: one uniform periodic patch level ---- */
+   int dim;      /* 2 or 3 */
+   int n[3];     /* interior cells; n[2]=1 in 2D */
+   int ng;       /* ghost width of cell fields (>=1) */
+   double dx[3]; /* mesh spacing */
+
+   /* ---- phase equation (QuatModelParameters, PhaseRHSStrategyWithQ) ---- */
+   int flux_type;       /* AMPE_FLUX_* */
+   double epsilon_phi;  /* gradient energy coefficient epsilon */
+   double aniso_eps;    /* 2D: nu of eps(1+nu cos k(theta-phi)); 3D: eps4 */
+   int aniso_k;         /* 2D anisotropy fold knumber */
+   int qlen;            /* quaternion components seen by the flux (2 or 4) */
+   double phase_well_scale; /* w of -w g'(phi) */
+   double phase_mobility;   /* constant M_phi */
+   char well_type;      /* 'd' double well 16 phi^2 (1-phi)^2, 's' single */
+   char energy_interp;  /* h(phi) of the driving force, functions.f types */
+   char conc_interp;    /* h(phi) of c=(1-h)cL+h cS */
+   char diff_interp;    /* h(phi) weighting the phase diffusivities */
+   char avg_type;       /* 'a' arithmetic, 'h' harmonic face average of phi */
+   char orient_interp1, orient_interp2; /* p1, p2 of the orientation term */
+   char pad0;
+   int with_orient;     /* add -2H T p1'|grad q| - p2' eps_q^2/2 |grad q|^2 */
+   double misorientation_factor; /* 2 H */
+   double epsilon_q;
+
+   /* ---- composition equation (EBSCompositionRHSStrategy) ---- */
+   double conc_mobility; /* M_c */
+   double D_liquid, Q_liquid, D_solid, Q_solid; /* D0 exp(-Q/RT) */
+
+   /* ---- thermodynamics ---- */
+   int thermo;                 /* AMPE_THERMO_* */
+   double inv_molar_volume[2]; /* 1e-6/Vm for liquid, solid (J/mol->pJ/um^3) */
+   double dilute_Tm, dilute_m, dilute_k; /* meltingT, liquidus_slope, keq */
+   ampe_gterm_t g[2][2];       /* [species A,B][phase L,S] */
+   double L[2][4][2];          /* [phase L,S][RK order k][a,b]: Lk=a+b T */
+   int newton_max_its;
+   double newton_tol;          /* on |dx| of the (cL,cS) Newton update */
+
+   /* ---- temperature ---- */
+   int temp_mode;  /* AMPE_TEMP_* */
+   double T0;
+   double gradT;   /* K per unit length along x */
+} ampe_model_t;
+
+/* Integrator / preconditioner controls (QuatIntegrator.cc:278-301,
+ * samrai/FACPreconditioner.cc:79-106, EllipticFACOps.cc:282-286). */
+typedef struct ampe_step_params {
+   double dt;          /* fixed step size */
+   int max_order;      /* 1 or 2 (BDF order after the first step) */
+   double atol, rtol;  /* WRMS weights 1/(rtol |y| + atol) */
+   int max_newton;     /* Newton corrections per step (CVODE maxcor=3) */
+   double newton_coef; /* Newton test: del*min(1,crate) <= newton_coef */
+   int max_krylov;     /* GMRES Krylov dimension (5), no restarts */
+   double lin_coef;    /* GMRES test: WRMS(P^-1 r) <= lin_coef*newton_coef */
+   int precond;        /* 0 none, 1 single-level red-black, 2 multigrid */
+   int fac_max_cycles; /* FAC cycles per block solve (10) */
+   int rb_sweeps;      /* red-black sweeps per cycle (coarse solve) */
+   double rb_tol;      /* red-black early-exit tolerance (<0 = never) */
+   int mg_levels;      /* multigrid levels incl. the fine one */
+   int mg_pre, mg_post, mg_coarse_sweeps;
+   int precision;      /* 0 FP64, 1 mixed (FP32 preconditioner + Jv) */
+   int surrogate;      /* 1: MLP initial guess for the cL,cS Newton */
+   int max_retries;    /* step-size halvings after a Newton failure */
+} ampe_step_params_t;
+
+typedef struct ampe_step_stats {
+   long long steps, newton_iters, gmres_iters, rhs_evals, precond_solves,
+       precond_setups, fac_cycles, newton_fail, kks_iters, kks_fallback,
+       kks_fail, step_retries;
+   double t;
+} ampe_step_stats_t;
+
+/* ---------------------------------------------------------------------
+ * Leaf kernels (one per reference Fortran/C++ routine they replace).
+ * ------------------------------------------------------------------- */
+
+/* Periodic ghost fill of one cell field (SAMRAI RefineSchedule::fillData for
+ * a periodic level, QuatIntegrator.cc:2948-2954). */
+int ampe_fill_ghosts(const ampe_model_t* m, double* field, void* stream);
+
+/* Replaces GRADIENT_FLUX (QuatFort.h:50, 3d/quatrhs.m4:12-66),
+ * COMPUTE_FLUX_ISOTROPIC (QuatFort.h:62, 2d/quatrhs.m4:106-151) and
+ * ANISOTROPIC_GRADIENT_FLUX (QuatFort.h:75, 2d/quatrhs.m4:154-256,
+ * 3d/quatrhs.m4:180-349) selected by m->flux_type.  quat: qlen cell fields
+ * back to back (may be NULL unless anisotropic). */
+int ampe_phase_flux(const ampe_model_t* m, const double* phase,
+                    const double* quat, double* flux0, double* flux1,
+                    double* flux2, void* stream);
+
+/* Replaces COMPUTERHSPBG (QuatFort.h:90, 3d/quatrhs.m4:357-512) with
+ * three_phase=0; temp and orient_grad_mod may be NULL when with_orient=0.
+ * rhs has ghost width 0. */
+int ampe_computerhspbg(const ampe_model_t* m, const double* flux0,
+                       const double* flux1, const double* flux2,
+                       const double* temp, const double* phi,
+                       const double* orient_grad_mod, double* rhs,
+                       void* stream);
+
+/* Replaces KKSdiluteBinary::addDrivingForceOnPatch (KKSdiluteBinary.cc:
+ * 507-626) and CALPHADFreeEnergyStrategyBinary::addDrivingForce (.cc:
+ * 521-670, two phases): rhs += h'(phi)[(fL - fS) - muS(cS)(cL - cS)]. */
+int ampe_add_driving_force(const ampe_model_t* m, const double* temp,
+                           const double* phi, const double* cl,
+                           const double* cs, double* rhs, void* stream);
+
+/* Replaces PhaseConcentrationsStrategy::computePhaseConcentrationsOnPatch
+ * (PhaseConcentrationsStrategy.h:27-35; CALPHAD .cc:162-454, dilute
+ * KKSdiluteEquilibriumPhaseConcentrationsStrategy.cc:41-190): per cell of
+ * the ghost box solve c=(1-h)cL+h cS, muL(cL)=muS(cS), starting from
+ * (cl_ref, cs_ref).  counters (device, may be NULL): [0] += Newton
+ * iterations, [1] += cells not converged. */
+int ampe_phase_concentrations(const ampe_model_t* m, const double* temp,
+                              const double* phi, const double* conc,
+                              const double* cl_ref, const double* cs_ref,
+                              double* cl, double* cs,
+                              unsigned long long* counters, void* stream);
+
+/* Replaces CONCENTRATION_PFMDIFFUSION_OF_TEMPERATURE (ConcFort.h:223,
+ * 3d/concentrationdiffusion.m4:310-428) on interior faces: face D_L, D_S. */
+int ampe_conc_diffusion(const ampe_model_t* m, const double* phi,
+                        const double* temp, double* dl0, double* dl1,
+                        double* dl2, double* ds0, double* ds1, double* ds2,
+                        void* stream);
+
+/* Replaces ADD_FLUX (ConcFort.h:139, 3d/flux.m4:15-100) for depth 1:
+ * flux_d += D_d * (u_i - u_{i-1}) / dx_d. */
+int ampe_add_flux(const ampe_model_t* m, const double* u, const double* d0,
+                  const double* d1, const double* d2, double* flux0,
+                  double* flux1, double* flux2, void* stream);
+
+/* Replaces COMPUTERHSCONCENTRATION (ConcFort.h:419,
+ * 3d/concentrationrhs.m4:412-456): rhs = M_c div(flux). */
+int ampe_computerhsconcentration(const ampe_model_t* m, const double* flux0,
+                                 const double* flux1, const double* flux2,
+                                 double* rhs, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Fused hot-path kernels.
+ * ------------------------------------------------------------------- */
+
+/* Whole phi+c right-hand side of QuatIntegrator::evaluateRHSFunction
+ * (QuatIntegrator.cc:3134-3295) for given cL, cS (already computed on the
+ * ghost box): phase flux + well + driving force times M_phi, and
+ * composition M_c div(D_L grad cL + D_S grad cS).  phi, cl, cs, temp with
+ * ghosts filled; outputs with ghost width 0. */
+int ampe_rhs_phase_conc(const ampe_model_t* m, const double* phi,
+                        const double* quat, const double* temp,
+                        const double* cl, const double* cs, double* phi_rhs,
+                        double* conc_rhs, void* stream);
+
+/* ---------------------------------------------------------------------
+ * FAC operator kernels, A u = C u + M div(D grad u)
+ * (EllipticFACOps, 3d/ellipticfacops.m4).  Cell arrays have ghost width
+ * m->ng; dface0..2 are side arrays (NULL -> constant d_const); mcell /
+ * ccell NULL -> constants m_const / c_const.
+ * ------------------------------------------------------------------- */
+
+/* One colour of EFO_RBGSWITHFLUXMAX* (3d/ellipticfacops.m4:83-177,
+ * 267-359; EllipticFACOps.cc:2294-2515): flux from the current u, then
+ * u += r/diag on cells of colour `offset` ((i+j+k)%2 == offset).  If
+ * maxres (device double) is non-NULL it receives max|r| over the colour. */
+int ampe_efo_rbgs(const ampe_model_t* m, const double* dface0,
+                  const double* dface1, const double* dface2, double d_const,
+                  const double* ccell, double c_const, const double* mcell,
+                  double m_const, const double* rhs, double* u, int offset,
+                  double* maxres, void* stream);
+
+/* EFO_COMPRES* (3d/ellipticfacops.m4:448-575): res = f - A u. */
+int ampe_efo_residual(const ampe_model_t* m, const double* dface0,
+                      const double* dface1, const double* dface2,
+                      double d_const, const double* ccell, double c_const,
+                      const double* mcell, double m_const, const double* rhs,
+                      const double* u, double* res, void* stream);
+
+/* PhaseFACOps::setCOnPatchPrivate (PhaseFACOps.cc:101-183):
+ * C = 1 + gamma M_phi w g''(phi) on interior cells (ghost width m->ng). */
+int ampe_phase_fac_set_c(const ampe_model_t* m, const double* phi,
+                         double gamma, double* ccell, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Implicit stepper (CVODEAbstractFunctions + CVODESolver role,
+ * samrai/CVODEAbstractFunctions.h:61-90, QuatIntegrator.cc:2096-3906).
+ * Allocates all its device workspace here, never in ampe_stepper_advance.
+ * ------------------------------------------------------------------- */
+int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
+                        void** handle);
+int ampe_stepper_destroy(void* handle);
+/* Copy the state in.  host!=0: pointers are host memory.  phi, conc and
+ * (CALPHAD) cl, cs warm starts are interior arrays n0*n1*n2 (no ghosts);
+ * temp may be NULL unless temp_mode==AMPE_TEMP_FIELD. */
+int ampe_stepper_set_state(void* handle, const double* phi,
+                           const double* conc, const double* cl,
+                           const double* cs, const double* temp, int host);
+int ampe_stepper_get_state(void* handle, double* phi, double* conc,
+                           double* cl, double* cs, int host);
+/* Advance nsteps accepted steps of size p->dt. */
+int ampe_stepper_advance(void* handle, int nsteps, ampe_step_stats_t* stats);
+/* Evaluate f(y) of the current state (fd_flag=0 path): outputs interior. */
+int ampe_stepper_eval_rhs(void* handle, double* phi_rhs, double* conc_rhs,
+                          int host);
+/* Replace the current state y_n (phi, conc interior arrays) keeping the BDF
+ * history and the Newton warm starts: for callers that own the fields in
+ * host memory and hand them in every step (a SAMRAI patch adapter). */
+int ampe_stepper_load_y(void* handle, const double* phi, const double* conc,
+                        int host);
+/* Launches of library kernels in this process (launch accounting). */
+long long ampe_stepper_kernel_launches(void* handle);
+/* The stepper's CUDA stream (cudaStream_t), for events around advance. */
+void* ampe_stepper_stream(void* handle);
+/* Per-kernel CUDA-event timing on the stepper stream.  kind: 0 KKS Newton,
+ * 1 fused RHS.  Enabling resets the totals. */
+int ampe_stepper_profile(void* handle, int enable);
+int ampe_stepper_kernel_time(void* handle, int kind, double* total_ms,
+                             long long* launches);
+
+/* Library identification. */
+const char* ampe_version(void);
+int ampe_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,96 @@
+/* C-ABI of the CPU oracle (liborc_ampe.so).  TEST INFRASTRUCTURE ONLY:
+ * loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg as the checker of libampe_gb300; never part of the product path.
+ * Arrays are host arrays in the layouts of include/ampe_gb300.h. */
+#ifndef AMPE_ORACLE_API_H
+#define AMPE_ORACLE_API_H
+
+#include "ampe_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* scalar functions (functions.f) */
+double orc_interp_func(double phi, char type);
+double orc_deriv_interp_func(double phi, char type);
+double orc_second_deriv_interp_func(double phi, char type);
+double orc_well_func(double phi, char type);
+double orc_deriv_well_func(double phi, char type);
+double orc_second_deriv_well_func(double phi, char type);
+double orc_average_func(double a, double b, char type);
+
+/* thermodynamics at one temperature (J/mol) */
+double orc_free_energy(const ampe_model_t* m, double T, double c, int phase);
+double orc_dfdc(const ampe_model_t* m, double T, double c, int phase);
+double orc_d2fdc2(const ampe_model_t* m, double T, double c, int phase);
+double orc_gterm(const ampe_gterm_t* g, double T);
+int orc_kks_cell(const ampe_model_t* m, double T, double h, double c,
+                 double* x);
+int orc_ceq(const ampe_model_t* m, double T, double* x);
+
+/* stencils */
+void orc_fill_ghosts(const ampe_model_t* m, double* f);
+void orc_phase_flux(const ampe_model_t* m, const double* ph,
+                    const double* quat, double* f0, double* f1, double* f2);
+void orc_computerhspbg(const ampe_model_t* m, const double* f0,
+                       const double* f1, const double* f2, const double* temp,
+                       const double* phi, const double* ogm, double* rhs);
+void orc_add_driving_force(const ampe_model_t* m, const double* temp,
+                           const double* phi, const double* cl,
+                           const double* cs, double* rhs);
+long orc_phase_concentrations(const ampe_model_t* m, const double* temp,
+                              const double* phi, const double* conc,
+                              const double* clr, const double* csr,
+                              double* cl, double* cs, long* nfail);
+void orc_conc_diffusion(const ampe_model_t* m, const double* phi,
+                        const double* temp, double* dl0, double* dl1,
+                        double* dl2, double* ds0, double* ds1, double* ds2);
+void orc_add_flux(const ampe_model_t* m, const double* u, const double* d0,
+                  const double* d1, const double* d2, double* f0, double* f1,
+                  double* f2);
+void orc_computerhsconcentration(const ampe_model_t* m, const double* f0,
+                                 const double* f1, const double* f2,
+                                 double* rhs);
+void orc_rhs_phase_conc(const ampe_model_t* m, const double* phi,
+                        const double* quat, const double* temp,
+                        const double* cl, const double* cs,
+                        const double* phi_d, double* phi_rhs,
+                        double* conc_rhs);
+
+/* FAC operator */
+double orc_efo_rbgs(const ampe_model_t* m, const double* d0, const double* d1,
+                    const double* d2, double dc, const double* ccell,
+                    double cc, const double* mcell, double mc,
+                    const double* f, double* u, int offset);
+void orc_efo_residual(const ampe_model_t* m, const double* d0,
+                      const double* d1, const double* d2, double dc,
+                      const double* ccell, double cc, const double* mcell,
+                      double mc, const double* f, const double* u,
+                      double* res);
+void orc_phase_fac_set_c(const ampe_model_t* m, const double* phi,
+                         double gamma, double* ccell);
+double orc_rms_interior(const ampe_model_t* m, const double* v);
+void* orc_fac_create(const ampe_model_t* m, int nlevels);
+void orc_fac_destroy(void* h);
+void orc_fac_set_operator(void* h, const double* d0, const double* d1,
+                          const double* d2, double dc, const double* ccell,
+                          double cc, const double* mcell, double mc);
+int orc_fac_solve(void* h, const ampe_step_params_t* p, int mode,
+                  const double* f, double* u, double tol, double* res);
+
+/* implicit stepper */
+void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p);
+void orc_stepper_destroy(void* h);
+void orc_stepper_set_state(void* h, const double* phi, const double* conc,
+                           const double* cl, const double* cs,
+                           const double* temp);
+void orc_stepper_get_state(void* h, double* phi, double* conc, double* cl,
+                           double* cs);
+void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs);
+int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,417 @@
+// CPU restatement of the phase / composition right-hand-side kernels.
+// TEST INFRASTRUCTURE ONLY.  Loops and expression order follow the
+// reference Fortran cited at each function.
+#include <cstring>
+
+#include "oracle_common.h"
+#include "oracle_api.h"
+
+using namespace orc;
+
+extern "C" {
+
+// SAMRAI periodic ghost fill of a cell field (all faces, edges, corners).
+void orc_fill_ghosts(const ampe_model_t* m, double* f)
+{
+   Layout L(*m);
+   for (int k = -L.gz; k < L.n2 + L.gz; k++)
+      for (int j = -L.ng; j < L.n1 + L.ng; j++)
+         for (int i = -L.ng; i < L.n0 + L.ng; i++) {
+            const bool in = i >= 0 && i < L.n0 && j >= 0 && j < L.n1 &&
+                            k >= 0 && k < L.n2;
+            if (in) continue;
+            const int iw = ((i % L.n0) + L.n0) % L.n0;
+            const int jw = ((j % L.n1) + L.n1) % L.n1;
+            const int kw = ((k % L.n2) + L.n2) % L.n2;
+            f[L.c(i, j, k)] = f[L.c(iw, jw, kw)];
+         }
+}
+
+// gradient_flux (2d/quatrhs.m4:12-53, 3d/quatrhs.m4:12-65),
+// compute_flux_isotropic (2d/quatrhs.m4:106-151),
+// anisotropic_gradient_flux (2d/quatrhs.m4:154-256, 3d/quatrhs.m4:180-349).
+static void quat_mult(const double* a, const double* b, double* q)
+{
+   // quat.f:867-894
+   q[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+   q[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+   q[2] = a[0] * b[2] + a[2] * b[0] + a[3] * b[1] - a[1] * b[3];
+   q[3] = a[0] * b[3] + a[3] * b[0] + a[1] * b[2] - a[2] * b[1];
+}
+
+// compute_dgamma, 3d/quatrhs.m4:149-177
+static void compute_dgamma(const double* q, const double* n, double* dg,
+                           double* n4)
+{
+   double qp[4] = {q[0], -q[1], -q[2], -q[3]}, tmp[4], np[4];
+   quat_mult(n, qp, tmp);
+   quat_mult(q, tmp, np);
+   *n4 = np[1] * np[1] * np[1] * np[1] + np[2] * np[2] * np[2] * np[2] +
+         np[3] * np[3] * np[3] * np[3];
+   double d[4] = {0.0, np[1] * (np[1] * np[1] - *n4),
+                  np[2] * (np[2] * np[2] - *n4),
+                  np[3] * (np[3] * np[3] - *n4)};
+   quat_mult(d, q, tmp);
+   quat_mult(qp, tmp, dg);
+}
+
+void orc_phase_flux(const ampe_model_t* m, const double* ph,
+                    const double* quat, double* f0, double* f1, double* f2)
+{
+   Layout L(*m);
+   const double* dx = m->dx;
+   const double eps = m->epsilon_phi, eps2 = eps * eps;
+   const long qs = L.cells_ghost();
+   const double fthr = (double)1.e-12f;  // REAL literal in the reference
+   if (m->flux_type == AMPE_FLUX_SIMPLE) {
+      const double dxi = eps2 / dx[0], dyi = eps2 / dx[1];
+      #pragma omp parallel for collapse(2) schedule(static)
+      for (int k = 0; k < L.n2; k++)
+         for (int j = 0; j < L.n1; j++)
+            for (int i = 0; i <= L.n0; i++)
+               f0[L.fx(i, j, k)] = (ph[L.c(i, j, k)] - ph[L.c(i - 1, j, k)]) * dxi;
+      #pragma omp parallel for collapse(2) schedule(static)
+      for (int k = 0; k < L.n2; k++)
+         for (int j = 0; j <= L.n1; j++)
+            for (int i = 0; i < L.n0; i++)
+               f1[L.fy(i, j, k)] = (ph[L.c(i, j, k)] - ph[L.c(i, j - 1, k)]) * dyi;
+      if (L.dim == 3) {
+         const double dzi = eps2 / dx[2];
+         #pragma omp parallel for collapse(2) schedule(static)
+         for (int k = 0; k <= L.n2; k++)
+            for (int j = 0; j < L.n1; j++)
+               for (int i = 0; i < L.n0; i++)
+                  f2[L.fz(i, j, k)] =
+                      (ph[L.c(i, j, k)] - ph[L.c(i, j, k - 1)]) * dzi;
+      }
+      return;
+   }
+   if (m->flux_type == AMPE_FLUX_ISOTROPIC) {
+      // 2D only: the 3D variant stops in the reference (3d/quatrhs.m4:90-92)
+      const double dxi = (1.0 / 12.0) * eps2 / dx[0];
+      const double dyi = (1.0 / 12.0) * eps2 / dx[1];
+      const int k = 0;
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i <= L.n0; i++)
+            f0[L.fx(i, j, k)] =
+                dxi * ((ph[L.c(i, j - 1, k)] - ph[L.c(i - 1, j - 1, k)]) +
+                       (ph[L.c(i, j, k)] - ph[L.c(i - 1, j, k)]) * 10.0 +
+                       (ph[L.c(i, j + 1, k)] - ph[L.c(i - 1, j + 1, k)]));
+      for (int j = 0; j <= L.n1; j++)
+         for (int i = 0; i < L.n0; i++)
+            f1[L.fy(i, j, k)] =
+                dyi * ((ph[L.c(i - 1, j, k)] - ph[L.c(i - 1, j - 1, k)]) +
+                       (ph[L.c(i, j, k)] - ph[L.c(i, j - 1, k)]) * 10.0 +
+                       (ph[L.c(i + 1, j, k)] - ph[L.c(i + 1, j - 1, k)]));
+      return;
+   }
+   // anisotropic
+   const double dxi = 1.0 / dx[0], dyi = 1.0 / dx[1];
+   if (L.dim == 2) {
+      const double pi = 4.0 * std::atan(1.0);
+      const double nu = m->aniso_eps;
+      const double kn = (double)m->aniso_k;
+      const int k = 0;
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i <= L.n0; i++) {
+            const double dpx = (ph[L.c(i, j, k)] - ph[L.c(i - 1, j, k)]) * dxi;
+            const double dpy =
+                0.25 * (ph[L.c(i - 1, j + 1, k)] - ph[L.c(i - 1, j - 1, k)] +
+                        ph[L.c(i, j + 1, k)] - ph[L.c(i, j - 1, k)]) * dyi;
+            const double theta =
+                std::fabs(dpx) > fthr ? std::atan(dpy / dpx) : 0.5 * pi;
+            double q = 0.5 * (quat[L.c(i - 1, j, k)] + quat[L.c(i, j, k)]);
+            if (q > 1.0) q = 1.0;
+            if (q < -1.0) q = -1.0;
+            const double phi = (m->qlen == 4) ? 2.0 * std::acos(q) : std::acos(q);
+            const double et = eps * (1.0 + nu * std::cos(kn * (theta - phi)));
+            const double de = -kn * eps * nu * std::sin(kn * (theta - phi));
+            f0[L.fx(i, j, k)] = et * et * dpx - et * de * dpy;
+         }
+      for (int j = 0; j <= L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            const double dpx =
+                0.25 * (ph[L.c(i + 1, j - 1, k)] - ph[L.c(i - 1, j - 1, k)] +
+                        ph[L.c(i + 1, j, k)] - ph[L.c(i - 1, j, k)]) * dxi;
+            const double dpy = (ph[L.c(i, j, k)] - ph[L.c(i, j - 1, k)]) * dyi;
+            const double theta =
+                std::fabs(dpx) > fthr ? std::atan(dpy / dpx) : 0.5 * pi;
+            double q = 0.5 * (quat[L.c(i, j - 1, k)] + quat[L.c(i, j, k)]);
+            if (q > 1.0) q = 1.0;
+            if (q < -1.0) q = -1.0;
+            const double phi = (m->qlen == 4) ? 2.0 * std::acos(q) : std::acos(q);
+            const double et = eps * (1.0 + nu * std::cos(kn * (theta - phi)));
+            const double de = -kn * eps * nu * std::sin(kn * (theta - phi));
+            f1[L.fy(i, j, k)] = et * et * dpy + et * de * dpx;
+         }
+      return;
+   }
+   const double dzi = 1.0 / dx[2];
+   const double e4 = m->aniso_eps;
+   const double factor = 4.0 * e4 / (1.0 - 3.0 * e4);
+   for (int dir = 0; dir < 3; dir++) {
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const int ni = L.n0 + ei, nj = L.n1 + ej, nk = L.n2 + ek;
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int k = 0; k < nk; k++)
+         for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+               // neighbour cell across the face is (i-ei, j-ej, k-ek)
+               double g[3];
+               auto P = [&](int a, int b, int c) { return ph[L.c(a, b, c)]; };
+               if (dir == 0) {
+                  g[0] = (P(i, j, k) - P(i - 1, j, k)) * dxi;
+                  g[1] = 0.25 * (P(i - 1, j + 1, k) - P(i - 1, j - 1, k) +
+                                 P(i, j + 1, k) - P(i, j - 1, k)) * dyi;
+                  g[2] = 0.25 * (P(i - 1, j, k + 1) - P(i - 1, j, k - 1) +
+                                 P(i, j, k + 1) - P(i, j, k - 1)) * dzi;
+               } else if (dir == 1) {
+                  g[0] = 0.25 * (P(i + 1, j - 1, k) - P(i - 1, j - 1, k) +
+                                 P(i + 1, j, k) - P(i - 1, j, k)) * dxi;
+                  g[1] = (P(i, j, k) - P(i, j - 1, k)) * dyi;
+                  g[2] = 0.25 * (P(i, j - 1, k + 1) - P(i, j - 1, k - 1) +
+                                 P(i, j, k + 1) - P(i, j, k - 1)) * dzi;
+               } else {
+                  g[0] = 0.25 * (P(i + 1, j, k - 1) - P(i - 1, j, k - 1) +
+                                 P(i + 1, j, k) - P(i - 1, j, k)) * dxi;
+                  g[1] = 0.25 * (P(i, j + 1, k - 1) - P(i, j - 1, k - 1) +
+                                 P(i, j + 1, k) - P(i, j - 1, k)) * dyi;
+                  g[2] = (P(i, j, k) - P(i, j, k - 1)) * dzi;
+               }
+               const double gphi2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+               double dg[4], n4;
+               if (std::fabs(gphi2) > fthr) {
+                  const double nni = 1.0 / std::sqrt(gphi2);
+                  const double n[4] = {0.0, g[0] * nni, g[1] * nni, g[2] * nni};
+                  double q[4];
+                  for (int c = 0; c < 4; c++)
+                     q[c] = 0.5 * (quat[c * qs + L.c(i - ei, j - ej, k - ek)] +
+                                   quat[c * qs + L.c(i, j, k)]);
+                  compute_dgamma(q, n, dg, &n4);
+               } else {
+                  // reference defaults: (0,0,0,1) on x,y faces, (0,0,1,0) on z
+                  dg[0] = dg[1] = 0.0;
+                  dg[2] = dir == 2 ? 1.0 : 0.0;
+                  dg[3] = dir == 2 ? 0.0 : 1.0;
+                  n4 = 0.0;
+               }
+               const double gamma = eps * (1.0 - 3.0 * e4) * (1.0 + factor * n4);
+               const double v = gamma * gamma * g[dir] +
+                                16.0 * eps * gamma * e4 * std::sqrt(gphi2) *
+                                    dg[dir + 1];
+               if (dir == 0) f0[L.fx(i, j, k)] = v;
+               if (dir == 1) f1[L.fy(i, j, k)] = v;
+               if (dir == 2) f2[L.fz(i, j, k)] = v;
+            }
+   }
+}
+
+// computerhspbg (2d/quatrhs.m4:264-405, 3d/quatrhs.m4:357-512), two phases
+void orc_computerhspbg(const ampe_model_t* m, const double* f0,
+                       const double* f1, const double* f2, const double* temp,
+                       const double* phi, const double* ogm, double* rhs)
+{
+   Layout L(*m);
+   const double dxi = 1.0 / m->dx[0], dyi = 1.0 / m->dx[1];
+   const double dzi = L.dim == 3 ? 1.0 / m->dx[2] : 0.0;
+   const double eq2 = 0.5 * m->epsilon_q * m->epsilon_q;
+#pragma omp parallel for collapse(2) schedule(static)
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            double d = (f0[L.fx(i + 1, j, k)] - f0[L.fx(i, j, k)]) * dxi +
+                       (f1[L.fy(i, j + 1, k)] - f1[L.fy(i, j, k)]) * dyi;
+            if (L.dim == 3)
+               d = (f0[L.fx(i + 1, j, k)] - f0[L.fx(i, j, k)]) * dxi +
+                   (f1[L.fy(i, j + 1, k)] - f1[L.fy(i, j, k)]) * dyi +
+                   (f2[L.fz(i, j, k + 1)] - f2[L.fz(i, j, k)]) * dzi;
+            const double p = phi[L.c(i, j, k)];
+            double r = d - m->phase_well_scale * deriv_well_func(p, m->well_type);
+            if (m->with_orient) {
+               const double p1 = deriv_interp_func(p, m->orient_interp1);
+               const double p2 = deriv_interp_func(p, m->orient_interp2);
+               const double g = ogm[L.interior(i, j, k)];
+               const double T = temperature_at(*m, temp, L, i, j, k);
+               r = r - m->misorientation_factor * T * p1 * g - p2 * eq2 * g * g;
+            }
+            rhs[L.interior(i, j, k)] = r;
+         }
+}
+
+// KKSdiluteBinary.cc:507-626 / CALPHADFreeEnergyStrategyBinary.cc:521-670
+void orc_add_driving_force(const ampe_model_t* m, const double* temp,
+                           const double* phi, const double* cl,
+                           const double* cs, double* rhs)
+{
+   Layout L(*m);
+#pragma omp parallel for collapse(2) schedule(static)
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            const long ci = L.c(i, j, k);
+            const double T = temperature_at(*m, temp, L, i, j, k);
+            ThermoT th = thermo_at(*m, T);
+            const double a = cl[ci], b = cs[ci];
+            const double fl = free_energy(th, a, 0) * m->inv_molar_volume[0];
+            const double fa = free_energy(th, b, 1) * m->inv_molar_volume[1];
+            const double mu = dfdc(th, b, 1) * m->inv_molar_volume[1];
+            const double hp = deriv_interp_func(phi[ci], m->energy_interp);
+            rhs[L.interior(i, j, k)] += hp * ((fl - fa) - mu * (a - b));
+         }
+}
+
+// PhaseConcentrationsStrategy::computePhaseConcentrationsOnPatch over the
+// ghost box (CALPHADequilibriumPhaseConcentrationsStrategy.cc:325-452).
+// Returns the summed iterations; *nfail receives failed cells.
+long orc_phase_concentrations(const ampe_model_t* m, const double* temp,
+                              const double* phi, const double* conc,
+                              const double* clr, const double* csr,
+                              double* cl, double* cs, long* nfail)
+{
+   Layout L(*m);
+   long nits = 0, fails = 0;
+#pragma omp parallel for collapse(2) reduction(+ : nits, fails) schedule(static)
+   for (int k = -L.gz; k < L.n2 + L.gz; k++)
+      for (int j = -L.ng; j < L.n1 + L.ng; j++)
+         for (int i = -L.ng; i < L.n0 + L.ng; i++) {
+            const long ci = L.c(i, j, k);
+            const double T = temperature_at(*m, temp, L, i, j, k);
+            ThermoT th = thermo_at(*m, T);
+            const double h = interp_func(phi[ci], m->conc_interp);
+            double x[2] = {clr[ci], csr[ci]};
+            const int it = kks_newton(*m, th, h, conc[ci], x);
+            if (it < 0) {
+               fails++;
+               nits += m->newton_max_its;
+            } else {
+               nits += it;
+            }
+            cl[ci] = x[0];
+            cs[ci] = x[1];
+         }
+   if (nfail) *nfail = fails;
+   return nits;
+}
+
+// concentration_pfmdiffusion_of_temperature (3d/concentrationdiffusion.m4:
+// 310-428) on interior faces.
+void orc_conc_diffusion(const ampe_model_t* m, const double* phi,
+                        const double* temp, double* dl0, double* dl1,
+                        double* dl2, double* ds0, double* ds1, double* ds2)
+{
+   Layout L(*m);
+   const double qlR = m->Q_liquid / kGasR, qsR = m->Q_solid / kGasR;
+   for (int dir = 0; dir < L.dim; dir++) {
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int k = 0; k < L.n2 + ek; k++)
+         for (int j = 0; j < L.n1 + ej; j++)
+            for (int i = 0; i < L.n0 + ei; i++) {
+               const double vphi = average_func(phi[L.c(i - ei, j - ej, k - ek)],
+                                                phi[L.c(i, j, k)], m->avg_type);
+               const double hphi = interp_func(vphi, m->diff_interp);
+               const double invT =
+                   2.0 / (temperature_at(*m, temp, L, i - ei, j - ej, k - ek) +
+                          temperature_at(*m, temp, L, i, j, k));
+               const double dlq = m->D_liquid * std::exp(-qlR * invT);
+               const double dsq = m->D_solid * std::exp(-qsR * invT);
+               const long f = dir == 0 ? L.fx(i, j, k)
+                                       : (dir == 1 ? L.fy(i, j, k) : L.fz(i, j, k));
+               double* DL = dir == 0 ? dl0 : (dir == 1 ? dl1 : dl2);
+               double* DS = dir == 0 ? ds0 : (dir == 1 ? ds1 : ds2);
+               DL[f] = (1.0 - hphi) * dlq;
+               DS[f] = hphi * dsq;
+            }
+   }
+}
+
+// add_flux (2d/flux.m4:11-58, 3d/flux.m4:15-100), depth 1
+void orc_add_flux(const ampe_model_t* m, const double* u, const double* d0,
+                  const double* d1, const double* d2, double* f0, double* f1,
+                  double* f2)
+{
+   Layout L(*m);
+   const double dxi = 1.0 / m->dx[0], dyi = 1.0 / m->dx[1];
+   #pragma omp parallel for collapse(2) schedule(static)
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i <= L.n0; i++) {
+            const long f = L.fx(i, j, k);
+            f0[f] = f0[f] + dxi * d0[f] * (u[L.c(i, j, k)] - u[L.c(i - 1, j, k)]);
+         }
+   #pragma omp parallel for collapse(2) schedule(static)
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j <= L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            const long f = L.fy(i, j, k);
+            f1[f] = f1[f] + dyi * d1[f] * (u[L.c(i, j, k)] - u[L.c(i, j - 1, k)]);
+         }
+   if (L.dim == 3) {
+      const double dzi = 1.0 / m->dx[2];
+      #pragma omp parallel for collapse(2) schedule(static)
+      for (int k = 0; k <= L.n2; k++)
+         for (int j = 0; j < L.n1; j++)
+            for (int i = 0; i < L.n0; i++) {
+               const long f = L.fz(i, j, k);
+               f2[f] = f2[f] + dzi * d2[f] * (u[L.c(i, j, k)] - u[L.c(i, j, k - 1)]);
+            }
+   }
+}
+
+// computerhsconcentration (3d/concentrationrhs.m4:412-456)
+void orc_computerhsconcentration(const ampe_model_t* m, const double* f0,
+                                 const double* f1, const double* f2,
+                                 double* rhs)
+{
+   Layout L(*m);
+   const double dxi = 1.0 / m->dx[0], dyi = 1.0 / m->dx[1];
+   const double dzi = L.dim == 3 ? 1.0 / m->dx[2] : 0.0;
+#pragma omp parallel for collapse(2) schedule(static)
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            double s = dxi * (f0[L.fx(i + 1, j, k)] - f0[L.fx(i, j, k)]) +
+                       dyi * (f1[L.fy(i, j + 1, k)] - f1[L.fy(i, j, k)]);
+            if (L.dim == 3)
+               s = dxi * (f0[L.fx(i + 1, j, k)] - f0[L.fx(i, j, k)]) +
+                   dyi * (f1[L.fy(i, j + 1, k)] - f1[L.fy(i, j, k)]) +
+                   dzi * (f2[L.fz(i, j, k + 1)] - f2[L.fz(i, j, k)]);
+            rhs[L.interior(i, j, k)] = m->conc_mobility * s;
+         }
+}
+
+// Whole phi + c right-hand side for given (ghost-filled) phi, cl, cs:
+// PhaseRHSStrategyWithQ::evaluateRHS (.cc:90-313) followed by
+// QuatIntegrator::evaluateConcentrationRHS (QuatIntegrator.cc:2578-2689).
+// phi_d: phase field used for the face diffusivities (lagged in
+// finite-difference Jacobian evaluations); outputs are interior arrays.
+void orc_rhs_phase_conc(const ampe_model_t* m, const double* phi,
+                        const double* quat, const double* temp,
+                        const double* cl, const double* cs,
+                        const double* phi_d, double* phi_rhs,
+                        double* conc_rhs)
+{
+   Layout L(*m);
+   std::vector<double> f0(L.nfx()), f1(L.nfy()), f2(L.dim == 3 ? L.nfz() : 1);
+   orc_phase_flux(m, phi, quat, f0.data(), f1.data(), f2.data());
+   orc_computerhspbg(m, f0.data(), f1.data(), f2.data(), temp, phi, nullptr,
+                     phi_rhs);
+   orc_add_driving_force(m, temp, phi, cl, cs, phi_rhs);
+   const long N = L.cells();
+   for (long c = 0; c < N; c++) phi_rhs[c] *= m->phase_mobility;
+
+   std::vector<double> dl0(L.nfx()), dl1(L.nfy()), dl2(f2.size());
+   std::vector<double> ds0(L.nfx()), ds1(L.nfy()), ds2(f2.size());
+   orc_conc_diffusion(m, phi_d ? phi_d : phi, temp, dl0.data(), dl1.data(),
+                      dl2.data(), ds0.data(), ds1.data(), ds2.data());
+   std::fill(f0.begin(), f0.end(), 0.0);
+   std::fill(f1.begin(), f1.end(), 0.0);
+   std::fill(f2.begin(), f2.end(), 0.0);
+   orc_add_flux(m, cl, dl0.data(), dl1.data(), dl2.data(), f0.data(),
+                f1.data(), f2.data());
+   orc_add_flux(m, cs, ds0.data(), ds1.data(), ds2.data(), f0.data(),
+                f1.data(), f2.data());
+   orc_computerhsconcentration(m, f0.data(), f1.data(), f2.data(), conc_rhs);
+}
+
+}  // extern "C"

@@ -1,0 +1,391 @@
+// CPU restatement of the implicit step (FP64): fixed-step BDF(<=2),
+// Newton with CVODE's convergence/divergence tests, left-preconditioned
+// GMRES (modified Gram-Schmidt, no restarts) with WRMS scaling and
+// finite-difference Jacobian-vector products, and the block-diagonal
+// phase / composition FAC preconditioner.  TEST INFRASTRUCTURE ONLY.
+//
+// Reference roles: QuatIntegrator::evaluateRHSFunction (QuatIntegrator.cc:
+// 3134-3295), CVSpgmrPrecondSet (:3300-3375), CVSpgmrPrecondSolve
+// (:3666-3769), CVODESolver (samrai/CVODESolver.cc:112-258; SUNDIALS
+// CVODE 5.7.0 cvNls / SPGMR algorithms restated from their published
+// descriptions).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "oracle_api.h"
+#include "oracle_common.h"
+
+using namespace orc;
+
+namespace {
+
+struct OStepper {
+   ampe_model_t m;
+   ampe_step_params_t p;
+   long N, NG;  // interior cells, ghost-box cells
+   std::vector<double> phi_g, c_g, cl, cs, clr, csr, temp, phi_lag;
+   std::vector<double> cl_nf, cs_nf;  // cL, cS of the last f(y) with fd_flag=0
+   std::vector<double> yn, ynm1;  // 2N: [phi | c]
+   std::vector<double> Cphi, Dc[3];
+   void* fac_phi = nullptr;
+   void* fac_conc = nullptr;
+   int nsteps_done = 0;
+   int hist = 0;  // 1 when ynm1 is one step of size dt behind yn
+   double t = 0.0;
+   ampe_step_stats_t st{};
+};
+
+void to_ghosted(const OStepper& s, const double* src, std::vector<double>& g)
+{
+   Layout L(s.m);
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++)
+            g[L.c(i, j, k)] = src[L.interior(i, j, k)];
+   orc_fill_ghosts(&s.m, g.data());
+}
+
+void from_ghosted(const OStepper& s, const std::vector<double>& g, double* dst)
+{
+   Layout L(s.m);
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++)
+            dst[L.interior(i, j, k)] = g[L.c(i, j, k)];
+}
+
+const double* temp_ptr(const OStepper& s)
+{
+   return s.m.temp_mode == AMPE_TEMP_FIELD ? s.temp.data() : nullptr;
+}
+
+// f(y): fd_flag != 0 lags the face diffusivities (QuatIntegrator.cc:3189,
+// 3262-3263).
+void eval_rhs(OStepper& s, const double* y, double* fy, int fd_flag)
+{
+   to_ghosted(s, y, s.phi_g);
+   to_ghosted(s, y + s.N, s.c_g);
+   long nfail = 0;
+   long its = orc_phase_concentrations(&s.m, temp_ptr(s), s.phi_g.data(),
+                                       s.c_g.data(), s.clr.data(),
+                                       s.csr.data(), s.cl.data(), s.cs.data(),
+                                       &nfail);
+   s.st.kks_iters += its;
+   s.st.kks_fail += nfail;
+   if (!fd_flag) {
+      s.phi_lag = s.phi_g;
+      s.cl_nf = s.cl;
+      s.cs_nf = s.cs;
+   }
+   orc_rhs_phase_conc(&s.m, s.phi_g.data(), nullptr, temp_ptr(s),
+                      s.cl.data(), s.cs.data(), s.phi_lag.data(), fy,
+                      fy + s.N);
+   s.st.rhs_evals++;
+}
+
+double wrms(const OStepper& s, const double* v, const double* w)
+{
+   double acc = 0.0;
+   #pragma omp parallel for reduction(+ : acc) schedule(static)
+   for (long c = 0; c < 2 * s.N; c++) {
+      const double x = v[c] * w[c];
+      acc += x * x;
+   }
+   return std::sqrt(acc / (double)(2 * s.N));
+}
+
+// PhaseFACOps::setOperatorCoefficients + ConcFACOps::setOperatorCoefficients
+// at the state whose phi is in s.phi_g (C) and s.phi_lag (face D).
+void precond_setup(OStepper& s, double gamma)
+{
+   Layout L(s.m);
+   orc_phase_fac_set_c(&s.m, s.phi_g.data(), gamma, s.Cphi.data());
+   orc_fill_ghosts(&s.m, s.Cphi.data());
+   const double eps2 = s.m.epsilon_phi * s.m.epsilon_phi;
+   orc_fac_set_operator(s.fac_phi, nullptr, nullptr, nullptr, -gamma * eps2,
+                        s.Cphi.data(), 0.0, nullptr, s.m.phase_mobility);
+   // composition: D = -gamma (D_L + D_S), C = 1, M = M_c
+   std::vector<double> l0(L.nfx()), l1(L.nfy()), l2(L.dim == 3 ? L.nfz() : 1);
+   std::vector<double> s0(L.nfx()), s1(L.nfy()), s2(l2.size());
+   orc_conc_diffusion(&s.m, s.phi_lag.data(), temp_ptr(s), l0.data(),
+                      l1.data(), l2.data(), s0.data(), s1.data(), s2.data());
+   for (long f = 0; f < L.nfx(); f++) s.Dc[0][f] = -gamma * (l0[f] + s0[f]);
+   for (long f = 0; f < L.nfy(); f++) s.Dc[1][f] = -gamma * (l1[f] + s1[f]);
+   if (L.dim == 3)
+      for (long f = 0; f < L.nfz(); f++) s.Dc[2][f] = -gamma * (l2[f] + s2[f]);
+   orc_fac_set_operator(s.fac_conc, s.Dc[0].data(), s.Dc[1].data(),
+                        L.dim == 3 ? s.Dc[2].data() : nullptr, 0.0, nullptr,
+                        1.0, nullptr, s.m.conc_mobility);
+   s.st.precond_setups++;
+}
+
+void precond_solve(OStepper& s, const double* r, double* z, double delta)
+{
+   if (s.p.precond == 0) {
+      std::copy(r, r + 2 * s.N, z);
+      return;
+   }
+   Layout L(s.m);
+   std::vector<double> fg(s.NG, 0.0), ug(s.NG, 0.0);
+   for (int blk = 0; blk < 2; blk++) {
+      to_ghosted(s, r + blk * s.N, fg);
+      double res;
+      int cyc = orc_fac_solve(blk == 0 ? s.fac_phi : s.fac_conc, &s.p,
+                              s.p.precond, fg.data(), ug.data(), delta, &res);
+      s.st.fac_cycles += cyc;
+      from_ghosted(s, ug, z + blk * s.N);
+   }
+   s.st.precond_solves++;
+}
+
+// A v = v - gamma (f(y + sig v) - f(y)) / sig, sig = 1/WRMS(v)
+void matvec(OStepper& s, const double* y, const double* fy, const double* w,
+            double gamma, const double* v, double* out)
+{
+   const long n2 = 2 * s.N;
+   const double sig = 1.0 / wrms(s, v, w);
+   std::vector<double> yp(n2), fp(n2);
+   for (long c = 0; c < n2; c++) yp[c] = y[c] + sig * v[c];
+   eval_rhs(s, yp.data(), fp.data(), 1);
+   #pragma omp parallel for schedule(static)
+   for (long c = 0; c < n2; c++)
+      out[c] = v[c] - gamma * (fp[c] - fy[c]) / sig;
+}
+
+// Left-preconditioned scaled GMRES, x0 = 0.  Returns iterations.
+int gmres(OStepper& s, const double* y, const double* fy, const double* w,
+          double gamma, const double* b, double* x, double tol)
+{
+   const long n2 = 2 * s.N;
+   const int maxl = s.p.max_krylov;
+   const double sqrtN = std::sqrt((double)n2);
+   std::vector<std::vector<double>> V(maxl + 1, std::vector<double>(n2));
+   std::vector<double> H((maxl + 1) * maxl, 0.0), g(maxl + 1, 0.0);
+   std::vector<double> cs(maxl), sn(maxl), tmp(n2), av(n2);
+   std::fill(x, x + n2, 0.0);
+   precond_solve(s, b, tmp.data(), tol * sqrtN);
+   for (long c = 0; c < n2; c++) V[0][c] = w[c] * tmp[c];
+   double beta = 0.0;
+   for (long c = 0; c < n2; c++) beta += V[0][c] * V[0][c];
+   beta = std::sqrt(beta);
+   if (beta / sqrtN <= tol) return 0;
+   for (long c = 0; c < n2; c++) V[0][c] /= beta;
+   g[0] = beta;
+   int l = 0;
+   for (; l < maxl; l++) {
+      for (long c = 0; c < n2; c++) tmp[c] = V[l][c] / w[c];
+      matvec(s, y, fy, w, gamma, tmp.data(), av.data());
+      precond_solve(s, av.data(), tmp.data(), tol * sqrtN);
+      for (long c = 0; c < n2; c++) V[l + 1][c] = w[c] * tmp[c];
+      for (int i = 0; i <= l; i++) {  // modified Gram-Schmidt
+         double h = 0.0;
+         for (long c = 0; c < n2; c++) h += V[i][c] * V[l + 1][c];
+         H[i * maxl + l] = h;
+         for (long c = 0; c < n2; c++) V[l + 1][c] -= h * V[i][c];
+      }
+      double hn = 0.0;
+      for (long c = 0; c < n2; c++) hn += V[l + 1][c] * V[l + 1][c];
+      hn = std::sqrt(hn);
+      H[(l + 1) * maxl + l] = hn;
+      if (hn > 0.0)
+         for (long c = 0; c < n2; c++) V[l + 1][c] /= hn;
+      // apply previous Givens rotations to column l
+      for (int i = 0; i < l; i++) {
+         const double a = H[i * maxl + l], bb = H[(i + 1) * maxl + l];
+         H[i * maxl + l] = cs[i] * a + sn[i] * bb;
+         H[(i + 1) * maxl + l] = -sn[i] * a + cs[i] * bb;
+      }
+      const double a = H[l * maxl + l], bb = H[(l + 1) * maxl + l];
+      const double rr = std::sqrt(a * a + bb * bb);
+      cs[l] = a / rr;
+      sn[l] = bb / rr;
+      H[l * maxl + l] = rr;
+      H[(l + 1) * maxl + l] = 0.0;
+      g[l + 1] = -sn[l] * g[l];
+      g[l] = cs[l] * g[l];
+      if (std::fabs(g[l + 1]) / sqrtN <= tol || hn == 0.0) {
+         l++;
+         break;
+      }
+   }
+   const int k = std::min(l, maxl);
+   std::vector<double> yk(k, 0.0);
+   for (int i = k - 1; i >= 0; i--) {
+      double acc = g[i];
+      for (int j = i + 1; j < k; j++) acc -= H[i * maxl + j] * yk[j];
+      yk[i] = acc / H[i * maxl + i];
+   }
+   for (int i = 0; i < k; i++)
+      for (long c = 0; c < n2; c++) x[c] += yk[i] * V[i][c];
+   for (long c = 0; c < n2; c++) x[c] /= w[c];
+   return k;
+}
+
+// One BDF step of size h and order q from yn (and ynm1 for q=2).
+// Returns 0 on convergence, 1 on Newton failure.
+int bdf_step(OStepper& s, double h, int q, std::vector<double>& ynew)
+{
+   const long n2 = 2 * s.N;
+   std::vector<double> a(n2), y(n2), fy(n2), b(n2), d(n2), w(n2);
+   double gamma;
+   if (q == 1) {
+      gamma = h;
+      #pragma omp parallel for schedule(static)
+      for (long c = 0; c < n2; c++) {
+         a[c] = s.yn[c];
+         y[c] = s.yn[c];
+      }
+   } else {
+      gamma = 2.0 * h / 3.0;
+      #pragma omp parallel for schedule(static)
+      for (long c = 0; c < n2; c++) {
+         a[c] = (4.0 * s.yn[c] - s.ynm1[c]) / 3.0;
+         y[c] = 2.0 * s.yn[c] - s.ynm1[c];
+      }
+   }
+   #pragma omp parallel for schedule(static)
+   for (long c = 0; c < n2; c++)
+      w[c] = 1.0 / (s.p.rtol * std::fabs(s.yn[c]) + s.p.atol);
+   double crate = 1.0, delp = 0.0;
+   const double lintol = s.p.lin_coef * s.p.newton_coef;
+   for (int it = 0; it < s.p.max_newton; it++) {
+      eval_rhs(s, y.data(), fy.data(), 0);
+      if (it == 0 && s.p.precond) precond_setup(s, gamma);
+      for (long c = 0; c < n2; c++) b[c] = -(y[c] - gamma * fy[c] - a[c]);
+      const int li = gmres(s, y.data(), fy.data(), w.data(), gamma, b.data(),
+                           d.data(), lintol);
+      s.st.gmres_iters += li;
+      s.st.newton_iters++;
+      for (long c = 0; c < n2; c++) y[c] += d[c];
+      const double del = wrms(s, d.data(), w.data());
+      if (it > 0) crate = std::max(0.3 * crate, del / delp);
+      const double dcon = del * std::min(1.0, crate) / s.p.newton_coef;
+      if (dcon <= 1.0) {
+         ynew = y;
+         return 0;
+      }
+      if (it >= 1 && del > 2.0 * delp) break;
+      delp = del;
+   }
+   s.st.newton_fail++;
+   return 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p)
+{
+   OStepper* s = new OStepper;
+   s->m = *m;
+   s->p = *p;
+   Layout L(*m);
+   s->N = L.cells();
+   s->NG = L.cells_ghost();
+   for (auto* v : {&s->phi_g, &s->c_g, &s->cl, &s->cs, &s->clr, &s->csr,
+                   &s->phi_lag, &s->Cphi})
+      v->assign(s->NG, 0.0);
+   s->temp.assign(s->NG, m->T0);
+   s->Dc[0].assign(L.nfx(), 0.0);
+   s->Dc[1].assign(L.nfy(), 0.0);
+   s->Dc[2].assign(L.dim == 3 ? L.nfz() : 1, 0.0);
+   s->yn.assign(2 * s->N, 0.0);
+   s->ynm1.assign(2 * s->N, 0.0);
+   const int nl = p->precond == 2 ? p->mg_levels : 1;
+   s->fac_phi = orc_fac_create(m, nl);
+   s->fac_conc = orc_fac_create(m, nl);
+   return s;
+}
+
+void orc_stepper_destroy(void* h)
+{
+   OStepper* s = (OStepper*)h;
+   orc_fac_destroy(s->fac_phi);
+   orc_fac_destroy(s->fac_conc);
+   delete s;
+}
+
+void orc_stepper_set_state(void* h, const double* phi, const double* conc,
+                           const double* cl, const double* cs,
+                           const double* temp)
+{
+   OStepper* s = (OStepper*)h;
+   std::copy(phi, phi + s->N, s->yn.begin());
+   std::copy(conc, conc + s->N, s->yn.begin() + s->N);
+   s->ynm1 = s->yn;
+   to_ghosted(*s, cl ? cl : conc, s->clr);
+   to_ghosted(*s, cs ? cs : conc, s->csr);
+   s->cl = s->clr;
+   s->cs = s->csr;
+   s->cl_nf = s->clr;
+   s->cs_nf = s->csr;
+   s->hist = 0;
+   if (temp) to_ghosted(*s, temp, s->temp);
+   s->nsteps_done = 0;
+   s->t = 0.0;
+}
+
+void orc_stepper_get_state(void* h, double* phi, double* conc, double* cl,
+                           double* cs)
+{
+   OStepper* s = (OStepper*)h;
+   if (phi) std::copy(s->yn.begin(), s->yn.begin() + s->N, phi);
+   if (conc) std::copy(s->yn.begin() + s->N, s->yn.end(), conc);
+   if (cl) from_ghosted(*s, s->clr, cl);
+   if (cs) from_ghosted(*s, s->csr, cs);
+}
+
+void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs)
+{
+   OStepper* s = (OStepper*)h;
+   std::vector<double> fy(2 * s->N);
+   eval_rhs(*s, s->yn.data(), fy.data(), 0);
+   std::copy(fy.begin(), fy.begin() + s->N, phi_rhs);
+   std::copy(fy.begin() + s->N, fy.end(), conc_rhs);
+}
+
+// Advance nsteps accepted steps.  Returns 0, or 1 if a step failed after
+// max_retries step-size halvings.
+int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
+{
+   OStepper* s = (OStepper*)h;
+   std::vector<double> ynew;
+   int ret = 0;
+   for (int n = 0; n < nsteps; n++) {
+      double hstep = s->p.dt;
+      int q = s->hist ? std::min(2, s->p.max_order) : 1;
+      int fail = bdf_step(*s, hstep, q, ynew);
+      int retries = 0;
+      while (fail && retries < s->p.max_retries) {
+         // restart at order 1 with half the step, twice
+         retries++;
+         s->st.step_retries++;
+         hstep *= 0.5;
+         std::vector<double> ymid;
+         fail = bdf_step(*s, hstep, 1, ymid);
+         if (fail) continue;
+         s->ynm1 = s->yn;
+         s->yn = ymid;
+         fail = bdf_step(*s, hstep, 1, ynew);
+      }
+      if (fail) {
+         ret = 1;
+         break;
+      }
+      s->hist = retries == 0 ? 1 : 0;
+      s->ynm1 = s->yn;
+      s->yn = ynew;
+      s->clr = s->cl_nf;  // QuatModel::resetRefPhaseConcentrations
+      s->csr = s->cs_nf;
+      s->nsteps_done++;
+      s->t += s->p.dt;
+      s->st.steps++;
+   }
+   s->st.t = s->t;
+   if (stats) *stats = s->st;
+   return ret;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+"""ctypes access to the CPU oracle (oracle/_build/liborc_ampe.so).
+
+Test infrastructure: the oracle is the checker of the CUDA library and is
+only loaded by tests, __graft_entry__.smoke() and bench.py's CPU baseline.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "liborc_ampe.so")
+
+import sys  # noqa: E402
+
+sys.path.insert(0, ROOT)
+from ampe_gb300 import abi  # noqa: E402
+
+
+def build_oracle():
+    subprocess.run(["make", "-C", ORACLE_DIR, "-j8", "-s"], check=True)
+    return ORACLE_LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_oracle()
+        L = C.CDLL(ORACLE_LIB)
+        P, D, I = C.c_void_p, C.c_double, C.c_int
+        MP = C.POINTER(abi.Model)
+        SP = C.POINTER(abi.StepParams)
+        protos = {
+            "orc_interp_func": (D, [D, C.c_char]),
+            "orc_deriv_interp_func": (D, [D, C.c_char]),
+            "orc_second_deriv_interp_func": (D, [D, C.c_char]),
+            "orc_well_func": (D, [D, C.c_char]),
+            "orc_deriv_well_func": (D, [D, C.c_char]),
+            "orc_second_deriv_well_func": (D, [D, C.c_char]),
+            "orc_average_func": (D, [D, D, C.c_char]),
+            "orc_free_energy": (D, [MP, D, D, I]),
+            "orc_dfdc": (D, [MP, D, D, I]),
+            "orc_d2fdc2": (D, [MP, D, D, I]),
+            "orc_kks_cell": (I, [MP, D, D, D, P]),
+            "orc_ceq": (I, [MP, D, P]),
+            "orc_fill_ghosts": (None, [MP, P]),
+            "orc_phase_flux": (None, [MP, P, P, P, P, P]),
+            "orc_computerhspbg": (None, [MP, P, P, P, P, P, P, P]),
+            "orc_add_driving_force": (None, [MP, P, P, P, P, P]),
+            "orc_phase_concentrations": (C.c_long, [MP, P, P, P, P, P, P, P, P]),
+            "orc_conc_diffusion": (None, [MP, P, P, P, P, P, P, P, P]),
+            "orc_add_flux": (None, [MP, P, P, P, P, P, P, P]),
+            "orc_computerhsconcentration": (None, [MP, P, P, P, P]),
+            "orc_rhs_phase_conc": (None, [MP, P, P, P, P, P, P, P, P]),
+            "orc_efo_rbgs": (D, [MP, P, P, P, D, P, D, P, D, P, P, I]),
+            "orc_efo_residual": (None, [MP, P, P, P, D, P, D, P, D, P, P, P]),
+            "orc_phase_fac_set_c": (None, [MP, P, D, P]),
+            "orc_rms_interior": (D, [MP, P]),
+            "orc_fac_create": (P, [MP, I]),
+            "orc_fac_destroy": (None, [P]),
+            "orc_fac_set_operator": (None, [P, P, P, P, D, P, D, P, D]),
+            "orc_fac_solve": (I, [P, SP, I, P, P, D, P]),
+            "orc_stepper_create": (P, [MP, SP]),
+            "orc_stepper_destroy": (None, [P]),
+            "orc_stepper_set_state": (None, [P, P, P, P, P, P]),
+            "orc_stepper_get_state": (None, [P, P, P, P, P]),
+            "orc_stepper_eval_rhs": (None, [P, P, P]),
+            "orc_stepper_advance": (I, [P, I, C.POINTER(abi.StepStats)]),
+        }
+        for name, (res, args) in protos.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+class OracleStepper:
+    def __init__(self, model, params):
+        self.L = lib()
+        self.model = model
+        self.h = self.L.orc_stepper_create(C.byref(model), C.byref(params))
+        self.n = model.cells()
+
+    def close(self):
+        if self.h:
+            self.L.orc_stepper_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, phi, c, cl=None, cs=None, temp=None):
+        a = [None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+             for x in (phi, c, cl, cs, temp)]
+        self.L.orc_stepper_set_state(self.h, *[ptr(x) for x in a])
+
+    def get_state(self):
+        out = [np.empty(self.n) for _ in range(4)]
+        self.L.orc_stepper_get_state(self.h, *[ptr(x) for x in out])
+        shp = self.model.interior_shape()
+        return tuple(x.reshape(shp) for x in out)
+
+    def eval_rhs(self):
+        fp, fc = np.empty(self.n), np.empty(self.n)
+        self.L.orc_stepper_eval_rhs(self.h, ptr(fp), ptr(fc))
+        shp = self.model.interior_shape()
+        return fp.reshape(shp), fc.reshape(shp)
+
+    def advance(self, n):
+        st = abi.StepStats()
+        rc = self.L.orc_stepper_advance(self.h, int(n), C.byref(st))
+        return rc, st.as_dict()
+
+
+def ghosted(model, interior):
+    """Interior (z,y,x) array -> ghosted array with periodic ghosts."""
+    g = model.ng
+    gz = g if model.dim == 3 else 0
+    pad = ((gz, gz), (g, g), (g, g))
+    return np.ascontiguousarray(np.pad(interior, pad, mode="wrap"))
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b.ravel())
+    num = np.linalg.norm((a - b).ravel())
+    return num / den if den > 0 else num
