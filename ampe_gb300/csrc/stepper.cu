@@ -785,11 +785,9 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    for (double** q : vv) *q = dvec(*S, S->N2, &err);
    for (int l = 0; l <= p->max_krylov; l++) S->V.push_back(dvec(*S, S->N2, &err));
    S->counters = (unsigned long long*)dalloc<unsigned long long>(S->pool, 2, &err);
-   if (m->temp_mode != AMPE_TEMP_FIELD) {
-      const int nt = m->temp_mode == AMPE_TEMP_GRADIENT ? m->n[0] : 1;
+   const int nt = m->temp_mode == AMPE_TEMP_GRADIENT ? m->n[0] : 1;
+   if (m->temp_mode != AMPE_TEMP_FIELD)
       S->tab = (ThermoCoef*)dalloc<ThermoCoef>(S->pool, nt, &err);
-      if (!err) err = build_thermo_table(*m, S->tab, nt, S->s);
-   }
    const int nl = p->precond == 2 ? std::max(1, p->mg_levels) : 1;
    if (!err && p->precond) {
       if (p->precision == 1) {
@@ -800,6 +798,10 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
          if (!err) err = fac_create(S->facc64, *m, nl, true, false, S->pool);
       }
    }
+   // the zero fills of dalloc run on the legacy stream, which does not
+   // order with the non-blocking stepper stream: finish them first
+   if (!err && cudaDeviceSynchronize() != cudaSuccess) err = AMPE_ERR_CUDA;
+   if (!err && S->tab) err = build_thermo_table(*m, S->tab, nt, S->s);
    if (!err && cudaStreamSynchronize(S->s) != cudaSuccess) err = AMPE_ERR_CUDA;
    if (err) {
       ampe_stepper_destroy(S);

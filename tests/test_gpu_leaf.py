@@ -13,10 +13,23 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12
 
 
+_KEEP = []
+
+
+@pytest.fixture(autouse=True)
+def _keep_alive():
+    """Device copies handed to the C-ABI as raw pointers must outlive the
+    call: a temporary tensor's memory would be recycled by the allocator."""
+    yield
+    _KEEP.clear()
+
+
 def dev(a):
     import torch
 
-    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+    t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+    _KEEP.append(t)
+    return t
 
 
 def host(t):
