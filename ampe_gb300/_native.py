@@ -48,6 +48,7 @@ _PROTOS = {
     "ampe_stepper_eval_rhs": (I, [P, P, P, I]),
     "ampe_stepper_kernel_launches": (C.c_longlong, [P]),
     "ampe_stepper_load_y": (I, [P, P, P, I]),
+    "ampe_stepper_jv": (I, [P, P, D, P, I]),
     "ampe_stepper_stream": (P, [P]),
     "ampe_stepper_profile": (I, [P, I]),
     "ampe_stepper_kernel_time": (I, [P, I, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),

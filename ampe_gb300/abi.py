@@ -137,6 +137,7 @@ class StepStats(C.Structure):
             "kks_fallback",
             "kks_fail",
             "step_retries",
+            "kks_fp64_cells",
         )
     ] + [("t", C.c_double)]
 

@@ -1,0 +1,454 @@
+// Mixed-precision kernels of the phi + c implicit step.
+//
+// The outer Newton residual G(y) = y - gamma f(y) - a, the Krylov vectors,
+// their inner products and the WRMS norms stay FP64 (stepper.cu).  Inside:
+//  k_kks_mixed   per-cell KKS Newton in FP32 (logf, FP32 Redlich-Kister
+//                polynomials); cells whose iterates come within 1e-3 of
+//                c = 0 or 1 switch to the FP64 Newton.  Optional initial
+//                guess from the surrogate MLP; cells not converged within
+//                3 iterations from it restart from the plain warm start.
+//  k_rhs_mixed   the fused phase + composition right-hand side in FP32
+//                arithmetic, FP64 in/out.
+//  k_jv_point /  the Jacobian-vector product of f written out analytically
+//  k_jv_stencil  (linearised KKS split from its own 2x2 Jacobian, the
+//                chemical driving force, the well, the flux stencils with
+//                the diffusivities held fixed as the reference's
+//                finite-difference products hold them, QuatIntegrator.cc:
+//                3189, 3262-3263), in FP32.
+#include "common.cuh"
+#include "mixed.cuh"
+#include "phase_flux.cuh"
+
+namespace ampe {
+
+struct CoefF {
+   float RT, iRT, dG[2], GB[2], L[2][4];
+};
+
+__device__ __forceinline__ CoefF to_f(const ThermoCoef& t)
+{
+   CoefF f;
+   f.RT = (float)t.RT;
+   f.iRT = (float)t.iRT;
+   for (int p = 0; p < 2; p++) {
+      f.dG[p] = (float)t.dG[p];
+      f.GB[p] = (float)t.GB[p];
+      for (int k = 0; k < 4; k++) f.L[p][k] = (float)t.L[p][k];
+   }
+   return f;
+}
+
+__device__ __forceinline__ void rk_f(const float* L, float u, float& S,
+                                     float& S1, float& S2)
+{
+   S = L[0] + u * (L[1] + u * (L[2] + u * L[3]));
+   S1 = L[1] + u * (2.f * L[2] + u * 3.f * L[3]);
+   S2 = 2.f * L[2] + u * 6.f * L[3];
+}
+
+__device__ __forceinline__ float xi_f(const CoefF& th, float c, int p)
+{
+   const float u = 2.f * c - 1.f;
+   float S, S1, S2;
+   rk_f(th.L[p], u, S, S1, S2);
+   return th.dG[p] - u * S + c * (1.f - c) * 2.f * S1;
+}
+
+__device__ __forceinline__ float dxi_f(const CoefF& th, float c, int p)
+{
+   const float u = 2.f * c - 1.f;
+   float S, S1, S2;
+   rk_f(th.L[p], u, S, S1, S2);
+   return -2.f * S - 4.f * u * S1 + 4.f * c * (1.f - c) * S2;
+}
+
+constexpr float kEdge = 1.0e-3f;  // FP64 Newton within this of c = 0 or 1
+
+__device__ __forceinline__ bool near_bound(float a)
+{
+   return a < kEdge || a > 1.f - kEdge;
+}
+
+// FP32 Newton; returns iterations (>0), 0 = hand over to FP64 (bounds),
+// -1 = not converged within max_its.
+__device__ __forceinline__ int kks_newton_f32(const CoefF& th, float h,
+                                              float c, float x[2],
+                                              int max_its)
+{
+   for (int it = 1; it <= max_its; it++) {
+      const float a = x[0], b = x[1];
+      if (near_bound(a) || near_bound(b)) return 0;
+      const float F0 = (1.f - h) * a + h * b - c;
+      const float F1 = logf(a * (1.f - b) / ((1.f - a) * b)) +
+                       (xi_f(th, a, 0) - xi_f(th, b, 1)) * th.iRT;
+      const float J00 = 1.f - h, J01 = h;
+      const float J10 = 1.f / (a * (1.f - a)) + dxi_f(th, a, 0) * th.iRT;
+      const float J11 = -1.f / (b * (1.f - b)) - dxi_f(th, b, 1) * th.iRT;
+      const float idet = 1.f / (J00 * J11 - J01 * J10);
+      const float d0 = (F0 * J11 - F1 * J01) * idet;
+      const float d1 = (J00 * F1 - J10 * F0) * idet;
+      float na = a - d0, nb = b - d1;
+      if (na <= 0.f) na = 0.5f * a;
+      if (na >= 1.f) na = 0.5f * (1.f + a);
+      if (nb <= 0.f) nb = 0.5f * b;
+      if (nb >= 1.f) nb = 0.5f * (1.f + b);
+      x[0] = na;
+      x[1] = nb;
+      if (fmaxf(fabsf(d0), fabsf(d1)) < 2.0e-6f) return it;
+      if (!(isfinite(na) && isfinite(nb))) return -1;
+   }
+   return -1;
+}
+
+__device__ __forceinline__ float driving_force_f32(const CoefF& th, float a,
+                                                   float b)
+{
+   const float ua = 2.f * a - 1.f, ub = 2.f * b - 1.f;
+   float SLa, S1La, S2La, SSb, S1Sb, S2Sb;
+   rk_f(th.L[0], ua, SLa, S1La, S2La);
+   rk_f(th.L[1], ub, SSb, S1Sb, S2Sb);
+   const float ideal =
+       th.RT * (a * logf(a / b) + (1.f - a) * logf((1.f - a) / (1.f - b)));
+   const float fl = a * th.dG[0] + th.GB[0] + a * (1.f - a) * SLa;
+   const float fs = b * th.dG[1] + th.GB[1] + b * (1.f - b) * SSb;
+   const float xs = th.dG[1] - ub * SSb + b * (1.f - b) * 2.f * S1Sb;
+   return ideal + (fl - fs) - xs * (a - b);
+}
+
+__global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
+                            const double* tfield, const double* phi,
+                            const double* conc, const float* guess_l,
+                            const float* guess_s, const float* clr,
+                            const float* csr, float* cl, float* cs, float* dF,
+                            unsigned long long* counters)
+{
+   // counters: [0] FP32 iterations, [1] failed cells, [2] FP64 cells,
+   //           [3] surrogate fallbacks, [4] FP64 iterations
+   unsigned long long it32 = 0, fails = 0, n64 = 0, nfb = 0, it64 = 0;
+   const float ivm = (float)m.inv_molar_volume[1];
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long ci = g.c(i, j, k);
+      const ThermoCoef th =
+          tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
+              : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
+      const CoefF tf = to_f(th);
+      const double phd = phi[ci], cd = conc[ci];
+      const float h = interp_func((float)phd, m.conc_interp);
+      const float c = (float)cd;
+      float x[2];
+      int st = -1;
+      if (guess_l) {
+         x[0] = guess_l[t];
+         x[1] = guess_s[t];
+         if (!(x[0] > 0.f && x[0] < 1.f)) x[0] = c;
+         if (!(x[1] > 0.f && x[1] < 1.f)) x[1] = c;
+         st = kks_newton_f32(tf, h, c, x, 3);
+         if (st > 0) it32 += st;
+         if (st < 0) {
+            it32 += 3;
+            nfb++;
+         }
+      }
+      if (st < 0) {  // plain warm start
+         x[0] = clr[ci];
+         x[1] = csr[ci];
+         if (!(x[0] > 0.f && x[0] < 1.f)) x[0] = c;
+         if (!(x[1] > 0.f && x[1] < 1.f)) x[1] = c;
+         st = kks_newton_f32(tf, h, c, x, 12);
+         if (st > 0) it32 += st;
+      }
+      float a, b;
+      if (st > 0) {
+         a = x[0];
+         b = x[1];
+      } else {
+         // FP64 Newton near c = 0 or 1 (or after an FP32 failure)
+         n64++;
+         double xd[2] = {(double)clr[ci], (double)csr[ci]};
+         const double hd = interp_func(phd, m.conc_interp);
+         const int s64 = kks_newton(th, hd, cd, xd, m.newton_max_its, 1.0e-10);
+         if (s64 < 0) {
+            fails++;
+            it64 += m.newton_max_its;
+         } else {
+            it64 += s64;
+         }
+         a = (float)xd[0];
+         b = (float)xd[1];
+      }
+      cl[ci] = a;
+      cs[ci] = b;
+      for_each_image(g, i, j, k, [&](long long idx) {
+         cl[idx] = a;
+         cs[idx] = b;
+      });
+      dF[t] = driving_force_f32(tf, a, b) * ivm;
+   }
+   if (counters) {
+      unsigned long long v[5] = {it32, fails, n64, nfb, it64};
+      for (int q = 0; q < 5; q++) {
+         unsigned long long x = v[q];
+         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+         if ((threadIdx.x & 31) == 0 && x) atomicAdd(&counters[q], x);
+      }
+   }
+}
+
+int kks_mixed(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
+              const double* tfield, const double* phi, const double* conc,
+              const float* guess_l, const float* guess_s, const float* clr,
+              const float* csr, float* cl, float* cs, float* dF,
+              unsigned long long* counters, cudaStream_t s)
+{
+   long long b = (g.cells() + 255) / 256;
+   if (b > 152 * 16) b = 152 * 16;
+   k_kks_mixed<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tfield, phi, conc,
+                                           guess_l, guess_s, clr, csr, cl, cs,
+                                           dF, counters);
+   return launch_status();
+}
+
+// ---------------------------------------------------------------------------
+// FP32 fused right-hand side (simple / isotropic phase flux)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float face_flux_lin(const ampe_model_t& m, int d,
+                                               const float* pf, const Grid& g,
+                                               int i, int j, int k)
+{
+   // linear phase flux on face d whose upper cell is (i,j,k)
+   const float eps2 = (float)(m.epsilon_phi * m.epsilon_phi);
+   if (m.flux_type == AMPE_FLUX_SIMPLE || g.dim == 3) {
+      const float dinv = eps2 / (float)m.dx[d];
+      const int ei = d == 0, ej = d == 1, ek = d == 2;
+      return (pf[g.c(i, j, k)] - pf[g.c(i - ei, j - ej, k - ek)]) * dinv;
+   }
+   const float dinv = (1.f / 12.f) * eps2 / (float)m.dx[d];
+   auto P = [&](int a, int b) { return pf[g.c(a, b, 0)]; };
+   if (d == 0)
+      return dinv * ((P(i, j - 1) - P(i - 1, j - 1)) + (P(i, j) - P(i - 1, j)) * 10.f +
+                     (P(i, j + 1) - P(i - 1, j + 1)));
+   return dinv * ((P(i - 1, j) - P(i - 1, j - 1)) + (P(i, j) - P(i, j - 1)) * 10.f +
+                  (P(i + 1, j) - P(i + 1, j - 1)));
+}
+
+__global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
+{
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells_ghost(); t += (long long)gridDim.x * blockDim.x)
+      pf[t] = (float)phi[t];
+}
+
+__global__ void k_rhs_mixed(ampe_model_t m, Grid g, const double* tfield,
+                            const float* pf, const float* cl, const float* cs,
+                            const float* dF, double* phi_rhs, double* conc_rhs)
+{
+   const float dxi[3] = {(float)(1.0 / m.dx[0]), (float)(1.0 / m.dx[1]),
+                         g.dim == 3 ? (float)(1.0 / m.dx[2]) : 0.f};
+   const float qlR = (float)(m.Q_liquid / kGasR), qsR = (float)(m.Q_solid / kGasR);
+   const bool tdep = (m.Q_liquid != 0.0 || m.Q_solid != 0.0);
+   const float Dl0 = (float)m.D_liquid, Ds0 = (float)m.D_solid;
+   const float w = (float)m.phase_well_scale, Mphi = (float)m.phase_mobility;
+   const float Mc = (float)m.conc_mobility;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long c = g.c(i, j, k);
+      float diff = 0.f, div = 0.f;
+      for (int d = 0; d < g.dim; d++) {
+         const int ei = d == 0, ej = d == 1, ek = d == 2;
+         const float fm = face_flux_lin(m, d, pf, g, i, j, k);
+         const float fp = face_flux_lin(m, d, pf, g, i + ei, j + ej, k + ek);
+         diff += (fp - fm) * dxi[d];
+         float fl[2];
+         for (int side = 0; side < 2; side++) {
+            const int a0 = i + side * ei, a1 = j + side * ej, a2 = k + side * ek;
+            const long long up = g.c(a0, a1, a2);
+            const long long lo = g.c(a0 - ei, a1 - ej, a2 - ek);
+            const float vphi = average_func(pf[lo], pf[up], m.avg_type);
+            const float hphi = interp_func(vphi, m.diff_interp);
+            float dlq = Dl0, dsq = Ds0;
+            if (tdep) {
+               const float invT =
+                   2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
+                                 temperature_at(m, g, tfield, a0, a1, a2));
+               dlq = Dl0 * expf(-qlR * invT);
+               dsq = Ds0 * expf(-qsR * invT);
+            }
+            fl[side] = dxi[d] * ((1.f - hphi) * dlq * (cl[up] - cl[lo]) +
+                                 hphi * dsq * (cs[up] - cs[lo]));
+         }
+         div += dxi[d] * (fl[1] - fl[0]);
+      }
+      const float p = pf[c];
+      float r = diff - w * deriv_well_func(p, m.well_type);
+      r += deriv_interp_func(p, m.energy_interp) * dF[t];
+      phi_rhs[t] = (double)(r * Mphi);
+      conc_rhs[t] = (double)(Mc * div);
+   }
+}
+
+int rhs_mixed(const ampe_model_t& m, const Grid& g, const double* tfield,
+              const double* phi, float* pf, const float* cl, const float* cs,
+              const float* dF, double* phi_rhs, double* conc_rhs,
+              cudaStream_t s)
+{
+   long long b = (g.cells_ghost() + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   k_phi_to_f32<<<(unsigned)b, 256, 0, s>>>(g, phi, pf);
+   launch_status();
+   b = (g.cells() + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   k_rhs_mixed<<<(unsigned)b, 256, 0, s>>>(m, g, tfield, pf, cl, cs, dF,
+                                           phi_rhs, conc_rhs);
+   return launch_status();
+}
+
+// ---------------------------------------------------------------------------
+// analytic Jacobian-vector product
+// ---------------------------------------------------------------------------
+// pointwise: dphi, and the linearised KKS split (da, db) solving
+//   J [da; db] = [dc - (b - a) h_c'(phi) dphi; 0]
+__global__ void k_jv_point(ampe_model_t m, Grid g, const ThermoCoef* tab,
+                           const double* tfield, const float* pf,
+                           const float* cl, const float* cs, const double* v,
+                           float* dphi, float* da, float* db)
+{
+   const long long N = g.cells();
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
+        t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long c = g.c(i, j, k);
+      const ThermoCoef th =
+          tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
+              : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
+      const CoefF tf = to_f(th);
+      const float p = pf[c], a = cl[c], b = cs[c];
+      const float h = interp_func(p, m.conc_interp);
+      const float vp = (float)v[t], vc = (float)v[t + N];
+      const float J00 = 1.f - h, J01 = h;
+      const float J10 = 1.f / (a * (1.f - a)) + dxi_f(tf, a, 0) * tf.iRT;
+      const float J11 = -1.f / (b * (1.f - b)) - dxi_f(tf, b, 1) * tf.iRT;
+      const float idet = 1.f / (J00 * J11 - J01 * J10);
+      const float r0 = vc - (b - a) * deriv_interp_func(p, m.conc_interp) * vp;
+      const float xa = J11 * r0 * idet, xb = -J10 * r0 * idet;
+      dphi[c] = vp;
+      da[c] = xa;
+      db[c] = xb;
+      for_each_image(g, i, j, k, [&](long long idx) {
+         dphi[idx] = vp;
+         da[idx] = xa;
+         db[idx] = xb;
+      });
+   }
+}
+
+__device__ __forceinline__ float second_deriv_interp_f(float phi, char type)
+{
+   float p;
+   switch (type) {
+      case 'p':
+         p = clamp01(phi);
+         return 60.f * p * (1.f - 3.f * p + 2.f * p * p);
+      case 'h':
+         p = clamp01(phi);
+         return 6.f * (1.f - 2.f * p);
+      case 'q':
+         return phi >= 0.f ? 2.f : 0.f;
+      case 'w':
+         p = phi > 0.f ? phi : 0.f;
+         return 4.f - 6.f * p;
+      default:
+         return 0.f;
+   }
+}
+
+// out = v - gamma J v
+__global__ void k_jv_stencil(ampe_model_t m, Grid g, const ThermoCoef* tab,
+                             const double* tfield, const float* pf,
+                             const float* cl, const float* cs, const float* dF,
+                             const float* dphi, const float* da,
+                             const float* db, const double* v, double gamma,
+                             double* out)
+{
+   const float dxi[3] = {(float)(1.0 / m.dx[0]), (float)(1.0 / m.dx[1]),
+                         g.dim == 3 ? (float)(1.0 / m.dx[2]) : 0.f};
+   const float qlR = (float)(m.Q_liquid / kGasR), qsR = (float)(m.Q_solid / kGasR);
+   const bool tdep = (m.Q_liquid != 0.0 || m.Q_solid != 0.0);
+   const float Dl0 = (float)m.D_liquid, Ds0 = (float)m.D_solid;
+   const float w = (float)m.phase_well_scale, Mphi = (float)m.phase_mobility;
+   const float Mc = (float)m.conc_mobility;
+   const float ivm = (float)m.inv_molar_volume[1];
+   const long long N = g.cells();
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
+        t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long c = g.c(i, j, k);
+      float diff = 0.f, div = 0.f;
+      for (int d = 0; d < g.dim; d++) {
+         const int ei = d == 0, ej = d == 1, ek = d == 2;
+         const float fm = face_flux_lin(m, d, dphi, g, i, j, k);
+         const float fp = face_flux_lin(m, d, dphi, g, i + ei, j + ej, k + ek);
+         diff += (fp - fm) * dxi[d];
+         float fl[2];
+         for (int side = 0; side < 2; side++) {
+            const int a0 = i + side * ei, a1 = j + side * ej, a2 = k + side * ek;
+            const long long up = g.c(a0, a1, a2);
+            const long long lo = g.c(a0 - ei, a1 - ej, a2 - ek);
+            const float vphi = average_func(pf[lo], pf[up], m.avg_type);
+            const float hphi = interp_func(vphi, m.diff_interp);
+            float dlq = Dl0, dsq = Ds0;
+            if (tdep) {
+               const float invT =
+                   2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
+                                 temperature_at(m, g, tfield, a0, a1, a2));
+               dlq = Dl0 * expf(-qlR * invT);
+               dsq = Ds0 * expf(-qsR * invT);
+            }
+            fl[side] = dxi[d] * ((1.f - hphi) * dlq * (da[up] - da[lo]) +
+                                 hphi * dsq * (db[up] - db[lo]));
+         }
+         div += dxi[d] * (fl[1] - fl[0]);
+      }
+      const ThermoCoef th =
+          tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
+              : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
+      const CoefF tf = to_f(th);
+      const float p = pf[c], a = cl[c], b = cs[c], vp = dphi[c];
+      // d(dF)/db = -f_S''(b) (a - b), d(dF)/da = muL - muS = 0
+      const float fS2 = tf.RT / (b * (1.f - b)) + dxi_f(tf, b, 1);
+      const float ddF = -fS2 * (a - b) * ivm * db[c];
+      const float jp = Mphi * (diff - w * second_deriv_well_func(p, m.well_type) * vp +
+                               second_deriv_interp_f(p, m.energy_interp) * dF[t] * vp +
+                               deriv_interp_func(p, m.energy_interp) * ddF);
+      const float jc = Mc * div;
+      out[t] = v[t] - gamma * (double)jp;
+      out[t + N] = v[t + N] - gamma * (double)jc;
+   }
+}
+
+int jv_mixed(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
+             const double* tfield, const float* pf, const float* cl,
+             const float* cs, const float* dF, const double* v, double gamma,
+             float* dphi, float* da, float* db, double* out, cudaStream_t s)
+{
+   long long b = (g.cells() + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tfield, pf, cl, cs, v,
+                                          dphi, da, db);
+   launch_status();
+   k_jv_stencil<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tfield, pf, cl, cs, dF,
+                                            dphi, da, db, v, gamma, out);
+   return launch_status();
+}
+
+}  // namespace ampe

@@ -26,6 +26,7 @@
 #include "devvec.cuh"
 #include "fac.cuh"
 #include "fused.cuh"
+#include "mixed.cuh"
 
 namespace ampe {
 
@@ -439,6 +440,12 @@ struct Stepper {
    // 2N interior vectors
    double *yn, *ynm1, *ynew, *a, *y, *fy, *b, *d, *w, *tmp, *av, *fp;
    std::vector<double*> V;
+   // mixed path (FP32 working copies)
+   float *cl32 = nullptr, *cs32 = nullptr, *clr32 = nullptr, *csr32 = nullptr;
+   float *dF32 = nullptr, *pf32 = nullptr, *dphi32 = nullptr, *da32 = nullptr,
+         *db32 = nullptr;
+   float *guess_l = nullptr, *guess_s = nullptr;  // surrogate initial guess
+   unsigned long long* mcount = nullptr;          // mixed KKS counters [5]
    // preconditioner (FP64 or FP32)
    DevFac<double> facp64, facc64;
    DevFac<float> facp32, facc32;
@@ -457,7 +464,7 @@ struct Stepper {
 };
 
 // kernel classes timed in profiling mode
-enum { KT_KKS = 0, KT_RHS = 1, KT_PACK = 2, KT_NKINDS = 3 };
+enum { KT_KKS = 0, KT_RHS = 1, KT_JV = 2, KT_NKINDS = 3 };
 
 static cudaEvent_t prof_event(Stepper& S)
 {
@@ -510,6 +517,22 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    to_ghosted<double>(S.g, y, v, sig, S.phi_g, S.s);
    to_ghosted<double>(S.g, y + S.N, v ? v + S.N : nullptr, sig, S.c_g, S.s);
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
+   if (S.p.precision == 1) {
+      {
+         ProfScope ps(S, KT_KKS);
+         kks_mixed(S.m, S.g, S.tab, tf, S.phi_g, S.c_g,
+                   S.p.surrogate ? S.guess_l : nullptr,
+                   S.p.surrogate ? S.guess_s : nullptr, S.clr32, S.csr32,
+                   S.cl32, S.cs32, S.dF32, S.mcount, S.s);
+      }
+      {
+         ProfScope ps(S, KT_RHS);
+         rhs_mixed(S.m, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32, out,
+                   out + S.N, S.s);
+      }
+      S.st.rhs_evals++;
+      return;
+   }
    {
       ProfScope ps(S, KT_KKS);
       kks_interior(S.m, S.g, S.tab, tf, S.phi_g, S.c_g, S.clr, S.csr, S.cl,
@@ -561,8 +584,9 @@ static void precond_setup_t(Stepper& S, DevFac<R>& fp, DevFac<R>& fc,
    fac_coarsen_operator(fp, S.s);
    DevLevel<R>& C0 = fc.lev[0];
    const long long nf = S.g.nfx() + S.g.nfy() + (S.g.dim == 3 ? S.g.nfz() : 0);
+   const double* phid = S.p.precision == 1 ? S.phi_g : S.phi_lag;
    k_conc_precond_faces<R><<<map_blocks(nf), 256, 0, S.s>>>(
-       S.m, S.g, S.phi_lag, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
+       S.m, S.g, phid, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
    launch_status();
    for (auto& L : fc.lev) {
       L.dc = 0;
@@ -606,6 +630,13 @@ static void matvec(Stepper& S, const double* y, const double* fy,
                    const double* w, double gamma, const double* v,
                    double* out)
 {
+   if (S.p.precision == 1) {
+      const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
+      ProfScope ps(S, KT_JV);
+      jv_mixed(S.m, S.g, S.tab, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma,
+               S.dphi32, S.da32, S.db32, out, S.s);
+      return;
+   }
    const double sig = 1.0 / wrms(S, v, w);
    eval_rhs(S, y, v, sig, S.fp, 1);
    const double* fp = S.fp;
@@ -785,6 +816,17 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    for (double** q : vv) *q = dvec(*S, S->N2, &err);
    for (int l = 0; l <= p->max_krylov; l++) S->V.push_back(dvec(*S, S->N2, &err));
    S->counters = (unsigned long long*)dalloc<unsigned long long>(S->pool, 2, &err);
+   if (p->precision == 1) {
+      float** f32g[] = {&S->cl32, &S->cs32, &S->clr32, &S->csr32, &S->pf32,
+                        &S->dphi32, &S->da32, &S->db32};
+      for (float** q : f32g) *q = (float*)dalloc<float>(S->pool, S->NG, &err);
+      S->dF32 = (float*)dalloc<float>(S->pool, S->N, &err);
+      S->mcount = (unsigned long long*)dalloc<unsigned long long>(S->pool, 5, &err);
+      if (p->surrogate) {
+         S->guess_l = (float*)dalloc<float>(S->pool, S->N, &err);
+         S->guess_s = (float*)dalloc<float>(S->pool, S->N, &err);
+      }
+   }
    const int nt = m->temp_mode == AMPE_TEMP_GRADIENT ? m->n[0] : 1;
    if (m->temp_mode != AMPE_TEMP_FIELD)
       S->tab = (ThermoCoef*)dalloc<ThermoCoef>(S->pool, nt, &err);
@@ -847,6 +889,13 @@ int ampe_stepper_set_state(void* h, const double* phi, const double* conc,
    cudaMemcpyAsync(S->cs, S->csr, gb, cudaMemcpyDeviceToDevice, S->s);
    cudaMemcpyAsync(S->cl_nf, S->clr, gb, cudaMemcpyDeviceToDevice, S->s);
    cudaMemcpyAsync(S->cs_nf, S->csr, gb, cudaMemcpyDeviceToDevice, S->s);
+   if (S->p.precision == 1) {
+      to_ghosted<float>(S->g, stage, nullptr, 0.0, S->clr32, S->s);
+      to_ghosted<float>(S->g, stage + S->N, nullptr, 0.0, S->csr32, S->s);
+      const size_t gf = sizeof(float) * (size_t)S->NG;
+      cudaMemcpyAsync(S->cl32, S->clr32, gf, cudaMemcpyDeviceToDevice, S->s);
+      cudaMemcpyAsync(S->cs32, S->csr32, gf, cudaMemcpyDeviceToDevice, S->s);
+   }
    if (temp) {
       cudaMemcpyAsync(stage, temp, bytes, kind, S->s);
       to_ghosted<double>(S->g, stage, nullptr, 0.0, S->tfield, S->s);
@@ -867,8 +916,13 @@ int ampe_stepper_get_state(void* h, double* phi, double* conc, double* cl,
    if (phi) cudaMemcpyAsync(phi, S->yn, bytes, kind, S->s);
    if (conc) cudaMemcpyAsync(conc, S->yn + S->N, bytes, kind, S->s);
    if (cl || cs) {
-      k_from_ghosted<double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr, S->tmp);
-      k_from_ghosted<double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->csr, S->tmp + S->N);
+      if (S->p.precision == 1) {
+         k_from_ghosted<float><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr32, S->tmp);
+         k_from_ghosted<float><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->csr32, S->tmp + S->N);
+      } else {
+         k_from_ghosted<double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr, S->tmp);
+         k_from_ghosted<double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->csr, S->tmp + S->N);
+      }
       g_launches += 2;
       if (cl) cudaMemcpyAsync(cl, S->tmp, bytes, kind, S->s);
       if (cs) cudaMemcpyAsync(cs, S->tmp + S->N, bytes, kind, S->s);
@@ -919,8 +973,14 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
       S->hist = retries == 0 ? 1 : 0;
       swap_ptr(S->ynm1, S->yn);  // ynm1 <- yn
       swap_ptr(S->yn, S->ynew);  // yn <- ynew
-      cudaMemcpyAsync(S->clr, S->cl_nf, gb, cudaMemcpyDeviceToDevice, S->s);
-      cudaMemcpyAsync(S->csr, S->cs_nf, gb, cudaMemcpyDeviceToDevice, S->s);
+      if (S->p.precision == 1) {
+         const size_t gf = sizeof(float) * (size_t)S->NG;
+         cudaMemcpyAsync(S->clr32, S->cl32, gf, cudaMemcpyDeviceToDevice, S->s);
+         cudaMemcpyAsync(S->csr32, S->cs32, gf, cudaMemcpyDeviceToDevice, S->s);
+      } else {
+         cudaMemcpyAsync(S->clr, S->cl_nf, gb, cudaMemcpyDeviceToDevice, S->s);
+         cudaMemcpyAsync(S->csr, S->cs_nf, gb, cudaMemcpyDeviceToDevice, S->s);
+      }
       S->t += S->p.dt;
       S->st.steps++;
       if (S->prof) {
@@ -928,11 +988,15 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
          prof_collect(*S);
       }
    }
-   unsigned long long c[2] = {0, 0};
+   unsigned long long c[2] = {0, 0}, mc[5] = {0, 0, 0, 0, 0};
    cudaMemcpyAsync(c, S->counters, sizeof(c), cudaMemcpyDeviceToHost, S->s);
+   if (S->mcount)
+      cudaMemcpyAsync(mc, S->mcount, sizeof(mc), cudaMemcpyDeviceToHost, S->s);
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
-   S->st.kks_iters = (long long)c[0];
-   S->st.kks_fail = (long long)c[1];
+   S->st.kks_iters = (long long)(c[0] + mc[0] + mc[4]);
+   S->st.kks_fail = (long long)(c[1] + mc[1]);
+   S->st.kks_fp64_cells = (long long)mc[2];
+   S->st.kks_fallback = (long long)mc[3];
    S->st.t = S->t;
    if (stats) *stats = S->st;
    return ret;
@@ -978,6 +1042,26 @@ int ampe_stepper_kernel_time(void* h, int kind, double* total_ms,
    prof_collect(*S);
    if (total_ms) *total_ms = S->kms[kind];
    if (launches) *launches = S->kcount[kind];
+   return AMPE_OK;
+}
+
+int ampe_stepper_jv(void* h, const double* v, double gamma, double* out,
+                    int host)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || !v || !out) return AMPE_ERR_INVALID;
+   const cudaMemcpyKind in = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+   const cudaMemcpyKind ot = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+   const size_t b2 = sizeof(double) * (size_t)S->N2;
+   double *w = S->w, *yn = S->yn;
+   const double rtol = S->p.rtol, atol = S->p.atol;
+   map(S->N2, [=] __device__(long long t) { w[t] = 1.0 / (rtol * fabs(yn[t]) + atol); },
+       S->s);
+   eval_rhs(*S, S->yn, nullptr, 0.0, S->fy, 0);
+   cudaMemcpyAsync(S->b, v, b2, in, S->s);
+   matvec(*S, S->yn, S->fy, S->w, gamma, S->b, S->d);
+   cudaMemcpyAsync(out, S->d, b2, ot, S->s);
+   if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
    return AMPE_OK;
 }
 

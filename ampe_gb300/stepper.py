@@ -79,6 +79,14 @@ class ImplicitStepper:
         shp = self.model.interior_shape()
         return fp.reshape(shp), fc.reshape(shp)
 
+    def jv(self, v, gamma):
+        """v - gamma J v at the current state (v: [phi | conc] interior)."""
+        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        out = np.empty_like(v)
+        check(lib.ampe_stepper_jv(self._h, _ptr(v), float(gamma), _ptr(out), 1),
+              "ampe_stepper_jv")
+        return out
+
     def advance(self, nsteps):
         st = abi.StepStats()
         check(lib.ampe_stepper_advance(self._h, int(nsteps), C.byref(st)),

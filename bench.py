@@ -36,6 +36,10 @@ UNIT = "cell-updates/s"
 # read phi, c, cL_ref, cS_ref (4 x 8 B), write cL, cS, dF (3 x 8 B)
 KKS_BYTES_PER_CELL = 56
 RHS_BYTES_PER_CELL = 56  # read phi, phi_lag, cL, cS, dF; write phi', c'
+# mixed path KKS kernel: read phi, c (FP64), cL_ref, cS_ref (FP32); write cL,
+# cS, dF (FP32)
+KKS_MIXED_BYTES_PER_CELL = 36
+ATOL = 1.0e-6
 
 
 def parse():
@@ -45,7 +49,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
-    ap.add_argument("--path", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--path", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--precond", type=int, default=2)
     ap.add_argument("--cpu-n", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -149,7 +153,7 @@ def workload(n, seed=3):
 def step_params(args, path):
     from ampe_gb300 import configs
 
-    return configs.step_params(dt=0.1, precond=args.precond, mg_levels=5,
+    return configs.step_params(dt=0.1, precond=args.precond, mg_levels=5, atol=ATOL,
                                precision=1 if path == "mixed" else 0)
 
 
@@ -208,29 +212,21 @@ def run_reference(args):
     print(json.dumps(out))
 
 
-def run_ours(args):
+def timed_path(args, m, phi, c, path, local):
+    """Warm up, then time args.steps accepted steps of one path on the device.
+    Returns (result dict, final host state, stepper)."""
     import torch
-    import torch.distributed as dist
 
-    ws, rank, local = dist_env()
-    if ws > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    torch.cuda.set_device(local)
     from ampe_gb300 import _native
     from ampe_gb300.stepper import ImplicitStepper
 
     L = _native.lib
-    m, phi, c = workload(args.n)
     N = m.cells()
-    path = args.path
-    p = step_params(args, path)
-    g = ImplicitStepper(m, p)
+    g = ImplicitStepper(m, step_params(args, path))
     g.set_state(phi, c)
     g.advance(args.warmup)
     stream = torch.cuda.ExternalStream(L.ampe_stepper_stream(g._h))
     torch.cuda.synchronize()
-    if ws > 1:
-        dist.barrier()
     L.ampe_stepper_profile(g._h, 1)
     launches0 = L.ampe_stepper_kernel_launches(g._h)
     clocks = ClockSampler(local)
@@ -243,17 +239,38 @@ def run_ours(args):
     e1.record(stream)
     torch.cuda.synchronize()
     clocks.stop()
-    if ws > 1:
-        dist.barrier()
     ms = e0.elapsed_time(e1)
     launches = L.ampe_stepper_kernel_launches(g._h) - launches0
     kt = {}
-    for kind, name in ((0, "kks_newton"), (1, "rhs_fused")):
+    for kind, name in ((0, "kks_newton"), (1, "rhs_fused"), (2, "jv_analytic")):
         tot, cnt = C.c_double(), C.c_longlong()
         L.ampe_stepper_kernel_time(g._h, kind, C.byref(tot), C.byref(cnt))
-        kt[name] = (tot.value, cnt.value)
+        kt[name] = {"ms": tot.value, "launches": cnt.value}
     L.ampe_stepper_profile(g._h, 0)
-    ms_max, updates = aggregate(ms, N * st["steps"] if False else N * args.steps)
+    state = g.get_state()
+    return {"ms": ms, "stats": st, "launches": int(launches), "kernels": kt,
+            "clocks": clocks.summary(), "value": N * args.steps / (ms / 1e3)}, state, g
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from ampe_gb300 import _native
+
+    L = _native.lib
+    m, phi, c = workload(args.n)
+    N = m.cells()
+    head = args.path
+    other = "fp64" if head == "mixed" else "mixed"
+    if ws > 1:
+        dist.barrier()
+    res_h, st_h, g = timed_path(args, m, phi, c, head, local)
+    ms_max, updates = aggregate(res_h["ms"], N * args.steps)
     value = updates / (ms_max / 1e3)
 
     # end to end through the C-ABI, state from pinned host memory each step
@@ -273,38 +290,57 @@ def run_ours(args):
                                      None, None, 1)
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
-        _, upd_e = aggregate(te * 1e3, N * ke)
-        te_max, _ = aggregate(te * 1e3, 0)
+        te_max, upd_e = aggregate(te * 1e3, N * ke)
         e2e = {"value": upd_e / (te_max / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * N * 8, "d2h_bytes_per_step": 2 * N * 8,
                "steps": ke}
+    g.close()
+    del g
+    torch.cuda.empty_cache()
+
+    # the other path on the same input, for the speed ratio and the error
+    res_o, st_o, g2 = timed_path(args, m, phi, c, other, local)
+    g2.close()
+    del g2
+    fields = ("phi", "c")
+    errs = {}
+    for name, a, b in zip(fields, st_h[:2], st_o[:2]):
+        ref = b if head == "mixed" else a
+        mix = a if head == "mixed" else b
+        errs[name] = float(np.linalg.norm((mix - ref).ravel()) / np.linalg.norm(ref.ravel()))
+    v_fp64 = res_o["value"] if head == "mixed" else res_h["value"]
+    v_mixed = res_h["value"] if head == "mixed" else res_o["value"]
 
     pk, pk_kind = peaks()
-    tot, cnt = kt["kks_newton"]
+    kind = "kks_newton"
+    tot = res_h["kernels"][kind]["ms"]
+    cnt = res_h["kernels"][kind]["launches"]
     avg_ms = tot / max(cnt, 1)
-    kks_bytes = KKS_BYTES_PER_CELL * N
+    kks_bytes = (KKS_BYTES_PER_CELL if head == "fp64" else KKS_MIXED_BYTES_PER_CELL) * N
     achieved = kks_bytes / (avg_ms / 1e3) / 1e9 if cnt else None
-    roof = {"bound": "hbm", "kernel": "k_kks_interior", "achieved": achieved,
-            "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s",
+    roof = {"bound": "hbm", "kernel": "k_kks_interior" if head == "fp64" else "k_kks_mixed",
+            "achieved": achieved, "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s",
             "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
             "algorithmic_bytes_per_launch": kks_bytes, "avg_launch_ms": avg_ms,
-            "launches": cnt, "share_of_step": tot / ms if ms else None}
-    rtot, rcnt = kt["rhs_fused"]
+            "launches": cnt, "share_of_step": tot / res_h["ms"]}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if path == "fp64" else "f32+f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32+f64",
         "data": "synthetic",
         "config": {"workload": "phi+c CALPHAD implicit step %d^3 (dt=0.1, BDF<=2, "
-                               "Newton-GMRES(5), MG-preconditioned FAC blocks)" % args.n,
-                   "path": path, "cells": N, "l2": "inputs larger than L2 (state 2 x %d MB)" %
-                   (N * 8 // 2 ** 20), "parallelism": "replicas" if ws > 1 else "single"},
+                               "Newton-GMRES(5), MG-preconditioned FAC blocks, atol %g)"
+                               % (args.n, ATOL), "path": head, "cells": N,
+                   "l2": "inputs larger than L2 (state 2 x %d MB)" % (N * 8 // 2 ** 20),
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "paths": {"mixed": v_mixed, "fp64": v_fp64, "speedup_mixed_vs_fp64": v_mixed / v_fp64,
+                  "rel_l2_err_mixed_vs_fp64": errs},
         "roofline": roof,
-        "kernels": {"kks_newton_ms": tot, "kks_launches": cnt, "rhs_fused_ms": rtot,
-                    "rhs_launches": rcnt},
-        "stats": st,
-        "gpu_launches": int(launches),
-        "clocks": clocks.summary(),
+        "kernels": res_h["kernels"],
+        "stats": res_h["stats"],
+        "stats_other_path": res_o["stats"],
+        "gpu_launches": res_h["launches"],
+        "clocks": res_h["clocks"],
         "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:

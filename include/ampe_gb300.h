@@ -137,7 +137,7 @@ typedef struct ampe_step_params {
 typedef struct ampe_step_stats {
    long long steps, newton_iters, gmres_iters, rhs_evals, precond_solves,
        precond_setups, fac_cycles, newton_fail, kks_iters, kks_fallback,
-       kks_fail, step_retries;
+       kks_fail, step_retries, kks_fp64_cells;
    double t;
 } ampe_step_stats_t;
 
@@ -269,6 +269,12 @@ int ampe_stepper_advance(void* handle, int nsteps, ampe_step_stats_t* stats);
 /* Evaluate f(y) of the current state (fd_flag=0 path): outputs interior. */
 int ampe_stepper_eval_rhs(void* handle, double* phi_rhs, double* conc_rhs,
                           int host);
+/* out = v - gamma J v at the current state (J the Jacobian of f): the
+ * finite-difference product of CVODE (QuatIntegrator::
+ * evaluateJTimesRHSFunction role) on the FP64 path, the analytic FP32
+ * linearisation on the mixed path.  v, out: [phi | conc] interior. */
+int ampe_stepper_jv(void* handle, const double* v, double gamma, double* out,
+                    int host);
 /* Replace the current state y_n (phi, conc interior arrays) keeping the BDF
  * history and the Newton warm starts: for callers that own the fields in
  * host memory and hand them in every step (a SAMRAI patch adapter). */
@@ -279,7 +285,8 @@ long long ampe_stepper_kernel_launches(void* handle);
 /* The stepper's CUDA stream (cudaStream_t), for events around advance. */
 void* ampe_stepper_stream(void* handle);
 /* Per-kernel CUDA-event timing on the stepper stream.  kind: 0 KKS Newton,
- * 1 fused RHS.  Enabling resets the totals. */
+ * 1 fused RHS, 2 analytic Jacobian-vector product (mixed path).  Enabling
+ * resets the totals. */
 int ampe_stepper_profile(void* handle, int enable);
 int ampe_stepper_kernel_time(void* handle, int kind, double* total_ms,
                              long long* launches);

@@ -58,6 +58,10 @@ void orc_rhs_phase_conc(const ampe_model_t* m, const double* phi,
                         const double* phi_d, double* phi_rhs,
                         double* conc_rhs);
 
+void orc_jv_analytic(const ampe_model_t* m, const double* phi,
+                     const double* cl, const double* cs, const double* v,
+                     double gamma, double* out);
+
 /* FAC operator */
 double orc_efo_rbgs(const ampe_model_t* m, const double* d0, const double* d1,
                     const double* d2, double dc, const double* ccell,
@@ -89,6 +93,8 @@ void orc_stepper_get_state(void* h, double* phi, double* conc, double* cl,
                            double* cs);
 void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs);
 int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats);
+void orc_stepper_jv(void* h, const double* v, double gamma, double* out,
+                    int analytic);
 
 #ifdef __cplusplus
 }

@@ -414,4 +414,84 @@ void orc_rhs_phase_conc(const ampe_model_t* m, const double* phi,
    orc_computerhsconcentration(m, f0.data(), f1.data(), f2.data(), conc_rhs);
 }
 
+// Analytic Jacobian-vector product of the phi + c right-hand side at the
+// state (phi, cL, cS) (ghosted) with the face diffusivities held fixed:
+//   J [da; db] = [dc - (b - a) h_c'(phi) dphi; 0]            (KKS split)
+//   d(phi') = M [div(eps^2 grad dphi) - w g'' dphi + h_e'' dF dphi
+//                + h_e' (-f_S''(b) (a - b)) db]
+//   d(c')   = M_c div(D_L grad da + D_S grad db)
+// out = v - gamma J v; v, out interior [dphi | dc].  Simple / isotropic
+// flux only.
+void orc_jv_analytic(const ampe_model_t* m, const double* phi,
+                     const double* cl, const double* cs, const double* v,
+                     double gamma, double* out)
+{
+   Layout L(*m);
+   const long N = L.cells(), NG = L.cells_ghost();
+   std::vector<double> dp(NG), da(NG), db(NG);
+#pragma omp parallel for collapse(2) schedule(static)
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            const long c = L.c(i, j, k), t = L.interior(i, j, k);
+            ThermoT th = thermo_at(*m, temperature_at(*m, nullptr, L, i, j, k));
+            const double a = cl[c], b = cs[c], p = phi[c];
+            const double h = interp_func(p, m->conc_interp);
+            const double J00 = 1.0 - h, J01 = h;
+            const double J10 = 1.0 / (a * (1.0 - a)) + dxi(th, a, 0) / th.RT;
+            const double J11 = -1.0 / (b * (1.0 - b)) - dxi(th, b, 1) / th.RT;
+            const double det = J00 * J11 - J01 * J10;
+            const double r0 = v[t + N] - (b - a) * deriv_interp_func(p, m->conc_interp) * v[t];
+            dp[c] = v[t];
+            da[c] = J11 * r0 / det;
+            db[c] = -J10 * r0 / det;
+         }
+   orc_fill_ghosts(m, dp.data());
+   orc_fill_ghosts(m, da.data());
+   orc_fill_ghosts(m, db.data());
+   // phase part: linear flux of dphi + pointwise terms
+   std::vector<double> f0(L.nfx()), f1(L.nfy()), f2(L.dim == 3 ? L.nfz() : 1);
+   orc_phase_flux(m, dp.data(), nullptr, f0.data(), f1.data(), f2.data());
+   std::vector<double> lap(N);
+   ampe_model_t m0 = *m;
+   m0.phase_well_scale = 0.0;
+   m0.with_orient = 0;
+   orc_computerhspbg(&m0, f0.data(), f1.data(), f2.data(), nullptr, dp.data(),
+                     nullptr, lap.data());
+   // composition part
+   std::vector<double> l0(L.nfx()), l1(L.nfy()), l2(f2.size());
+   std::vector<double> s0(L.nfx()), s1(L.nfy()), s2(f2.size());
+   orc_conc_diffusion(m, phi, nullptr, l0.data(), l1.data(), l2.data(),
+                      s0.data(), s1.data(), s2.data());
+   std::fill(f0.begin(), f0.end(), 0.0);
+   std::fill(f1.begin(), f1.end(), 0.0);
+   std::fill(f2.begin(), f2.end(), 0.0);
+   orc_add_flux(m, da.data(), l0.data(), l1.data(), l2.data(), f0.data(),
+                f1.data(), f2.data());
+   orc_add_flux(m, db.data(), s0.data(), s1.data(), s2.data(), f0.data(),
+                f1.data(), f2.data());
+   std::vector<double> jc(N);
+   orc_computerhsconcentration(m, f0.data(), f1.data(), f2.data(), jc.data());
+#pragma omp parallel for collapse(2) schedule(static)
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            const long c = L.c(i, j, k), t = L.interior(i, j, k);
+            ThermoT th = thermo_at(*m, temperature_at(*m, nullptr, L, i, j, k));
+            const double a = cl[c], b = cs[c], p = phi[c];
+            const double fl = free_energy(th, a, 0) * m->inv_molar_volume[0];
+            const double fa = free_energy(th, b, 1) * m->inv_molar_volume[1];
+            const double mu = dfdc(th, b, 1) * m->inv_molar_volume[1];
+            const double dF = (fl - fa) - mu * (a - b);
+            const double ddF = -d2fdc2(th, b, 1) * (a - b) * m->inv_molar_volume[1] * db[c];
+            const double jp =
+                m->phase_mobility *
+                (lap[t] - m->phase_well_scale * second_deriv_well_func(p, m->well_type) * v[t] +
+                 second_deriv_interp_func(p, m->energy_interp) * dF * v[t] +
+                 deriv_interp_func(p, m->energy_interp) * ddF);
+            out[t] = v[t] - gamma * jp;
+            out[t + N] = v[t + N] - gamma * jc[t];
+         }
+}
+
 }  // extern "C"

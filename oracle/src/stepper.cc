@@ -388,4 +388,22 @@ int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
    return ret;
 }
 
+// out = v - gamma J v at the current state y_n: finite differences of f
+// (analytic = 0, the CVODE product) or the analytic linearisation.
+void orc_stepper_jv(void* h, const double* v, double gamma, double* out,
+                    int analytic)
+{
+   OStepper* s = (OStepper*)h;
+   const long n2 = 2 * s->N;
+   std::vector<double> fy(n2), w(n2);
+   eval_rhs(*s, s->yn.data(), fy.data(), 0);
+   for (long c = 0; c < n2; c++)
+      w[c] = 1.0 / (s->p.rtol * std::fabs(s->yn[c]) + s->p.atol);
+   if (analytic)
+      orc_jv_analytic(&s->m, s->phi_g.data(), s->cl.data(), s->cs.data(), v,
+                      gamma, out);
+   else
+      matvec(*s, s->yn.data(), fy.data(), w.data(), gamma, v, out);
+}
+
 }  // extern "C"

@@ -71,6 +71,8 @@ def lib():
             "orc_stepper_get_state": (None, [P, P, P, P, P]),
             "orc_stepper_eval_rhs": (None, [P, P, P]),
             "orc_stepper_advance": (I, [P, I, C.POINTER(abi.StepStats)]),
+            "orc_stepper_jv": (None, [P, P, D, P, I]),
+            "orc_jv_analytic": (None, [MP, P, P, P, P, D, P]),
         }
         for name, (res, args) in protos.items():
             f = getattr(L, name)
@@ -118,6 +120,12 @@ class OracleStepper:
         self.L.orc_stepper_eval_rhs(self.h, ptr(fp), ptr(fc))
         shp = self.model.interior_shape()
         return fp.reshape(shp), fc.reshape(shp)
+
+    def jv(self, v, gamma, analytic):
+        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        out = np.empty_like(v)
+        self.L.orc_stepper_jv(self.h, ptr(v), gamma, ptr(out), int(analytic))
+        return out
 
     def advance(self, n):
         st = abi.StepStats()
