@@ -3,10 +3,11 @@
 // The outer Newton residual G(y) = y - gamma f(y) - a, the Krylov vectors,
 // their inner products and the WRMS norms stay FP64 (stepper.cu).  Inside:
 //  k_kks_mixed   per-cell KKS Newton in FP32 (logf, FP32 Redlich-Kister
-//                polynomials); cells whose iterates come within 1e-3 of
-//                c = 0 or 1 switch to the FP64 Newton.  Optional initial
-//                guess from the surrogate MLP; cells not converged within
-//                3 iterations from it restart from the plain warm start.
+//                polynomials); cells whose solution lies within 1e-4 of
+//                c = 0 or 1 get an FP64 Newton polish from the FP32 result
+//                (and an FP64 driving force).  Optional initial guess from
+//                the surrogate MLP; cells not converged within 3 iterations
+//                from it restart from the plain warm start.
 //  k_rhs_mixed   the fused phase + composition right-hand side in FP32
 //                arithmetic, FP64 in/out.
 //  k_jv_point /  the Jacobian-vector product of f written out analytically
@@ -20,10 +21,6 @@
 #include "phase_flux.cuh"
 
 namespace ampe {
-
-struct CoefF {
-   float RT, iRT, dG[2], GB[2], L[2][4];
-};
 
 __device__ __forceinline__ CoefF to_f(const ThermoCoef& t)
 {
@@ -62,22 +59,21 @@ __device__ __forceinline__ float dxi_f(const CoefF& th, float c, int p)
    return -2.f * S - 4.f * u * S1 + 4.f * c * (1.f - c) * S2;
 }
 
-constexpr float kEdge = 1.0e-3f;  // FP64 Newton within this of c = 0 or 1
+constexpr float kEdge = 1.0e-4f;  // FP64 polish within this of c = 0 or 1
 
 __device__ __forceinline__ bool near_bound(float a)
 {
    return a < kEdge || a > 1.f - kEdge;
 }
 
-// FP32 Newton; returns iterations (>0), 0 = hand over to FP64 (bounds),
-// -1 = not converged within max_its.
+// FP32 Newton; returns iterations (>0) or -1 when not converged within
+// max_its (or a non-finite iterate).
 __device__ __forceinline__ int kks_newton_f32(const CoefF& th, float h,
                                               float c, float x[2],
                                               int max_its)
 {
    for (int it = 1; it <= max_its; it++) {
       const float a = x[0], b = x[1];
-      if (near_bound(a) || near_bound(b)) return 0;
       const float F0 = (1.f - h) * a + h * b - c;
       const float F1 = logf(a * (1.f - b) / ((1.f - a) * b)) +
                        (xi_f(th, a, 0) - xi_f(th, b, 1)) * th.iRT;
@@ -100,6 +96,17 @@ __device__ __forceinline__ int kks_newton_f32(const CoefF& th, float h,
    return -1;
 }
 
+__device__ __forceinline__ double driving_force_scaled(const ampe_model_t& m,
+                                                       const ThermoCoef& th,
+                                                       double a, double b)
+{
+   // (fL - fS) - muS (a - b) in FP64 (fused.cu writes the same quantity)
+   const double fl = free_energy_of(th, a, 0) * m.inv_molar_volume[0];
+   const double fa = free_energy_of(th, b, 1) * m.inv_molar_volume[1];
+   const double mu = dfdc_of(th, b, 1) * m.inv_molar_volume[1];
+   return (fl - fa) - mu * (a - b);
+}
+
 __device__ __forceinline__ float driving_force_f32(const CoefF& th, float a,
                                                    float b)
 {
@@ -115,15 +122,30 @@ __device__ __forceinline__ float driving_force_f32(const CoefF& th, float a,
    return ideal + (fl - fs) - xs * (a - b);
 }
 
-__global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
-                            const double* tfield, const double* phi,
-                            const double* conc, const float* guess_l,
-                            const float* guess_s, const float* clr,
-                            const float* csr, float* cl, float* cs, float* dF,
-                            unsigned long long* counters)
+__global__ void k_build_coef_f(int n, const ThermoCoef* tab, CoefF* tabf)
 {
-   // counters: [0] FP32 iterations, [1] failed cells, [2] FP64 cells,
-   //           [3] surrogate fallbacks, [4] FP64 iterations
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) tabf[i] = to_f(tab[i]);
+}
+
+__device__ __forceinline__ CoefF coef_f_at(const ampe_model_t& m,
+                                          const Grid& g, const CoefF* tabf,
+                                          const double* tfield, int i, int j,
+                                          int k)
+{
+   if (tabf) return tabf[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0];
+   return to_f(thermo_coef(m, temperature_at(m, g, tfield, i, j, k)));
+}
+
+__global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
+                            const CoefF* tabf, const double* tfield,
+                            const double* phi, const double* conc,
+                            const float* guess_l, const float* guess_s,
+                            const float* clr, const float* csr, float* cl,
+                            float* cs, float* dF, unsigned long long* counters)
+{
+   // counters: [0] FP32 iterations, [1] failed cells, [2] FP64-polished
+   //           cells, [3] surrogate fallbacks, [4] FP64 iterations
    unsigned long long it32 = 0, fails = 0, n64 = 0, nfb = 0, it64 = 0;
    const float ivm = (float)m.inv_molar_volume[1];
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -132,10 +154,7 @@ __global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
       const int j = (int)((t / g.n0) % g.n1);
       const int k = (int)(t / ((long long)g.n0 * g.n1));
       const long long ci = g.c(i, j, k);
-      const ThermoCoef th =
-          tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
-              : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
-      const CoefF tf = to_f(th);
+      const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
       const double phd = phi[ci], cd = conc[ci];
       const float h = interp_func((float)phd, m.conc_interp);
       const float c = (float)cd;
@@ -159,16 +178,26 @@ __global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
          if (!(x[0] > 0.f && x[0] < 1.f)) x[0] = c;
          if (!(x[1] > 0.f && x[1] < 1.f)) x[1] = c;
          st = kks_newton_f32(tf, h, c, x, 12);
-         if (st > 0) it32 += st;
+         it32 += st > 0 ? st : 12;
       }
-      float a, b;
-      if (st > 0) {
-         a = x[0];
-         b = x[1];
+      float a = x[0], b = x[1], dfv;
+      if (st > 0 && !near_bound(a) && !near_bound(b)) {
+         dfv = driving_force_f32(tf, a, b) * ivm;
       } else {
-         // FP64 Newton near c = 0 or 1 (or after an FP32 failure)
+         // FP64 polish from the FP32 iterate near c = 0 or 1 (full FP64
+         // Newton from the warm start if FP32 did not converge)
          n64++;
-         double xd[2] = {(double)clr[ci], (double)csr[ci]};
+         const ThermoCoef th =
+             tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
+                 : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
+         double xd[2];
+         if (st > 0) {
+            xd[0] = a;
+            xd[1] = b;
+         } else {
+            xd[0] = clr[ci];
+            xd[1] = csr[ci];
+         }
          const double hd = interp_func(phd, m.conc_interp);
          const int s64 = kks_newton(th, hd, cd, xd, m.newton_max_its, 1.0e-10);
          if (s64 < 0) {
@@ -179,6 +208,7 @@ __global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
          }
          a = (float)xd[0];
          b = (float)xd[1];
+         dfv = (float)driving_force_scaled(m, th, xd[0], xd[1]);
       }
       cl[ci] = a;
       cs[ci] = b;
@@ -186,7 +216,7 @@ __global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
          cl[idx] = a;
          cs[idx] = b;
       });
-      dF[t] = driving_force_f32(tf, a, b) * ivm;
+      dF[t] = dfv;
    }
    if (counters) {
       unsigned long long v[5] = {it32, fails, n64, nfb, it64};
@@ -198,15 +228,21 @@ __global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
    }
 }
 
+int build_coef_f(const ThermoCoef* tab, CoefF* tabf, int n, cudaStream_t s)
+{
+   k_build_coef_f<<<(n + 127) / 128, 128, 0, s>>>(n, tab, tabf);
+   return launch_status();
+}
+
 int kks_mixed(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
-              const double* tfield, const double* phi, const double* conc,
-              const float* guess_l, const float* guess_s, const float* clr,
-              const float* csr, float* cl, float* cs, float* dF,
-              unsigned long long* counters, cudaStream_t s)
+              const CoefF* tabf, const double* tfield, const double* phi,
+              const double* conc, const float* guess_l, const float* guess_s,
+              const float* clr, const float* csr, float* cl, float* cs,
+              float* dF, unsigned long long* counters, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > 152 * 16) b = 152 * 16;
-   k_kks_mixed<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tfield, phi, conc,
+   k_kks_mixed<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tabf, tfield, phi, conc,
                                            guess_l, guess_s, clr, csr, cl, cs,
                                            dF, counters);
    return launch_status();
@@ -314,7 +350,7 @@ int rhs_mixed(const ampe_model_t& m, const Grid& g, const double* tfield,
 // ---------------------------------------------------------------------------
 // pointwise: dphi, and the linearised KKS split (da, db) solving
 //   J [da; db] = [dc - (b - a) h_c'(phi) dphi; 0]
-__global__ void k_jv_point(ampe_model_t m, Grid g, const ThermoCoef* tab,
+__global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
                            const double* tfield, const float* pf,
                            const float* cl, const float* cs, const double* v,
                            float* dphi, float* da, float* db)
@@ -326,10 +362,7 @@ __global__ void k_jv_point(ampe_model_t m, Grid g, const ThermoCoef* tab,
       const int j = (int)((t / g.n0) % g.n1);
       const int k = (int)(t / ((long long)g.n0 * g.n1));
       const long long c = g.c(i, j, k);
-      const ThermoCoef th =
-          tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
-              : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
-      const CoefF tf = to_f(th);
+      const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
       const float p = pf[c], a = cl[c], b = cs[c];
       const float h = interp_func(p, m.conc_interp);
       const float vp = (float)v[t], vc = (float)v[t + N];
@@ -371,7 +404,7 @@ __device__ __forceinline__ float second_deriv_interp_f(float phi, char type)
 }
 
 // out = v - gamma J v
-__global__ void k_jv_stencil(ampe_model_t m, Grid g, const ThermoCoef* tab,
+__global__ void k_jv_stencil(ampe_model_t m, Grid g, const CoefF* tabf,
                              const double* tfield, const float* pf,
                              const float* cl, const float* cs, const float* dF,
                              const float* dphi, const float* da,
@@ -419,10 +452,7 @@ __global__ void k_jv_stencil(ampe_model_t m, Grid g, const ThermoCoef* tab,
          }
          div += dxi[d] * (fl[1] - fl[0]);
       }
-      const ThermoCoef th =
-          tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
-              : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
-      const CoefF tf = to_f(th);
+      const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
       const float p = pf[c], a = cl[c], b = cs[c], vp = dphi[c];
       // d(dF)/db = -f_S''(b) (a - b), d(dF)/da = muL - muS = 0
       const float fS2 = tf.RT / (b * (1.f - b)) + dxi_f(tf, b, 1);
@@ -436,17 +466,17 @@ __global__ void k_jv_stencil(ampe_model_t m, Grid g, const ThermoCoef* tab,
    }
 }
 
-int jv_mixed(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
+int jv_mixed(const ampe_model_t& m, const Grid& g, const CoefF* tabf,
              const double* tfield, const float* pf, const float* cl,
              const float* cs, const float* dF, const double* v, double gamma,
              float* dphi, float* da, float* db, double* out, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
-   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tfield, pf, cl, cs, v,
+   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v,
                                           dphi, da, db);
    launch_status();
-   k_jv_stencil<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tfield, pf, cl, cs, dF,
+   k_jv_stencil<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, dF,
                                             dphi, da, db, v, gamma, out);
    return launch_status();
 }

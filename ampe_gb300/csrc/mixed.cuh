@@ -5,16 +5,22 @@
 
 namespace ampe {
 
+// FP32 copy of ThermoCoef for the mixed kernels
+struct CoefF {
+   float RT, iRT, dG[2], GB[2], L[2][4];
+};
+
+int build_coef_f(const ThermoCoef* tab, CoefF* tabf, int n, cudaStream_t s);
 int kks_mixed(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
-              const double* tfield, const double* phi, const double* conc,
-              const float* guess_l, const float* guess_s, const float* clr,
-              const float* csr, float* cl, float* cs, float* dF,
-              unsigned long long* counters, cudaStream_t s);
+              const CoefF* tabf, const double* tfield, const double* phi,
+              const double* conc, const float* guess_l, const float* guess_s,
+              const float* clr, const float* csr, float* cl, float* cs,
+              float* dF, unsigned long long* counters, cudaStream_t s);
 int rhs_mixed(const ampe_model_t& m, const Grid& g, const double* tfield,
               const double* phi, float* pf, const float* cl, const float* cs,
               const float* dF, double* phi_rhs, double* conc_rhs,
               cudaStream_t s);
-int jv_mixed(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
+int jv_mixed(const ampe_model_t& m, const Grid& g, const CoefF* tabf,
              const double* tfield, const float* pf, const float* cl,
              const float* cs, const float* dF, const double* v, double gamma,
              float* dphi, float* da, float* db, double* out, cudaStream_t s);

@@ -436,6 +436,7 @@ struct Stepper {
    double *phi_g, *c_g, *cl, *cs, *clr, *csr, *cl_nf, *cs_nf, *phi_lag, *tfield;
    double* dF;                 // interior driving force
    ThermoCoef* tab = nullptr;  // per-x (or single) thermodynamic table
+   CoefF* tabf = nullptr;      // its FP32 copy (mixed path)
    unsigned long long* counters;
    // 2N interior vectors
    double *yn, *ynm1, *ynew, *a, *y, *fy, *b, *d, *w, *tmp, *av, *fp;
@@ -520,7 +521,7 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    if (S.p.precision == 1) {
       {
          ProfScope ps(S, KT_KKS);
-         kks_mixed(S.m, S.g, S.tab, tf, S.phi_g, S.c_g,
+         kks_mixed(S.m, S.g, S.tab, S.tabf, tf, S.phi_g, S.c_g,
                    S.p.surrogate ? S.guess_l : nullptr,
                    S.p.surrogate ? S.guess_s : nullptr, S.clr32, S.csr32,
                    S.cl32, S.cs32, S.dF32, S.mcount, S.s);
@@ -633,7 +634,7 @@ static void matvec(Stepper& S, const double* y, const double* fy,
    if (S.p.precision == 1) {
       const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
       ProfScope ps(S, KT_JV);
-      jv_mixed(S.m, S.g, S.tab, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma,
+      jv_mixed(S.m, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma,
                S.dphi32, S.da32, S.db32, out, S.s);
       return;
    }
@@ -828,8 +829,10 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
       }
    }
    const int nt = m->temp_mode == AMPE_TEMP_GRADIENT ? m->n[0] : 1;
-   if (m->temp_mode != AMPE_TEMP_FIELD)
+   if (m->temp_mode != AMPE_TEMP_FIELD) {
       S->tab = (ThermoCoef*)dalloc<ThermoCoef>(S->pool, nt, &err);
+      if (p->precision == 1) S->tabf = (CoefF*)dalloc<CoefF>(S->pool, nt, &err);
+   }
    const int nl = p->precond == 2 ? std::max(1, p->mg_levels) : 1;
    if (!err && p->precond) {
       if (p->precision == 1) {
@@ -844,6 +847,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    // order with the non-blocking stepper stream: finish them first
    if (!err && cudaDeviceSynchronize() != cudaSuccess) err = AMPE_ERR_CUDA;
    if (!err && S->tab) err = build_thermo_table(*m, S->tab, nt, S->s);
+   if (!err && S->tabf) err = build_coef_f(S->tab, S->tabf, nt, S->s);
    if (!err && cudaStreamSynchronize(S->s) != cudaSuccess) err = AMPE_ERR_CUDA;
    if (err) {
       ampe_stepper_destroy(S);
