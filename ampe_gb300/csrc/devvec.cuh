@@ -41,7 +41,7 @@ __global__ void k_partial(long long n, F f, double* part)
    if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-__global__ void k_finish(const double* part, int np, double* out, int slot)
+static __global__ void k_finish(const double* part, int np, double* out, int slot)
 {
    __shared__ double sh[32];
    double acc = 0.0;

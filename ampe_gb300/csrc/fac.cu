@@ -5,6 +5,7 @@
 // Templated on the arithmetic type R so that the mixed-precision
 // preconditioner runs the same code in FP32.
 #include "common.cuh"
+#include "devvec.cuh"
 #include "fac.cuh"
 
 namespace ampe {
@@ -157,6 +158,50 @@ template int phase_set_c<double>(const ampe_model_t&, const Grid&,
 template int phase_set_c<float>(const ampe_model_t&, const Grid&,
                                 const double*, double, float*, cudaStream_t);
 
+// sum of squares of the interior of a ghosted field -> sqrt(sum / cells)
+__global__ void k_rms_finish(const double* part, int np, double inv_cells,
+                             double* out)
+{
+   __shared__ double sh[32];
+   double acc = 0.0;
+   for (int t = threadIdx.x; t < np; t += blockDim.x) acc += part[t];
+   acc = block_sum<NoOp>(acc, sh);
+   if (threadIdx.x == 0) *out = sqrt(acc * inv_cells);
+}
+
+long long residual_rms_scratch_doubles(const Grid& g)
+{
+   // residual field (ghost box), then kRedBlocks partial sums
+   return g.cells_ghost() + kRedBlocks;
+}
+
+// res = f - A u into scratch, then its interior RMS into *rms (device);
+// deterministic: fixed block count, fixed summation order.
+int residual_rms_into(const FacOp<double>& op, const Grid& g, const double* f,
+                      const double* u, double* scratch, double* rms,
+                      cudaStream_t s)
+{
+   double* res = scratch;
+   double* part = scratch + g.cells_ghost();
+   int rc = residual(op, g, f, u, res, s);
+   if (rc) return rc;
+   const long long n = g.cells();
+   long long nb = (n + kRedThreads - 1) / kRedThreads;
+   const int blocks = (int)(nb < kRedBlocks ? (nb < 1 ? 1 : nb) : kRedBlocks);
+   const Grid gg = g;
+   auto sq = [=] __device__(long long t) {
+      const int i = (int)(t % gg.n0);
+      const int j = (int)((t / gg.n0) % gg.n1);
+      const int k = (int)(t / ((long long)gg.n0 * gg.n1));
+      const double x = res[gg.c(i, j, k)];
+      return x * x;
+   };
+   k_partial<<<blocks, kRedThreads, 0, s>>>(n, sq, part);
+   g_launches++;
+   k_rms_finish<<<1, 1024, 0, s>>>(part, blocks, 1.0 / (double)n, rms);
+   return launch_status();
+}
+
 }  // namespace ampe
 
 using namespace ampe;
@@ -207,6 +252,28 @@ int ampe_efo_residual(const ampe_model_t* m, const double* dface0,
    FacOp<double> op = make_op(m, dface0, dface1, dface2, d_const, ccell,
                               c_const, mcell, m_const);
    return residual(op, make_grid(*m), rhs, u, res, (cudaStream_t)stream);
+}
+
+size_t ampe_efo_residual_rms_scratch_doubles(const ampe_model_t* m)
+{
+   if (check_model(m)) return 0;
+   return (size_t)residual_rms_scratch_doubles(make_grid(*m));
+}
+
+int ampe_efo_residual_rms(const ampe_model_t* m, const double* dface0,
+                          const double* dface1, const double* dface2,
+                          double d_const, const double* ccell, double c_const,
+                          const double* mcell, double m_const,
+                          const double* rhs, const double* u, double* scratch,
+                          double* rms, void* stream)
+{
+   if (check_model(m) || !rhs || !u || !scratch || !rms)
+      return AMPE_ERR_INVALID;
+   if (dface0 && (!dface1 || (m->dim == 3 && !dface2))) return AMPE_ERR_INVALID;
+   FacOp<double> op = make_op(m, dface0, dface1, dface2, d_const, ccell,
+                              c_const, mcell, m_const);
+   return residual_rms_into(op, make_grid(*m), rhs, u, scratch, rms,
+                            (cudaStream_t)stream);
 }
 
 int ampe_phase_fac_set_c(const ampe_model_t* m, const double* phi,

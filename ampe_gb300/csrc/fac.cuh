@@ -30,5 +30,9 @@ int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
                 double gamma, R* ccell, cudaStream_t s);
 
 int fill_ghosts(const Grid& g, double* f, cudaStream_t s);
+long long residual_rms_scratch_doubles(const Grid& g);
+int residual_rms_into(const FacOp<double>& op, const Grid& g, const double* f,
+                      const double* u, double* scratch, double* rms,
+                      cudaStream_t s);
 
 }  // namespace ampe

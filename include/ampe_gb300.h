@@ -243,6 +243,21 @@ int ampe_efo_residual(const ampe_model_t* m, const double* dface0,
                       const double* mcell, double m_const, const double* rhs,
                       const double* u, double* res, void* stream);
 
+/* Residual res = f - A u (EFO_COMPRES*) and its RMS over the interior cells
+ * (EllipticFACOps::computeResidualNorm, EllipticFACOps.cc:1760-1786, the
+ * norm the FAC loop tests after every cycle, samrai/FACPreconditioner.cc:
+ * 365-416).  `scratch` is caller-allocated device memory of
+ * ampe_efo_residual_rms_scratch_doubles(m) doubles (the residual field and
+ * the partial sums of a deterministic two-pass reduction); *rms is a device
+ * double written asynchronously on `stream`. */
+size_t ampe_efo_residual_rms_scratch_doubles(const ampe_model_t* m);
+int ampe_efo_residual_rms(const ampe_model_t* m, const double* dface0,
+                          const double* dface1, const double* dface2,
+                          double d_const, const double* ccell, double c_const,
+                          const double* mcell, double m_const,
+                          const double* rhs, const double* u, double* scratch,
+                          double* rms, void* stream);
+
 /* PhaseFACOps::setCOnPatchPrivate (PhaseFACOps.cc:101-183):
  * C = 1 + gamma M_phi w g''(phi) on interior cells (ghost width m->ng). */
 int ampe_phase_fac_set_c(const ampe_model_t* m, const double* phi,

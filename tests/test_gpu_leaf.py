@@ -270,6 +270,28 @@ def test_rbgs_and_residual(cuda, orc, name, m, vard):
     assert O.rel_l2(host(r_d)[sl], r_o[sl]) <= TOL
 
 
+@pytest.mark.parametrize("name,m", models()[:4])
+def test_residual_rms(cuda, orc, name, m):
+    import torch
+
+    rng = np.random.default_rng(8)
+    D = [np.ascontiguousarray(-rng.uniform(0.5, 1.5, s)) for s in m.face_shapes()]
+    Cc = rnd_ghosted(m, rng, 1.0, 2.0)
+    f = rnd_ghosted(m, rng, -1, 1)
+    u = rnd_ghosted(m, rng, -1, 1)
+    r_o = np.zeros(m.ghost_shape())
+    orc.orc_efo_residual(C.byref(m), *[O.ptr(a) for a in D], 0.0, O.ptr(Cc), 0.0, None, 1.3,
+                         O.ptr(f), O.ptr(u), O.ptr(r_o))
+    rms_o = orc.orc_rms_interior(C.byref(m), O.ptr(r_o))
+    nsc = cuda.lib.ampe_efo_residual_rms_scratch_doubles(C.byref(m))
+    assert nsc >= np.prod(m.ghost_shape())
+    scratch = torch.empty(nsc, dtype=torch.float64, device="cuda")
+    rms = torch.zeros(1, dtype=torch.float64, device="cuda")
+    assert cuda.lib.ampe_efo_residual_rms(C.byref(m), *[P(dev(a)) for a in D], 0.0, P(dev(Cc)), 0.0, None,
+                                          1.3, P(dev(f)), P(dev(u)), P(scratch), P(rms), None) == 0
+    assert abs(float(rms[0]) - rms_o) <= 1e-12 * rms_o
+
+
 def test_phase_set_c(cuda, orc):
     m = configs.calphad3d(8)
     rng = np.random.default_rng(7)
