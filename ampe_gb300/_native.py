@@ -42,6 +42,7 @@ _PROTOS = {
     "ampe_phase_fac_set_c": (I, [MP, P, D, P, P]),
     "ampe_efo_residual_rms_scratch_doubles": (C.c_size_t, [MP]),
     "ampe_efo_residual_rms": (I, [MP, P, P, P, D, P, D, P, D, P, P, P, P, P]),
+    "ampe_efo_residual_rms_noalloc": (I, [MP, P, P, P, D, P, D, P, D, P, P, P, P]),
     "ampe_stepper_create": (I, [MP, SP, C.POINTER(P)]),
     "ampe_stepper_destroy": (I, [P]),
     "ampe_stepper_set_state": (I, [P, P, P, P, P, P, I]),

@@ -10,6 +10,8 @@ AMPE_ERR_INVALID = -1
 AMPE_ERR_CUDA = -2
 AMPE_ERR_NOT_CONVERGED = -3
 AMPE_ERR_NO_DEVICE = -4
+AMPE_ERR_TOO_LARGE = -5
+NOALLOC_SCRATCH_DOUBLES = 1 << 19
 
 FLUX_SIMPLE, FLUX_ISOTROPIC, FLUX_ANISOTROPIC = 0, 1, 2
 THERMO_DILUTE, THERMO_CALPHAD = 0, 1

@@ -30,6 +30,8 @@
 #ifndef AMPE_GB300_H
 #define AMPE_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -39,6 +41,7 @@ extern "C" {
 #define AMPE_ERR_CUDA (-2)
 #define AMPE_ERR_NOT_CONVERGED (-3)
 #define AMPE_ERR_NO_DEVICE (-4)
+#define AMPE_ERR_TOO_LARGE (-5) /* level too large for a fixed-size buffer */
 
 /* phase flux discretisations (PhaseFluxStrategyFactory.h:12-40) */
 #define AMPE_FLUX_SIMPLE 0      /* gradient_flux, quatrhs.m4 */
@@ -257,6 +260,30 @@ int ampe_efo_residual_rms(const ampe_model_t* m, const double* dface0,
                           const double* mcell, double m_const,
                           const double* rhs, const double* u, double* scratch,
                           double* rms, void* stream);
+
+/* Same result as ampe_efo_residual_rms, without any device allocation and
+ * without a scratch argument.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory themselves -- a host framework
+ * that owns all GPU memory through its own pool and gives this library a
+ * fixed budget, or code that must not call cudaMalloc/cudaFree because those
+ * calls synchronise the device (a latency-critical solver loop).  Its
+ * working memory is one library-owned buffer of AMPE_NOALLOC_SCRATCH_DOUBLES
+ * doubles (4 MiB) that every GPU which loads the library keeps until the
+ * process exits; levels whose ghost box plus the reduction partials do not
+ * fit (ghost box above ~523,000 cells, e.g. 80^3) are refused with
+ * AMPE_ERR_TOO_LARGE before any launch.  The first call on a device looks up
+ * the buffer's device address (cudaGetSymbolAddress), so make that first call
+ * outside any CUDA stream capture.  All calls share the one buffer: calls
+ * whose work overlaps on the GPU (different streams, or different host
+ * threads) race and give wrong norms -- serialise them.  No part of the
+ * buffer has to start at zero: each call overwrites what it reads. */
+#define AMPE_NOALLOC_SCRATCH_DOUBLES (1 << 19)
+int ampe_efo_residual_rms_noalloc(const ampe_model_t* m, const double* dface0,
+                                  const double* dface1, const double* dface2,
+                                  double d_const, const double* ccell,
+                                  double c_const, const double* mcell,
+                                  double m_const, const double* rhs,
+                                  const double* u, double* rms, void* stream);
 
 /* PhaseFACOps::setCOnPatchPrivate (PhaseFACOps.cc:101-183):
  * C = 1 + gamma M_phi w g''(phi) on interior cells (ghost width m->ng). */
