@@ -55,6 +55,18 @@ _PROTOS = {
     "ampe_stepper_stream": (P, [P]),
     "ampe_stepper_profile": (I, [P, I]),
     "ampe_stepper_kernel_time": (I, [P, I, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
+    "ampe_stepper_attach_surrogate": (I, [P, P]),
+    "ampe_mlp_create": (I, [MP, I, C.c_uint, C.POINTER(P)]),
+    "ampe_mlp_destroy": (I, [P]),
+    "ampe_mlp_nparams": (I, [P]),
+    "ampe_mlp_generate": (I, [P, C.c_longlong, C.c_uint, D, D, D, D, C.POINTER(C.c_longlong)]),
+    "ampe_mlp_train": (I, [P, I, I, C.c_float, C.POINTER(C.c_float)]),
+    "ampe_mlp_grad": (I, [P, P, P, I, C.POINTER(C.c_float)]),
+    "ampe_mlp_get": (I, [P, P, P, I]),
+    "ampe_mlp_set": (I, [P, P, I]),
+    "ampe_mlp_set_normalization": (I, [P, D, D]),
+    "ampe_mlp_infer": (I, [P, MP, P, P, P, P, P, I, P]),
+    "ampe_mlp_status": (I, [P]),
 }
 
 for _name, (_res, _args) in _PROTOS.items():

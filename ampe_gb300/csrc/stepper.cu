@@ -27,6 +27,7 @@
 #include "fac.cuh"
 #include "fused.cuh"
 #include "mixed.cuh"
+#include "mlp.cuh"
 
 namespace ampe {
 
@@ -446,6 +447,7 @@ struct Stepper {
    float *dF32 = nullptr, *pf32 = nullptr, *dphi32 = nullptr, *da32 = nullptr,
          *db32 = nullptr;
    float *guess_l = nullptr, *guess_s = nullptr;  // surrogate initial guess
+   Mlp* mlp = nullptr;                            // attached surrogate
    unsigned long long* mcount = nullptr;          // mixed KKS counters [5]
    // preconditioner (FP64 or FP32)
    DevFac<double> facp64, facc64;
@@ -465,7 +467,7 @@ struct Stepper {
 };
 
 // kernel classes timed in profiling mode
-enum { KT_KKS = 0, KT_RHS = 1, KT_JV = 2, KT_NKINDS = 3 };
+enum { KT_KKS = 0, KT_RHS = 1, KT_JV = 2, KT_MLP = 3, KT_NKINDS = 4 };
 
 static cudaEvent_t prof_event(Stepper& S)
 {
@@ -519,11 +521,15 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    to_ghosted<double>(S.g, y + S.N, v ? v + S.N : nullptr, sig, S.c_g, S.s);
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
    if (S.p.precision == 1) {
+      if (S.p.surrogate && S.mlp) {
+         ProfScope ps(S, KT_MLP);
+         S.mlp->infer(S.g, S.phi_g, S.c_g, tf, S.guess_l, S.guess_s, true, S.s);
+      }
       {
          ProfScope ps(S, KT_KKS);
          kks_mixed(S.m, S.g, S.tab, S.tabf, tf, S.phi_g, S.c_g,
-                   S.p.surrogate ? S.guess_l : nullptr,
-                   S.p.surrogate ? S.guess_s : nullptr, S.clr32, S.csr32,
+                   (S.p.surrogate && S.mlp) ? S.guess_l : nullptr,
+                   (S.p.surrogate && S.mlp) ? S.guess_s : nullptr, S.clr32, S.csr32,
                    S.cl32, S.cs32, S.dF32, S.mcount, S.s);
       }
       {
@@ -1010,6 +1016,20 @@ long long ampe_stepper_kernel_launches(void* h)
 {
    (void)h;
    return g_launches;
+}
+
+int ampe_stepper_attach_surrogate(void* h, void* mlp)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || !mlp || !S->guess_l) return AMPE_ERR_INVALID;
+   Mlp* M = (Mlp*)mlp;
+   // the network sees the stepper's temperature field
+   M->m.temp_mode = S->m.temp_mode;
+   M->m.T0 = S->m.T0;
+   M->m.gradT = S->m.gradT;
+   for (int d = 0; d < 3; d++) M->m.dx[d] = S->m.dx[d];
+   S->mlp = M;
+   return AMPE_OK;
 }
 
 void* ampe_stepper_stream(void* h)

@@ -291,6 +291,41 @@ int ampe_phase_fac_set_c(const ampe_model_t* m, const double* phi,
                          double gamma, double* ccell, void* stream);
 
 /* ---------------------------------------------------------------------
+ * Surrogate MLP for the KKS initial guess: (phi, c, T) -> (cL, cS),
+ * 3 -> 64 -> 64 -> 64 -> 2, SiLU, BF16 weights, FP32 accumulation.  No
+ * counterpart in the reference (its Newton starts from the previous step's
+ * cL, cS, QuatModel.cc:5218-5231).  Trained on samples labelled by the FP64
+ * KKS Newton of the model given at create; inference on the tensor cores.
+ * ------------------------------------------------------------------- */
+int ampe_mlp_create(const ampe_model_t* m, int batch, unsigned seed,
+                    void** handle);
+int ampe_mlp_destroy(void* handle);
+int ampe_mlp_nparams(void* handle);
+/* n samples phi~U[0,1], c~U[c_lo,c_hi], T~U[t_lo,t_hi], labelled by the
+ * FP64 Newton from (c, c); sets the T normalisation to [t_lo, t_hi]. */
+int ampe_mlp_generate(void* handle, long long n, unsigned seed, double t_lo,
+                      double t_hi, double c_lo, double c_hi,
+                      long long* newton_failures);
+/* Adam on minibatches of the generated samples (loss: 1/2 mean squared
+ * error of the two logits); repacks the BF16 tensor-core operands. */
+int ampe_mlp_train(void* handle, int steps, int batch, float lr,
+                   float* final_loss);
+/* gradient of the loss on one batch (x: [batch][4] encoded inputs, target:
+ * [batch][2] logits; device pointers) into the handle's gradient buffer. */
+int ampe_mlp_grad(void* handle, const float* x, const float* target,
+                  int batch, float* loss);
+int ampe_mlp_get(void* handle, float* params, float* grads, int host);
+int ampe_mlp_set(void* handle, const float* params, int host);
+int ampe_mlp_set_normalization(void* handle, double t_lo, double t_hi);
+/* guesses for the interior cells of `grid` (phi, conc ghosted FP64);
+ * tensor_cores=1: tcgen05 kernel, 0: CUDA-core reference kernel. */
+int ampe_mlp_infer(void* handle, const ampe_model_t* grid, const double* phi,
+                   const double* conc, const double* temp, float* guess_l,
+                   float* guess_s, int tensor_cores, void* stream);
+/* AMPE_OK, or AMPE_ERR_NOT_CONVERGED if a tensor-core wait timed out. */
+int ampe_mlp_status(void* handle);
+
+/* ---------------------------------------------------------------------
  * Implicit stepper (CVODEAbstractFunctions + CVODESolver role,
  * samrai/CVODEAbstractFunctions.h:61-90, QuatIntegrator.cc:2096-3906).
  * Allocates all its device workspace here, never in ampe_stepper_advance.
@@ -322,13 +357,18 @@ int ampe_stepper_jv(void* handle, const double* v, double gamma, double* out,
  * host memory and hand them in every step (a SAMRAI patch adapter). */
 int ampe_stepper_load_y(void* handle, const double* phi, const double* conc,
                         int host);
+/* Use a trained surrogate (ampe_mlp_*) for the KKS initial guesses of the
+ * mixed path (params surrogate=1): each cell starts from the network's
+ * guess and falls back to the previous step's values when 3 FP32 Newton
+ * iterations do not converge.  The handle must outlive the stepper. */
+int ampe_stepper_attach_surrogate(void* handle, void* mlp);
 /* Launches of library kernels in this process (launch accounting). */
 long long ampe_stepper_kernel_launches(void* handle);
 /* The stepper's CUDA stream (cudaStream_t), for events around advance. */
 void* ampe_stepper_stream(void* handle);
 /* Per-kernel CUDA-event timing on the stepper stream.  kind: 0 KKS Newton,
- * 1 fused RHS, 2 analytic Jacobian-vector product (mixed path).  Enabling
- * resets the totals. */
+ * 1 fused RHS, 2 analytic Jacobian-vector product (mixed path), 3 surrogate
+ * inference.  Enabling resets the totals. */
 int ampe_stepper_profile(void* handle, int enable);
 int ampe_stepper_kernel_time(void* handle, int kind, double* total_ms,
                              long long* launches);
