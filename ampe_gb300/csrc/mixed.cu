@@ -137,7 +137,7 @@ __device__ __forceinline__ CoefF coef_f_at(const ampe_model_t& m,
    return to_f(thermo_coef(m, temperature_at(m, g, tfield, i, j, k)));
 }
 
-__global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
+__global__ void k_kks_mixed(ampe_model_t m, MixParams mp, Grid g, const ThermoCoef* tab,
                             const CoefF* tabf, const double* tfield,
                             const double* phi, const double* conc,
                             const float* guess_l, const float* guess_s,
@@ -147,7 +147,7 @@ __global__ void k_kks_mixed(ampe_model_t m, Grid g, const ThermoCoef* tab,
    // counters: [0] FP32 iterations, [1] failed cells, [2] FP64-polished
    //           cells, [3] surrogate fallbacks, [4] FP64 iterations
    unsigned long long it32 = 0, fails = 0, n64 = 0, nfb = 0, it64 = 0;
-   const float ivm = (float)m.inv_molar_volume[1];
+   const float ivm = mp.ivm;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       const int i = (int)(t % g.n0);
@@ -234,41 +234,86 @@ int build_coef_f(const ThermoCoef* tab, CoefF* tabf, int n, cudaStream_t s)
    return launch_status();
 }
 
-int kks_mixed(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
-              const CoefF* tabf, const double* tfield, const double* phi,
-              const double* conc, const float* guess_l, const float* guess_s,
+int kks_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+              const ThermoCoef* tab, const CoefF* tabf, const double* tfield,
+              const double* phi, const double* conc, const float* guess_l, const float* guess_s,
               const float* clr, const float* csr, float* cl, float* cs,
               float* dF, unsigned long long* counters, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > 152 * 16) b = 152 * 16;
-   k_kks_mixed<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tabf, tfield, phi, conc,
+   k_kks_mixed<<<(unsigned)b, 256, 0, s>>>(m, mp, g, tab, tabf, tfield, phi, conc,
                                            guess_l, guess_s, clr, csr, cl, cs,
                                            dF, counters);
    return launch_status();
 }
 
+MixParams make_mix_params(const ampe_model_t& m)
+{
+   MixParams p;
+   const double eps2 = m.epsilon_phi * m.epsilon_phi;
+   const bool iso = m.flux_type == AMPE_FLUX_ISOTROPIC && m.dim == 2;
+   for (int d = 0; d < 3; d++) {
+      const double dx = d < m.dim ? m.dx[d] : 1.0;
+      p.dxi[d] = d < m.dim ? (float)(1.0 / dx) : 0.f;
+      p.flux_dinv[d] = (float)((iso ? 1.0 / 12.0 : 1.0) * eps2 / dx);
+   }
+   p.w = (float)m.phase_well_scale;
+   p.Mphi = (float)m.phase_mobility;
+   p.Mc = (float)m.conc_mobility;
+   p.Dl = (float)m.D_liquid;
+   p.Ds = (float)m.D_solid;
+   p.qlR = (float)(m.Q_liquid / kGasR);
+   p.qsR = (float)(m.Q_solid / kGasR);
+   p.ivm = (float)m.inv_molar_volume[1];
+   p.tdep = (m.Q_liquid != 0.0 || m.Q_solid != 0.0) ? 1 : 0;
+   p.iso = iso ? 1 : 0;
+   return p;
+}
+
 // ---------------------------------------------------------------------------
-// FP32 fused right-hand side (simple / isotropic phase flux)
+// FP32 stencil helpers (DIM known at compile time)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float face_flux_lin(const ampe_model_t& m, int d,
+template <int DIM>
+__device__ __forceinline__ float face_flux_lin(const MixParams& mp, int d,
                                                const float* pf, const Grid& g,
                                                int i, int j, int k)
 {
    // linear phase flux on face d whose upper cell is (i,j,k)
-   const float eps2 = (float)(m.epsilon_phi * m.epsilon_phi);
-   if (m.flux_type == AMPE_FLUX_SIMPLE || g.dim == 3) {
-      const float dinv = eps2 / (float)m.dx[d];
+   if (DIM == 3 || !mp.iso) {
       const int ei = d == 0, ej = d == 1, ek = d == 2;
-      return (pf[g.c(i, j, k)] - pf[g.c(i - ei, j - ej, k - ek)]) * dinv;
+      return (pf[g.c(i, j, k)] - pf[g.c(i - ei, j - ej, k - ek)]) * mp.flux_dinv[d];
    }
-   const float dinv = (1.f / 12.f) * eps2 / (float)m.dx[d];
    auto P = [&](int a, int b) { return pf[g.c(a, b, 0)]; };
+   const float dinv = mp.flux_dinv[d];
    if (d == 0)
       return dinv * ((P(i, j - 1) - P(i - 1, j - 1)) + (P(i, j) - P(i - 1, j)) * 10.f +
                      (P(i, j + 1) - P(i - 1, j + 1)));
    return dinv * ((P(i - 1, j) - P(i - 1, j - 1)) + (P(i, j) - P(i, j - 1)) * 10.f +
                   (P(i + 1, j) - P(i + 1, j - 1)));
+}
+
+// face weights (1-h) D_L, h D_S from the phases of the two cells
+template <int DIM>
+__device__ __forceinline__ void face_diff(const ampe_model_t& m,
+                                          const MixParams& mp, const Grid& g,
+                                          const double* tfield, const float* pf,
+                                          long long lo, long long up, int a0,
+                                          int a1, int a2, int ei, int ej,
+                                          int ek, float& DL, float& DS)
+{
+   const float vphi = average_func(pf[lo], pf[up], m.avg_type);
+   const float hphi = interp_func(vphi, m.diff_interp);
+   float dlq = mp.Dl, dsq = mp.Ds;
+   if (mp.tdep) {
+      const float invT =
+          2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
+                        temperature_at(m, g, tfield, a0, a1, a2));
+      dlq = mp.Dl * expf(-mp.qlR * invT);
+      dsq = mp.Ds * expf(-mp.qsR * invT);
+   }
+   DL = (1.f - hphi) * dlq;
+   DS = hphi * dsq;
 }
 
 __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
@@ -278,17 +323,12 @@ __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
       pf[t] = (float)phi[t];
 }
 
-__global__ void k_rhs_mixed(ampe_model_t m, Grid g, const double* tfield,
-                            const float* pf, const float* cl, const float* cs,
-                            const float* dF, double* phi_rhs, double* conc_rhs)
+template <int DIM>
+__global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
+                            const double* tfield, const float* pf,
+                            const float* cl, const float* cs, const float* dF,
+                            double* phi_rhs, double* conc_rhs)
 {
-   const float dxi[3] = {(float)(1.0 / m.dx[0]), (float)(1.0 / m.dx[1]),
-                         g.dim == 3 ? (float)(1.0 / m.dx[2]) : 0.f};
-   const float qlR = (float)(m.Q_liquid / kGasR), qsR = (float)(m.Q_solid / kGasR);
-   const bool tdep = (m.Q_liquid != 0.0 || m.Q_solid != 0.0);
-   const float Dl0 = (float)m.D_liquid, Ds0 = (float)m.D_solid;
-   const float w = (float)m.phase_well_scale, Mphi = (float)m.phase_mobility;
-   const float Mc = (float)m.conc_mobility;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       const int i = (int)(t % g.n0);
@@ -296,43 +336,35 @@ __global__ void k_rhs_mixed(ampe_model_t m, Grid g, const double* tfield,
       const int k = (int)(t / ((long long)g.n0 * g.n1));
       const long long c = g.c(i, j, k);
       float diff = 0.f, div = 0.f;
-      for (int d = 0; d < g.dim; d++) {
+#pragma unroll
+      for (int d = 0; d < DIM; d++) {
          const int ei = d == 0, ej = d == 1, ek = d == 2;
-         const float fm = face_flux_lin(m, d, pf, g, i, j, k);
-         const float fp = face_flux_lin(m, d, pf, g, i + ei, j + ej, k + ek);
-         diff += (fp - fm) * dxi[d];
-         float fl[2];
-         for (int side = 0; side < 2; side++) {
-            const int a0 = i + side * ei, a1 = j + side * ej, a2 = k + side * ek;
-            const long long up = g.c(a0, a1, a2);
-            const long long lo = g.c(a0 - ei, a1 - ej, a2 - ek);
-            const float vphi = average_func(pf[lo], pf[up], m.avg_type);
-            const float hphi = interp_func(vphi, m.diff_interp);
-            float dlq = Dl0, dsq = Ds0;
-            if (tdep) {
-               const float invT =
-                   2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
-                                 temperature_at(m, g, tfield, a0, a1, a2));
-               dlq = Dl0 * expf(-qlR * invT);
-               dsq = Ds0 * expf(-qsR * invT);
-            }
-            fl[side] = dxi[d] * ((1.f - hphi) * dlq * (cl[up] - cl[lo]) +
-                                 hphi * dsq * (cs[up] - cs[lo]));
-         }
-         div += dxi[d] * (fl[1] - fl[0]);
+         const float fm = face_flux_lin<DIM>(mp, d, pf, g, i, j, k);
+         const float fp = face_flux_lin<DIM>(mp, d, pf, g, i + ei, j + ej, k + ek);
+         diff += (fp - fm) * mp.dxi[d];
+         const long long up = g.c(i + ei, j + ej, k + ek);
+         float DLm, DSm, DLp, DSp;
+         face_diff<DIM>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), c, i, j, k, ei,
+                        ej, ek, DLm, DSm);
+         face_diff<DIM>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek,
+                        DLp, DSp);
+         const long long lo = g.c(i - ei, j - ej, k - ek);
+         const float flm = mp.dxi[d] * (DLm * (cl[c] - cl[lo]) + DSm * (cs[c] - cs[lo]));
+         const float flp = mp.dxi[d] * (DLp * (cl[up] - cl[c]) + DSp * (cs[up] - cs[c]));
+         div += mp.dxi[d] * (flp - flm);
       }
       const float p = pf[c];
-      float r = diff - w * deriv_well_func(p, m.well_type);
+      float r = diff - mp.w * deriv_well_func(p, m.well_type);
       r += deriv_interp_func(p, m.energy_interp) * dF[t];
-      phi_rhs[t] = (double)(r * Mphi);
-      conc_rhs[t] = (double)(Mc * div);
+      phi_rhs[t] = (double)(r * mp.Mphi);
+      conc_rhs[t] = (double)(mp.Mc * div);
    }
 }
 
-int rhs_mixed(const ampe_model_t& m, const Grid& g, const double* tfield,
-              const double* phi, float* pf, const float* cl, const float* cs,
-              const float* dF, double* phi_rhs, double* conc_rhs,
-              cudaStream_t s)
+int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+              const double* tfield, const double* phi, float* pf,
+              const float* cl, const float* cs, const float* dF,
+              double* phi_rhs, double* conc_rhs, cudaStream_t s)
 {
    long long b = (g.cells_ghost() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
@@ -340,8 +372,12 @@ int rhs_mixed(const ampe_model_t& m, const Grid& g, const double* tfield,
    launch_status();
    b = (g.cells() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
-   k_rhs_mixed<<<(unsigned)b, 256, 0, s>>>(m, g, tfield, pf, cl, cs, dF,
-                                           phi_rhs, conc_rhs);
+   if (g.dim == 3)
+      k_rhs_mixed<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, phi_rhs,
+                                                 conc_rhs);
+   else
+      k_rhs_mixed<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, phi_rhs,
+                                                 conc_rhs);
    return launch_status();
 }
 
@@ -404,21 +440,14 @@ __device__ __forceinline__ float second_deriv_interp_f(float phi, char type)
 }
 
 // out = v - gamma J v
-__global__ void k_jv_stencil(ampe_model_t m, Grid g, const CoefF* tabf,
-                             const double* tfield, const float* pf,
-                             const float* cl, const float* cs, const float* dF,
-                             const float* dphi, const float* da,
-                             const float* db, const double* v, double gamma,
-                             double* out)
+template <int DIM>
+__global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
+                             const CoefF* tabf, const double* tfield,
+                             const float* pf, const float* cl, const float* cs,
+                             const float* dF, const float* dphi,
+                             const float* da, const float* db, const double* v,
+                             double gamma, double* out)
 {
-   const float dxi[3] = {(float)(1.0 / m.dx[0]), (float)(1.0 / m.dx[1]),
-                         g.dim == 3 ? (float)(1.0 / m.dx[2]) : 0.f};
-   const float qlR = (float)(m.Q_liquid / kGasR), qsR = (float)(m.Q_solid / kGasR);
-   const bool tdep = (m.Q_liquid != 0.0 || m.Q_solid != 0.0);
-   const float Dl0 = (float)m.D_liquid, Ds0 = (float)m.D_solid;
-   const float w = (float)m.phase_well_scale, Mphi = (float)m.phase_mobility;
-   const float Mc = (float)m.conc_mobility;
-   const float ivm = (float)m.inv_molar_volume[1];
    const long long N = g.cells();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
         t += (long long)gridDim.x * blockDim.x) {
@@ -427,57 +456,52 @@ __global__ void k_jv_stencil(ampe_model_t m, Grid g, const CoefF* tabf,
       const int k = (int)(t / ((long long)g.n0 * g.n1));
       const long long c = g.c(i, j, k);
       float diff = 0.f, div = 0.f;
-      for (int d = 0; d < g.dim; d++) {
+#pragma unroll
+      for (int d = 0; d < DIM; d++) {
          const int ei = d == 0, ej = d == 1, ek = d == 2;
-         const float fm = face_flux_lin(m, d, dphi, g, i, j, k);
-         const float fp = face_flux_lin(m, d, dphi, g, i + ei, j + ej, k + ek);
-         diff += (fp - fm) * dxi[d];
-         float fl[2];
-         for (int side = 0; side < 2; side++) {
-            const int a0 = i + side * ei, a1 = j + side * ej, a2 = k + side * ek;
-            const long long up = g.c(a0, a1, a2);
-            const long long lo = g.c(a0 - ei, a1 - ej, a2 - ek);
-            const float vphi = average_func(pf[lo], pf[up], m.avg_type);
-            const float hphi = interp_func(vphi, m.diff_interp);
-            float dlq = Dl0, dsq = Ds0;
-            if (tdep) {
-               const float invT =
-                   2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
-                                 temperature_at(m, g, tfield, a0, a1, a2));
-               dlq = Dl0 * expf(-qlR * invT);
-               dsq = Ds0 * expf(-qsR * invT);
-            }
-            fl[side] = dxi[d] * ((1.f - hphi) * dlq * (da[up] - da[lo]) +
-                                 hphi * dsq * (db[up] - db[lo]));
-         }
-         div += dxi[d] * (fl[1] - fl[0]);
+         const float fm = face_flux_lin<DIM>(mp, d, dphi, g, i, j, k);
+         const float fp = face_flux_lin<DIM>(mp, d, dphi, g, i + ei, j + ej, k + ek);
+         diff += (fp - fm) * mp.dxi[d];
+         const long long up = g.c(i + ei, j + ej, k + ek);
+         const long long lo = g.c(i - ei, j - ej, k - ek);
+         float DLm, DSm, DLp, DSp;
+         face_diff<DIM>(m, mp, g, tfield, pf, lo, c, i, j, k, ei, ej, ek, DLm, DSm);
+         face_diff<DIM>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek, DLp,
+                        DSp);
+         const float flm = mp.dxi[d] * (DLm * (da[c] - da[lo]) + DSm * (db[c] - db[lo]));
+         const float flp = mp.dxi[d] * (DLp * (da[up] - da[c]) + DSp * (db[up] - db[c]));
+         div += mp.dxi[d] * (flp - flm);
       }
       const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
       const float p = pf[c], a = cl[c], b = cs[c], vp = dphi[c];
       // d(dF)/db = -f_S''(b) (a - b), d(dF)/da = muL - muS = 0
       const float fS2 = tf.RT / (b * (1.f - b)) + dxi_f(tf, b, 1);
-      const float ddF = -fS2 * (a - b) * ivm * db[c];
-      const float jp = Mphi * (diff - w * second_deriv_well_func(p, m.well_type) * vp +
-                               second_deriv_interp_f(p, m.energy_interp) * dF[t] * vp +
-                               deriv_interp_func(p, m.energy_interp) * ddF);
-      const float jc = Mc * div;
-      out[t] = v[t] - gamma * (double)jp;
-      out[t + N] = v[t + N] - gamma * (double)jc;
+      const float ddF = -fS2 * (a - b) * mp.ivm * db[c];
+      const float jp = mp.Mphi * (diff - mp.w * second_deriv_well_func(p, m.well_type) * vp +
+                                  second_deriv_interp_f(p, m.energy_interp) * dF[t] * vp +
+                                  deriv_interp_func(p, m.energy_interp) * ddF);
+      const float jc = mp.Mc * div;
+      out[t] = v[t] - (double)((float)gamma * jp);
+      out[t + N] = v[t + N] - (double)((float)gamma * jc);
    }
 }
 
-int jv_mixed(const ampe_model_t& m, const Grid& g, const CoefF* tabf,
-             const double* tfield, const float* pf, const float* cl,
-             const float* cs, const float* dF, const double* v, double gamma,
-             float* dphi, float* da, float* db, double* out, cudaStream_t s)
+int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+             const CoefF* tabf, const double* tfield, const float* pf,
+             const float* cl, const float* cs, const float* dF, const double* v,
+             double gamma, float* dphi, float* da, float* db, double* out,
+             cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
-   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v,
-                                          dphi, da, db);
+   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da, db);
    launch_status();
-   k_jv_stencil<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, dF,
-                                            dphi, da, db, v, gamma, out);
+   if (g.dim == 3)
+      k_jv_stencil<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
+                                                  da, db, v, gamma, out);
+   else
+      k_jv_stencil<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
+                                                  da, db, v, gamma, out);
    return launch_status();
 }
 

@@ -438,6 +438,7 @@ struct Stepper {
    double* dF;                 // interior driving force
    ThermoCoef* tab = nullptr;  // per-x (or single) thermodynamic table
    CoefF* tabf = nullptr;      // its FP32 copy (mixed path)
+   MixParams mp;               // FP32 constants of the mixed kernels
    unsigned long long* counters;
    // 2N interior vectors
    double *yn, *ynm1, *ynew, *a, *y, *fy, *b, *d, *w, *tmp, *av, *fp;
@@ -527,14 +528,14 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
       }
       {
          ProfScope ps(S, KT_KKS);
-         kks_mixed(S.m, S.g, S.tab, S.tabf, tf, S.phi_g, S.c_g,
+         kks_mixed(S.m, S.mp, S.g, S.tab, S.tabf, tf, S.phi_g, S.c_g,
                    (S.p.surrogate && S.mlp) ? S.guess_l : nullptr,
                    (S.p.surrogate && S.mlp) ? S.guess_s : nullptr, S.clr32, S.csr32,
                    S.cl32, S.cs32, S.dF32, S.mcount, S.s);
       }
       {
          ProfScope ps(S, KT_RHS);
-         rhs_mixed(S.m, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32, out,
+         rhs_mixed(S.m, S.mp, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32, out,
                    out + S.N, S.s);
       }
       S.st.rhs_evals++;
@@ -640,7 +641,7 @@ static void matvec(Stepper& S, const double* y, const double* fy,
    if (S.p.precision == 1) {
       const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
       ProfScope ps(S, KT_JV);
-      jv_mixed(S.m, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma,
+      jv_mixed(S.m, S.mp, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma,
                S.dphi32, S.da32, S.db32, out, S.s);
       return;
    }
@@ -809,6 +810,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    S->N = S->g.cells();
    S->NG = S->g.cells_ghost();
    S->N2 = 2 * S->N;
+   S->mp = make_mix_params(*m);
    std::memset(&S->st, 0, sizeof(S->st));
    int err = AMPE_OK;
    if (cudaStreamCreateWithFlags(&S->s, cudaStreamNonBlocking) != cudaSuccess)

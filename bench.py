@@ -39,6 +39,19 @@ RHS_BYTES_PER_CELL = 56  # read phi, phi_lag, cL, cS, dF; write phi', c'
 # mixed path KKS kernel: read phi, c (FP64), cL_ref, cS_ref (FP32); write cL,
 # cS, dF (FP32)
 KKS_MIXED_BYTES_PER_CELL = 36
+# mixed RHS: read phi (FP32 copy), cL, cS, dF (FP32), write phi', c' (FP64)
+RHS_MIXED_BYTES_PER_CELL = 36
+# analytic Jv: point pass 44 B (v FP64, phi, cL, cS; write dphi, dcL, dcS
+# FP32) + stencil pass 64 B (dphi, dcL, dcS, phi, cL, cS, dF, v; write out)
+JV_BYTES_PER_CELL = 108
+# MLP inference: 2 (3*64 + 64*64 + 64*64 + 64*2) multiply-adds per cell
+MLP_FLOPS_PER_CELL = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
+KERNEL_NAMES = {
+    False: {"kks_newton": "k_kks_mixed", "rhs_fused": "k_rhs_mixed",
+            "jv_analytic": "k_jv_point+k_jv_stencil"},
+    True: {"kks_newton": "k_kks_interior", "rhs_fused": "k_rhs_fused<0>",
+           "jv_analytic": "-"},
+}
 ATOL = 1.0e-6
 
 
@@ -49,11 +62,16 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
-    ap.add_argument("--path", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--path", default="mixed+surrogate",
+                    choices=["fp64", "mixed", "mixed+surrogate"])
+    ap.add_argument("--surrogate-samples", type=int, default=1 << 22)
+    ap.add_argument("--surrogate-steps", type=int, default=2000)
     ap.add_argument("--precond", type=int, default=2)
     ap.add_argument("--cpu-n", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--only-head", action="store_true",
+                    help="time only the headline path (no FP64 / mixed comparison)")
     return ap.parse_args()
 
 
@@ -154,7 +172,8 @@ def step_params(args, path):
     from ampe_gb300 import configs
 
     return configs.step_params(dt=0.1, precond=args.precond, mg_levels=5, atol=ATOL,
-                               precision=1 if path == "mixed" else 0)
+                               precision=0 if path == "fp64" else 1,
+                               surrogate=1 if path == "mixed+surrogate" else 0)
 
 
 def cpu_baseline(args, threads=None):
@@ -212,7 +231,36 @@ def run_reference(args):
     print(json.dumps(out))
 
 
-def timed_path(args, m, phi, c, path, local):
+def train_surrogate(args, m, local):
+    """Train the KKS-guess MLP for this workload's thermodynamics on 2^22
+    samples labelled by the FP64 Newton (outside the timed region)."""
+    import torch
+
+    from ampe_gb300 import _native
+
+    L = _native.lib
+    h = C.c_void_p()
+    _native.check(L.ampe_mlp_create(C.byref(m), 4096, 11, C.byref(h)), "ampe_mlp_create")
+    t_lo = m.T0
+    t_hi = m.T0 + m.gradT * m.n[0] * m.dx[0]
+    fails = C.c_longlong()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _native.check(L.ampe_mlp_generate(h, args.surrogate_samples, 99, t_lo, t_hi, 0.01, 0.99,
+                                      C.byref(fails)), "ampe_mlp_generate")
+    t1 = time.perf_counter()
+    loss = C.c_float()
+    _native.check(L.ampe_mlp_train(h, args.surrogate_steps, 4096, 3e-3, C.byref(loss)),
+                  "ampe_mlp_train")
+    t2 = time.perf_counter()
+    info = {"samples": args.surrogate_samples, "label_newton_failures": fails.value,
+            "label_s": t1 - t0, "train_steps": args.surrogate_steps, "batch": 4096,
+            "train_s": t2 - t1, "final_loss": loss.value,
+            "arch": "3-64-64-64-2 SiLU, BF16 weights, FP32 accumulate; inference tcgen05"}
+    return h, info
+
+
+def timed_path(args, m, phi, c, path, local, mlp=None):
     """Warm up, then time args.steps accepted steps of one path on the device.
     Returns (result dict, final host state, stepper)."""
     import torch
@@ -223,6 +271,8 @@ def timed_path(args, m, phi, c, path, local):
     L = _native.lib
     N = m.cells()
     g = ImplicitStepper(m, step_params(args, path))
+    if path == "mixed+surrogate":
+        _native.check(L.ampe_stepper_attach_surrogate(g._h, mlp), "attach_surrogate")
     g.set_state(phi, c)
     g.advance(args.warmup)
     stream = torch.cuda.ExternalStream(L.ampe_stepper_stream(g._h))
@@ -242,7 +292,8 @@ def timed_path(args, m, phi, c, path, local):
     ms = e0.elapsed_time(e1)
     launches = L.ampe_stepper_kernel_launches(g._h) - launches0
     kt = {}
-    for kind, name in ((0, "kks_newton"), (1, "rhs_fused"), (2, "jv_analytic")):
+    for kind, name in ((0, "kks_newton"), (1, "rhs_fused"), (2, "jv_analytic"),
+                       (3, "mlp_infer_tc")):
         tot, cnt = C.c_double(), C.c_longlong()
         L.ampe_stepper_kernel_time(g._h, kind, C.byref(tot), C.byref(cnt))
         kt[name] = {"ms": tot.value, "launches": cnt.value}
@@ -266,10 +317,12 @@ def run_ours(args):
     m, phi, c = workload(args.n)
     N = m.cells()
     head = args.path
-    other = "fp64" if head == "mixed" else "mixed"
+    mlp, sur_info = None, None
+    if head == "mixed+surrogate":
+        mlp, sur_info = train_surrogate(args, m, local)
     if ws > 1:
         dist.barrier()
-    res_h, st_h, g = timed_path(args, m, phi, c, head, local)
+    res_h, st_h, g = timed_path(args, m, phi, c, head, local, mlp)
     ms_max, updates = aggregate(res_h["ms"], N * args.steps)
     value = updates / (ms_max / 1e3)
 
@@ -298,31 +351,57 @@ def run_ours(args):
     del g
     torch.cuda.empty_cache()
 
-    # the other path on the same input, for the speed ratio and the error
-    res_o, st_o, g2 = timed_path(args, m, phi, c, other, local)
-    g2.close()
-    del g2
-    fields = ("phi", "c")
-    errs = {}
-    for name, a, b in zip(fields, st_h[:2], st_o[:2]):
-        ref = b if head == "mixed" else a
-        mix = a if head == "mixed" else b
-        errs[name] = float(np.linalg.norm((mix - ref).ravel()) / np.linalg.norm(ref.ravel()))
-    v_fp64 = res_o["value"] if head == "mixed" else res_h["value"]
-    v_mixed = res_h["value"] if head == "mixed" else res_o["value"]
+    # the other paths on the same input: speed ratios and errors vs FP64
+    results = {head: (res_h, st_h)}
+    for other in ("mixed", "fp64", "mixed+surrogate"):
+        if other in results or args.only_head:
+            continue
+        if other == "mixed+surrogate" and mlp is None:
+            continue
+        r, st, g2 = timed_path(args, m, phi, c, other, local, mlp)
+        g2.close()
+        del g2
+        torch.cuda.empty_cache()
+        results[other] = (r, st)
+    paths = {}
+    ref = results.get("fp64")
+    for name, (r, st) in results.items():
+        d = {"value": r["value"], "ms_per_step": r["ms"] / args.steps,
+             "kks_iters": r["stats"]["kks_iters"], "kks_fallback": r["stats"]["kks_fallback"],
+             "newton_iters": r["stats"]["newton_iters"], "gmres_iters": r["stats"]["gmres_iters"]}
+        if ref is not None and name != "fp64":
+            d["speedup_vs_fp64"] = r["value"] / ref[0]["value"]
+            d["rel_l2_err_vs_fp64"] = {
+                f: float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+                for f, a, b in zip(("phi", "c"), st[:2], ref[1][:2])}
+        paths[name] = d
+    if mlp is not None:
+        L.ampe_mlp_destroy(mlp)
 
     pk, pk_kind = peaks()
-    kind = "kks_newton"
-    tot = res_h["kernels"][kind]["ms"]
-    cnt = res_h["kernels"][kind]["launches"]
+    # dominant instrumented kernel of the headline path and its roofline
+    kt = res_h["kernels"]
+    per_cell = {"kks_newton": KKS_BYTES_PER_CELL if head == "fp64" else KKS_MIXED_BYTES_PER_CELL,
+                "rhs_fused": RHS_BYTES_PER_CELL if head == "fp64" else RHS_MIXED_BYTES_PER_CELL,
+                "jv_analytic": JV_BYTES_PER_CELL}
+    kname = max((k for k in kt if kt[k]["launches"]), key=lambda k: kt[k]["ms"])
+    tot, cnt = kt[kname]["ms"], kt[kname]["launches"]
     avg_ms = tot / max(cnt, 1)
-    kks_bytes = (KKS_BYTES_PER_CELL if head == "fp64" else KKS_MIXED_BYTES_PER_CELL) * N
-    achieved = kks_bytes / (avg_ms / 1e3) / 1e9 if cnt else None
-    roof = {"bound": "hbm", "kernel": "k_kks_interior" if head == "fp64" else "k_kks_mixed",
-            "achieved": achieved, "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s",
-            "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
-            "algorithmic_bytes_per_launch": kks_bytes, "avg_launch_ms": avg_ms,
-            "launches": cnt, "share_of_step": tot / res_h["ms"]}
+    if kname == "mlp_infer_tc":
+        flops = MLP_FLOPS_PER_CELL * N
+        achieved = flops / (avg_ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "kernel": "k_mlp_infer_tc", "achieved": achieved,
+                "peak": pk["bf16_tflops"], "peak_kind": pk_kind, "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                "algorithmic_flops_per_launch": flops}
+    else:
+        nbytes = per_cell[kname] * N
+        achieved = nbytes / (avg_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": KERNEL_NAMES[head == "fp64"][kname],
+                "achieved": achieved, "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "algorithmic_bytes_per_launch": nbytes}
+    roof.update({"avg_launch_ms": avg_ms, "launches": cnt, "share_of_step": tot / res_h["ms"]})
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -333,12 +412,11 @@ def run_ours(args):
                                % (args.n, ATOL), "path": head, "cells": N,
                    "l2": "inputs larger than L2 (state 2 x %d MB)" % (N * 8 // 2 ** 20),
                    "parallelism": "replicas" if ws > 1 else "single"},
-        "paths": {"mixed": v_mixed, "fp64": v_fp64, "speedup_mixed_vs_fp64": v_mixed / v_fp64,
-                  "rel_l2_err_mixed_vs_fp64": errs},
+        "paths": paths,
+        "surrogate": sur_info,
         "roofline": roof,
         "kernels": res_h["kernels"],
         "stats": res_h["stats"],
-        "stats_other_path": res_o["stats"],
         "gpu_launches": res_h["launches"],
         "clocks": res_h["clocks"],
         "e2e": e2e,
