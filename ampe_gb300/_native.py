@@ -40,6 +40,10 @@ _PROTOS = {
     "ampe_efo_rbgs": (I, [MP, P, P, P, D, P, D, P, D, P, P, I, P, P]),
     "ampe_efo_residual": (I, [MP, P, P, P, D, P, D, P, D, P, P, P, P]),
     "ampe_phase_fac_set_c": (I, [MP, P, D, P, P]),
+    "ampe_quat_grad_modulus": (I, [MP, P, P, P]),
+    "ampe_quat_mobility": (I, [MP, P, P, P]),
+    "ampe_quat_face_coef": (I, [MP, P, P, P, P, P, P, P]),
+    "ampe_quat_rhs": (I, [MP, P, P, P, P, P, P, P]),
     "ampe_efo_residual_rms_scratch_doubles": (C.c_size_t, [MP]),
     "ampe_efo_residual_rms": (I, [MP, P, P, P, D, P, D, P, D, P, P, P, P, P]),
     "ampe_efo_residual_rms_noalloc": (I, [MP, P, P, P, D, P, D, P, D, P, P, P, P]),
@@ -52,6 +56,10 @@ _PROTOS = {
     "ampe_stepper_kernel_launches": (C.c_longlong, [P]),
     "ampe_stepper_load_y": (I, [P, P, P, I]),
     "ampe_stepper_jv": (I, [P, P, D, P, I]),
+    "ampe_stepper_set_quat": (I, [P, P, I]),
+    "ampe_stepper_get_quat": (I, [P, P, I]),
+    "ampe_stepper_size": (C.c_longlong, [P]),
+    "ampe_stepper_eval_rhs_full": (I, [P, P, I]),
     "ampe_stepper_stream": (P, [P]),
     "ampe_stepper_profile": (I, [P, I]),
     "ampe_stepper_kernel_time": (I, [P, I, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),

@@ -71,6 +71,13 @@ class Model(C.Structure):
         ("temp_mode", C.c_int),
         ("T0", C.c_double),
         ("gradT", C.c_double),
+        ("evolve_quat", C.c_int),
+        ("quat_mobility", C.c_double),
+        ("min_quat_mobility", C.c_double),
+        ("quat_grad_floor", C.c_double),
+        ("quat_floor_type", C.c_char),
+        ("quat_mobility_type", C.c_char),
+        ("pad1", C.c_char * 6),
     ]
 
     def cells(self):

@@ -54,6 +54,12 @@ def _blank_model(dim, n, ng=1):
     m.newton_max_its = 50
     m.newton_tol = 1.0e-12
     m.temp_mode = abi.TEMP_CONSTANT
+    m.evolve_quat = 0
+    m.quat_mobility = 1.0
+    m.min_quat_mobility = 1.0e-6
+    m.quat_grad_floor = 1.0e-2
+    m.quat_floor_type = b"s"
+    m.quat_mobility_type = b"p"
     return m
 
 
@@ -106,6 +112,24 @@ def calphad3d(n=256, seed=3, T_run=None, gradT_total=50.0):
     m.T0 = T_run - 0.5 * gradT_total
     m.gradT = gradT_total / (n * m.dx[0])
     m.temp_mode = abi.TEMP_GRADIENT
+    return m
+
+
+def polycrystal3d(n=128, seed=3, T=1500.0):
+    """phi + c + quaternion polycrystal: CALPHAD as calphad3d at constant T,
+    quaternion mobility with the 1/|grad q| regularisation (floor 1e-2)."""
+    m = calphad3d(n, seed=seed, T_run=T, gradT_total=0.0)
+    m.temp_mode = abi.TEMP_CONSTANT
+    m.T0 = T
+    m.gradT = 0.0
+    m.with_orient = 1
+    m.evolve_quat = 1
+    m.epsilon_q = 0.5
+    m.misorientation_factor = 2.0e-5  # 2 H: 2H T |grad q| ~ w at a boundary
+    m.quat_mobility = 1.0
+    m.min_quat_mobility = 1.0e-6
+    m.quat_grad_floor = 1.0e-2
+    m.quat_floor_type = b"s"
     return m
 
 

@@ -134,10 +134,11 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
                             const double* quat, const double* tfield,
                             const ThermoCoef* tab, const double* cl,
                             const double* cs, const double* dF,
-                            const double* phid, double* phi_rhs,
-                            double* conc_rhs)
+                            const double* phid, const double* ogm,
+                            double* phi_rhs, double* conc_rhs)
 {
    const long long qs = g.cells_ghost();
+   const double eq2 = 0.5 * m.epsilon_q * m.epsilon_q;
    auto P = [&](int a, int b, int c) { return phi[g.c(a, b, c)]; };
    auto Q = [&](int comp, int a, int b, int c) {
       return HAS_Q ? quat[comp * qs + g.c(a, b, c)] : 0.0;
@@ -169,6 +170,13 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
       } else {
          const ThermoCoef th = coef_at(m, g, tab, tfield, i, j, k);
          df = driving_force_scaled(m, th, cl[c], cs[c]);
+      }
+      if (ogm) {  // orientation term of COMPUTERHSPBG, 3d/quatrhs.m4:481-509
+         const double p1 = deriv_interp_func(p, m.orient_interp1);
+         const double p2 = deriv_interp_func(p, m.orient_interp2);
+         const double gm = ogm[t];
+         const double T = temperature_at(m, g, tfield, i, j, k);
+         r = r - m.misorientation_factor * T * p1 * gm - p2 * eq2 * gm * gm;
       }
       r += deriv_interp_func(p, m.energy_interp) * df;
       phi_rhs[t] = r * m.phase_mobility;
@@ -207,17 +215,17 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
 int rhs_fused(const ampe_model_t& m, const Grid& g, const double* phi,
               const double* quat, const double* tfield, const ThermoCoef* tab,
               const double* cl, const double* cs, const double* dF,
-              const double* phid, double* phi_rhs, double* conc_rhs,
-              cudaStream_t s)
+              const double* phid, const double* ogm, double* phi_rhs,
+              double* conc_rhs, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
    if (quat)
       k_rhs_fused<true><<<(unsigned)b, 256, 0, s>>>(
-          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, phi_rhs, conc_rhs);
+          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, phi_rhs, conc_rhs);
    else
       k_rhs_fused<false><<<(unsigned)b, 256, 0, s>>>(
-          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, phi_rhs, conc_rhs);
+          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, phi_rhs, conc_rhs);
    return launch_status();
 }
 
@@ -236,5 +244,5 @@ extern "C" int ampe_rhs_phase_conc(const ampe_model_t* m, const double* phi,
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC && !quat) return AMPE_ERR_INVALID;
    if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
    return rhs_fused(*m, make_grid(*m), phi, quat, temp, nullptr, cl, cs,
-                    nullptr, phi, phi_rhs, conc_rhs, (cudaStream_t)stream);
+                    nullptr, phi, nullptr, phi_rhs, conc_rhs, (cudaStream_t)stream);
 }

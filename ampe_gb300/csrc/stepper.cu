@@ -28,6 +28,7 @@
 #include "fused.cuh"
 #include "mixed.cuh"
 #include "mlp.cuh"
+#include "quat.cuh"
 
 namespace ampe {
 
@@ -213,9 +214,9 @@ template <class R>
 struct DevLevel {
    Grid g;
    double dx[3];
-   R *u = nullptr, *f = nullptr, *r = nullptr, *C = nullptr;
+   R *u = nullptr, *f = nullptr, *r = nullptr, *C = nullptr, *M = nullptr;
    R* D[3] = {nullptr, nullptr, nullptr};
-   bool hasC = false, hasD = false;
+   bool hasC = false, hasD = false, hasM = false;
    R cc = 0, dc = 0, mc = 0;
    FacOp<R> op() const
    {
@@ -228,7 +229,7 @@ struct DevLevel {
       o.dc = dc;
       o.C = hasC ? C : nullptr;
       o.cc = cc;
-      o.M = nullptr;
+      o.M = hasM ? M : nullptr;
       o.mc = mc;
       for (int d = 0; d < 3; d++) o.dxi[d] = d < g.dim ? R(1.0 / dx[d]) : R(0);
       return o;
@@ -258,7 +259,7 @@ static void* dalloc(std::vector<void*>& pool, long long n, int* err)
 
 template <class R>
 int fac_create(DevFac<R>& F, const ampe_model_t& m, int nlevels, bool hasD,
-               bool hasC, std::vector<void*>& pool)
+               bool hasC, std::vector<void*>& pool, bool hasM = false)
 {
    int err = AMPE_OK;
    ampe_model_t mm = m;
@@ -273,6 +274,8 @@ int fac_create(DevFac<R>& F, const ampe_model_t& m, int nlevels, bool hasD,
       L.hasC = hasC;
       L.hasD = hasD;
       if (hasC) L.C = (R*)dalloc<R>(pool, ng, &err);
+      L.hasM = hasM;
+      if (hasM) L.M = (R*)dalloc<R>(pool, ng, &err);
       if (hasD) {
          L.D[0] = (R*)dalloc<R>(pool, L.g.nfx(), &err);
          L.D[1] = (R*)dalloc<R>(pool, L.g.nfy(), &err);
@@ -310,6 +313,11 @@ void fac_coarsen_operator(DevFac<R>& F, cudaStream_t s)
          k_restrict<R><<<map_blocks(c.g.cells()), 256, 0, s>>>(f.g, c.g, f.C, c.C);
          launch_status();
          fill_ghosts_t(c.g, c.C, s);
+      }
+      if (c.hasM) {
+         k_restrict<R><<<map_blocks(c.g.cells()), 256, 0, s>>>(f.g, c.g, f.M, c.M);
+         launch_status();
+         fill_ghosts_t(c.g, c.M, s);
       }
       if (c.hasD)
          for (int d = 0; d < c.g.dim; d++) {
@@ -429,7 +437,8 @@ struct Stepper {
    ampe_model_t m;
    ampe_step_params_t p;
    Grid g;
-   long long N = 0, NG = 0, N2 = 0;
+   long long N = 0, NG = 0, NY = 0;
+   int nb = 2;  // scalar fields in y: phi, c (+ q0..q3 when evolve_quat)
    cudaStream_t s = nullptr;
    Reducer red;
    std::vector<void*> pool;
@@ -450,9 +459,13 @@ struct Stepper {
    float *guess_l = nullptr, *guess_s = nullptr;  // surrogate initial guess
    Mlp* mlp = nullptr;                            // attached surrogate
    unsigned long long* mcount = nullptr;          // mixed KKS counters [5]
+   // quaternion fields: ghosted q (4 NG) and its lagged copy, the cell
+   // modulus |grad q| of the lagged copy, M_q(phi), face coefficients
+   double *q_g = nullptr, *q_lag = nullptr, *ogm = nullptr, *mq = nullptr;
+   double* fcq[3] = {nullptr, nullptr, nullptr};
    // preconditioner (FP64 or FP32)
-   DevFac<double> facp64, facc64;
-   DevFac<float> facp32, facc32;
+   DevFac<double> facp64, facc64, facq64;
+   DevFac<float> facp32, facc32, facq32;
    int hist = 0;
    double t = 0.0;
    ampe_step_stats_t st;
@@ -468,7 +481,7 @@ struct Stepper {
 };
 
 // kernel classes timed in profiling mode
-enum { KT_KKS = 0, KT_RHS = 1, KT_JV = 2, KT_MLP = 3, KT_NKINDS = 4 };
+enum { KT_KKS = 0, KT_RHS = 1, KT_JV = 2, KT_MLP = 3, KT_QUAT = 4, KT_NKINDS = 5 };
 
 static cudaEvent_t prof_event(Stepper& S)
 {
@@ -521,6 +534,19 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    to_ghosted<double>(S.g, y, v, sig, S.phi_g, S.s);
    to_ghosted<double>(S.g, y + S.N, v ? v + S.N : nullptr, sig, S.c_g, S.s);
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
+   const bool quat = S.nb == 6;
+   if (quat) {
+      for (int c = 0; c < 4; c++)
+         to_ghosted<double>(S.g, y + (2 + c) * S.N, v ? v + (2 + c) * S.N : nullptr,
+                            sig, S.q_g + c * S.NG, S.s);
+      // QuatIntegrator::computeQuatGradients; the finite-difference calls
+      // keep the gradients of the last f(y) (QuatIntegrator.cc:3189)
+      if (!fd_flag) {
+         cudaMemcpyAsync(S.q_lag, S.q_g, sizeof(double) * 4 * (size_t)S.NG,
+                         cudaMemcpyDeviceToDevice, S.s);
+         quat_grad_modulus<double>(S.m, S.g, S.q_lag, S.ogm, S.s);
+      }
+   }
    if (S.p.precision == 1) {
       if (S.p.surrogate && S.mlp) {
          ProfScope ps(S, KT_MLP);
@@ -555,29 +581,38 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    {
       ProfScope ps(S, KT_RHS);
       rhs_fused(S.m, S.g, S.phi_g, nullptr, tf, S.tab, S.cl, S.cs, S.dF,
-                S.phi_lag, out, out + S.N, S.s);
+                S.phi_lag, quat && S.m.with_orient ? S.ogm : nullptr, out,
+                out + S.N, S.s);
+   }
+   if (quat) {
+      ProfScope ps(S, KT_QUAT);
+      quat_mobility<double>(S.m, S.g, S.phi_g, S.mq, S.s);
+      quat_face_coef<double, double>(S.m, S.g, S.phi_g, tf, S.q_lag, 1.0, S.fcq[0], S.fcq[1],
+                             S.fcq[2], S.s);
+      quat_rhs<double>(S.m, S.g, S.fcq[0], S.fcq[1], S.fcq[2], S.mq, S.q_g,
+                       out + 2 * S.N, S.s);
    }
    S.st.rhs_evals++;
 }
 
 static double wrms(Stepper& S, const double* v, const double* w)
 {
-   const long long n2 = S.N2;
-   const double ss = S.red.sum(n2, [=] __device__(long long t) {
+   const long long ny = S.NY;
+   const double ss = S.red.sum(ny, [=] __device__(long long t) {
       const double x = v[t] * w[t];
       return x * x;
    });
-   return sqrt(ss / (double)n2);
+   return sqrt(ss / (double)ny);
 }
 
 static double dot(Stepper& S, const double* a, const double* b)
 {
-   return S.red.sum(S.N2, [=] __device__(long long t) { return a[t] * b[t]; });
+   return S.red.sum(S.NY, [=] __device__(long long t) { return a[t] * b[t]; });
 }
 
 template <class R>
 static void precond_setup_t(Stepper& S, DevFac<R>& fp, DevFac<R>& fc,
-                            double gamma)
+                            DevFac<R>& fq, double gamma)
 {
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
    DevLevel<R>& P0 = fp.lev[0];
@@ -602,14 +637,29 @@ static void precond_setup_t(Stepper& S, DevFac<R>& fp, DevFac<R>& fc,
       L.mc = (R)S.m.conc_mobility;
    }
    fac_coarsen_operator(fc, S.s);
+   if (S.nb == 6) {
+      // QuatFACOps::setOperatorCoefficients: C = 1, M = M_q(phi) per cell,
+      // D = gamma fc at the faces (lagged gradients)
+      DevLevel<R>& Q0 = fq.lev[0];
+      quat_mobility<R>(S.m, S.g, S.phi_g, Q0.M, S.s);
+      fill_ghosts_t(S.g, Q0.M, S.s);
+      quat_face_coef<double, R>(S.m, S.g, S.phi_g, tf, S.q_lag, gamma, Q0.D[0], Q0.D[1],
+                                Q0.D[2], S.s);
+      for (auto& L : fq.lev) {
+         L.dc = 0;
+         L.cc = (R)1.0;
+         L.mc = 0;
+      }
+      fac_coarsen_operator(fq, S.s);
+   }
 }
 
 static void precond_setup(Stepper& S, double gamma)
 {
    if (S.p.precision == 1)
-      precond_setup_t(S, S.facp32, S.facc32, gamma);
+      precond_setup_t(S, S.facp32, S.facc32, S.facq32, gamma);
    else
-      precond_setup_t(S, S.facp64, S.facc64, gamma);
+      precond_setup_t(S, S.facp64, S.facc64, S.facq64, gamma);
    S.st.precond_setups++;
 }
 
@@ -617,18 +667,18 @@ static void precond_solve(Stepper& S, const double* r, double* z,
                           double delta)
 {
    if (S.p.precond == 0) {
-      cudaMemcpyAsync(z, r, sizeof(double) * S.N2, cudaMemcpyDeviceToDevice,
+      cudaMemcpyAsync(z, r, sizeof(double) * S.NY, cudaMemcpyDeviceToDevice,
                       S.s);
       return;
    }
    Ctx cx = S.ctx();
-   for (int blk = 0; blk < 2; blk++) {
+   for (int blk = 0; blk < S.nb; blk++) {
       if (S.p.precision == 1)
-         fac_solve(cx, blk == 0 ? S.facp32 : S.facc32, S.p.precond,
-                   r + blk * S.N, z + blk * S.N, delta);
+         fac_solve(cx, blk == 0 ? S.facp32 : (blk == 1 ? S.facc32 : S.facq32),
+                   S.p.precond, r + blk * S.N, z + blk * S.N, delta);
       else
-         fac_solve(cx, blk == 0 ? S.facp64 : S.facc64, S.p.precond,
-                   r + blk * S.N, z + blk * S.N, delta);
+         fac_solve(cx, blk == 0 ? S.facp64 : (blk == 1 ? S.facc64 : S.facq64),
+                   S.p.precond, r + blk * S.N, z + blk * S.N, delta);
    }
    S.st.precond_solves++;
 }
@@ -648,7 +698,7 @@ static void matvec(Stepper& S, const double* y, const double* fy,
    const double sig = 1.0 / wrms(S, v, w);
    eval_rhs(S, y, v, sig, S.fp, 1);
    const double* fp = S.fp;
-   map(S.N2, [=] __device__(long long t) {
+   map(S.NY, [=] __device__(long long t) {
       out[t] = v[t] - gamma * (fp[t] - fy[t]) / sig;
    }, S.s);
 }
@@ -657,41 +707,41 @@ static int gmres(Stepper& S, const double* y, const double* fy,
                  const double* w, double gamma, const double* b, double* x,
                  double tol)
 {
-   const long long n2 = S.N2;
+   const long long ny = S.NY;
    const int maxl = S.p.max_krylov;
-   const double sqrtN = std::sqrt((double)n2);
+   const double sqrtN = std::sqrt((double)ny);
    std::vector<double> H((maxl + 1) * maxl, 0.0), gv(maxl + 1, 0.0), cs(maxl),
        sn(maxl);
    double* tmp = S.tmp;
    double* av = S.av;
-   cudaMemsetAsync(x, 0, sizeof(double) * n2, S.s);
+   cudaMemsetAsync(x, 0, sizeof(double) * ny, S.s);
    precond_solve(S, b, tmp, tol * sqrtN);
    double* V0 = S.V[0];
-   map(n2, [=] __device__(long long t) { V0[t] = w[t] * tmp[t]; }, S.s);
+   map(ny, [=] __device__(long long t) { V0[t] = w[t] * tmp[t]; }, S.s);
    double beta = std::sqrt(dot(S, V0, V0));
    if (beta / sqrtN <= tol) return 0;
    {
       const double ib = beta;
-      map(n2, [=] __device__(long long t) { V0[t] /= ib; }, S.s);
+      map(ny, [=] __device__(long long t) { V0[t] /= ib; }, S.s);
    }
    gv[0] = beta;
    int l = 0;
    for (; l < maxl; l++) {
       double* Vl = S.V[l];
       double* Vn = S.V[l + 1];
-      map(n2, [=] __device__(long long t) { tmp[t] = Vl[t] / w[t]; }, S.s);
+      map(ny, [=] __device__(long long t) { tmp[t] = Vl[t] / w[t]; }, S.s);
       matvec(S, y, fy, w, gamma, tmp, av);
       precond_solve(S, av, tmp, tol * sqrtN);
-      map(n2, [=] __device__(long long t) { Vn[t] = w[t] * tmp[t]; }, S.s);
+      map(ny, [=] __device__(long long t) { Vn[t] = w[t] * tmp[t]; }, S.s);
       for (int i = 0; i <= l; i++) {
          double* Vi = S.V[i];
          const double h = dot(S, Vi, Vn);
          H[i * maxl + l] = h;
-         map(n2, [=] __device__(long long t) { Vn[t] -= h * Vi[t]; }, S.s);
+         map(ny, [=] __device__(long long t) { Vn[t] -= h * Vi[t]; }, S.s);
       }
       const double hn = std::sqrt(dot(S, Vn, Vn));
       H[(l + 1) * maxl + l] = hn;
-      if (hn > 0.0) map(n2, [=] __device__(long long t) { Vn[t] /= hn; }, S.s);
+      if (hn > 0.0) map(ny, [=] __device__(long long t) { Vn[t] /= hn; }, S.s);
       for (int i = 0; i < l; i++) {
          const double aa = H[i * maxl + l], bb = H[(i + 1) * maxl + l];
          H[i * maxl + l] = cs[i] * aa + sn[i] * bb;
@@ -720,34 +770,34 @@ static int gmres(Stepper& S, const double* y, const double* fy,
    for (int i = 0; i < k; i++) {
       const double c = yk[i];
       double* Vi = S.V[i];
-      map(n2, [=] __device__(long long t) { x[t] += c * Vi[t]; }, S.s);
+      map(ny, [=] __device__(long long t) { x[t] += c * Vi[t]; }, S.s);
    }
-   map(n2, [=] __device__(long long t) { x[t] /= w[t]; }, S.s);
+   map(ny, [=] __device__(long long t) { x[t] /= w[t]; }, S.s);
    return k;
 }
 
 // one BDF step of size h, order q; result in S.ynew.  0 = converged.
 static int bdf_step(Stepper& S, double h, int q)
 {
-   const long long n2 = S.N2;
+   const long long ny = S.NY;
    double *a = S.a, *y = S.y, *yn = S.yn, *ynm1 = S.ynm1, *w = S.w;
    double *fy = S.fy, *b = S.b, *d = S.d;
    double gamma;
    if (q == 1) {
       gamma = h;
-      map(n2, [=] __device__(long long t) {
+      map(ny, [=] __device__(long long t) {
          a[t] = yn[t];
          y[t] = yn[t];
       }, S.s);
    } else {
       gamma = 2.0 * h / 3.0;
-      map(n2, [=] __device__(long long t) {
+      map(ny, [=] __device__(long long t) {
          a[t] = (4.0 * yn[t] - ynm1[t]) / 3.0;
          y[t] = 2.0 * yn[t] - ynm1[t];
       }, S.s);
    }
    const double rtol = S.p.rtol, atol = S.p.atol;
-   map(n2, [=] __device__(long long t) { w[t] = 1.0 / (rtol * fabs(yn[t]) + atol); },
+   map(ny, [=] __device__(long long t) { w[t] = 1.0 / (rtol * fabs(yn[t]) + atol); },
        S.s);
    double crate = 1.0, delp = 0.0;
    const double lintol = S.p.lin_coef * S.p.newton_coef;
@@ -755,18 +805,20 @@ static int bdf_step(Stepper& S, double h, int q)
       eval_rhs(S, y, nullptr, 0.0, fy, 0);
       if (it == 0 && S.p.precond) precond_setup(S, gamma);
       const double gm = gamma;
-      map(n2, [=] __device__(long long t) { b[t] = -(y[t] - gm * fy[t] - a[t]); },
+      map(ny, [=] __device__(long long t) { b[t] = -(y[t] - gm * fy[t] - a[t]); },
           S.s);
       const int li = gmres(S, y, fy, w, gamma, b, d, lintol);
       S.st.gmres_iters += li;
       S.st.newton_iters++;
-      map(n2, [=] __device__(long long t) { y[t] += d[t]; }, S.s);
+      map(ny, [=] __device__(long long t) { y[t] += d[t]; }, S.s);
       const double del = wrms(S, d, w);
       if (it > 0) crate = std::max(0.3 * crate, del / delp);
       const double dcon = del * std::min(1.0, crate) / S.p.newton_coef;
       if (dcon <= 1.0) {
-         cudaMemcpyAsync(S.ynew, y, sizeof(double) * n2,
+         cudaMemcpyAsync(S.ynew, y, sizeof(double) * ny,
                          cudaMemcpyDeviceToDevice, S.s);
+         // QuatIntegrator::applyProjection (QuatIntegrator.cc:3911-3940)
+         if (S.nb == 6) quat_project(S.N, S.ynew + 2 * S.N, S.s);
          return 0;
       }
       if (it >= 1 && del > 2.0 * delp) break;
@@ -801,6 +853,9 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
        p->precision > 1)
       return AMPE_ERR_INVALID;
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC) return AMPE_ERR_INVALID;
+   if (m->evolve_quat && (m->quat_mobility_type != 'p' || !(m->quat_grad_floor > 0.0)))
+      return AMPE_ERR_INVALID;
+   if (m->evolve_quat && p->precision == 1) return AMPE_ERR_INVALID;
    if (ampe_device_count() < 1) return AMPE_ERR_NO_DEVICE;
    Stepper* S = new (std::nothrow) Stepper;
    if (!S) return AMPE_ERR_INVALID;
@@ -809,7 +864,8 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    S->g = make_grid(*m);
    S->N = S->g.cells();
    S->NG = S->g.cells_ghost();
-   S->N2 = 2 * S->N;
+   S->nb = m->evolve_quat ? 6 : 2;
+   S->NY = S->nb * S->N;
    S->mp = make_mix_params(*m);
    std::memset(&S->st, 0, sizeof(S->st));
    int err = AMPE_OK;
@@ -822,9 +878,18 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    S->dF = dvec(*S, S->N, &err);
    double** vv[] = {&S->yn, &S->ynm1, &S->ynew, &S->a, &S->y, &S->fy,
                     &S->b,  &S->d,    &S->w,    &S->tmp, &S->av, &S->fp};
-   for (double** q : vv) *q = dvec(*S, S->N2, &err);
-   for (int l = 0; l <= p->max_krylov; l++) S->V.push_back(dvec(*S, S->N2, &err));
+   for (double** q : vv) *q = dvec(*S, S->NY, &err);
+   for (int l = 0; l <= p->max_krylov; l++) S->V.push_back(dvec(*S, S->NY, &err));
    S->counters = (unsigned long long*)dalloc<unsigned long long>(S->pool, 2, &err);
+   if (S->nb == 6) {
+      S->q_g = dvec(*S, 4 * S->NG, &err);
+      S->q_lag = dvec(*S, 4 * S->NG, &err);
+      S->ogm = dvec(*S, S->N, &err);
+      S->mq = dvec(*S, S->NG, &err);
+      S->fcq[0] = dvec(*S, S->g.nfx(), &err);
+      S->fcq[1] = dvec(*S, S->g.nfy(), &err);
+      if (S->g.dim == 3) S->fcq[2] = dvec(*S, S->g.nfz(), &err);
+   }
    if (p->precision == 1) {
       float** f32g[] = {&S->cl32, &S->cs32, &S->clr32, &S->csr32, &S->pf32,
                         &S->dphi32, &S->da32, &S->db32};
@@ -846,9 +911,13 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
       if (p->precision == 1) {
          err = fac_create(S->facp32, *m, nl, false, true, S->pool);
          if (!err) err = fac_create(S->facc32, *m, nl, true, false, S->pool);
+         if (!err && S->nb == 6)
+            err = fac_create(S->facq32, *m, nl, true, false, S->pool, true);
       } else {
          err = fac_create(S->facp64, *m, nl, false, true, S->pool);
          if (!err) err = fac_create(S->facc64, *m, nl, true, false, S->pool);
+         if (!err && S->nb == 6)
+            err = fac_create(S->facq64, *m, nl, true, false, S->pool, true);
       }
    }
    // the zero fills of dalloc run on the legacy stream, which does not
@@ -889,7 +958,12 @@ int ampe_stepper_set_state(void* h, const double* phi, const double* conc,
    const size_t bytes = sizeof(double) * (size_t)S->N;
    cudaMemcpyAsync(S->yn, phi, bytes, kind, S->s);
    cudaMemcpyAsync(S->yn + S->N, conc, bytes, kind, S->s);
-   cudaMemcpyAsync(S->ynm1, S->yn, 2 * bytes, cudaMemcpyDeviceToDevice, S->s);
+   if (S->nb == 6) {  // orientation (1, 0, 0, 0) until ampe_stepper_set_quat
+      double* q = S->yn + 2 * S->N;
+      const long long n4 = 4 * S->N, N = S->N;
+      map(n4, [=] __device__(long long t) { q[t] = t < N ? 1.0 : 0.0; }, S->s);
+   }
+   cudaMemcpyAsync(S->ynm1, S->yn, S->nb * bytes, cudaMemcpyDeviceToDevice, S->s);
    // warm starts (interior) -> ghosted refs; default (c, c)
    double* stage = S->tmp;
    cudaMemcpyAsync(stage, cl ? cl : conc, bytes, cl ? kind : kind, S->s);
@@ -961,7 +1035,7 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
    Stepper* S = (Stepper*)h;
    if (!S || nsteps < 0) return AMPE_ERR_INVALID;
    int ret = AMPE_OK;
-   const size_t b2 = sizeof(double) * (size_t)S->N2;
+   const size_t b2 = sizeof(double) * (size_t)S->NY;
    const size_t gb = sizeof(double) * (size_t)S->NG;
    for (int n = 0; n < nsteps; n++) {
       double hstep = S->p.dt;
@@ -1078,10 +1152,10 @@ int ampe_stepper_jv(void* h, const double* v, double gamma, double* out,
    if (!S || !v || !out) return AMPE_ERR_INVALID;
    const cudaMemcpyKind in = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
    const cudaMemcpyKind ot = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-   const size_t b2 = sizeof(double) * (size_t)S->N2;
+   const size_t b2 = sizeof(double) * (size_t)S->NY;
    double *w = S->w, *yn = S->yn;
    const double rtol = S->p.rtol, atol = S->p.atol;
-   map(S->N2, [=] __device__(long long t) { w[t] = 1.0 / (rtol * fabs(yn[t]) + atol); },
+   map(S->NY, [=] __device__(long long t) { w[t] = 1.0 / (rtol * fabs(yn[t]) + atol); },
        S->s);
    eval_rhs(*S, S->yn, nullptr, 0.0, S->fy, 0);
    cudaMemcpyAsync(S->b, v, b2, in, S->s);
@@ -1089,6 +1163,47 @@ int ampe_stepper_jv(void* h, const double* v, double gamma, double* out,
    cudaMemcpyAsync(out, S->d, b2, ot, S->s);
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
    return AMPE_OK;
+}
+
+int ampe_stepper_set_quat(void* h, const double* q, int host)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || !q || S->nb != 6) return AMPE_ERR_INVALID;
+   const cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+   const size_t b4 = sizeof(double) * 4 * (size_t)S->N;
+   cudaMemcpyAsync(S->yn + 2 * S->N, q, b4, kind, S->s);
+   cudaMemcpyAsync(S->ynm1 + 2 * S->N, S->yn + 2 * S->N, b4, cudaMemcpyDeviceToDevice,
+                   S->s);
+   S->hist = 0;
+   if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
+   return AMPE_OK;
+}
+
+int ampe_stepper_get_quat(void* h, double* q, int host)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || !q || S->nb != 6) return AMPE_ERR_INVALID;
+   const cudaMemcpyKind kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+   cudaMemcpyAsync(q, S->yn + 2 * S->N, sizeof(double) * 4 * (size_t)S->N, kind, S->s);
+   if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
+   return AMPE_OK;
+}
+
+int ampe_stepper_eval_rhs_full(void* h, double* out, int host)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || !out) return AMPE_ERR_INVALID;
+   eval_rhs(*S, S->yn, nullptr, 0.0, S->fy, 0);
+   const cudaMemcpyKind kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+   cudaMemcpyAsync(out, S->fy, sizeof(double) * (size_t)S->NY, kind, S->s);
+   if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
+   return AMPE_OK;
+}
+
+long long ampe_stepper_size(void* h)
+{
+   Stepper* S = (Stepper*)h;
+   return S ? S->NY : 0;
 }
 
 int ampe_stepper_load_y(void* h, const double* phi, const double* conc,

@@ -36,3 +36,41 @@ def calphad3d_state(n=256, seed=0, nseeds=16, radius=None, width=3.0,
     phi = tanh_seed((n, n, n), centers, [radius] * nseeds, width)
     c = rng.uniform(clo, chi, size=(n, n, n))
     return phi, c
+
+
+def random_unit_quaternions(rng, k):
+    """k unit quaternions uniform on S^3 (normalised Gaussian 4-vectors)."""
+    q = rng.standard_normal((k, 4))
+    return q / np.linalg.norm(q, axis=1, keepdims=True)
+
+
+def polycrystal_state(n=128, ngrains=8, seed=0, channel=6.0, width=1.5,
+                      clo=0.3, chi=0.5):
+    """Periodic Voronoi polycrystal: grain interiors solid (phi = 1), a liquid
+    channel `channel` cells wide along the grain boundaries, each grain's
+    orientation a random unit quaternion (the channel cells take their
+    nearest grain's), c ~ U[clo, chi].  Returns phi, c, q (4, z, y, x)."""
+    rng = np.random.default_rng(seed)
+    seeds = rng.uniform(0, n, size=(ngrains, 3))
+    quats = random_unit_quaternions(rng, ngrains)
+    ax = np.arange(n) + 0.5
+    z, y, x = np.meshgrid(ax, ax, ax, indexing="ij")
+    d1 = np.full((n, n, n), np.inf)
+    d2 = np.full((n, n, n), np.inf)
+    g1 = np.zeros((n, n, n), dtype=np.int64)
+    for g, s in enumerate(seeds):
+        dd = np.zeros((n, n, n))
+        for coord, sc in zip((x, y, z), s):
+            d = np.abs(coord - sc)
+            d = np.minimum(d, n - d)
+            dd += d * d
+        dd = np.sqrt(dd)
+        closer = dd < d1
+        d2 = np.where(closer, d1, np.minimum(d2, dd))
+        g1 = np.where(closer, g, g1)
+        d1 = np.where(closer, dd, d1)
+    dist_gb = 0.5 * (d2 - d1)  # distance to the nearest grain boundary
+    phi = 0.5 * (1.0 + np.tanh((dist_gb - 0.5 * channel) / width))
+    q = np.ascontiguousarray(np.moveaxis(quats[g1], -1, 0))
+    c = rng.uniform(clo, chi, size=(n, n, n))
+    return phi, c, q

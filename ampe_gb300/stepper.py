@@ -24,7 +24,8 @@ def _ptr(a):
 
 
 class ImplicitStepper:
-    """One uniform periodic level, phi + c, on the current CUDA device."""
+    """One uniform periodic level, phi + c (+ quaternion q when the model
+    has evolve_quat), on the current CUDA device."""
 
     def __init__(self, model, params):
         self.model = model
@@ -71,6 +72,31 @@ class ImplicitStepper:
         check(lib.ampe_stepper_get_state(self._h, _ptr(phi), _ptr(conc), None,
                                          None, 0), "ampe_stepper_get_state")
 
+    def size(self):
+        """Length of the state vector y (2N, or 6N with quaternions)."""
+        return lib.ampe_stepper_size(self._h)
+
+    def set_quat(self, q):
+        """Orientation part of y_n: array (4, *interior shape) of unit
+        quaternions, component-major."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if q.size != 4 * self.n:
+            raise ValueError("need 4 x cells values")
+        self._keep_q = q
+        check(lib.ampe_stepper_set_quat(self._h, _ptr(q), 1), "ampe_stepper_set_quat")
+
+    def get_quat(self):
+        q = np.empty(4 * self.n)
+        check(lib.ampe_stepper_get_quat(self._h, _ptr(q), 1), "ampe_stepper_get_quat")
+        return q.reshape((4,) + tuple(self.model.interior_shape()))
+
+    def eval_rhs_full(self):
+        """f(y_n) for the whole state vector."""
+        out = np.empty(self.size())
+        check(lib.ampe_stepper_eval_rhs_full(self._h, _ptr(out), 1),
+              "ampe_stepper_eval_rhs_full")
+        return out
+
     def eval_rhs(self):
         fp = np.empty(self.n)
         fc = np.empty(self.n)
@@ -80,7 +106,7 @@ class ImplicitStepper:
         return fp.reshape(shp), fc.reshape(shp)
 
     def jv(self, v, gamma):
-        """v - gamma J v at the current state (v: [phi | conc] interior)."""
+        """v - gamma J v at the current state (v: [phi | conc (| q)] interior)."""
         v = np.ascontiguousarray(v, dtype=np.float64).ravel()
         out = np.empty_like(v)
         check(lib.ampe_stepper_jv(self._h, _ptr(v), float(gamma), _ptr(out), 1),

@@ -114,6 +114,15 @@ typedef struct ampe_model {
    int temp_mode;  /* AMPE_TEMP_* */
    double T0;
    double gradT;   /* K per unit length along x */
+
+   /* ---- quaternion orientation field (QuatFACOps, QuatModelParameters) ---- */
+   int evolve_quat;          /* 1: q (4 components) is part of the state */
+   double quat_mobility;     /* orient_mobility (scale of M_q) */
+   double min_quat_mobility; /* min_orient_mobility (1e-6 default) */
+   double quat_grad_floor;   /* orient_grad_floor (1e-2 default) */
+   char quat_floor_type;     /* 'm' max, 's' smooth, 't' tanh (quat.f:1497) */
+   char quat_mobility_type;  /* 'p' 1 - pbg(phi) (3d/mobility.m4:13-95) */
+   char pad1[6];
 } ampe_model_t;
 
 /* Integrator / preconditioner controls (QuatIntegrator.cc:278-301,
@@ -285,6 +294,36 @@ int ampe_efo_residual_rms_noalloc(const ampe_model_t* m, const double* dface0,
                                   double m_const, const double* rhs,
                                   const double* u, double* rms, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Quaternion orientation kernels (evolve_quat models).  q is 4 ghosted
+ * cell fields back to back (CellData depth 4), ghosts filled.
+ * ------------------------------------------------------------------- */
+
+/* |grad q| at cells from the normal differences on the cell's faces:
+ * QUATDIFFS (3d/quatdiffs.m4:70-128) + QUATGRAD_MODULUS_FROM_SIDES_COMPACT
+ * (3d/quatgrad.m4:725-790), the path of QuatModel::computeQuatGradients.
+ * ogm: interior (ghost width 0). */
+int ampe_quat_grad_modulus(const ampe_model_t* m, const double* q,
+                           double* ogm, void* stream);
+/* QUATMOBILITY (3d/mobility.m4:13-95, quat_mobility_type 'p'):
+ * M_q = min + (M - min)(1 - p(phi)) on interior cells of mq (ghost width
+ * m->ng). */
+int ampe_quat_mobility(const ampe_model_t* m, const double* phi, double* mq,
+                       void* stream);
+/* COMPUTE_FACE_COEF3D (3d/quatfacops.m4:14-155) with the side gradients of
+ * QUATGRAD_SIDE (3d/quatgrad.m4:213-335) and the floor types of
+ * eval_grad_normi (quat.f:1497-1537): fc = -2H T p1(phibar) / |grad q|_f
+ * - eps_q^2 p2(phibar) on every face (side arrays). */
+int ampe_quat_face_coef(const ampe_model_t* m, const double* phi,
+                        const double* temp, const double* q, double* fc0,
+                        double* fc1, double* fc2, void* stream);
+/* COMPUTE_FLUX3D + ADD_QUAT_OP3D (3d/quatfacops.m4:227-311, 596-657) as
+ * used by QuatModel's RHS: out_c = -M_q div(fc grad q_c), c = 0..3,
+ * interior output 4N (component-major). */
+int ampe_quat_rhs(const ampe_model_t* m, const double* fc0, const double* fc1,
+                  const double* fc2, const double* mq, const double* q,
+                  double* out, void* stream);
+
 /* PhaseFACOps::setCOnPatchPrivate (PhaseFACOps.cc:101-183):
  * C = 1 + gamma M_phi w g''(phi) on interior cells (ghost width m->ng). */
 int ampe_phase_fac_set_c(const ampe_model_t* m, const double* phi,
@@ -357,6 +396,17 @@ int ampe_stepper_jv(void* handle, const double* v, double gamma, double* out,
  * host memory and hand them in every step (a SAMRAI patch adapter). */
 int ampe_stepper_load_y(void* handle, const double* phi, const double* conc,
                         int host);
+/* evolve_quat models: the orientation part of y_n, 4N doubles (component-
+ * major interior arrays, unit quaternions).  set_state initialises it to
+ * (1, 0, 0, 0); set_quat replaces it and restarts the BDF history.
+ * Accepted steps are projected onto unit quaternions
+ * (QuatIntegrator::applyProjection, QuatIntegrator.cc:3911-3940). */
+int ampe_stepper_set_quat(void* handle, const double* q, int host);
+int ampe_stepper_get_quat(void* handle, double* q, int host);
+/* Length of the stepper's state vector y: 2N, or 6N with quaternions. */
+long long ampe_stepper_size(void* handle);
+/* f(y_n) for the whole state vector (ampe_stepper_size doubles). */
+int ampe_stepper_eval_rhs_full(void* handle, double* out, int host);
 /* Use a trained surrogate (ampe_mlp_*) for the KKS initial guesses of the
  * mixed path (params surrogate=1): each cell starts from the network's
  * guess and falls back to the previous step's values when 3 FP32 Newton
@@ -368,7 +418,8 @@ long long ampe_stepper_kernel_launches(void* handle);
 void* ampe_stepper_stream(void* handle);
 /* Per-kernel CUDA-event timing on the stepper stream.  kind: 0 KKS Newton,
  * 1 fused RHS, 2 analytic Jacobian-vector product (mixed path), 3 surrogate
- * inference.  Enabling resets the totals. */
+ * inference, 4 quaternion RHS (mobility, face coefficients, divergence).
+ * Enabling resets the totals. */
 int ampe_stepper_profile(void* handle, int enable);
 int ampe_stepper_kernel_time(void* handle, int kind, double* total_ms,
                              long long* launches);

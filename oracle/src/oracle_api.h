@@ -58,6 +58,22 @@ void orc_rhs_phase_conc(const ampe_model_t* m, const double* phi,
                         const double* phi_d, double* phi_rhs,
                         double* conc_rhs);
 
+void orc_rhs_phase_conc_q(const ampe_model_t* m, const double* phi,
+                          const double* quat, const double* temp,
+                          const double* cl, const double* cs,
+                          const double* phi_d, const double* ogm,
+                          double* phi_rhs, double* conc_rhs);
+/* quaternion kernels (quat.cc) */
+void orc_quat_grad_modulus(const ampe_model_t* m, const double* q, double* ogm);
+void orc_quat_mobility(const ampe_model_t* m, const double* phi, double* mq);
+void orc_quat_face_coef(const ampe_model_t* m, const double* phi,
+                        const double* temp, const double* qlag, double* fc0,
+                        double* fc1, double* fc2);
+void orc_quat_rhs(const ampe_model_t* m, const double* fc0, const double* fc1,
+                  const double* fc2, const double* mq, const double* q,
+                  double* out);
+void orc_quat_project(long ncells, double* q);
+
 void orc_jv_analytic(const ampe_model_t* m, const double* phi,
                      const double* cl, const double* cs, const double* v,
                      double gamma, double* out);
@@ -89,9 +105,14 @@ void orc_stepper_destroy(void* h);
 void orc_stepper_set_state(void* h, const double* phi, const double* conc,
                            const double* cl, const double* cs,
                            const double* temp);
+/* q: 4 interior component arrays back to back (evolve_quat models) */
+void orc_stepper_set_quat(void* h, const double* q);
+void orc_stepper_get_quat(void* h, double* q);
 void orc_stepper_get_state(void* h, double* phi, double* conc, double* cl,
                            double* cs);
 void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs);
+void orc_stepper_eval_rhs_full(void* h, double* out);
+long orc_stepper_size(void* h);
 int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats);
 void orc_stepper_jv(void* h, const double* v, double gamma, double* out,
                     int analytic);

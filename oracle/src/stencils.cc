@@ -391,10 +391,24 @@ void orc_rhs_phase_conc(const ampe_model_t* m, const double* phi,
                         const double* phi_d, double* phi_rhs,
                         double* conc_rhs)
 {
+   ampe_model_t mm = *m;
+   mm.with_orient = 0;
+   orc_rhs_phase_conc_q(&mm, phi, quat, temp, cl, cs, phi_d, nullptr, phi_rhs,
+                        conc_rhs);
+}
+
+// as orc_rhs_phase_conc, with the orientation term of COMPUTERHSPBG
+// (3d/quatrhs.m4:481-509) from the cell modulus |grad q| when with_orient
+void orc_rhs_phase_conc_q(const ampe_model_t* m, const double* phi,
+                          const double* quat, const double* temp,
+                          const double* cl, const double* cs,
+                          const double* phi_d, const double* ogm,
+                          double* phi_rhs, double* conc_rhs)
+{
    Layout L(*m);
    std::vector<double> f0(L.nfx()), f1(L.nfy()), f2(L.dim == 3 ? L.nfz() : 1);
    orc_phase_flux(m, phi, quat, f0.data(), f1.data(), f2.data());
-   orc_computerhspbg(m, f0.data(), f1.data(), f2.data(), temp, phi, nullptr,
+   orc_computerhspbg(m, f0.data(), f1.data(), f2.data(), temp, phi, ogm,
                      phi_rhs);
    orc_add_driving_force(m, temp, phi, cl, cs, phi_rhs);
    const long N = L.cells();

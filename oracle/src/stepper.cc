@@ -24,9 +24,13 @@ struct OStepper {
    ampe_model_t m;
    ampe_step_params_t p;
    long N, NG;  // interior cells, ghost-box cells
+   int nb = 2;  // scalar fields in y: phi, c (+ q0..q3)
+   long NY = 0; // nb * N
+   std::vector<double> q_g, q_lag, ogm, mq, fcq[3], Dq[3];
+   void* fac_quat = nullptr;
    std::vector<double> phi_g, c_g, cl, cs, clr, csr, temp, phi_lag;
    std::vector<double> cl_nf, cs_nf;  // cL, cS of the last f(y) with fd_flag=0
-   std::vector<double> yn, ynm1;  // 2N: [phi | c]
+   std::vector<double> yn, ynm1;  // NY: [phi | c | q0..q3]
    std::vector<double> Cphi, Dc[3];
    void* fac_phi = nullptr;
    void* fac_conc = nullptr;
@@ -66,6 +70,13 @@ void eval_rhs(OStepper& s, const double* y, double* fy, int fd_flag)
 {
    to_ghosted(s, y, s.phi_g);
    to_ghosted(s, y + s.N, s.c_g);
+   const bool quat = s.m.evolve_quat != 0;
+   if (quat)
+      for (int c = 0; c < 4; c++) {
+         std::vector<double> tmp(s.NG);
+         to_ghosted(s, y + (2 + c) * s.N, tmp);
+         std::copy(tmp.begin(), tmp.end(), s.q_g.begin() + c * s.NG);
+      }
    long nfail = 0;
    long its = orc_phase_concentrations(&s.m, temp_ptr(s), s.phi_g.data(),
                                        s.c_g.data(), s.clr.data(),
@@ -77,10 +88,21 @@ void eval_rhs(OStepper& s, const double* y, double* fy, int fd_flag)
       s.phi_lag = s.phi_g;
       s.cl_nf = s.cl;
       s.cs_nf = s.cs;
+      if (quat) {  // QuatIntegrator::computeQuatGradients, lagged in FD calls
+         s.q_lag = s.q_g;
+         orc_quat_grad_modulus(&s.m, s.q_lag.data(), s.ogm.data());
+      }
    }
-   orc_rhs_phase_conc(&s.m, s.phi_g.data(), nullptr, temp_ptr(s),
-                      s.cl.data(), s.cs.data(), s.phi_lag.data(), fy,
-                      fy + s.N);
+   orc_rhs_phase_conc_q(&s.m, s.phi_g.data(), nullptr, temp_ptr(s),
+                        s.cl.data(), s.cs.data(), s.phi_lag.data(),
+                        quat ? s.ogm.data() : nullptr, fy, fy + s.N);
+   if (quat) {
+      orc_quat_mobility(&s.m, s.phi_g.data(), s.mq.data());
+      orc_quat_face_coef(&s.m, s.phi_g.data(), temp_ptr(s), s.q_lag.data(),
+                         s.fcq[0].data(), s.fcq[1].data(), s.fcq[2].data());
+      orc_quat_rhs(&s.m, s.fcq[0].data(), s.fcq[1].data(), s.fcq[2].data(),
+                   s.mq.data(), s.q_g.data(), fy + 2 * s.N);
+   }
    s.st.rhs_evals++;
 }
 
@@ -88,11 +110,11 @@ double wrms(const OStepper& s, const double* v, const double* w)
 {
    double acc = 0.0;
    #pragma omp parallel for reduction(+ : acc) schedule(static)
-   for (long c = 0; c < 2 * s.N; c++) {
+   for (long c = 0; c < s.NY; c++) {
       const double x = v[c] * w[c];
       acc += x * x;
    }
-   return std::sqrt(acc / (double)(2 * s.N));
+   return std::sqrt(acc / (double)s.NY);
 }
 
 // PhaseFACOps::setOperatorCoefficients + ConcFACOps::setOperatorCoefficients
@@ -117,22 +139,36 @@ void precond_setup(OStepper& s, double gamma)
    orc_fac_set_operator(s.fac_conc, s.Dc[0].data(), s.Dc[1].data(),
                         L.dim == 3 ? s.Dc[2].data() : nullptr, 0.0, nullptr,
                         1.0, nullptr, s.m.conc_mobility);
+   if (s.m.evolve_quat) {
+      // QuatFACOps::setOperatorCoefficients: C = 1, M = M_q(phi),
+      // D = gamma fc (face coefficients of the lagged gradients)
+      orc_quat_mobility(&s.m, s.phi_g.data(), s.mq.data());
+      orc_fill_ghosts(&s.m, s.mq.data());
+      orc_quat_face_coef(&s.m, s.phi_g.data(), temp_ptr(s), s.q_lag.data(),
+                         s.Dq[0].data(), s.Dq[1].data(), s.Dq[2].data());
+      for (int d = 0; d < L.dim; d++)
+         for (auto& x : s.Dq[d]) x *= gamma;
+      orc_fac_set_operator(s.fac_quat, s.Dq[0].data(), s.Dq[1].data(),
+                           L.dim == 3 ? s.Dq[2].data() : nullptr, 0.0, nullptr,
+                           1.0, s.mq.data(), 0.0);
+   }
    s.st.precond_setups++;
 }
 
 void precond_solve(OStepper& s, const double* r, double* z, double delta)
 {
    if (s.p.precond == 0) {
-      std::copy(r, r + 2 * s.N, z);
+      std::copy(r, r + s.NY, z);
       return;
    }
    Layout L(s.m);
    std::vector<double> fg(s.NG, 0.0), ug(s.NG, 0.0);
-   for (int blk = 0; blk < 2; blk++) {
+   for (int blk = 0; blk < s.nb; blk++) {
       to_ghosted(s, r + blk * s.N, fg);
       double res;
-      int cyc = orc_fac_solve(blk == 0 ? s.fac_phi : s.fac_conc, &s.p,
-                              s.p.precond, fg.data(), ug.data(), delta, &res);
+      void* fac = blk == 0 ? s.fac_phi : (blk == 1 ? s.fac_conc : s.fac_quat);
+      int cyc = orc_fac_solve(fac, &s.p, s.p.precond, fg.data(), ug.data(),
+                              delta, &res);
       s.st.fac_cycles += cyc;
       from_ghosted(s, ug, z + blk * s.N);
    }
@@ -143,7 +179,7 @@ void precond_solve(OStepper& s, const double* r, double* z, double delta)
 void matvec(OStepper& s, const double* y, const double* fy, const double* w,
             double gamma, const double* v, double* out)
 {
-   const long n2 = 2 * s.N;
+   const long n2 = s.NY;
    const double sig = 1.0 / wrms(s, v, w);
    std::vector<double> yp(n2), fp(n2);
    for (long c = 0; c < n2; c++) yp[c] = y[c] + sig * v[c];
@@ -157,7 +193,7 @@ void matvec(OStepper& s, const double* y, const double* fy, const double* w,
 int gmres(OStepper& s, const double* y, const double* fy, const double* w,
           double gamma, const double* b, double* x, double tol)
 {
-   const long n2 = 2 * s.N;
+   const long n2 = s.NY;
    const int maxl = s.p.max_krylov;
    const double sqrtN = std::sqrt((double)n2);
    std::vector<std::vector<double>> V(maxl + 1, std::vector<double>(n2));
@@ -226,7 +262,7 @@ int gmres(OStepper& s, const double* y, const double* fy, const double* w,
 // Returns 0 on convergence, 1 on Newton failure.
 int bdf_step(OStepper& s, double h, int q, std::vector<double>& ynew)
 {
-   const long n2 = 2 * s.N;
+   const long n2 = s.NY;
    std::vector<double> a(n2), y(n2), fy(n2), b(n2), d(n2), w(n2);
    double gamma;
    if (q == 1) {
@@ -263,6 +299,9 @@ int bdf_step(OStepper& s, double h, int q, std::vector<double>& ynew)
       const double dcon = del * std::min(1.0, crate) / s.p.newton_coef;
       if (dcon <= 1.0) {
          ynew = y;
+         // projection of the accepted state (QuatIntegrator::applyProjection,
+         // QuatIntegrator.cc:3911-3940; project3d)
+         if (s.m.evolve_quat) orc_quat_project(s.N, ynew.data() + 2 * s.N);
          return 0;
       }
       if (it >= 1 && del > 2.0 * delp) break;
@@ -291,11 +330,25 @@ void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p)
    s->Dc[0].assign(L.nfx(), 0.0);
    s->Dc[1].assign(L.nfy(), 0.0);
    s->Dc[2].assign(L.dim == 3 ? L.nfz() : 1, 0.0);
-   s->yn.assign(2 * s->N, 0.0);
-   s->ynm1.assign(2 * s->N, 0.0);
+   s->nb = m->evolve_quat ? 6 : 2;
+   s->NY = s->nb * s->N;
+   s->yn.assign(s->NY, 0.0);
+   s->ynm1.assign(s->NY, 0.0);
    const int nl = p->precond == 2 ? p->mg_levels : 1;
    s->fac_phi = orc_fac_create(m, nl);
    s->fac_conc = orc_fac_create(m, nl);
+   if (m->evolve_quat) {
+      s->q_g.assign(4 * s->NG, 0.0);
+      s->q_lag.assign(4 * s->NG, 0.0);
+      s->ogm.assign(s->N, 0.0);
+      s->mq.assign(s->NG, 0.0);
+      const long nf[3] = {L.nfx(), L.nfy(), L.dim == 3 ? L.nfz() : 1};
+      for (int d = 0; d < 3; d++) {
+         s->fcq[d].assign(nf[d], 0.0);
+         s->Dq[d].assign(nf[d], 0.0);
+      }
+      s->fac_quat = orc_fac_create(m, nl);
+   }
    return s;
 }
 
@@ -304,6 +357,7 @@ void orc_stepper_destroy(void* h)
    OStepper* s = (OStepper*)h;
    orc_fac_destroy(s->fac_phi);
    orc_fac_destroy(s->fac_conc);
+   if (s->fac_quat) orc_fac_destroy(s->fac_quat);
    delete s;
 }
 
@@ -314,6 +368,10 @@ void orc_stepper_set_state(void* h, const double* phi, const double* conc,
    OStepper* s = (OStepper*)h;
    std::copy(phi, phi + s->N, s->yn.begin());
    std::copy(conc, conc + s->N, s->yn.begin() + s->N);
+   if (s->m.evolve_quat)  // default orientation (1,0,0,0) until set_quat
+      for (int c = 0; c < 4; c++)
+         std::fill(s->yn.begin() + (2 + c) * s->N, s->yn.begin() + (3 + c) * s->N,
+                   c == 0 ? 1.0 : 0.0);
    s->ynm1 = s->yn;
    to_ghosted(*s, cl ? cl : conc, s->clr);
    to_ghosted(*s, cs ? cs : conc, s->csr);
@@ -332,19 +390,42 @@ void orc_stepper_get_state(void* h, double* phi, double* conc, double* cl,
 {
    OStepper* s = (OStepper*)h;
    if (phi) std::copy(s->yn.begin(), s->yn.begin() + s->N, phi);
-   if (conc) std::copy(s->yn.begin() + s->N, s->yn.end(), conc);
+   if (conc) std::copy(s->yn.begin() + s->N, s->yn.begin() + 2 * s->N, conc);
    if (cl) from_ghosted(*s, s->clr, cl);
    if (cs) from_ghosted(*s, s->csr, cs);
+}
+
+void orc_stepper_set_quat(void* h, const double* q)
+{
+   OStepper* s = (OStepper*)h;
+   if (!s->m.evolve_quat) return;
+   std::copy(q, q + 4 * s->N, s->yn.begin() + 2 * s->N);
+   std::copy(q, q + 4 * s->N, s->ynm1.begin() + 2 * s->N);
+}
+
+void orc_stepper_get_quat(void* h, double* q)
+{
+   OStepper* s = (OStepper*)h;
+   if (s->m.evolve_quat) std::copy(s->yn.begin() + 2 * s->N, s->yn.end(), q);
 }
 
 void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs)
 {
    OStepper* s = (OStepper*)h;
-   std::vector<double> fy(2 * s->N);
+   std::vector<double> fy(s->NY);
    eval_rhs(*s, s->yn.data(), fy.data(), 0);
    std::copy(fy.begin(), fy.begin() + s->N, phi_rhs);
-   std::copy(fy.begin() + s->N, fy.end(), conc_rhs);
+   std::copy(fy.begin() + s->N, fy.begin() + 2 * s->N, conc_rhs);
 }
+
+// f(y_n) over the whole state vector (NY doubles)
+void orc_stepper_eval_rhs_full(void* h, double* out)
+{
+   OStepper* s = (OStepper*)h;
+   eval_rhs(*s, s->yn.data(), out, 0);
+}
+
+long orc_stepper_size(void* h) { return ((OStepper*)h)->NY; }
 
 // Advance nsteps accepted steps.  Returns 0, or 1 if a step failed after
 // max_retries step-size halvings.
@@ -394,7 +475,7 @@ void orc_stepper_jv(void* h, const double* v, double gamma, double* out,
                     int analytic)
 {
    OStepper* s = (OStepper*)h;
-   const long n2 = 2 * s->N;
+   const long n2 = s->NY;
    std::vector<double> fy(n2), w(n2);
    eval_rhs(*s, s->yn.data(), fy.data(), 0);
    for (long c = 0; c < n2; c++)

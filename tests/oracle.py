@@ -72,6 +72,15 @@ def lib():
             "orc_stepper_eval_rhs": (None, [P, P, P]),
             "orc_stepper_advance": (I, [P, I, C.POINTER(abi.StepStats)]),
             "orc_stepper_jv": (None, [P, P, D, P, I]),
+            "orc_stepper_set_quat": (None, [P, P]),
+            "orc_stepper_get_quat": (None, [P, P]),
+            "orc_quat_grad_modulus": (None, [MP, P, P]),
+            "orc_quat_mobility": (None, [MP, P, P]),
+            "orc_quat_face_coef": (None, [MP, P, P, P, P, P, P]),
+            "orc_quat_rhs": (None, [MP, P, P, P, P, P, P]),
+            "orc_stepper_eval_rhs_full": (None, [P, P]),
+            "orc_stepper_size": (C.c_long, [P]),
+            "orc_rhs_phase_conc_q": (None, [MP, P, P, P, P, P, P, P, P, P]),
             "orc_jv_analytic": (None, [MP, P, P, P, P, D, P]),
         }
         for name, (res, args) in protos.items():
@@ -109,6 +118,15 @@ class OracleStepper:
              for x in (phi, c, cl, cs, temp)]
         self.L.orc_stepper_set_state(self.h, *[ptr(x) for x in a])
 
+    def set_quat(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        self.L.orc_stepper_set_quat(self.h, ptr(q))
+
+    def get_quat(self):
+        q = np.empty((4,) + tuple(self.model.interior_shape()))
+        self.L.orc_stepper_get_quat(self.h, ptr(q))
+        return q
+
     def get_state(self):
         out = [np.empty(self.n) for _ in range(4)]
         self.L.orc_stepper_get_state(self.h, *[ptr(x) for x in out])
@@ -120,6 +138,11 @@ class OracleStepper:
         self.L.orc_stepper_eval_rhs(self.h, ptr(fp), ptr(fc))
         shp = self.model.interior_shape()
         return fp.reshape(shp), fc.reshape(shp)
+
+    def eval_rhs_full(self):
+        out = np.empty(self.L.orc_stepper_size(self.h))
+        self.L.orc_stepper_eval_rhs_full(self.h, ptr(out))
+        return out
 
     def jv(self, v, gamma, analytic):
         v = np.ascontiguousarray(v, dtype=np.float64).ravel()
