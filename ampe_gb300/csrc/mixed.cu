@@ -16,9 +16,15 @@
 //                the diffusivities held fixed as the reference's
 //                finite-difference products hold them, QuatIntegrator.cc:
 //                3189, 3262-3263), in FP32.
+//  k_quat_cells_f32 / k_quat_faces_f32 / k_jv_quat
+//                the quaternion equation of evolve_quat models in FP32:
+//                |grad q|, M_q, the face coefficients and their phi
+//                derivative, and the q rows of the Jacobian-vector product
+//                (gradients lagged as in the finite-difference products).
 #include "common.cuh"
 #include "mixed.cuh"
 #include "phase_flux.cuh"
+#include "quat.cuh"
 
 namespace ampe {
 
@@ -268,6 +274,16 @@ MixParams make_mix_params(const ampe_model_t& m)
    p.ivm = (float)m.inv_molar_volume[1];
    p.tdep = (m.Q_liquid != 0.0 || m.Q_solid != 0.0) ? 1 : 0;
    p.iso = iso ? 1 : 0;
+   p.misor = (float)m.misorientation_factor;
+   p.eq2h = (float)(0.5 * m.epsilon_q * m.epsilon_q);
+   p.epsq2 = (float)(m.epsilon_q * m.epsilon_q);
+   p.qM = (float)m.quat_mobility;
+   p.qMmin = (float)m.min_quat_mobility;
+   p.qfloor2 = (float)(m.quat_grad_floor * m.quat_grad_floor);
+   p.qmaxi = m.quat_grad_floor > 0.0 ? (float)(1.0 / m.quat_grad_floor) : 0.f;
+   p.T0 = (float)m.T0;
+   p.gdx = (float)(m.gradT * m.dx[0]);
+   p.qfloor = m.quat_floor_type;
    return p;
 }
 
@@ -316,6 +332,19 @@ __device__ __forceinline__ void face_diff(const ampe_model_t& m,
    DS = hphi * dsq;
 }
 
+// temperature of cell (i,j,k) in FP32 (ghost cells take their periodic image)
+__device__ __forceinline__ float temp_f(const ampe_model_t& m, const MixParams& mp,
+                                        const Grid& g, const double* tfield, int i,
+                                        int j, int k)
+{
+   if (m.temp_mode == AMPE_TEMP_CONSTANT) return mp.T0;
+   if (m.temp_mode == AMPE_TEMP_GRADIENT) {
+      const int iw = i < 0 ? i + g.n0 : (i >= g.n0 ? i - g.n0 : i);
+      return mp.T0 + mp.gdx * ((float)iw + 0.5f);
+   }
+   return (float)tfield[g.c(i, j, k)];
+}
+
 __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -327,7 +356,7 @@ template <int DIM>
 __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
                             const double* tfield, const float* pf,
                             const float* cl, const float* cs, const float* dF,
-                            double* phi_rhs, double* conc_rhs)
+                            const float* ogm, double* phi_rhs, double* conc_rhs)
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
@@ -355,6 +384,12 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
       }
       const float p = pf[c];
       float r = diff - mp.w * deriv_well_func(p, m.well_type);
+      if (ogm) {  // orientation term, 3d/quatrhs.m4:481-509
+         const float gm = ogm[t];
+         const float T = temp_f(m, mp, g, tfield, i, j, k);
+         r = r - mp.misor * T * deriv_interp_func(p, m.orient_interp1) * gm -
+             deriv_interp_func(p, m.orient_interp2) * mp.eq2h * gm * gm;
+      }
       r += deriv_interp_func(p, m.energy_interp) * dF[t];
       phi_rhs[t] = (double)(r * mp.Mphi);
       conc_rhs[t] = (double)(mp.Mc * div);
@@ -364,7 +399,7 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
 int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield, const double* phi, float* pf,
               const float* cl, const float* cs, const float* dF,
-              double* phi_rhs, double* conc_rhs, cudaStream_t s)
+              const float* ogm, double* phi_rhs, double* conc_rhs, cudaStream_t s)
 {
    long long b = (g.cells_ghost() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
@@ -373,11 +408,11 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    b = (g.cells() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
    if (g.dim == 3)
-      k_rhs_mixed<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, phi_rhs,
-                                                 conc_rhs);
+      k_rhs_mixed<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, ogm,
+                                                 phi_rhs, conc_rhs);
    else
-      k_rhs_mixed<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, phi_rhs,
-                                                 conc_rhs);
+      k_rhs_mixed<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, ogm,
+                                                 phi_rhs, conc_rhs);
    return launch_status();
 }
 
@@ -389,9 +424,9 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
                            const double* tfield, const float* pf,
                            const float* cl, const float* cs, const double* v,
-                           float* dphi, float* da, float* db)
+                           float* dphi, float* da, float* db, float* dq)
 {
-   const long long N = g.cells();
+   const long long N = g.cells(), NG = g.cells_ghost();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
         t += (long long)gridDim.x * blockDim.x) {
       const int i = (int)(t % g.n0);
@@ -416,6 +451,15 @@ __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
          da[idx] = xa;
          db[idx] = xb;
       });
+      if (dq) {
+#pragma unroll
+         for (int q = 0; q < 4; q++) {
+            const float x = (float)v[t + (2 + q) * N];
+            float* dqq = dq + q * NG;
+            dqq[c] = x;
+            for_each_image(g, i, j, k, [&](long long idx) { dqq[idx] = x; });
+         }
+      }
    }
 }
 
@@ -434,7 +478,21 @@ __device__ __forceinline__ float second_deriv_interp_f(float phi, char type)
       case 'w':
          p = phi > 0.f ? phi : 0.f;
          return 4.f - 6.f * p;
-      default:
+      case '3':
+         p = phi > 0.f ? phi : 0.f;
+         return 6.f * p;
+      case 'm': {
+         p = clamp01(phi);
+         const float t = 2.f * p * (p - 1.f) + 1.f;
+         return 2.f * (1.f - 2.f * p) / (t * t) -
+                4.f * p * (1.f - p) * (4.f * p - 2.f) / (t * t * t);
+      }
+      case 's': {
+         p = phi > 0.f ? phi : 0.f;
+         const float th = tanhf(10.f * p);
+         return 100.f * (1.f - th * th) / logf(coshf(10.f));
+      }
+      default:  // 'l', 'c': piecewise linear / constant
          return 0.f;
    }
 }
@@ -446,7 +504,7 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
                              const float* pf, const float* cl, const float* cs,
                              const float* dF, const float* dphi,
                              const float* da, const float* db, const double* v,
-                             double gamma, double* out)
+                             const float* ogm, double gamma, double* out)
 {
    const long long N = g.cells();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
@@ -477,7 +535,16 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
       // d(dF)/db = -f_S''(b) (a - b), d(dF)/da = muL - muS = 0
       const float fS2 = tf.RT / (b * (1.f - b)) + dxi_f(tf, b, 1);
       const float ddF = -fS2 * (a - b) * mp.ivm * db[c];
-      const float jp = mp.Mphi * (diff - mp.w * second_deriv_well_func(p, m.well_type) * vp +
+      float orient = 0.f;
+      if (ogm) {  // phi-derivative of the orientation term at lagged |grad q|
+         const float gm = ogm[t];
+         const float T = temp_f(m, mp, g, tfield, i, j, k);
+         orient = (mp.misor * T * second_deriv_interp_f(p, m.orient_interp1) * gm +
+                   second_deriv_interp_f(p, m.orient_interp2) * mp.eq2h * gm * gm) *
+                  vp;
+      }
+      const float jp = mp.Mphi * (diff - mp.w * second_deriv_well_func(p, m.well_type) * vp -
+                                  orient +
                                   second_deriv_interp_f(p, m.energy_interp) * dF[t] * vp +
                                   deriv_interp_func(p, m.energy_interp) * ddF);
       const float jc = mp.Mc * div;
@@ -486,22 +553,194 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
    }
 }
 
+// ---------------------------------------------------------------------------
+// quaternion equation, FP32
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_quat_cells_f32(MixParams mp, Grid g, const double* phi,
+                                 const float* q, float* ogm, float* mq)
+{
+   const long long qs = g.cells_ghost();
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long c = g.c(i, j, k);
+      const long long st[3] = {1, g.sx, g.sy};
+      float s = 0.f;
+#pragma unroll
+      for (int d = 0; d < DIM; d++)
+#pragma unroll
+         for (int comp = 0; comp < 4; comp++) {
+            const float* qc = q + comp * qs;
+            const float a = mp.dxi[d] * (qc[c] - qc[c - st[d]]);
+            const float b = mp.dxi[d] * (qc[c + st[d]] - qc[c]);
+            s += a * a + b * b;
+         }
+      ogm[t] = sqrtf(0.5f * s);
+      mq[c] = mp.qMmin + (mp.qM - mp.qMmin) * (1.f - interp_func((float)phi[c], 'p'));
+   }
+}
+
+struct FacePtrs {
+   float* fc[3];
+   float* dfc[3];
+};
+
+template <int DIM>
+__global__ void k_quat_faces_f32(ampe_model_t m, MixParams mp, Grid g,
+                                 const double* tfield, const float* pf,
+                                 const float* q, float scale, FacePtrs f)
+{
+   const long long tot = g.nfx() + g.nfy() + (DIM == 3 ? g.nfz() : 0);
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      face_of(g, t, dir, i, j, k);
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const float phia = average_func(pf[g.c(i - ei, j - ej, k - ek)], pf[g.c(i, j, k)],
+                                      m.avg_type);
+      const float tempa = 0.5f * (temp_f(m, mp, g, tfield, i - ei, j - ej, k - ek) +
+                                  temp_f(m, mp, g, tfield, i, j, k));
+      const float g2 = face_grad_norm2<DIM, float>(g, mp.dxi, q, dir, i, j, k);
+      const float gni = eval_grad_normi(g2, mp.qfloor, mp.qfloor2, mp.qmaxi);
+      const float a1 = gni * mp.misor * tempa;
+      const float v = scale * (-a1 * interp_func(phia, m.orient_interp1) -
+                               mp.epsq2 * interp_func(phia, m.orient_interp2));
+      const long long fi = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+      f.fc[dir][fi] = v;
+      if (f.dfc[0])
+         f.dfc[dir][fi] = -a1 * deriv_interp_func(phia, m.orient_interp1) -
+                          mp.epsq2 * deriv_interp_func(phia, m.orient_interp2);
+   }
+}
+
+// derivative of the face average of phi along (da, db)
+__device__ __forceinline__ float d_average_f(float a, float b, float da, float db,
+                                             char type)
+{
+   if (type == 'a') return 0.5f * (da + db);
+   if (a < 1.0e-16f || b < 1.0e-16f) return 0.f;  // harmonic
+   const float s = a + b;
+   return 2.f * (b * b * da + a * a * db) / (s * s);
+}
+
+// q rows of v - gamma J v:
+//   J_q dq = -M_q div(fc grad dq) - dM_q div(fc grad q) - M_q div(dfc grad q)
+// with dM_q = M_q'(phi) dphi and dfc = (d fc / d phibar) dphibar at each face
+template <int DIM>
+__global__ void k_jv_quat(ampe_model_t m, MixParams mp, Grid g, const float* pf,
+                          const float* dphi, QuatF32 qf, const double* v,
+                          double gamma, double* out)
+{
+   const long long N = g.cells(), qs = g.cells_ghost();
+   const float gm = (float)gamma;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
+        t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      const long long c = g.c(i, j, k);
+      const long long st[3] = {1, g.sx, g.sy};
+      // per face (d, side): fc, and dfc * dphibar
+      float F[3][2], dF[3][2];
+#pragma unroll
+      for (int d = 0; d < DIM; d++)
+#pragma unroll
+         for (int side = 0; side < 2; side++) {
+            const int ii = i + (d == 0 ? side : 0), jj = j + (d == 1 ? side : 0),
+                      kk = k + (d == 2 ? side : 0);
+            const long long fi = d == 0 ? g.fx(ii, jj, kk)
+                                        : (d == 1 ? g.fy(ii, jj, kk) : g.fz(ii, jj, kk));
+            const long long up = c + side * st[d], lo = up - st[d];
+            F[d][side] = qf.fc[d][fi];
+            dF[d][side] = qf.dfc[d][fi] *
+                          d_average_f(pf[lo], pf[up], dphi[lo], dphi[up], m.avg_type);
+         }
+      const float p = pf[c];
+      const float mqc = qf.mq[c];
+      const float dmq = -(mp.qM - mp.qMmin) * deriv_interp_func(p, 'p') * dphi[c];
+#pragma unroll
+      for (int comp = 0; comp < 4; comp++) {
+         const float* qc = qf.q + comp * qs;
+         const float* dqc = qf.dq + comp * qs;
+         float A = 0.f, B = 0.f, Cc = 0.f;
+#pragma unroll
+         for (int d = 0; d < DIM; d++) {
+            const float h = mp.dxi[d];
+            const float gqm = h * (qc[c] - qc[c - st[d]]), gqp = h * (qc[c + st[d]] - qc[c]);
+            const float gdm = h * (dqc[c] - dqc[c - st[d]]),
+                        gdp = h * (dqc[c + st[d]] - dqc[c]);
+            A += h * (F[d][1] * gdp - F[d][0] * gdm);
+            B += h * (F[d][1] * gqp - F[d][0] * gqm);
+            Cc += h * (dF[d][1] * gqp - dF[d][0] * gqm);
+         }
+         const float jq = -(mqc * (A + Cc) + dmq * B);
+         const long long o = t + (2 + comp) * N;
+         out[o] = v[o] - (double)(gm * jq);
+      }
+   }
+}
+
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf, const double* tfield, const float* pf,
              const float* cl, const float* cs, const float* dF, const double* v,
-             double gamma, float* dphi, float* da, float* db, double* out,
-             cudaStream_t s)
+             double gamma, float* dphi, float* da, float* db, const QuatF32* qf,
+             double* out, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
-   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da, db);
+   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da, db,
+                                          qf ? qf->dq : nullptr);
    launch_status();
+   const float* ogm = (qf && m.with_orient) ? qf->ogm : nullptr;
    if (g.dim == 3)
       k_jv_stencil<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
-                                                  da, db, v, gamma, out);
+                                                  da, db, v, ogm, gamma, out);
    else
       k_jv_stencil<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
-                                                  da, db, v, gamma, out);
+                                                  da, db, v, ogm, gamma, out);
+   int rc = launch_status();
+   if (qf && !rc) {
+      if (g.dim == 3)
+         k_jv_quat<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, pf, dphi, *qf, v, gamma, out);
+      else
+         k_jv_quat<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, pf, dphi, *qf, v, gamma, out);
+      rc = launch_status();
+   }
+   return rc;
+}
+
+int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                   const double* phi, QuatF32& qf, cudaStream_t s)
+{
+   long long b = (g.cells() + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   if (g.dim == 3)
+      k_quat_cells_f32<3><<<(unsigned)b, 256, 0, s>>>(mp, g, phi, qf.q, qf.ogm, qf.mq);
+   else
+      k_quat_cells_f32<2><<<(unsigned)b, 256, 0, s>>>(mp, g, phi, qf.q, qf.ogm, qf.mq);
+   return launch_status();
+}
+
+int quat_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                   const double* tfield, const float* pf, const float* q,
+                   double scale, float* const fc[3], float* const dfc[3],
+                   cudaStream_t s)
+{
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   long long b = (tot + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   FacePtrs f;
+   for (int d = 0; d < 3; d++) {
+      f.fc[d] = fc[d];
+      f.dfc[d] = dfc ? dfc[d] : nullptr;
+   }
+   if (g.dim == 3)
+      k_quat_faces_f32<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, q, (float)scale, f);
+   else
+      k_quat_faces_f32<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, q, (float)scale, f);
    return launch_status();
 }
 

@@ -19,6 +19,23 @@ struct MixParams {
    float flux_dinv[3]; // eps^2/dx (simple) or eps^2/(12 dx) (isotropic)
    float w, Mphi, Mc, Dl, Ds, qlR, qsR, ivm;
    int tdep, iso;
+   // orientation term and quaternion equation
+   float misor;        // 2H
+   float eq2h, epsq2;  // eps_q^2 / 2, eps_q^2
+   float qM, qMmin;    // M_q scale and floor
+   float qfloor2, qmaxi;  // grad floor^2, 1/floor
+   float T0, gdx;      // T = T0 (+ gdx (i + 1/2) for a gradient along x)
+   char qfloor;        // eval_grad_normi type
+};
+
+// FP32 working set of the quaternion equation in the mixed path
+struct QuatF32 {
+   float* q = nullptr;    // ghosted q, 4 components
+   float* dq = nullptr;   // ghosted q-part of a Jv direction, 4 components
+   float* ogm = nullptr;  // |grad q| at cells (interior)
+   float* mq = nullptr;   // M_q(phi) (ghosted layout)
+   float* fc[3] = {nullptr, nullptr, nullptr};   // face coefficients
+   float* dfc[3] = {nullptr, nullptr, nullptr};  // d fc / d phibar
 };
 MixParams make_mix_params(const ampe_model_t& m);
 int kks_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
@@ -30,12 +47,24 @@ int kks_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield,
               const double* phi, float* pf, const float* cl, const float* cs,
-              const float* dF, double* phi_rhs, double* conc_rhs,
-              cudaStream_t s);
+              const float* dF, const float* ogm, double* phi_rhs,
+              double* conc_rhs, cudaStream_t s);
+// out = v - gamma J v; qf (null without quaternions) adds the q rows and
+// the orientation term of the phase row
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf,
              const double* tfield, const float* pf, const float* cl,
              const float* cs, const float* dF, const double* v, double gamma,
-             float* dphi, float* da, float* db, double* out, cudaStream_t s);
+             float* dphi, float* da, float* db, const QuatF32* qf, double* out,
+             cudaStream_t s);
+// |grad q| (from qf.q) and M_q(phi) at cells
+int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                   const double* phi, QuatF32& qf, cudaStream_t s);
+// fc = scale (-grad_normi 2H T p1 - eps_q^2 p2) into fc[], and (when dfc is
+// non-null) d fc / d phibar at scale 1
+int quat_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                   const double* tfield, const float* pf, const float* q,
+                   double scale, float* const fc[3], float* const dfc[3],
+                   cudaStream_t s);
 
 }  // namespace ampe

@@ -9,78 +9,33 @@
 //   k_quat_rhs           COMPUTE_FLUX3D + ADD_QUAT_OP3D (3d/quatfacops.m4:227-311,
 //                        596-657): q' = -M_q div(fc grad q)
 //   k_quat_project       PROJECT3D (3d/quatfacops.m4:1022-1075) on the state
+// The FP32 face coefficients of the mixed path live in mixed.cu.
 #include "common.cuh"
 #include "quat.cuh"
 
 namespace ampe {
 
-__device__ __forceinline__ double eval_grad_normi(double g2, char type,
-                                                  double floor2, double maxi)
-{
-   if (type == 'm') return g2 > floor2 ? pow(g2, -0.5) : maxi;
-   if (type == 't') {
-      const double gng2 = g2 * maxi * maxi;
-      if (gng2 > 0.01) {
-         const double gn = sqrt(g2);
-         return tanh(maxi * gn) / gn;
-      }
-      return maxi * (1.0 - gng2 * (5.0 - 2.0 * gng2) / 15.0);
-   }
-   return pow(g2 + floor2, -0.5);
-}
-
-template <class R>
-__device__ __forceinline__ R face_grad_norm2(const Grid& g, const double* dx,
-                                             const R* q, int dir, int i,
-                                             int j, int k)
+template <int DIM, class R>
+__global__ void k_quat_grad_modulus(Grid g, Inv3<R> dinv, const R* q, R* ogm)
 {
    const long long qs = g.cells_ghost();
-   const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
-   R gsum[3][4];
-   for (int m = 0; m < 4; m++) {
-      const R* Q = q + m * qs;
-      for (int n = 0; n < g.dim; n++) {
-         const R dinv = (R)(1.0 / dx[n]);
-         if (n == dir) {
-            gsum[n][m] = dinv * (Q[g.c(i, j, k)] - Q[g.c(i - ei, j - ej, k - ek)]);
-            continue;
-         }
-         const int fi = n == 0, fj = n == 1, fk = n == 2;
-         auto D = [&](int a, int b, int c) {
-            return Q[g.c(a, b, c)] - Q[g.c(a - fi, b - fj, c - fk)];
-         };
-         const R p25 = (R)0.25 * dinv;
-         gsum[n][m] = p25 * (D(i - ei + fi, j - ej + fj, k - ek + fk) + D(i - ei, j - ej, k - ek) +
-                             D(i + fi, j + fj, k + fk) + D(i, j, k));
-      }
-   }
-   R s = 0;
-   for (int n = 0; n < g.dim; n++)
-      for (int m = 0; m < 4; m++) s += gsum[n][m] * gsum[n][m];
-   return s;
-}
-
-template <class R>
-__global__ void k_quat_grad_modulus(Grid g, double dx0, double dx1, double dx2,
-                                    const R* q, R* ogm)
-{
-   const long long qs = g.cells_ghost();
-   const double dxs[3] = {dx0, dx1, dx2};
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       const int i = (int)(t % g.n0);
       const int j = (int)((t / g.n0) % g.n1);
       const int k = (int)(t / ((long long)g.n0 * g.n1));
       R s = 0;
-      for (int d = 0; d < g.dim; d++) {
+#pragma unroll
+      for (int d = 0; d < DIM; d++) {
          const int ei = d == 0, ej = d == 1, ek = d == 2;
-         const R dinv = (R)(1.0 / dxs[d]);
+#pragma unroll
          for (int side = 0; side < 2; side++)
+#pragma unroll
             for (int c = 0; c < 4; c++) {
                const R* qc = q + c * qs;
-               const R gd = dinv * (qc[g.c(i + side * ei, j + side * ej, k + side * ek)] -
-                                    qc[g.c(i + side * ei - ei, j + side * ej - ej,
-                                           k + side * ek - ek)]);
+               const R gd = dinv.v[d] * (qc[g.c(i + side * ei, j + side * ej, k + side * ek)] -
+                                         qc[g.c(i + side * ei - ei, j + side * ej - ej,
+                                                k + side * ek - ek)]);
                s += gd * gd;
             }
       }
@@ -105,37 +60,20 @@ __global__ void k_quat_mobility(Grid g, double mmin, double mscale,
    }
 }
 
-template <class QT, class R>
-__global__ void k_quat_face_coef(ampe_model_t m, Grid g, const double* phi,
-                                 const double* tfield, const QT* qlag,
-                                 double scale, R* fc0, R* fc1, R* fc2)
+template <int DIM>
+__global__ void k_quat_face_coef(ampe_model_t m, Grid g, Inv3<double> dinv,
+                                 const double* phi, const double* tfield,
+                                 const double* qlag, double scale, double* fc0,
+                                 double* fc1, double* fc2)
 {
    const double floor2 = m.quat_grad_floor * m.quat_grad_floor;
    const double maxi = 1.0 / m.quat_grad_floor;
    const double eps2 = m.epsilon_q * m.epsilon_q;
-   const long long nx = g.nfx(), ny = g.nfy();
-   const long long nz = g.dim == 3 ? g.nfz() : 0;
-   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-        t < nx + ny + nz; t += (long long)gridDim.x * blockDim.x) {
+   const long long tot = g.nfx() + g.nfy() + (DIM == 3 ? g.nfz() : 0);
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
       int dir, i, j, k;
-      long long r = t;
-      if (r < nx) {
-         dir = 0;
-         i = (int)(r % (g.n0 + 1));
-         j = (int)((r / (g.n0 + 1)) % g.n1);
-         k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
-      } else if ((r -= nx) < ny) {
-         dir = 1;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % (g.n1 + 1));
-         k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
-      } else {
-         r -= ny;
-         dir = 2;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % g.n1);
-         k = (int)(r / ((long long)g.n0 * g.n1));
-      }
+      face_of(g, t, dir, i, j, k);
       const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
       const double phia = average_func(phi[g.c(i - ei, j - ej, k - ek)], phi[g.c(i, j, k)],
                                        m.avg_type);
@@ -143,40 +81,47 @@ __global__ void k_quat_face_coef(ampe_model_t m, Grid g, const double* phi,
                                   temperature_at(m, g, tfield, i, j, k));
       const double diff = m.misorientation_factor * tempa * interp_func(phia, m.orient_interp1);
       const double hphi2 = interp_func(phia, m.orient_interp2);
-      const double g2 = (double)face_grad_norm2<QT>(g, m.dx, qlag, dir, i, j, k);
+      const double g2 = face_grad_norm2<DIM, double>(g, dinv.v, qlag, dir, i, j, k);
       const double gni = eval_grad_normi(g2, m.quat_floor_type, floor2, maxi);
-      const R v = (R)(scale * (-gni * diff - eps2 * hphi2));
+      const double v = scale * (-gni * diff - eps2 * hphi2);
       if (dir == 0) fc0[g.fx(i, j, k)] = v;
       if (dir == 1) fc1[g.fy(i, j, k)] = v;
       if (dir == 2) fc2[g.fz(i, j, k)] = v;
    }
 }
 
-template <class R>
-__global__ void k_quat_rhs(Grid g, double dx0, double dx1, double dx2,
-                           const R* fc0, const R* fc1, const R* fc2,
-                           const R* mq, const R* q, double* out)
+template <int DIM, class R>
+__global__ void k_quat_rhs(Grid g, Inv3<R> hinv, const R* fc0, const R* fc1,
+                           const R* fc2, const R* mq, const R* q, double* out)
 {
    const long long qs = g.cells_ghost(), N = g.cells();
-   const R hinv[3] = {(R)(1.0 / dx0), (R)(1.0 / dx1), g.dim == 3 ? (R)(1.0 / dx2) : (R)0};
-   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4 * N;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
         t += (long long)gridDim.x * blockDim.x) {
-      const int c = (int)(t / N);
-      const long long tt = t - c * N;
-      const int i = (int)(tt % g.n0);
-      const int j = (int)((tt / g.n0) % g.n1);
-      const int k = (int)(tt / ((long long)g.n0 * g.n1));
-      const R* qc = q + c * qs;
-      auto flux = [&](int dir, int a, int b, int cc) {
-         const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
-         const R f = dir == 0 ? fc0[g.fx(a, b, cc)]
-                              : (dir == 1 ? fc1[g.fy(a, b, cc)] : fc2[g.fz(a, b, cc)]);
-         return f * hinv[dir] * (qc[g.c(a, b, cc)] - qc[g.c(a - ei, b - ej, cc - ek)]);
-      };
-      R div = (flux(0, i + 1, j, k) - flux(0, i, j, k)) * hinv[0] +
-              (flux(1, i, j + 1, k) - flux(1, i, j, k)) * hinv[1];
-      if (g.dim == 3) div = div + (flux(2, i, j, k + 1) - flux(2, i, j, k)) * hinv[2];
-      out[c * N + tt] = (double)((R)0 - mq[g.c(i, j, k)] * div);
+      const int i = (int)(t % g.n0);
+      const int j = (int)((t / g.n0) % g.n1);
+      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      // the six face coefficients are shared by the four components
+      const R fxm = fc0[g.fx(i, j, k)], fxp = fc0[g.fx(i + 1, j, k)];
+      const R fym = fc1[g.fy(i, j, k)], fyp = fc1[g.fy(i, j + 1, k)];
+      R fzm = 0, fzp = 0;
+      if (DIM == 3) {
+         fzm = fc2[g.fz(i, j, k)];
+         fzp = fc2[g.fz(i, j, k + 1)];
+      }
+      const long long cc = g.c(i, j, k);
+      const R mqc = mq[cc];
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+         const R* qc = q + c * qs;
+         const R q0 = qc[cc];
+         auto flux = [&](R f, int dir, R qa, R qb) { return f * hinv.v[dir] * (qa - qb); };
+         R div = (flux(fxp, 0, qc[cc + 1], q0) - flux(fxm, 0, q0, qc[cc - 1])) * hinv.v[0] +
+                 (flux(fyp, 1, qc[cc + g.sx], q0) - flux(fym, 1, q0, qc[cc - g.sx])) * hinv.v[1];
+         if (DIM == 3)
+            div = div + (flux(fzp, 2, qc[cc + g.sy], q0) - flux(fzm, 2, q0, qc[cc - g.sy])) *
+                            hinv.v[2];
+         out[c * N + t] = (double)((R)0 - mqc * div);
+      }
    }
 }
 
@@ -202,7 +147,11 @@ template <class R>
 int quat_grad_modulus(const ampe_model_t& m, const Grid& g, const R* q, R* ogm,
                       cudaStream_t s)
 {
-   k_quat_grad_modulus<R><<<nb(g.cells()), 256, 0, s>>>(g, m.dx[0], m.dx[1], m.dx[2], q, ogm);
+   const Inv3<R> dinv = inv_spacing<R>(m);
+   if (g.dim == 3)
+      k_quat_grad_modulus<3, R><<<nb(g.cells()), 256, 0, s>>>(g, dinv, q, ogm);
+   else
+      k_quat_grad_modulus<2, R><<<nb(g.cells()), 256, 0, s>>>(g, dinv, q, ogm);
    return launch_status();
 }
 
@@ -215,13 +164,18 @@ int quat_mobility(const ampe_model_t& m, const Grid& g, const double* phi, R* mq
    return launch_status();
 }
 
-template <class QT, class R>
 int quat_face_coef(const ampe_model_t& m, const Grid& g, const double* phi,
-                   const double* tfield, const QT* qlag, double scale, R* fc0,
-                   R* fc1, R* fc2, cudaStream_t s)
+                   const double* tfield, const double* qlag, double scale,
+                   double* fc0, double* fc1, double* fc2, cudaStream_t s)
 {
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
-   k_quat_face_coef<QT, R><<<nb(tot), 256, 0, s>>>(m, g, phi, tfield, qlag, scale, fc0, fc1, fc2);
+   const Inv3<double> dinv = inv_spacing<double>(m);
+   if (g.dim == 3)
+      k_quat_face_coef<3><<<nb(tot), 256, 0, s>>>(m, g, dinv, phi, tfield, qlag, scale, fc0,
+                                                  fc1, fc2);
+   else
+      k_quat_face_coef<2><<<nb(tot), 256, 0, s>>>(m, g, dinv, phi, tfield, qlag, scale, fc0,
+                                                  fc1, fc2);
    return launch_status();
 }
 
@@ -229,8 +183,11 @@ template <class R>
 int quat_rhs(const ampe_model_t& m, const Grid& g, const R* fc0, const R* fc1,
              const R* fc2, const R* mq, const R* q, double* out, cudaStream_t s)
 {
-   k_quat_rhs<R><<<nb(4 * g.cells()), 256, 0, s>>>(g, m.dx[0], m.dx[1], m.dx[2], fc0, fc1,
-                                                   fc2, mq, q, out);
+   const Inv3<R> hinv = inv_spacing<R>(m);
+   if (g.dim == 3)
+      k_quat_rhs<3, R><<<nb(g.cells()), 256, 0, s>>>(g, hinv, fc0, fc1, fc2, mq, q, out);
+   else
+      k_quat_rhs<2, R><<<nb(g.cells()), 256, 0, s>>>(g, hinv, fc0, fc1, fc2, mq, q, out);
    return launch_status();
 }
 
@@ -250,12 +207,6 @@ int quat_project(long long N, double* q, cudaStream_t s)
 INST(double)
 INST(float)
 #undef INST
-template int quat_face_coef<double, double>(const ampe_model_t&, const Grid&, const double*,
-                                            const double*, const double*, double, double*,
-                                            double*, double*, cudaStream_t);
-template int quat_face_coef<double, float>(const ampe_model_t&, const Grid&, const double*,
-                                           const double*, const double*, double, float*,
-                                           float*, float*, cudaStream_t);
 
 }  // namespace ampe
 
@@ -286,8 +237,8 @@ int ampe_quat_face_coef(const ampe_model_t* m, const double* phi,
       return AMPE_ERR_INVALID;
    if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
    if (!(m->quat_grad_floor > 0.0)) return AMPE_ERR_INVALID;
-   return quat_face_coef<double, double>(*m, make_grid(*m), phi, temp, q, 1.0, fc0, fc1, fc2,
-                                 (cudaStream_t)stream);
+   return quat_face_coef(*m, make_grid(*m), phi, temp, q, 1.0, fc0, fc1, fc2,
+                         (cudaStream_t)stream);
 }
 
 int ampe_quat_rhs(const ampe_model_t* m, const double* fc0, const double* fc1,

@@ -463,6 +463,7 @@ struct Stepper {
    // modulus |grad q| of the lagged copy, M_q(phi), face coefficients
    double *q_g = nullptr, *q_lag = nullptr, *ogm = nullptr, *mq = nullptr;
    double* fcq[3] = {nullptr, nullptr, nullptr};
+   QuatF32 qf32;  // FP32 quaternion working set (mixed path)
    // preconditioner (FP64 or FP32)
    DevFac<double> facp64, facc64, facq64;
    DevFac<float> facp32, facc32, facq32;
@@ -535,7 +536,13 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    to_ghosted<double>(S.g, y + S.N, v ? v + S.N : nullptr, sig, S.c_g, S.s);
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
    const bool quat = S.nb == 6;
-   if (quat) {
+   if (quat && S.p.precision == 1) {
+      for (int c = 0; c < 4; c++)
+         to_ghosted<float>(S.g, y + (2 + c) * S.N, v ? v + (2 + c) * S.N : nullptr, sig,
+                           S.qf32.q + c * S.NG, S.s);
+      ProfScope ps(S, KT_QUAT);
+      quat_cells_f32(S.m, S.mp, S.g, S.phi_g, S.qf32, S.s);
+   } else if (quat) {
       for (int c = 0; c < 4; c++)
          to_ghosted<double>(S.g, y + (2 + c) * S.N, v ? v + (2 + c) * S.N : nullptr,
                             sig, S.q_g + c * S.NG, S.s);
@@ -561,8 +568,15 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
       }
       {
          ProfScope ps(S, KT_RHS);
-         rhs_mixed(S.m, S.mp, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32, out,
-                   out + S.N, S.s);
+         rhs_mixed(S.m, S.mp, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32,
+                   quat && S.m.with_orient ? S.qf32.ogm : nullptr, out, out + S.N, S.s);
+      }
+      if (quat) {
+         ProfScope ps(S, KT_QUAT);
+         quat_faces_f32(S.m, S.mp, S.g, tf, S.pf32, S.qf32.q, 1.0, S.qf32.fc, S.qf32.dfc,
+                        S.s);
+         quat_rhs<float>(S.m, S.g, S.qf32.fc[0], S.qf32.fc[1], S.qf32.fc[2], S.qf32.mq,
+                         S.qf32.q, out + 2 * S.N, S.s);
       }
       S.st.rhs_evals++;
       return;
@@ -587,7 +601,7 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    if (quat) {
       ProfScope ps(S, KT_QUAT);
       quat_mobility<double>(S.m, S.g, S.phi_g, S.mq, S.s);
-      quat_face_coef<double, double>(S.m, S.g, S.phi_g, tf, S.q_lag, 1.0, S.fcq[0], S.fcq[1],
+      quat_face_coef(S.m, S.g, S.phi_g, tf, S.q_lag, 1.0, S.fcq[0], S.fcq[1],
                              S.fcq[2], S.s);
       quat_rhs<double>(S.m, S.g, S.fcq[0], S.fcq[1], S.fcq[2], S.mq, S.q_g,
                        out + 2 * S.N, S.s);
@@ -608,6 +622,20 @@ static double wrms(Stepper& S, const double* v, const double* w)
 static double dot(Stepper& S, const double* a, const double* b)
 {
    return S.red.sum(S.NY, [=] __device__(long long t) { return a[t] * b[t]; });
+}
+
+// D = gamma fc of the quaternion block: FP64 from the lagged q, or FP32 from
+// the FP32 working copy (mixed path)
+static void quat_precond_faces(Stepper& S, const double* tf, double gamma,
+                               DevLevel<double>& Q0)
+{
+   quat_face_coef(S.m, S.g, S.phi_g, tf, S.q_lag, gamma, Q0.D[0], Q0.D[1], Q0.D[2], S.s);
+}
+
+static void quat_precond_faces(Stepper& S, const double* tf, double gamma,
+                               DevLevel<float>& Q0)
+{
+   quat_faces_f32(S.m, S.mp, S.g, tf, S.pf32, S.qf32.q, gamma, Q0.D, nullptr, S.s);
 }
 
 template <class R>
@@ -643,8 +671,7 @@ static void precond_setup_t(Stepper& S, DevFac<R>& fp, DevFac<R>& fc,
       DevLevel<R>& Q0 = fq.lev[0];
       quat_mobility<R>(S.m, S.g, S.phi_g, Q0.M, S.s);
       fill_ghosts_t(S.g, Q0.M, S.s);
-      quat_face_coef<double, R>(S.m, S.g, S.phi_g, tf, S.q_lag, gamma, Q0.D[0], Q0.D[1],
-                                Q0.D[2], S.s);
+      quat_precond_faces(S, tf, gamma, Q0);
       for (auto& L : fq.lev) {
          L.dc = 0;
          L.cc = (R)1.0;
@@ -692,7 +719,7 @@ static void matvec(Stepper& S, const double* y, const double* fy,
       const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
       ProfScope ps(S, KT_JV);
       jv_mixed(S.m, S.mp, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma,
-               S.dphi32, S.da32, S.db32, out, S.s);
+               S.dphi32, S.da32, S.db32, S.nb == 6 ? &S.qf32 : nullptr, out, S.s);
       return;
    }
    const double sig = 1.0 / wrms(S, v, w);
@@ -855,7 +882,6 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC) return AMPE_ERR_INVALID;
    if (m->evolve_quat && (m->quat_mobility_type != 'p' || !(m->quat_grad_floor > 0.0)))
       return AMPE_ERR_INVALID;
-   if (m->evolve_quat && p->precision == 1) return AMPE_ERR_INVALID;
    if (ampe_device_count() < 1) return AMPE_ERR_NO_DEVICE;
    Stepper* S = new (std::nothrow) Stepper;
    if (!S) return AMPE_ERR_INVALID;
@@ -899,6 +925,18 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
       if (p->surrogate) {
          S->guess_l = (float*)dalloc<float>(S->pool, S->N, &err);
          S->guess_s = (float*)dalloc<float>(S->pool, S->N, &err);
+      }
+      if (S->nb == 6) {
+         QuatF32& Q = S->qf32;
+         Q.q = (float*)dalloc<float>(S->pool, 4 * S->NG, &err);
+         Q.dq = (float*)dalloc<float>(S->pool, 4 * S->NG, &err);
+         Q.ogm = (float*)dalloc<float>(S->pool, S->N, &err);
+         Q.mq = (float*)dalloc<float>(S->pool, S->NG, &err);
+         const long long nf[3] = {S->g.nfx(), S->g.nfy(), S->g.dim == 3 ? S->g.nfz() : 0};
+         for (int d = 0; d < S->g.dim; d++) {
+            Q.fc[d] = (float*)dalloc<float>(S->pool, nf[d], &err);
+            Q.dfc[d] = (float*)dalloc<float>(S->pool, nf[d], &err);
+         }
       }
    }
    const int nt = m->temp_mode == AMPE_TEMP_GRADIENT ? m->n[0] : 1;

@@ -188,3 +188,52 @@ def test_fd_jv_parity(cuda):
     jo = o.jv(v, 0.05, analytic=False)
     jg = g.jv(v, 0.05)
     assert O.rel_l2(jg, jo) <= 1e-9
+
+
+def test_mixed_jv_vs_fd(cuda):
+    """FP32 analytic product (q rows, orientation term of the phase row,
+    lagged gradients) against the oracle's FP64 finite-difference product."""
+    m, phi, c, q = poly_case()
+    p64 = configs.step_params(precond=2, mg_levels=3, atol=1e-6)
+    o = O.OracleStepper(m, p64)
+    o.set_state(phi, c)
+    o.set_quat(q)
+    o.advance(2)
+    ph, cc, cl, cs = o.get_state()
+    qq = o.get_quat()
+    o.set_state(ph, cc, cl, cs)
+    o.set_quat(qq)
+    pm = configs.step_params(precond=2, mg_levels=3, atol=1e-6, precision=1)
+    gm = ImplicitStepper(m, pm)
+    gm.set_state(ph, cc, cl, cs)
+    gm.set_quat(qq)
+    v = np.random.default_rng(12).standard_normal(6 * m.cells()) * 1e-3
+    fd = o.jv(v, 0.1, 0)
+    an = gm.jv(v, 0.1)
+    N = m.cells()
+    for b in range(6):
+        s = slice(b * N, (b + 1) * N)
+        err = O.rel_l2(an[s] - v[s], fd[s] - v[s])
+        assert err <= 1e-4, (b, err)
+
+
+def test_mixed_steps_vs_oracle(cuda):
+    m, phi, c, q = poly_case()
+    nsteps = 4
+    p64 = configs.step_params(dt=0.1, precond=2, mg_levels=3, atol=1e-6)
+    o = O.OracleStepper(m, p64)
+    o.set_state(phi, c)
+    o.set_quat(q)
+    rc, so = o.advance(nsteps)
+    assert rc == 0
+    pm = configs.step_params(dt=0.1, precond=2, mg_levels=3, atol=1e-6, precision=1)
+    g = ImplicitStepper(m, pm)
+    g.set_state(phi, c)
+    g.set_quat(q)
+    sg = g.advance(nsteps)
+    assert sg["steps"] == nsteps and sg["kks_fail"] == 0
+    errs = [O.rel_l2(a, b) for a, b in zip(g.get_state()[:2], o.get_state()[:2])]
+    errs.append(O.rel_l2(g.get_quat(), o.get_quat()))
+    print("mixed polycrystal vs FP64 oracle rel L2 (phi, c, q):", errs, sg)
+    assert max(errs) <= 2e-6
+    assert np.abs(np.linalg.norm(g.get_quat(), axis=0) - 1.0).max() < 1e-12
