@@ -10,6 +10,8 @@
 #include <stdint.h>
 
 #include "ampe_gb300.h"
+#include "bitconv.h"
+#include "fastdiv.h"
 
 #define AMPE_HD __host__ __device__ __forceinline__
 
@@ -21,30 +23,38 @@ constexpr double kGasR = 8.314472;  // J/(K mol), KKSdiluteBinary.cc:45
 // layout of a ghosted cell field (SAMRAI CellData ghost box, x fastest)
 // ---------------------------------------------------------------------------
 struct Grid {
+   // Index math is 32-bit: ghost boxes and face sets stay below 2^31
+   // entries (enforced by check_model).
    int dim, n0, n1, n2, ng, gz;
-   long long sx, sy;  // row and plane pitch of the ghosted layout
-   AMPE_HD long long c(int i, int j, int k) const
+   int sx, sy;  // row and plane pitch of the ghosted layout
+   // divisors of the index decompositions: n0, n1, n0+1, n1+1, (n0+1)/2
+   FastDiv fd0, fd1, fd0p, fd1p, fdh;
+   // linear index t < 2^31 over an (a.d x b.d x *) box -> (i, j, k)
+   AMPE_HD void split(long long t, const FastDiv& a, const FastDiv& b, int& i,
+                      int& j, int& k) const
    {
-      return ((long long)(k + gz) * (n1 + 2 * ng) + (j + ng)) * sx + (i + ng);
+      const unsigned u = (unsigned)t;
+      const unsigned q = a.div(u);
+      i = (int)(u - q * a.d);
+      const unsigned kk = b.div(q);
+      j = (int)(q - kk * b.d);
+      k = (int)kk;
    }
-   AMPE_HD long long interior(int i, int j, int k) const
+   // interior cell of linear index t (x fastest)
+   AMPE_HD void ijk(long long t, int& i, int& j, int& k) const
    {
-      return ((long long)k * n1 + j) * n0 + i;
+      split(t, fd0, fd1, i, j, k);
    }
-   AMPE_HD long long fx(int i, int j, int k) const
+   AMPE_HD int c(int i, int j, int k) const
    {
-      return ((long long)k * n1 + j) * (n0 + 1) + i;
+      return ((k + gz) * (n1 + 2 * ng) + (j + ng)) * sx + (i + ng);
    }
-   AMPE_HD long long fy(int i, int j, int k) const
-   {
-      return ((long long)k * (n1 + 1) + j) * n0 + i;
-   }
-   AMPE_HD long long fz(int i, int j, int k) const
-   {
-      return ((long long)k * n1 + j) * n0 + i;
-   }
+   AMPE_HD int interior(int i, int j, int k) const { return (k * n1 + j) * n0 + i; }
+   AMPE_HD int fx(int i, int j, int k) const { return (k * n1 + j) * (n0 + 1) + i; }
+   AMPE_HD int fy(int i, int j, int k) const { return (k * (n1 + 1) + j) * n0 + i; }
+   AMPE_HD int fz(int i, int j, int k) const { return (k * n1 + j) * n0 + i; }
    AMPE_HD long long cells() const { return (long long)n0 * n1 * n2; }
-   AMPE_HD long long cells_ghost() const { return sy * (n2 + 2 * gz); }
+   AMPE_HD long long cells_ghost() const { return (long long)sy * (n2 + 2 * gz); }
    AMPE_HD long long nfx() const { return (long long)(n0 + 1) * n1 * n2; }
    AMPE_HD long long nfy() const { return (long long)n0 * (n1 + 1) * n2; }
    AMPE_HD long long nfz() const { return (long long)n0 * n1 * (n2 + 1); }
@@ -61,6 +71,11 @@ inline Grid make_grid(const ampe_model_t& m)
    g.gz = m.dim == 3 ? m.ng : 0;
    g.sx = g.n0 + 2 * g.ng;
    g.sy = g.sx * (g.n1 + 2 * g.ng);
+   g.fd0 = FastDiv((unsigned)g.n0);
+   g.fd1 = FastDiv((unsigned)g.n1);
+   g.fd0p = FastDiv((unsigned)(g.n0 + 1));
+   g.fd1p = FastDiv((unsigned)(g.n1 + 1));
+   g.fdh = FastDiv((unsigned)((g.n0 + 1) / 2));
    return g;
 }
 
@@ -345,6 +360,24 @@ __device__ __forceinline__ double temperature_at(const ampe_model_t& m,
       return m.T0 + m.gradT * ((double)iw + 0.5) * m.dx[0];
    }
    return tfield[g.c(i, j, k)];
+}
+
+// value conversion between the FP64 and FP32 arrays of the stepper (integer
+// pipe for the float <-> double cases, see bitconv.h)
+template <class D, class S>
+__device__ __forceinline__ D cvt(S x)
+{
+   return (D)x;
+}
+template <>
+__device__ __forceinline__ float cvt<float, double>(double x)
+{
+   return d2f(x);
+}
+template <>
+__device__ __forceinline__ double cvt<double, float>(float x)
+{
+   return f2d(x);
 }
 
 }  // namespace ampe

@@ -41,6 +41,25 @@ __global__ void k_partial(long long n, F f, double* part)
    if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// as k_partial for FP32 terms: each thread sums its terms in FP32 with
+// Kahan compensation (no FP64 instruction per element), the block and the
+// finishing pass sum the per-thread results in FP64
+template <class F>
+__global__ void k_partial_f(long long n, F f, double* part)
+{
+   __shared__ double sh[32];
+   float acc = 0.f, comp = 0.f;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+        t += (long long)gridDim.x * blockDim.x) {
+      const float y = f(t) - comp;
+      const float s = acc + y;
+      comp = (s - acc) - y;
+      acc = s;
+   }
+   const double a = block_sum<NoOp>((double)acc, sh);
+   if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
 static __global__ void k_finish(const double* part, int np, double* out, int slot)
 {
    __shared__ double sh[32];
@@ -117,6 +136,17 @@ struct Reducer {
    double sum(long long n, F f)
    {
       enqueue(n, f, 0);
+      return fetch(1)[0];
+   }
+   // sum of FP32 terms (k_partial_f), FP64 result
+   template <class F>
+   double sumf(long long n, F f)
+   {
+      long long nb = (n + kRedThreads - 1) / kRedThreads;
+      int blocks = (int)(nb < kRedBlocks ? (nb < 1 ? 1 : nb) : kRedBlocks);
+      k_partial_f<<<blocks, kRedThreads, 0, s>>>(n, f, part);
+      k_finish<<<1, 1024, 0, s>>>(part, blocks, dres, 0);
+      g_launches += 2;
       return fetch(1)[0];
    }
 };

@@ -53,31 +53,112 @@ __device__ __forceinline__ void atomic_max_nonneg(double* a, double v)
    atomicMax((unsigned long long*)a, (unsigned long long)__double_as_longlong(v));
 }
 
+// periodic ghost fill as a gather: every ghost cell copies its wrapped
+// interior source (the same values as a SAMRAI periodic fill).  Threads run
+// over the ghost layers only: z slabs, then y slabs, then x columns.
+template <class R>
+__global__ void k_fill_ghosts_gather(Grid g, R* f)
+{
+   const int ng = g.ng;
+   const long long SX = g.n0 + 2 * ng, SY = g.n1 + 2 * ng;
+   const long long nzs = 2LL * g.gz * SX * SY;
+   const long long nys = (long long)g.n2 * 2 * ng * SX;
+   const long long nxs = (long long)g.n2 * g.n1 * 2 * ng;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < nzs + nys + nxs; t += (long long)gridDim.x * blockDim.x) {
+      int i, j, k;
+      long long r = t;
+      if (r < nzs) {
+         i = (int)(r % SX) - ng;
+         r /= SX;
+         j = (int)(r % SY) - ng;
+         const int l = (int)(r / SY);
+         k = l < g.gz ? l - g.gz : g.n2 + l - g.gz;
+      } else if ((r -= nzs) < nys) {
+         i = (int)(r % SX) - ng;
+         r /= SX;
+         const int l = (int)(r % (2 * ng));
+         j = l < ng ? l - ng : g.n1 + l - ng;
+         k = (int)(r / (2 * ng));
+      } else {
+         r -= nys;
+         const int l = (int)(r % (2 * ng));
+         i = l < ng ? l - ng : g.n0 + l - ng;
+         r /= 2 * ng;
+         k = (int)g.fd1.div((unsigned)r);
+         j = (int)r - k * g.n1;
+      }
+      const int si = i < 0 ? i + g.n0 : (i >= g.n0 ? i - g.n0 : i);
+      const int sj = j < 0 ? j + g.n1 : (j >= g.n1 ? j - g.n1 : j);
+      const int sk = k < 0 ? k + g.n2 : (k >= g.n2 ? k - g.n2 : k);
+      f[g.c(i, j, k)] = f[g.c(si, sj, sk)];
+   }
+}
+
+template <class R>
+int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s)
+{
+   const long long SX = g.n0 + 2 * g.ng, SY = g.n1 + 2 * g.ng;
+   const long long tot = 2LL * g.gz * SX * SY + (long long)g.n2 * 2 * g.ng * SX +
+                         (long long)g.n2 * g.n1 * 2 * g.ng;
+   long long b = (tot + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   k_fill_ghosts_gather<R><<<(unsigned)(b < 1 ? 1 : b), 256, 0, s>>>(g, f);
+   return launch_status();
+}
+
+// One colour of the red-black sweep.  images: also write each updated value
+// to its periodic ghost images, so that no ghost fill is needed between
+// colours (the stepper's smoother); the leaf entry point updates the
+// interior only.
 template <class R>
 __global__ void k_rbgs_color(FacOp<R> op, Grid g, const R* f, R* u,
-                             int offset, double* maxres)
+                             int offset, double* maxres, bool images)
 {
    // one thread per cell of the colour: i = 2*ih + parity(j,k)
    const int nh = (g.n0 + 1) / 2;
    const long long tot = (long long)nh * g.n1 * g.n2;
-   double mres = 0.0;
+   R mres = R(0);
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < tot; t += (long long)gridDim.x * blockDim.x) {
-      const int ih = (int)(t % nh);
-      const int j = (int)((t / nh) % g.n1);
-      const int k = (int)(t / ((long long)nh * g.n1));
+      int ih, j, k;
+      g.split(t, g.fdh, g.fd1, ih, j, k);
       const int i = 2 * ih + ((j + k + offset) & 1);
       if (i >= g.n0) continue;
       R dudr;
       const R r = cell_residual(op, g, f, u, i, j, k, &dudr);
-      u[g.c(i, j, k)] += -r * dudr;
-      mres = fmax(mres, (double)fabs(r));
+      const long long c = g.c(i, j, k);
+      const R un = u[c] + -r * dudr;
+      u[c] = un;
+      if (images) for_each_image(g, i, j, k, [&](long long idx) { u[idx] = un; });
+      if (maxres) mres = fmax(mres, fabs(r));
    }
    if (maxres) {
+      double mr = (double)mres;
       for (int o = 16; o > 0; o >>= 1)
-         mres = fmax(mres, __shfl_xor_sync(0xffffffffu, mres, o));
-      if ((threadIdx.x & 31) == 0) atomic_max_nonneg(maxres, mres);
+         mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+      if ((threadIdx.x & 31) == 0) atomic_max_nonneg(maxres, mr);
    }
+}
+
+// res = f - A u and part[block] = sum over the block's cells of res^2
+// (fixed grid, fixed order: deterministic with the finishing pass)
+template <class R>
+__global__ void k_residual_part(FacOp<R> op, Grid g, const R* f, const R* u,
+                                R* res, double* part)
+{
+   __shared__ double sh[32];
+   R accr = R(0);  // per-thread sum in R (FP32 in the mixed path)
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      int i, j, k;
+      g.ijk(t, i, j, k);
+      const R r = cell_residual(op, g, f, u, i, j, k, (R*)nullptr);
+      res[g.c(i, j, k)] = r;
+      accr += r * r;
+   }
+   double acc = block_sum<NoOp>((double)accr, sh);
+   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
 template <class R>
@@ -86,9 +167,8 @@ __global__ void k_residual(FacOp<R> op, Grid g, const R* f, const R* u,
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       res[g.c(i, j, k)] = cell_residual(op, g, f, u, i, j, k, (R*)nullptr);
    }
 }
@@ -100,9 +180,8 @@ __global__ void k_phase_set_c(Grid g, const double* phi, double gamma,
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       const double g2 = second_deriv_well_func(phi[c], wt);
       const double gm = gamma * mobility;
@@ -119,10 +198,22 @@ static unsigned nblocks(long long n)
 
 template <class R>
 int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
-               int offset, double* maxres, cudaStream_t s)
+               int offset, double* maxres, cudaStream_t s, bool images)
 {
    const long long tot = (long long)((g.n0 + 1) / 2) * g.n1 * g.n2;
-   k_rbgs_color<R><<<nblocks(tot), 256, 0, s>>>(op, g, f, u, offset, maxres);
+   k_rbgs_color<R><<<nblocks(tot), 256, 0, s>>>(op, g, f, u, offset, maxres, images);
+   return launch_status();
+}
+
+template <class R>
+int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
+                     R* res, double* part, int* nblk, cudaStream_t s)
+{
+   const long long n = g.cells();
+   long long nb = (n + kRedThreads - 1) / kRedThreads;
+   const int blocks = (int)(nb < kRedBlocks ? (nb < 1 ? 1 : nb) : kRedBlocks);
+   *nblk = blocks;
+   k_residual_part<R><<<blocks, kRedThreads, 0, s>>>(op, g, f, u, res, part);
    return launch_status();
 }
 
@@ -146,9 +237,16 @@ int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
 
 template int rbgs_color<double>(const FacOp<double>&, const Grid&,
                                 const double*, double*, int, double*,
-                                cudaStream_t);
+                                cudaStream_t, bool);
 template int rbgs_color<float>(const FacOp<float>&, const Grid&, const float*,
-                               float*, int, double*, cudaStream_t);
+                               float*, int, double*, cudaStream_t, bool);
+template int residual_partial<double>(const FacOp<double>&, const Grid&, const double*,
+                                      const double*, double*, double*, int*,
+                                      cudaStream_t);
+template int residual_partial<float>(const FacOp<float>&, const Grid&, const float*,
+                                     const float*, float*, double*, int*, cudaStream_t);
+template int fill_ghosts_t<double>(const Grid&, double*, cudaStream_t);
+template int fill_ghosts_t<float>(const Grid&, float*, cudaStream_t);
 template int residual<double>(const FacOp<double>&, const Grid&, const double*,
                               const double*, double*, cudaStream_t);
 template int residual<float>(const FacOp<float>&, const Grid&, const float*,
@@ -190,9 +288,8 @@ int residual_rms_into(const FacOp<double>& op, const Grid& g, const double* f,
    const int blocks = (int)(nb < kRedBlocks ? (nb < 1 ? 1 : nb) : kRedBlocks);
    const Grid gg = g;
    auto sq = [=] __device__(long long t) {
-      const int i = (int)(t % gg.n0);
-      const int j = (int)((t / gg.n0) % gg.n1);
-      const int k = (int)(t / ((long long)gg.n0 * gg.n1));
+      int i, j, k;
+      gg.ijk(t, i, j, k);
       const double x = res[gg.c(i, j, k)];
       return x * x;
    };
@@ -238,7 +335,7 @@ int ampe_efo_rbgs(const ampe_model_t* m, const double* dface0,
    FacOp<double> op = make_op(m, dface0, dface1, dface2, d_const, ccell,
                               c_const, mcell, m_const);
    return rbgs_color(op, make_grid(*m), rhs, u, offset, maxres,
-                     (cudaStream_t)stream);
+                     (cudaStream_t)stream, false);
 }
 
 int ampe_efo_residual(const ampe_model_t* m, const double* dface0,

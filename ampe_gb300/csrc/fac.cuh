@@ -21,7 +21,13 @@ struct FacOp {
 
 template <class R>
 int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
-               int offset, double* maxres, cudaStream_t s);
+               int offset, double* maxres, cudaStream_t s, bool images);
+// res = f - A u and per-block sums of res^2 into part (*nblk blocks)
+template <class R>
+int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
+                     R* res, double* part, int* nblk, cudaStream_t s);
+template <class R>
+int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s);
 template <class R>
 int residual(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
              R* res, cudaStream_t s);

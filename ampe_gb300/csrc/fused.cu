@@ -78,9 +78,8 @@ __global__ void k_kks_interior(ampe_model_t m, Grid g, const ThermoCoef* tab,
    unsigned long long its = 0, fails = 0;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long ci = g.c(i, j, k);
       const ThermoCoef th = coef_at(m, g, tab, tfield, i, j, k);
       const double h = interp_func(phi[ci], m.conc_interp);
@@ -149,9 +148,8 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
    const bool tdep = (m.Q_liquid != 0.0 || m.Q_solid != 0.0);
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       // ---- phase ----
       double diff = 0.0;

@@ -7,6 +7,7 @@
 #include <cstdio>
 
 #include "common.cuh"
+#include "fac.cuh"
 #include "phase_flux.cuh"
 
 namespace ampe {
@@ -24,33 +25,22 @@ int check_model(const ampe_model_t* m)
    if (m->dim == 2 && m->n[2] != 1) return AMPE_ERR_INVALID;
    if (m->flux_type == AMPE_FLUX_ISOTROPIC && m->dim == 3)
       return AMPE_ERR_INVALID;  // 3d/quatrhs.m4:90-92 stops: no 3D variant
+   // kernels split linear cell and face indices with 31-bit arithmetic
+   const long long lim = (1LL << 31) - 1;
+   const long long e0 = m->n[0], e1 = m->n[1], e2 = m->dim == 3 ? m->n[2] : 1;
+   const long long gz = m->dim == 3 ? m->ng : 0;
+   const long long ghost = (e0 + 2 * m->ng) * (e1 + 2 * m->ng) * (e2 + 2 * gz);
+   const long long faces = (e0 + 1) * e1 * e2 + e0 * (e1 + 1) * e2 + e0 * e1 * (e2 + 1);
+   if (ghost > lim || faces > lim) return AMPE_ERR_TOO_LARGE;
    return AMPE_OK;
 }
 
 // ---------------------------------------------------------------------------
 // periodic ghost fill
 // ---------------------------------------------------------------------------
-__global__ void k_fill_ghosts(Grid g, double* f)
-{
-   const long long n = g.cells();
-   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-        t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
-      const bool edge = i < g.ng || i >= g.n0 - g.ng || j < g.ng ||
-                        j >= g.n1 - g.ng ||
-                        (g.dim == 3 && (k < g.ng || k >= g.n2 - g.ng));
-      if (!edge) continue;
-      const double v = f[g.c(i, j, k)];
-      for_each_image(g, i, j, k, [&](long long idx) { f[idx] = v; });
-   }
-}
-
 int fill_ghosts(const Grid& g, double* f, cudaStream_t s)
 {
-   k_fill_ghosts<<<grid_for(g.cells(), 256), 256, 0, s>>>(g, f);
-   return launch_status();
+   return fill_ghosts_t<double>(g, f, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -74,20 +64,14 @@ __global__ void k_phase_flux(ampe_model_t m, Grid g, const double* ph,
       long long r = t;
       if (r < nx) {
          dir = 0;
-         i = (int)(r % (g.n0 + 1));
-         j = (int)((r / (g.n0 + 1)) % g.n1);
-         k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
+         g.split(r, g.fd0p, g.fd1, i, j, k);
       } else if ((r -= nx) < ny) {
          dir = 1;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % (g.n1 + 1));
-         k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
+         g.split(r, g.fd0, g.fd1p, i, j, k);
       } else {
          r -= ny;
          dir = 2;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % g.n1);
-         k = (int)(r / ((long long)g.n0 * g.n1));
+         g.ijk(r, i, j, k);
       }
       const double v = phase_face_flux(m, g.dim, dir, i, j, k, P, Q);
       if (dir == 0) f0[g.fx(i, j, k)] = v;
@@ -109,9 +93,8 @@ __global__ void k_computerhspbg(ampe_model_t m, Grid g, const double* f0,
    const double eq2 = 0.5 * m.epsilon_q * m.epsilon_q;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       double d = (f0[g.fx(i + 1, j, k)] - f0[g.fx(i, j, k)]) * dxi +
                  (f1[g.fy(i, j + 1, k)] - f1[g.fy(i, j, k)]) * dyi;
       if (g.dim == 3) d = d + (f2[g.fz(i, j, k + 1)] - f2[g.fz(i, j, k)]) * dzi;
@@ -135,9 +118,8 @@ __global__ void k_add_driving_force(ampe_model_t m, Grid g,
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long ci = g.c(i, j, k);
       const ThermoCoef th = thermo_coef(m, temperature_at(m, g, temp, i, j, k));
       const double a = cl[ci], b = cs[ci];
@@ -199,20 +181,14 @@ __global__ void k_conc_diffusion(ampe_model_t m, Grid g, const double* phi,
       long long r = t;
       if (r < nx) {
          dir = 0;
-         i = (int)(r % (g.n0 + 1));
-         j = (int)((r / (g.n0 + 1)) % g.n1);
-         k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
+         g.split(r, g.fd0p, g.fd1, i, j, k);
       } else if ((r -= nx) < ny) {
          dir = 1;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % (g.n1 + 1));
-         k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
+         g.split(r, g.fd0, g.fd1p, i, j, k);
       } else {
          r -= ny;
          dir = 2;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % g.n1);
-         k = (int)(r / ((long long)g.n0 * g.n1));
+         g.ijk(r, i, j, k);
       }
       const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
       const double vphi = average_func(phi[g.c(i - ei, j - ej, k - ek)],
@@ -246,22 +222,19 @@ __global__ void k_add_flux(ampe_model_t m, Grid g, const double* u,
         t < nx + ny + nz; t += (long long)gridDim.x * blockDim.x) {
       long long r = t;
       if (r < nx) {
-         const int i = (int)(r % (g.n0 + 1));
-         const int j = (int)((r / (g.n0 + 1)) % g.n1);
-         const int k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
+         int i, j, k;
+         g.split(r, g.fd0p, g.fd1, i, j, k);
          f0[r] = f0[r] + (1.0 / m.dx[0]) * d0[r] *
                              (u[g.c(i, j, k)] - u[g.c(i - 1, j, k)]);
       } else if ((r -= nx) < ny) {
-         const int i = (int)(r % g.n0);
-         const int j = (int)((r / g.n0) % (g.n1 + 1));
-         const int k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
+         int i, j, k;
+         g.split(r, g.fd0, g.fd1p, i, j, k);
          f1[r] = f1[r] + (1.0 / m.dx[1]) * d1[r] *
                              (u[g.c(i, j, k)] - u[g.c(i, j - 1, k)]);
       } else {
          r -= ny;
-         const int i = (int)(r % g.n0);
-         const int j = (int)((r / g.n0) % g.n1);
-         const int k = (int)(r / ((long long)g.n0 * g.n1));
+         int i, j, k;
+         g.ijk(r, i, j, k);
          f2[r] = f2[r] + (1.0 / m.dx[2]) * d2[r] *
                              (u[g.c(i, j, k)] - u[g.c(i, j, k - 1)]);
       }
@@ -275,9 +248,8 @@ __global__ void k_rhs_conc(ampe_model_t m, Grid g, const double* f0,
    const double dzi = g.dim == 3 ? 1.0 / m.dx[2] : 0.0;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       double s = dxi * (f0[g.fx(i + 1, j, k)] - f0[g.fx(i, j, k)]) +
                  dyi * (f1[g.fy(i, j + 1, k)] - f1[g.fy(i, j, k)]);
       if (g.dim == 3) s = s + dzi * (f2[g.fz(i, j, k + 1)] - f2[g.fz(i, j, k)]);

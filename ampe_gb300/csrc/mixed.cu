@@ -156,14 +156,13 @@ __global__ void k_kks_mixed(ampe_model_t m, MixParams mp, Grid g, const ThermoCo
    const float ivm = mp.ivm;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long ci = g.c(i, j, k);
       const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
       const double phd = phi[ci], cd = conc[ci];
-      const float h = interp_func((float)phd, m.conc_interp);
-      const float c = (float)cd;
+      const float h = interp_func(d2f(phd), m.conc_interp);
+      const float c = d2f(cd);
       float x[2];
       int st = -1;
       if (guess_l) {
@@ -349,7 +348,7 @@ __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells_ghost(); t += (long long)gridDim.x * blockDim.x)
-      pf[t] = (float)phi[t];
+      pf[t] = d2f(phi[t]);
 }
 
 template <int DIM>
@@ -360,9 +359,8 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       float diff = 0.f, div = 0.f;
 #pragma unroll
@@ -391,8 +389,8 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
              deriv_interp_func(p, m.orient_interp2) * mp.eq2h * gm * gm;
       }
       r += deriv_interp_func(p, m.energy_interp) * dF[t];
-      phi_rhs[t] = (double)(r * mp.Mphi);
-      conc_rhs[t] = (double)(mp.Mc * div);
+      phi_rhs[t] = f2d(r * mp.Mphi);
+      conc_rhs[t] = f2d(mp.Mc * div);
    }
 }
 
@@ -423,20 +421,19 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 //   J [da; db] = [dc - (b - a) h_c'(phi) dphi; 0]
 __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
                            const double* tfield, const float* pf,
-                           const float* cl, const float* cs, const double* v,
+                           const float* cl, const float* cs, const float* v,
                            float* dphi, float* da, float* db, float* dq)
 {
    const long long N = g.cells(), NG = g.cells_ghost();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
         t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
       const float p = pf[c], a = cl[c], b = cs[c];
       const float h = interp_func(p, m.conc_interp);
-      const float vp = (float)v[t], vc = (float)v[t + N];
+      const float vp = v[t], vc = v[t + N];
       const float J00 = 1.f - h, J01 = h;
       const float J10 = 1.f / (a * (1.f - a)) + dxi_f(tf, a, 0) * tf.iRT;
       const float J11 = -1.f / (b * (1.f - b)) - dxi_f(tf, b, 1) * tf.iRT;
@@ -454,7 +451,7 @@ __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
       if (dq) {
 #pragma unroll
          for (int q = 0; q < 4; q++) {
-            const float x = (float)v[t + (2 + q) * N];
+            const float x = v[t + (2 + q) * N];
             float* dqq = dq + q * NG;
             dqq[c] = x;
             for_each_image(g, i, j, k, [&](long long idx) { dqq[idx] = x; });
@@ -503,15 +500,14 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
                              const CoefF* tabf, const double* tfield,
                              const float* pf, const float* cl, const float* cs,
                              const float* dF, const float* dphi,
-                             const float* da, const float* db, const double* v,
-                             const float* ogm, double gamma, double* out)
+                             const float* da, const float* db, const float* v,
+                             const float* ogm, float gamma, float* out)
 {
    const long long N = g.cells();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
         t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       float diff = 0.f, div = 0.f;
 #pragma unroll
@@ -548,8 +544,8 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
                                   second_deriv_interp_f(p, m.energy_interp) * dF[t] * vp +
                                   deriv_interp_func(p, m.energy_interp) * ddF);
       const float jc = mp.Mc * div;
-      out[t] = v[t] - (double)((float)gamma * jp);
-      out[t + N] = v[t + N] - (double)((float)gamma * jc);
+      out[t] = v[t] - gamma * jp;
+      out[t + N] = v[t + N] - gamma * jc;
    }
 }
 
@@ -563,9 +559,8 @@ __global__ void k_quat_cells_f32(MixParams mp, Grid g, const double* phi,
    const long long qs = g.cells_ghost();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       const long long st[3] = {1, g.sx, g.sy};
       float s = 0.f;
@@ -579,7 +574,7 @@ __global__ void k_quat_cells_f32(MixParams mp, Grid g, const double* phi,
             s += a * a + b * b;
          }
       ogm[t] = sqrtf(0.5f * s);
-      mq[c] = mp.qMmin + (mp.qM - mp.qMmin) * (1.f - interp_func((float)phi[c], 'p'));
+      mq[c] = mp.qMmin + (mp.qM - mp.qMmin) * (1.f - interp_func(d2f(phi[c]), 'p'));
    }
 }
 
@@ -616,6 +611,26 @@ __global__ void k_quat_faces_f32(ampe_model_t m, MixParams mp, Grid g,
    }
 }
 
+// composition preconditioner faces D = -gamma ((1-h) D_L + h D_S) in FP32
+template <int DIM>
+__global__ void k_conc_faces_f32(ampe_model_t m, MixParams mp, Grid g,
+                                 const double* tfield, const float* pf, float gamma,
+                                 FacePtrs f)
+{
+   const long long tot = g.nfx() + g.nfy() + (DIM == 3 ? g.nfz() : 0);
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      face_of(g, t, dir, i, j, k);
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      float DL, DS;
+      face_diff<DIM>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), g.c(i, j, k), i, j, k,
+                     ei, ej, ek, DL, DS);
+      const long long fi = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+      f.fc[dir][fi] = -gamma * (DL + DS);
+   }
+}
+
 // derivative of the face average of phi along (da, db)
 __device__ __forceinline__ float d_average_f(float a, float b, float da, float db,
                                              char type)
@@ -631,16 +646,15 @@ __device__ __forceinline__ float d_average_f(float a, float b, float da, float d
 // with dM_q = M_q'(phi) dphi and dfc = (d fc / d phibar) dphibar at each face
 template <int DIM>
 __global__ void k_jv_quat(ampe_model_t m, MixParams mp, Grid g, const float* pf,
-                          const float* dphi, QuatF32 qf, const double* v,
-                          double gamma, double* out)
+                          const float* dphi, QuatF32 qf, const float* v,
+                          float gamma, float* out)
 {
    const long long N = g.cells(), qs = g.cells_ghost();
-   const float gm = (float)gamma;
+   const float gm = gamma;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
         t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       const long long st[3] = {1, g.sx, g.sy};
       // per face (d, side): fc, and dfc * dphibar
@@ -678,16 +692,16 @@ __global__ void k_jv_quat(ampe_model_t m, MixParams mp, Grid g, const float* pf,
          }
          const float jq = -(mqc * (A + Cc) + dmq * B);
          const long long o = t + (2 + comp) * N;
-         out[o] = v[o] - (double)(gm * jq);
+         out[o] = v[o] - gm * jq;
       }
    }
 }
 
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf, const double* tfield, const float* pf,
-             const float* cl, const float* cs, const float* dF, const double* v,
+             const float* cl, const float* cs, const float* dF, const float* v,
              double gamma, float* dphi, float* da, float* db, const QuatF32* qf,
-             double* out, cudaStream_t s)
+             float* out, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > 152 * 32) b = 152 * 32;
@@ -697,16 +711,16 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    const float* ogm = (qf && m.with_orient) ? qf->ogm : nullptr;
    if (g.dim == 3)
       k_jv_stencil<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
-                                                  da, db, v, ogm, gamma, out);
+                                                  da, db, v, ogm, (float)gamma, out);
    else
       k_jv_stencil<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
-                                                  da, db, v, ogm, gamma, out);
+                                                  da, db, v, ogm, (float)gamma, out);
    int rc = launch_status();
    if (qf && !rc) {
       if (g.dim == 3)
-         k_jv_quat<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, pf, dphi, *qf, v, gamma, out);
+         k_jv_quat<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, pf, dphi, *qf, v, (float)gamma, out);
       else
-         k_jv_quat<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, pf, dphi, *qf, v, gamma, out);
+         k_jv_quat<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, pf, dphi, *qf, v, (float)gamma, out);
       rc = launch_status();
    }
    return rc;
@@ -721,6 +735,25 @@ int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
       k_quat_cells_f32<3><<<(unsigned)b, 256, 0, s>>>(mp, g, phi, qf.q, qf.ogm, qf.mq);
    else
       k_quat_cells_f32<2><<<(unsigned)b, 256, 0, s>>>(mp, g, phi, qf.q, qf.ogm, qf.mq);
+   return launch_status();
+}
+
+int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                   const double* tfield, const float* pf, double gamma,
+                   float* const D[3], cudaStream_t s)
+{
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   long long b = (tot + 255) / 256;
+   if (b > 152 * 32) b = 152 * 32;
+   FacePtrs f;
+   for (int d = 0; d < 3; d++) {
+      f.fc[d] = D[d];
+      f.dfc[d] = nullptr;
+   }
+   if (g.dim == 3)
+      k_conc_faces_f32<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, (float)gamma, f);
+   else
+      k_conc_faces_f32<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, (float)gamma, f);
    return launch_status();
 }
 

@@ -54,9 +54,13 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf,
              const double* tfield, const float* pf, const float* cl,
-             const float* cs, const float* dF, const double* v, double gamma,
-             float* dphi, float* da, float* db, const QuatF32* qf, double* out,
+             const float* cs, const float* dF, const float* v, double gamma,
+             float* dphi, float* da, float* db, const QuatF32* qf, float* out,
              cudaStream_t s);
+// composition preconditioner faces D = -gamma ((1-h) D_L + h D_S), FP32
+int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                   const double* tfield, const float* pf, double gamma,
+                   float* const D[3], cudaStream_t s);
 // |grad q| (from qf.q) and M_q(phi) at cells
 int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                    const double* phi, QuatF32& qf, cudaStream_t s);

@@ -434,9 +434,8 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
       // ---- inputs ----
       float in[3] = {0.f, 0.f, 0.f};
       if (t < N) {
-         const int i = (int)(t % g.n0);
-         const int j = (int)((t / g.n0) % g.n1);
-         const int k = (int)(t / ((long long)g.n0 * g.n1));
+         int i, j, k;
+         g.ijk(t, i, j, k);
          const long long c = g.c(i, j, k);
          encode_inputs(nz, phi[c], conc[c], temperature_at(m, g, tfield, i, j, k), in);
       }
@@ -539,9 +538,8 @@ __global__ void k_mlp_infer_simt(ampe_model_t m, Grid g, MlpNorm nz,
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       float x[64], y[64];
       encode_inputs(nz, phi[c], conc[c], temperature_at(m, g, tfield, i, j, k), x);

@@ -21,9 +21,8 @@ __global__ void k_quat_grad_modulus(Grid g, Inv3<R> dinv, const R* q, R* ogm)
    const long long qs = g.cells_ghost();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       R s = 0;
 #pragma unroll
       for (int d = 0; d < DIM; d++) {
@@ -49,9 +48,8 @@ __global__ void k_quat_mobility(Grid g, double mmin, double mscale,
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       double p = phi[c];
       p = fmax(0.0, fmin(1.0, p));
@@ -97,9 +95,8 @@ __global__ void k_quat_rhs(Grid g, Inv3<R> hinv, const R* fc0, const R* fc1,
    const long long qs = g.cells_ghost(), N = g.cells();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
         t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       // the six face coefficients are shared by the four components
       const R fxm = fc0[g.fx(i, j, k)], fxp = fc0[g.fx(i + 1, j, k)];
       const R fym = fc1[g.fy(i, j, k)], fyp = fc1[g.fy(i, j + 1, k)];
@@ -120,7 +117,7 @@ __global__ void k_quat_rhs(Grid g, Inv3<R> hinv, const R* fc0, const R* fc1,
          if (DIM == 3)
             div = div + (flux(fzp, 2, qc[cc + g.sy], q0) - flux(fzm, 2, q0, qc[cc - g.sy])) *
                             hinv.v[2];
-         out[c * N + t] = (double)((R)0 - mqc * div);
+         out[c * N + t] = cvt<double, R>((R)0 - mqc * div);
       }
    }
 }

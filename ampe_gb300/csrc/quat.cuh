@@ -97,20 +97,14 @@ __device__ __forceinline__ void face_of(const Grid& g, long long t, int& dir,
    long long r = t;
    if (r < nx) {
       dir = 0;
-      i = (int)(r % (g.n0 + 1));
-      j = (int)((r / (g.n0 + 1)) % g.n1);
-      k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
+      g.split(r, g.fd0p, g.fd1, i, j, k);
    } else if ((r -= nx) < ny) {
       dir = 1;
-      i = (int)(r % g.n0);
-      j = (int)((r / g.n0) % (g.n1 + 1));
-      k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
+      g.split(r, g.fd0, g.fd1p, i, j, k);
    } else {
       r -= ny;
       dir = 2;
-      i = (int)(r % g.n0);
-      j = (int)((r / g.n0) % g.n1);
-      k = (int)(r / ((long long)g.n0 * g.n1));
+      g.ijk(r, i, j, k);
    }
 }
 

@@ -35,30 +35,6 @@ namespace ampe {
 // ---------------------------------------------------------------------------
 // templated ghost fill / transfers for the preconditioner's arithmetic type
 // ---------------------------------------------------------------------------
-template <class R>
-__global__ void k_fill_ghosts_t(Grid g, R* f)
-{
-   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
-      const bool edge = i < g.ng || i >= g.n0 - g.ng || j < g.ng ||
-                        j >= g.n1 - g.ng ||
-                        (g.dim == 3 && (k < g.ng || k >= g.n2 - g.ng));
-      if (!edge) continue;
-      const R v = f[g.c(i, j, k)];
-      for_each_image(g, i, j, k, [&](long long idx) { f[idx] = v; });
-   }
-}
-
-template <class R>
-int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s)
-{
-   k_fill_ghosts_t<R><<<map_blocks(g.cells()), 256, 0, s>>>(g, f);
-   return launch_status();
-}
-
 // dst(ghosted, with ghost images) = src + sig * v   (v may be null)
 template <class R>
 __global__ void k_to_ghosted(Grid g, const double* src, const double* v,
@@ -66,10 +42,9 @@ __global__ void k_to_ghosted(Grid g, const double* src, const double* v,
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
-      const R x = (R)(v ? src[t] + sig * v[t] : src[t]);
+      int i, j, k;
+      g.ijk(t, i, j, k);
+      const R x = cvt<R, double>(v ? src[t] + sig * v[t] : src[t]);
       dst[g.c(i, j, k)] = x;
       for_each_image(g, i, j, k, [&](long long idx) { dst[idx] = x; });
    }
@@ -83,15 +58,28 @@ int to_ghosted(const Grid& g, const double* src, const double* v, double sig,
    return launch_status();
 }
 
-template <class R>
-__global__ void k_from_ghosted(Grid g, const R* src, double* dst)
+template <class R, class D>
+__global__ void k_from_ghosted(Grid g, const R* src, D* dst)
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
-      dst[t] = (double)src[g.c(i, j, k)];
+      int i, j, k;
+      g.ijk(t, i, j, k);
+      dst[t] = cvt<D, R>(src[g.c(i, j, k)]);
+   }
+}
+
+// dst (ghosted, with ghost images) = interior src, same type
+template <class R>
+__global__ void k_copy_ghosted(Grid g, const R* src, R* dst)
+{
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
+      int i, j, k;
+      g.ijk(t, i, j, k);
+      const R x = src[t];
+      dst[g.c(i, j, k)] = x;
+      for_each_image(g, i, j, k, [&](long long idx) { dst[idx] = x; });
    }
 }
 
@@ -103,9 +91,8 @@ __global__ void k_restrict(Grid gf, Grid gc, const R* src, R* dst)
    const R w = gf.dim == 3 ? R(0.125) : R(0.25);
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < gc.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % gc.n0);
-      const int j = (int)((t / gc.n0) % gc.n1);
-      const int k = (int)(t / ((long long)gc.n0 * gc.n1));
+      int i, j, k;
+      gc.ijk(t, i, j, k);
       R s = R(0);
       for (int c = 0; c < dz; c++)
          for (int b = 0; b < 2; b++)
@@ -115,16 +102,20 @@ __global__ void k_restrict(Grid gf, Grid gc, const R* src, R* dst)
    }
 }
 
+// fine u += coarse u (piecewise constant), written through to the fine
+// level's periodic ghost images
 template <class R>
 __global__ void k_prolong_add(Grid gf, Grid gc, const R* cu, R* fu)
 {
    const int dz = gf.dim == 3 ? 2 : 1;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < gf.cells(); t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % gf.n0);
-      const int j = (int)((t / gf.n0) % gf.n1);
-      const int k = (int)(t / ((long long)gf.n0 * gf.n1));
-      fu[gf.c(i, j, k)] += cu[gc.c(i / 2, j / 2, k / dz)];
+      int i, j, k;
+      gf.ijk(t, i, j, k);
+      const long long c = gf.c(i, j, k);
+      const R v = fu[c] + cu[gc.c(i / 2, j / 2, k / dz)];
+      fu[c] = v;
+      for_each_image(gf, i, j, k, [&](long long idx) { fu[idx] = v; });
    }
 }
 
@@ -140,9 +131,8 @@ __global__ void k_coarsen_faces(Grid gf, Grid gc, int dir, const R* src,
    const long long tot = (long long)ni * nj * nk;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < tot; t += (long long)gridDim.x * blockDim.x) {
-      const int i = (int)(t % ni);
-      const int j = (int)((t / ni) % nj);
-      const int k = (int)(t / ((long long)ni * nj));
+      int i, j, k;
+      gc.split(t, dir == 0 ? gc.fd0p : gc.fd0, dir == 1 ? gc.fd1p : gc.fd1, i, j, k);
       R s = R(0);
       if (dir == 0) {
          for (int c = 0; c < dz; c++)
@@ -169,37 +159,23 @@ __global__ void k_conc_precond_faces(ampe_model_t m, Grid g, const double* phi,
                                      R* D0, R* D1, R* D2)
 {
    const double qlR = m.Q_liquid / kGasR, qsR = m.Q_solid / kGasR;
-   const long long nx = g.nfx(), ny = g.nfy();
+   const bool tdep = m.Q_liquid != 0.0 || m.Q_solid != 0.0;
    const long long nz = g.dim == 3 ? g.nfz() : 0;
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-        t < nx + ny + nz; t += (long long)gridDim.x * blockDim.x) {
+        t < g.nfx() + g.nfy() + nz; t += (long long)gridDim.x * blockDim.x) {
       int dir, i, j, k;
-      long long r = t;
-      if (r < nx) {
-         dir = 0;
-         i = (int)(r % (g.n0 + 1));
-         j = (int)((r / (g.n0 + 1)) % g.n1);
-         k = (int)(r / ((long long)(g.n0 + 1) * g.n1));
-      } else if ((r -= nx) < ny) {
-         dir = 1;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % (g.n1 + 1));
-         k = (int)(r / ((long long)g.n0 * (g.n1 + 1)));
-      } else {
-         r -= ny;
-         dir = 2;
-         i = (int)(r % g.n0);
-         j = (int)((r / g.n0) % g.n1);
-         k = (int)(r / ((long long)g.n0 * g.n1));
-      }
+      face_of(g, t, dir, i, j, k);
       const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
       const double vphi = average_func(phi[g.c(i - ei, j - ej, k - ek)],
                                        phi[g.c(i, j, k)], m.avg_type);
       const double hphi = interp_func(vphi, m.diff_interp);
-      const double invT = 2.0 / (temperature_at(m, g, tfield, i - ei, j - ej, k - ek) +
-                                 temperature_at(m, g, tfield, i, j, k));
-      const double dlq = m.D_liquid * exp(-qlR * invT);
-      const double dsq = m.D_solid * exp(-qsR * invT);
+      double dlq = m.D_liquid, dsq = m.D_solid;  // exp(0) = 1 exactly
+      if (tdep) {
+         const double invT = 2.0 / (temperature_at(m, g, tfield, i - ei, j - ej, k - ek) +
+                                    temperature_at(m, g, tfield, i, j, k));
+         dlq = m.D_liquid * exp(-qlR * invT);
+         dsq = m.D_solid * exp(-qsR * invT);
+      }
       const double v = -gamma * ((1.0 - hphi) * dlq + hphi * dsq);
       if (dir == 0) D0[g.fx(i, j, k)] = (R)v;
       if (dir == 1) D1[g.fy(i, j, k)] = (R)v;
@@ -339,24 +315,22 @@ template <class R>
 double rms_interior(Ctx& cx, const Grid& g, const R* v)
 {
    const double ss = cx.red->sum(g.cells(), [=] __device__(long long t) {
-      const int i = (int)(t % g.n0);
-      const int j = (int)((t / g.n0) % g.n1);
-      const int k = (int)(t / ((long long)g.n0 * g.n1));
+      int i, j, k;
+      g.ijk(t, i, j, k);
       const double x = (double)v[g.c(i, j, k)];
       return x * x;
    });
    return sqrt(ss / (double)g.cells());
 }
 
+// red then black; each colour writes through to the ghost images
 template <class R>
 void rb_sweep(Ctx& cx, DevLevel<R>& L, double* maxres)
 {
    FacOp<R> op = L.op();
    if (maxres) cudaMemsetAsync(maxres, 0, 2 * sizeof(double), cx.s);
-   rbgs_color(op, L.g, L.f, L.u, 0, maxres, cx.s);
-   fill_ghosts_t(L.g, L.u, cx.s);
-   rbgs_color(op, L.g, L.f, L.u, 1, maxres ? maxres + 1 : nullptr, cx.s);
-   fill_ghosts_t(L.g, L.u, cx.s);
+   rbgs_color(op, L.g, L.f, L.u, 0, maxres, cx.s, true);
+   rbgs_color(op, L.g, L.f, L.u, 1, maxres ? maxres + 1 : nullptr, cx.s, true);
 }
 
 template <class R>
@@ -375,30 +349,31 @@ void vcycle(Ctx& cx, DevFac<R>& F, int l)
    k_restrict<R><<<map_blocks(C.g.cells()), 256, 0, cx.s>>>(L.g, C.g, L.r, C.f);
    launch_status();
    vcycle(cx, F, l + 1);
-   fill_ghosts_t(C.g, C.u, cx.s);
    k_prolong_add<R><<<map_blocks(L.g.cells()), 256, 0, cx.s>>>(L.g, C.g, C.u, L.u);
    launch_status();
-   fill_ghosts_t(L.g, L.u, cx.s);
    for (int it = 0; it < cx.p->mg_post; it++) rb_sweep(cx, L, nullptr);
 }
 
-// FACPreconditioner::solveSystem on one level.  r: interior FP64 block of
-// the Krylov vector; z: interior FP64 output.
+// FACPreconditioner::solveSystem on one level.  r: interior block of the
+// Krylov vector; z: interior output (FP64 path: double, mixed path: float).
 template <class R>
-int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const double* r, double* z,
-              double tol)
+int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const R* r, R* z, double tol)
 {
    DevLevel<R>& L0 = F.lev[0];
    const Grid g = L0.g;
    const long long ng = g.cells_ghost();
-   to_ghosted<R>(g, r, nullptr, 0.0, F.f0, cx.s);
-   cudaMemsetAsync(F.sol, 0, sizeof(R) * ng, cx.s);
-   cudaMemcpyAsync(F.rr, F.f0, sizeof(R) * ng, cudaMemcpyDeviceToDevice, cx.s);
+   k_copy_ghosted<R><<<map_blocks(g.cells()), 256, 0, cx.s>>>(g, r, F.f0);
+   launch_status();
    FacOp<R> op = L0.op();
+   R* const f_own = L0.f;
+   R* const u_own = L0.u;
    double norm = 0.0;
    int it = 0;
    do {
-      cudaMemcpyAsync(L0.f, F.rr, sizeof(R) * ng, cudaMemcpyDeviceToDevice, cx.s);
+      // cycle 0 solves with the initial residual f0 straight into sol (the
+      // initial guess is zero); later cycles correct sol with u from rr
+      L0.f = it == 0 ? F.f0 : F.rr;
+      L0.u = it == 0 ? F.sol : u_own;
       if (mode == 2 && F.lev.size() > 1) {
          vcycle(cx, F, 0);
       } else {
@@ -416,15 +391,21 @@ int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const double* r, double* z,
             }
          }
       }
-      R* sol = F.sol;
-      const R* u = L0.u;
-      map(ng, [=] __device__(long long t) { sol[t] += u[t]; }, cx.s);
-      fill_ghosts_t(g, F.sol, cx.s);
-      residual(op, g, F.f0, F.sol, F.rr, cx.s);
-      norm = rms_interior(cx, g, F.rr);
+      if (it > 0) {  // ghosts included: u's ghosts are current
+         R* sol = F.sol;
+         const R* u = L0.u;
+         map(ng, [=] __device__(long long t) { sol[t] += u[t]; }, cx.s);
+      }
+      int nblk = 0;
+      residual_partial(op, g, F.f0, F.sol, F.rr, cx.red->part, &nblk, cx.s);
+      k_finish<<<1, 1024, 0, cx.s>>>(cx.red->part, nblk, cx.red->dres, 0);
+      g_launches++;
+      norm = sqrt(cx.red->fetch(1)[0] / (double)g.cells());
       it++;
    } while (norm > tol && it < cx.p->fac_max_cycles);
-   k_from_ghosted<R><<<map_blocks(g.cells()), 256, 0, cx.s>>>(g, F.sol, z);
+   L0.f = f_own;
+   L0.u = u_own;
+   k_from_ghosted<R, R><<<map_blocks(g.cells()), 256, 0, cx.s>>>(g, F.sol, z);
    launch_status();
    cx.st->fac_cycles += it;
    return it;
@@ -450,8 +431,11 @@ struct Stepper {
    MixParams mp;               // FP32 constants of the mixed kernels
    unsigned long long* counters;
    // 2N interior vectors
-   double *yn, *ynm1, *ynew, *a, *y, *fy, *b, *d, *w, *tmp, *av, *fp;
+   double *yn, *ynm1, *ynew, *a, *y, *fy, *b, *d, *w, *wi, *tmp, *av, *fp;
    std::vector<double*> V;
+   // mixed path Krylov vectors (FP32) and FP32 copies of the WRMS weights
+   std::vector<float*> Vf;
+   float *tmpf = nullptr, *avf = nullptr, *bf = nullptr, *w32 = nullptr, *wi32 = nullptr;
    // mixed path (FP32 working copies)
    float *cl32 = nullptr, *cs32 = nullptr, *clr32 = nullptr, *csr32 = nullptr;
    float *dF32 = nullptr, *pf32 = nullptr, *dphi32 = nullptr, *da32 = nullptr,
@@ -481,8 +465,29 @@ struct Stepper {
    Ctx ctx() { return Ctx{s, &red, &p, &st}; }
 };
 
+constexpr int kMaxKrylov = 16;  // Krylov dimension limit of the stepper
+
+// coefficients and basis vectors of the GMRES update, passed by value
+struct KrylovComb {
+   const double* v[kMaxKrylov];
+   double c[kMaxKrylov];
+};
+struct KrylovCombF {
+   const float* v[kMaxKrylov];
+   float c[kMaxKrylov];
+};
+
 // kernel classes timed in profiling mode
-enum { KT_KKS = 0, KT_RHS = 1, KT_JV = 2, KT_MLP = 3, KT_QUAT = 4, KT_NKINDS = 5 };
+enum {
+   KT_KKS = 0,
+   KT_RHS = 1,
+   KT_JV = 2,
+   KT_MLP = 3,
+   KT_QUAT = 4,
+   KT_PREC = 5,  // whole preconditioner solve (all blocks)
+   KT_PSET = 6,  // preconditioner setup
+   KT_NKINDS = 7
+};
 
 static cudaEvent_t prof_event(Stepper& S)
 {
@@ -624,6 +629,23 @@ static double dot(Stepper& S, const double* a, const double* b)
    return S.red.sum(S.NY, [=] __device__(long long t) { return a[t] * b[t]; });
 }
 
+// composition block faces D = -gamma (D_L + D_S): FP64 at the lagged phi, or
+// FP32 from the FP32 phi copy of the last f(y) (mixed path)
+static void conc_precond_faces(Stepper& S, const double* tf, double gamma,
+                               DevLevel<double>& C0)
+{
+   const long long nf = S.g.nfx() + S.g.nfy() + (S.g.dim == 3 ? S.g.nfz() : 0);
+   k_conc_precond_faces<double><<<map_blocks(nf), 256, 0, S.s>>>(
+       S.m, S.g, S.phi_lag, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
+   launch_status();
+}
+
+static void conc_precond_faces(Stepper& S, const double* tf, double gamma,
+                               DevLevel<float>& C0)
+{
+   conc_faces_f32(S.m, S.mp, S.g, tf, S.pf32, gamma, C0.D, S.s);
+}
+
 // D = gamma fc of the quaternion block: FP64 from the lagged q, or FP32 from
 // the FP32 working copy (mixed path)
 static void quat_precond_faces(Stepper& S, const double* tf, double gamma,
@@ -653,12 +675,7 @@ static void precond_setup_t(Stepper& S, DevFac<R>& fp, DevFac<R>& fc,
       L.mc = (R)S.m.phase_mobility;
    }
    fac_coarsen_operator(fp, S.s);
-   DevLevel<R>& C0 = fc.lev[0];
-   const long long nf = S.g.nfx() + S.g.nfy() + (S.g.dim == 3 ? S.g.nfz() : 0);
-   const double* phid = S.p.precision == 1 ? S.phi_g : S.phi_lag;
-   k_conc_precond_faces<R><<<map_blocks(nf), 256, 0, S.s>>>(
-       S.m, S.g, phid, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
-   launch_status();
+   conc_precond_faces(S, tf, gamma, fc.lev[0]);
    for (auto& L : fc.lev) {
       L.dc = 0;
       L.cc = (R)1.0;
@@ -683,6 +700,7 @@ static void precond_setup_t(Stepper& S, DevFac<R>& fp, DevFac<R>& fc,
 
 static void precond_setup(Stepper& S, double gamma)
 {
+   ProfScope ps(S, KT_PSET);
    if (S.p.precision == 1)
       precond_setup_t(S, S.facp32, S.facc32, S.facq32, gamma);
    else
@@ -690,6 +708,7 @@ static void precond_setup(Stepper& S, double gamma)
    S.st.precond_setups++;
 }
 
+// z = P^-1 r, one FAC solve per block (FP64 path)
 static void precond_solve(Stepper& S, const double* r, double* z,
                           double delta)
 {
@@ -698,15 +717,26 @@ static void precond_solve(Stepper& S, const double* r, double* z,
                       S.s);
       return;
    }
+   ProfScope ps(S, KT_PREC);
    Ctx cx = S.ctx();
-   for (int blk = 0; blk < S.nb; blk++) {
-      if (S.p.precision == 1)
-         fac_solve(cx, blk == 0 ? S.facp32 : (blk == 1 ? S.facc32 : S.facq32),
-                   S.p.precond, r + blk * S.N, z + blk * S.N, delta);
-      else
-         fac_solve(cx, blk == 0 ? S.facp64 : (blk == 1 ? S.facc64 : S.facq64),
-                   S.p.precond, r + blk * S.N, z + blk * S.N, delta);
+   for (int blk = 0; blk < S.nb; blk++)
+      fac_solve(cx, blk == 0 ? S.facp64 : (blk == 1 ? S.facc64 : S.facq64), S.p.precond,
+                r + blk * S.N, z + blk * S.N, delta);
+   S.st.precond_solves++;
+}
+
+// the same with FP32 Krylov vectors and FP32 FAC blocks (mixed path)
+static void precond_solve(Stepper& S, const float* r, float* z, double delta)
+{
+   if (S.p.precond == 0) {
+      cudaMemcpyAsync(z, r, sizeof(float) * S.NY, cudaMemcpyDeviceToDevice, S.s);
+      return;
    }
+   ProfScope ps(S, KT_PREC);
+   Ctx cx = S.ctx();
+   for (int blk = 0; blk < S.nb; blk++)
+      fac_solve(cx, blk == 0 ? S.facp32 : (blk == 1 ? S.facc32 : S.facq32), S.p.precond,
+                r + blk * S.N, z + blk * S.N, delta);
    S.st.precond_solves++;
 }
 
@@ -715,18 +745,12 @@ static void matvec(Stepper& S, const double* y, const double* fy,
                    const double* w, double gamma, const double* v,
                    double* out)
 {
-   if (S.p.precision == 1) {
-      const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
-      ProfScope ps(S, KT_JV);
-      jv_mixed(S.m, S.mp, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma,
-               S.dphi32, S.da32, S.db32, S.nb == 6 ? &S.qf32 : nullptr, out, S.s);
-      return;
-   }
-   const double sig = 1.0 / wrms(S, v, w);
+   const double wn = wrms(S, v, w);
+   const double sig = 1.0 / wn;
    eval_rhs(S, y, v, sig, S.fp, 1);
    const double* fp = S.fp;
    map(S.NY, [=] __device__(long long t) {
-      out[t] = v[t] - gamma * (fp[t] - fy[t]) / sig;
+      out[t] = v[t] - gamma * (fp[t] - fy[t]) * wn;
    }, S.s);
 }
 
@@ -741,34 +765,64 @@ static int gmres(Stepper& S, const double* y, const double* fy,
        sn(maxl);
    double* tmp = S.tmp;
    double* av = S.av;
-   cudaMemsetAsync(x, 0, sizeof(double) * ny, S.s);
+   const double* wi = S.wi;  // 1 / w
    precond_solve(S, b, tmp, tol * sqrtN);
    double* V0 = S.V[0];
-   map(ny, [=] __device__(long long t) { V0[t] = w[t] * tmp[t]; }, S.s);
-   double beta = std::sqrt(dot(S, V0, V0));
-   if (beta / sqrtN <= tol) return 0;
+   // V0 = w P^-1 b and |V0|^2 in one pass
+   double beta = std::sqrt(S.red.sum(ny, [=] __device__(long long t) {
+      const double xv = w[t] * tmp[t];
+      V0[t] = xv;
+      return xv * xv;
+   }));
+   if (beta / sqrtN <= tol) {
+      cudaMemsetAsync(x, 0, sizeof(double) * ny, S.s);
+      return 0;
+   }
    {
-      const double ib = beta;
-      map(ny, [=] __device__(long long t) { V0[t] /= ib; }, S.s);
+      const double ib = 1.0 / beta;
+      map(ny, [=] __device__(long long t) { V0[t] *= ib; }, S.s);
    }
    gv[0] = beta;
    int l = 0;
    for (; l < maxl; l++) {
       double* Vl = S.V[l];
       double* Vn = S.V[l + 1];
-      map(ny, [=] __device__(long long t) { tmp[t] = Vl[t] / w[t]; }, S.s);
+      map(ny, [=] __device__(long long t) { tmp[t] = Vl[t] * wi[t]; }, S.s);
       matvec(S, y, fy, w, gamma, tmp, av);
       precond_solve(S, av, tmp, tol * sqrtN);
-      map(ny, [=] __device__(long long t) { Vn[t] = w[t] * tmp[t]; }, S.s);
+      // modified Gram-Schmidt; every projection pass also forms the next
+      // inner product (with V_{i+1}, or |Vn|^2 after the last one)
+      double h = S.red.sum(ny, [=] __device__(long long t) {
+         const double xv = w[t] * tmp[t];
+         Vn[t] = xv;
+         return V0[t] * xv;
+      });
+      double hn2 = 0.0;
       for (int i = 0; i <= l; i++) {
-         double* Vi = S.V[i];
-         const double h = dot(S, Vi, Vn);
          H[i * maxl + l] = h;
-         map(ny, [=] __device__(long long t) { Vn[t] -= h * Vi[t]; }, S.s);
+         const double* Vi = S.V[i];
+         const double hh = h;
+         if (i < l) {
+            const double* Vj = S.V[i + 1];
+            h = S.red.sum(ny, [=] __device__(long long t) {
+               const double xv = Vn[t] - hh * Vi[t];
+               Vn[t] = xv;
+               return Vj[t] * xv;
+            });
+         } else {
+            hn2 = S.red.sum(ny, [=] __device__(long long t) {
+               const double xv = Vn[t] - hh * Vi[t];
+               Vn[t] = xv;
+               return xv * xv;
+            });
+         }
       }
-      const double hn = std::sqrt(dot(S, Vn, Vn));
+      const double hn = std::sqrt(hn2);
       H[(l + 1) * maxl + l] = hn;
-      if (hn > 0.0) map(ny, [=] __device__(long long t) { Vn[t] /= hn; }, S.s);
+      if (hn > 0.0) {
+         const double ih = 1.0 / hn;
+         map(ny, [=] __device__(long long t) { Vn[t] *= ih; }, S.s);
+      }
       for (int i = 0; i < l; i++) {
          const double aa = H[i * maxl + l], bb = H[(i + 1) * maxl + l];
          H[i * maxl + l] = cs[i] * aa + sn[i] * bb;
@@ -794,12 +848,137 @@ static int gmres(Stepper& S, const double* y, const double* fy,
       for (int j = i + 1; j < k; j++) acc -= H[i * maxl + j] * yk[j];
       yk[i] = acc / H[i * maxl + i];
    }
+   // x = (sum_i yk_i V_i) / w in one pass (same summation order)
+   KrylovComb cb;
    for (int i = 0; i < k; i++) {
-      const double c = yk[i];
-      double* Vi = S.V[i];
-      map(ny, [=] __device__(long long t) { x[t] += c * Vi[t]; }, S.s);
+      cb.v[i] = S.V[i];
+      cb.c[i] = yk[i];
    }
-   map(ny, [=] __device__(long long t) { x[t] /= w[t]; }, S.s);
+   map(ny, [=] __device__(long long t) {
+      double acc = 0.0;
+      for (int i = 0; i < k; i++) acc += cb.c[i] * cb.v[i][t];
+      x[t] = acc * wi[t];
+   }, S.s);
+   return k;
+}
+
+// out = v - gamma J v with the analytic FP32 product at the state of the
+// last f(y) (mixed path)
+static void matvec32(Stepper& S, double gamma, const float* v, float* out)
+{
+   const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
+   ProfScope ps(S, KT_JV);
+   jv_mixed(S.m, S.mp, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma, S.dphi32,
+            S.da32, S.db32, S.nb == 6 ? &S.qf32 : nullptr, out, S.s);
+}
+
+// GMRES of the mixed path: the same algorithm as gmres() (left
+// preconditioning, WRMS scaling, modified Gram-Schmidt) on FP32 Krylov
+// vectors.  Inner products: FP32 products, compensated FP32 sums per thread,
+// FP64 across threads and blocks.  b and the correction x are FP64.
+static int gmres32(Stepper& S, double gamma, const double* b, double* x,
+                   double tol)
+{
+   const long long ny = S.NY;
+   const int maxl = S.p.max_krylov;
+   const double sqrtN = std::sqrt((double)ny);
+   std::vector<double> H((maxl + 1) * maxl, 0.0), gv(maxl + 1, 0.0), cs(maxl),
+       sn(maxl);
+   float* tmp = S.tmpf;
+   float* av = S.avf;
+   const float* w = S.w32;
+   const float* wi = S.wi32;
+   float* bf = S.bf;
+   map(ny, [=] __device__(long long t) { bf[t] = d2f(b[t]); }, S.s);
+   precond_solve(S, bf, tmp, tol * sqrtN);
+   float* V0 = S.Vf[0];
+   double beta = std::sqrt(S.red.sumf(ny, [=] __device__(long long t) {
+      const float xv = w[t] * tmp[t];
+      V0[t] = xv;
+      return xv * xv;
+   }));
+   if (beta / sqrtN <= tol) {
+      cudaMemsetAsync(x, 0, sizeof(double) * ny, S.s);
+      return 0;
+   }
+   {
+      const float ib = (float)(1.0 / beta);
+      map(ny, [=] __device__(long long t) { V0[t] *= ib; }, S.s);
+   }
+   gv[0] = beta;
+   int l = 0;
+   for (; l < maxl; l++) {
+      float* Vl = S.Vf[l];
+      float* Vn = S.Vf[l + 1];
+      map(ny, [=] __device__(long long t) { tmp[t] = Vl[t] * wi[t]; }, S.s);
+      matvec32(S, gamma, tmp, av);
+      precond_solve(S, av, tmp, tol * sqrtN);
+      double h = S.red.sumf(ny, [=] __device__(long long t) {
+         const float xv = w[t] * tmp[t];
+         Vn[t] = xv;
+         return V0[t] * xv;
+      });
+      double hn2 = 0.0;
+      for (int i = 0; i <= l; i++) {
+         H[i * maxl + l] = h;
+         const float* Vi = S.Vf[i];
+         const float hh = (float)h;
+         if (i < l) {
+            const float* Vj = S.Vf[i + 1];
+            h = S.red.sumf(ny, [=] __device__(long long t) {
+               const float xv = Vn[t] - hh * Vi[t];
+               Vn[t] = xv;
+               return Vj[t] * xv;
+            });
+         } else {
+            hn2 = S.red.sumf(ny, [=] __device__(long long t) {
+               const float xv = Vn[t] - hh * Vi[t];
+               Vn[t] = xv;
+               return xv * xv;
+            });
+         }
+      }
+      const double hn = std::sqrt(hn2);
+      H[(l + 1) * maxl + l] = hn;
+      if (hn > 0.0) {
+         const float ih = (float)(1.0 / hn);
+         map(ny, [=] __device__(long long t) { Vn[t] *= ih; }, S.s);
+      }
+      for (int i = 0; i < l; i++) {
+         const double aa = H[i * maxl + l], bb = H[(i + 1) * maxl + l];
+         H[i * maxl + l] = cs[i] * aa + sn[i] * bb;
+         H[(i + 1) * maxl + l] = -sn[i] * aa + cs[i] * bb;
+      }
+      const double aa = H[l * maxl + l], bb = H[(l + 1) * maxl + l];
+      const double rr = std::sqrt(aa * aa + bb * bb);
+      cs[l] = aa / rr;
+      sn[l] = bb / rr;
+      H[l * maxl + l] = rr;
+      H[(l + 1) * maxl + l] = 0.0;
+      gv[l + 1] = -sn[l] * gv[l];
+      gv[l] = cs[l] * gv[l];
+      if (std::fabs(gv[l + 1]) / sqrtN <= tol || hn == 0.0) {
+         l++;
+         break;
+      }
+   }
+   const int k = std::min(l, maxl);
+   std::vector<double> yk(k, 0.0);
+   for (int i = k - 1; i >= 0; i--) {
+      double acc = gv[i];
+      for (int j = i + 1; j < k; j++) acc -= H[i * maxl + j] * yk[j];
+      yk[i] = acc / H[i * maxl + i];
+   }
+   KrylovCombF cb;
+   for (int i = 0; i < k; i++) {
+      cb.v[i] = S.Vf[i];
+      cb.c[i] = (float)yk[i];
+   }
+   map(ny, [=] __device__(long long t) {
+      float acc = 0.f;
+      for (int i = 0; i < k; i++) acc += cb.c[i] * cb.v[i][t];
+      x[t] = f2d(acc * wi[t]);
+   }, S.s);
    return k;
 }
 
@@ -818,14 +997,31 @@ static int bdf_step(Stepper& S, double h, int q)
       }, S.s);
    } else {
       gamma = 2.0 * h / 3.0;
+      const double third = 1.0 / 3.0;
       map(ny, [=] __device__(long long t) {
-         a[t] = (4.0 * yn[t] - ynm1[t]) / 3.0;
+         a[t] = (4.0 * yn[t] - ynm1[t]) * third;
          y[t] = 2.0 * yn[t] - ynm1[t];
       }, S.s);
    }
    const double rtol = S.p.rtol, atol = S.p.atol;
-   map(ny, [=] __device__(long long t) { w[t] = 1.0 / (rtol * fabs(yn[t]) + atol); },
-       S.s);
+   double* wi = S.wi;
+   if (S.p.precision == 1) {
+      float *w32 = S.w32, *wi32 = S.wi32;
+      map(ny, [=] __device__(long long t) {
+         const double e = rtol * fabs(yn[t]) + atol;
+         const double wv = 1.0 / e;
+         w[t] = wv;
+         wi[t] = e;
+         w32[t] = d2f(wv);
+         wi32[t] = d2f(e);
+      }, S.s);
+   } else {
+      map(ny, [=] __device__(long long t) {
+         const double e = rtol * fabs(yn[t]) + atol;
+         w[t] = 1.0 / e;
+         wi[t] = e;
+      }, S.s);
+   }
    double crate = 1.0, delp = 0.0;
    const double lintol = S.p.lin_coef * S.p.newton_coef;
    for (int it = 0; it < S.p.max_newton; it++) {
@@ -834,11 +1030,16 @@ static int bdf_step(Stepper& S, double h, int q)
       const double gm = gamma;
       map(ny, [=] __device__(long long t) { b[t] = -(y[t] - gm * fy[t] - a[t]); },
           S.s);
-      const int li = gmres(S, y, fy, w, gamma, b, d, lintol);
+      const int li = S.p.precision == 1 ? gmres32(S, gamma, b, d, lintol)
+                                        : gmres(S, y, fy, w, gamma, b, d, lintol);
       S.st.gmres_iters += li;
       S.st.newton_iters++;
-      map(ny, [=] __device__(long long t) { y[t] += d[t]; }, S.s);
-      const double del = wrms(S, d, w);
+      // y += d and WRMS(d) in one pass
+      const double del = std::sqrt(S.red.sum(ny, [=] __device__(long long t) {
+         y[t] += d[t];
+         const double xv = d[t] * w[t];
+         return xv * xv;
+      }) / (double)ny);
       if (it > 0) crate = std::max(0.3 * crate, del / delp);
       const double dcon = del * std::min(1.0, crate) / S.p.newton_coef;
       if (dcon <= 1.0) {
@@ -877,7 +1078,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
        p->max_order < 1 || p->atol <= 0.0)
       return AMPE_ERR_INVALID;
    if (p->precond < 0 || p->precond > 2 || p->precision < 0 ||
-       p->precision > 1)
+       p->precision > 1 || p->max_krylov > kMaxKrylov)
       return AMPE_ERR_INVALID;
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC) return AMPE_ERR_INVALID;
    if (m->evolve_quat && (m->quat_mobility_type != 'p' || !(m->quat_grad_floor > 0.0)))
@@ -902,10 +1103,17 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
                     &S->csr, &S->cl_nf, &S->cs_nf, &S->phi_lag, &S->tfield};
    for (double** q : gh) *q = dvec(*S, S->NG, &err);
    S->dF = dvec(*S, S->N, &err);
-   double** vv[] = {&S->yn, &S->ynm1, &S->ynew, &S->a, &S->y, &S->fy,
-                    &S->b,  &S->d,    &S->w,    &S->tmp, &S->av, &S->fp};
+   double** vv[] = {&S->yn, &S->ynm1, &S->ynew, &S->a,   &S->y,  &S->fy, &S->b,
+                    &S->d,  &S->w,    &S->wi,   &S->tmp, &S->av, &S->fp};
    for (double** q : vv) *q = dvec(*S, S->NY, &err);
-   for (int l = 0; l <= p->max_krylov; l++) S->V.push_back(dvec(*S, S->NY, &err));
+   if (p->precision == 1) {
+      for (int l = 0; l <= p->max_krylov; l++)
+         S->Vf.push_back((float*)dalloc<float>(S->pool, S->NY, &err));
+      float** fv[] = {&S->tmpf, &S->avf, &S->bf, &S->w32, &S->wi32};
+      for (float** q : fv) *q = (float*)dalloc<float>(S->pool, S->NY, &err);
+   } else {
+      for (int l = 0; l <= p->max_krylov; l++) S->V.push_back(dvec(*S, S->NY, &err));
+   }
    S->counters = (unsigned long long*)dalloc<unsigned long long>(S->pool, 2, &err);
    if (S->nb == 6) {
       S->q_g = dvec(*S, 4 * S->NG, &err);
@@ -1041,11 +1249,15 @@ int ampe_stepper_get_state(void* h, double* phi, double* conc, double* cl,
    if (conc) cudaMemcpyAsync(conc, S->yn + S->N, bytes, kind, S->s);
    if (cl || cs) {
       if (S->p.precision == 1) {
-         k_from_ghosted<float><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr32, S->tmp);
-         k_from_ghosted<float><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->csr32, S->tmp + S->N);
+         k_from_ghosted<float, double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr32,
+                                                                           S->tmp);
+         k_from_ghosted<float, double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->csr32,
+                                                                           S->tmp + S->N);
       } else {
-         k_from_ghosted<double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr, S->tmp);
-         k_from_ghosted<double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->csr, S->tmp + S->N);
+         k_from_ghosted<double, double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr,
+                                                                            S->tmp);
+         k_from_ghosted<double, double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->csr,
+                                                                            S->tmp + S->N);
       }
       g_launches += 2;
       if (cl) cudaMemcpyAsync(cl, S->tmp, bytes, kind, S->s);
@@ -1193,11 +1405,24 @@ int ampe_stepper_jv(void* h, const double* v, double gamma, double* out,
    const size_t b2 = sizeof(double) * (size_t)S->NY;
    double *w = S->w, *yn = S->yn;
    const double rtol = S->p.rtol, atol = S->p.atol;
-   map(S->NY, [=] __device__(long long t) { w[t] = 1.0 / (rtol * fabs(yn[t]) + atol); },
-       S->s);
+   double* wi = S->wi;
+   map(S->NY, [=] __device__(long long t) {
+      const double e = rtol * fabs(yn[t]) + atol;
+      w[t] = 1.0 / e;
+      wi[t] = e;
+   }, S->s);
    eval_rhs(*S, S->yn, nullptr, 0.0, S->fy, 0);
    cudaMemcpyAsync(S->b, v, b2, in, S->s);
-   matvec(*S, S->yn, S->fy, S->w, gamma, S->b, S->d);
+   if (S->p.precision == 1) {
+      const double* bd = S->b;
+      double* dd = S->d;
+      float *bf = S->bf, *of = S->avf;
+      map(S->NY, [=] __device__(long long t) { bf[t] = d2f(bd[t]); }, S->s);
+      matvec32(*S, gamma, bf, of);
+      map(S->NY, [=] __device__(long long t) { dd[t] = f2d(of[t]); }, S->s);
+   } else {
+      matvec(*S, S->yn, S->fy, S->w, gamma, S->b, S->d);
+   }
    cudaMemcpyAsync(out, S->d, b2, ot, S->s);
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
    return AMPE_OK;

@@ -41,9 +41,10 @@ RHS_BYTES_PER_CELL = 56  # read phi, phi_lag, cL, cS, dF; write phi', c'
 KKS_MIXED_BYTES_PER_CELL = 36
 # mixed RHS: read phi (FP32 copy), cL, cS, dF (FP32), write phi', c' (FP64)
 RHS_MIXED_BYTES_PER_CELL = 36
-# analytic Jv: point pass 44 B (v FP64, phi, cL, cS; write dphi, dcL, dcS
-# FP32) + stencil pass 64 B (dphi, dcL, dcS, phi, cL, cS, dF, v; write out)
-JV_BYTES_PER_CELL = 108
+# analytic Jv on FP32 Krylov vectors: point pass 32 B (v, phi, cL, cS; write
+# dphi, dcL, dcS) + stencil pass 44 B (dphi, dcL, dcS, phi, cL, cS, dF, v;
+# write out)
+JV_BYTES_PER_CELL = 76
 # MLP inference: 2 (3*64 + 64*64 + 64*64 + 64*2) multiply-adds per cell
 MLP_FLOPS_PER_CELL = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
 KERNEL_NAMES = {

@@ -418,8 +418,9 @@ long long ampe_stepper_kernel_launches(void* handle);
 void* ampe_stepper_stream(void* handle);
 /* Per-kernel CUDA-event timing on the stepper stream.  kind: 0 KKS Newton,
  * 1 fused RHS, 2 analytic Jacobian-vector product (mixed path), 3 surrogate
- * inference, 4 quaternion RHS (mobility, face coefficients, divergence).
- * Enabling resets the totals. */
+ * inference, 4 quaternion RHS (mobility, face coefficients, divergence),
+ * 5 preconditioner solves (all blocks, FAC cycles included), 6
+ * preconditioner setups.  Enabling resets the totals. */
 int ampe_stepper_profile(void* handle, int enable);
 int ampe_stepper_kernel_time(void* handle, int kind, double* total_ms,
                              long long* launches);
