@@ -39,6 +39,7 @@ _PROTOS = {
     "ampe_rhs_phase_conc": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_efo_rbgs": (I, [MP, P, P, P, D, P, D, P, D, P, P, I, P, P]),
     "ampe_efo_residual": (I, [MP, P, P, P, D, P, D, P, D, P, P, P, P]),
+    "ampe_efo_rbgs_sweep": (I, [MP, P, P, P, D, P, D, P, D, P, P, P, P]),
     "ampe_phase_fac_set_c": (I, [MP, P, D, P, P]),
     "ampe_quat_grad_modulus": (I, [MP, P, P, P]),
     "ampe_quat_mobility": (I, [MP, P, P, P]),

@@ -394,6 +394,12 @@ inline int launch_status()
    cudaError_t e = cudaGetLastError();
    return e == cudaSuccess ? AMPE_OK : AMPE_ERR_CUDA;
 }
+// grid cap of the grid-stride kernels: 32 blocks of 256 per SM.  Threads
+// then loop over several items and set up their per-thread constants once
+// (measured faster than one thread per item for the stencil kernels, whose
+// setup includes FP64 work; the smoother colour and residual kernels run one
+// thread per item instead)
+constexpr long long kMaxBlocks = 152 * 32;
 inline unsigned grid_for(long long n, int block)
 {
    return (unsigned)((n + block - 1) / block);

@@ -80,7 +80,7 @@ __global__ void k_map(long long n, F f)
 inline unsigned map_blocks(long long n)
 {
    long long b = (n + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    return (unsigned)(b < 1 ? 1 : b);
 }
 

@@ -102,7 +102,7 @@ int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s)
    const long long tot = 2LL * g.gz * SX * SY + (long long)g.n2 * 2 * g.ng * SX +
                          (long long)g.n2 * g.n1 * 2 * g.ng;
    long long b = (tot + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    k_fill_ghosts_gather<R><<<(unsigned)(b < 1 ? 1 : b), 256, 0, s>>>(g, f);
    return launch_status();
 }
@@ -112,26 +112,30 @@ int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s)
 // colours (the stepper's smoother); the leaf entry point updates the
 // interior only.
 template <class R>
-__global__ void k_rbgs_color(FacOp<R> op, Grid g, const R* f, R* u,
-                             int offset, double* maxres, bool images)
+__global__ void __launch_bounds__(256)
+    k_rbgs_color(FacOp<R> op, Grid g, const R* __restrict__ f, R* u, int offset,
+                 double* maxres, bool images)
 {
-   // one thread per cell of the colour: i = 2*ih + parity(j,k)
+   // one thread per cell of the colour, i = 2*ih + parity(j,k): every cell's
+   // loads are in flight at once (no grid-stride loop that would serialise
+   // them behind the in-place stores)
    const int nh = (g.n0 + 1) / 2;
    const long long tot = (long long)nh * g.n1 * g.n2;
    R mres = R(0);
-   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-        t < tot; t += (long long)gridDim.x * blockDim.x) {
+   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+   if (t < tot) {
       int ih, j, k;
       g.split(t, g.fdh, g.fd1, ih, j, k);
       const int i = 2 * ih + ((j + k + offset) & 1);
-      if (i >= g.n0) continue;
-      R dudr;
-      const R r = cell_residual(op, g, f, u, i, j, k, &dudr);
-      const long long c = g.c(i, j, k);
-      const R un = u[c] + -r * dudr;
-      u[c] = un;
-      if (images) for_each_image(g, i, j, k, [&](long long idx) { u[idx] = un; });
-      if (maxres) mres = fmax(mres, fabs(r));
+      if (i < g.n0) {
+         R dudr;
+         const R r = cell_residual(op, g, f, u, i, j, k, &dudr);
+         const int c = g.c(i, j, k);
+         const R un = u[c] + -r * dudr;
+         u[c] = un;
+         if (images) for_each_image(g, i, j, k, [&](long long idx) { u[idx] = un; });
+         if (maxres) mres = fmax(mres, fabs(r));
+      }
    }
    if (maxres) {
       double mr = (double)mres;
@@ -141,14 +145,216 @@ __global__ void k_rbgs_color(FacOp<R> op, Grid g, const R* f, R* u,
    }
 }
 
+// ---------------------------------------------------------------------------
+// One whole red-black sweep (red, then black) in one launch.
+//
+// Each block owns a box of cells (32 x 8 x 4 in 3D, 32 x 16 in 2D).  It
+// stages u over the box plus a halo of two cells, and f, C, M over the box
+// plus one, in shared memory with dense coalesced loads; updates the red
+// cells of the box plus its halo of one (neighbouring blocks repeat those
+// halo updates on identical inputs), then the black cells of the box, and
+// writes the box to uout with its periodic ghost images.  u is read from uin
+// and written to uout, so no block reads values another block has written
+// and the result is the two colour passes' result, bit for bit: every update
+// evaluates cell_residual's expression in the same order.  Colours follow
+// (i + j + k) % 2 of the interior index, which requires even extents.
+// ---------------------------------------------------------------------------
+template <int DIM>
+struct SweepBox {
+   static constexpr int TX = 32, TY = DIM == 3 ? 8 : 16, TZ = DIM == 3 ? 4 : 1;
+   static constexpr int BX = TX + 4, BY = TY + 4, BZ = DIM == 3 ? TZ + 4 : 1;  // u, halo 2
+   static constexpr int CX = TX + 2, CY = TY + 2, CZ = DIM == 3 ? TZ + 2 : 1;  // halo 1
+   static constexpr int NU = BX * BY * BZ, NC = CX * CY * CZ;
+};
+
+template <class R>
+size_t rb_sweep_smem(const FacOp<R>& op, int dim)
+{
+   const int nu = dim == 3 ? SweepBox<3>::NU : SweepBox<2>::NU;
+   const int nc = dim == 3 ? SweepBox<3>::NC : SweepBox<2>::NC;
+   return sizeof(R) * (size_t)(nu + nc * (1 + (op.C ? 1 : 0) + (op.M ? 1 : 0)));
+}
+
+// periodic wrap of an index a >= -2 into [0, n); extents below the halo
+// reach take the modulo
+__device__ __forceinline__ int wrap_idx(int a, int n)
+{
+   return a < 0 ? (a + n) % n : (a >= n ? (a - n < n ? a - n : a % n) : a);
+}
+
+// blockDim (32, 8): lane x along rows, warp y over rows
+template <class R, int DIM, bool ZERO>
+__global__ void __launch_bounds__(256)
+    k_rb_sweep(FacOp<R> op, Grid g, const R* __restrict__ f, const R* __restrict__ uin,
+               R* __restrict__ uout)
+{
+   using B = SweepBox<DIM>;
+   extern __shared__ __align__(16) unsigned char sweep_smem[];
+   R* U = (R*)sweep_smem;
+   R* Fs = U + B::NU;
+   R* Cs = Fs + B::NC;
+   R* Ms = Cs + (op.C ? B::NC : 0);
+   const int tx = threadIdx.x, ty = threadIdx.y;
+   const int i0 = blockIdx.x * B::TX, j0 = blockIdx.y * B::TY, k0 = blockIdx.z * B::TZ;
+   const int pitch_z = g.sy, pitch_y = g.sx;
+   // address of cell (i, 0, 0) minus i for row (j, k): c = rowc + i
+   auto rowc = [&](int j, int k) { return g.c(0, j, k); };
+   const int ia = wrap_idx(i0 + tx - 2, g.n0);            // x of lane tx in the u box
+   const int ib = tx < 4 ? wrap_idx(i0 + tx + 30, g.n0) : 0;  // x of lane tx + 32
+   const int ic = wrap_idx(i0 + tx - 1, g.n0);            // x of lane tx in the f box
+   const int id = tx < 2 ? wrap_idx(i0 + tx + 31, g.n0) : 0;
+   (void)pitch_z;
+   (void)pitch_y;
+   if (!ZERO) {
+      for (int z = 0; z < B::BZ; z++) {
+         const int kw = DIM == 3 ? wrap_idx(k0 + z - 2, g.n2) : 0;
+         for (int y = ty; y < B::BY; y += 8) {
+            const int rc = rowc(wrap_idx(j0 + y - 2, g.n1), kw);
+            R* dst = U + (z * B::BY + y) * B::BX;
+            dst[tx] = uin[rc + ia];
+            if (tx < 4) dst[tx + 32] = uin[rc + ib];
+         }
+      }
+   } else {
+      for (int p = ty * 32 + tx; p < B::NU; p += 256) U[p] = R(0);
+   }
+   for (int z = 0; z < B::CZ; z++) {
+      const int kw = DIM == 3 ? wrap_idx(k0 + z - 1, g.n2) : 0;
+      for (int y = ty; y < B::CY; y += 8) {
+         const int rc = rowc(wrap_idx(j0 + y - 1, g.n1), kw);
+         const int o = (z * B::CY + y) * B::CX;
+         Fs[o + tx] = f[rc + ic];
+         if (tx < 2) Fs[o + tx + 32] = f[rc + id];
+         if (op.C) {
+            Cs[o + tx] = op.C[rc + ic];
+            if (tx < 2) Cs[o + tx + 32] = op.C[rc + id];
+         }
+         if (op.M) {
+            Ms[o + tx] = op.M[rc + ic];
+            if (tx < 2) Ms[o + tx + 32] = op.M[rc + id];
+         }
+      }
+   }
+   __syncthreads();
+   // one colour on the u-box rows [lo, hiy) x [lo, hiz) (3D), lanes along x
+   auto colour = [&](int col, int lo, int nxh, int hiy, int hiz) {
+      const int zlo = DIM == 3 ? lo : 0, zhi = DIM == 3 ? hiz : 1;
+      const int ny = hiy - lo;
+      for (int rr = ty; rr < ny * (zhi - zlo); rr += 8) {
+         const int z = zlo + rr / ny, y = lo + rr % ny;
+         if (tx >= nxh) continue;
+         const int jg = j0 + y - 2, kg = DIM == 3 ? k0 + z - 2 : 0;
+         const int q = (col + i0 + jg + kg) & 1;  // parity of x for this colour
+         const int x = lo + ((q + lo) & 1) + 2 * tx;
+         const int u0 = (z * B::BY + y) * B::BX + x;
+         const int c0 = ((DIM == 3 ? z - 1 : 0) * B::CY + (y - 1)) * B::CX + (x - 1);
+         const R uc = U[u0];
+         R div = R(0), dsum = R(0);
+         int iw = 0, jw = 0, kw = 0;
+         if (op.D0) {
+            iw = wrap_idx(i0 + x - 2, g.n0);
+            jw = wrap_idx(jg, g.n1);
+            kw = DIM == 3 ? wrap_idx(kg, g.n2) : 0;
+         }
+         {
+            const R dxi = op.dxi[0];
+            const R Dm = op.D0 ? op.D0[g.fx(iw, jw, kw)] : op.dc;
+            const R Dp = op.D0 ? op.D0[g.fx(iw + 1, jw, kw)] : op.dc;
+            const R fm = dxi * Dm * (uc - U[u0 - 1]);
+            const R fp = dxi * Dp * (U[u0 + 1] - uc);
+            div += dxi * (fp - fm);
+            dsum += dxi * dxi * (Dp + Dm);
+         }
+         {
+            const R dxi = op.dxi[1];
+            const R Dm = op.D0 ? op.D1[g.fy(iw, jw, kw)] : op.dc;
+            const R Dp = op.D0 ? op.D1[g.fy(iw, jw + 1, kw)] : op.dc;
+            const R fm = dxi * Dm * (uc - U[u0 - B::BX]);
+            const R fp = dxi * Dp * (U[u0 + B::BX] - uc);
+            div += dxi * (fp - fm);
+            dsum += dxi * dxi * (Dp + Dm);
+         }
+         if (DIM == 3) {
+            const R dxi = op.dxi[2];
+            const R Dm = op.D0 ? op.D2[g.fz(iw, jw, kw)] : op.dc;
+            const R Dp = op.D0 ? op.D2[g.fz(iw, jw, kw + 1)] : op.dc;
+            const R fm = dxi * Dm * (uc - U[u0 - B::BX * B::BY]);
+            const R fp = dxi * Dp * (U[u0 + B::BX * B::BY] - uc);
+            div += dxi * (fp - fm);
+            dsum += dxi * dxi * (Dp + Dm);
+         }
+         const R M = op.M ? Ms[c0] : op.mc;
+         const R C = op.C ? Cs[c0] : op.cc;
+         const R dudr = R(1) / (M * dsum - C);
+         const R r = Fs[c0] - M * div - C * uc;
+         U[u0] = uc + -r * dudr;
+      }
+   };
+   colour(0, 1, B::CX / 2, B::BY - 1, B::BZ - 1);  // red: box + halo 1
+   __syncthreads();
+   colour(1, 2, B::TX / 2, B::BY - 2, B::BZ - 2);  // black: the box
+   __syncthreads();
+   const int i = i0 + tx;
+   if (i >= g.n0) return;
+   for (int zz = 0; zz < B::TZ; zz++) {
+      const int k = k0 + zz;
+      if (DIM == 3 && k >= g.n2) break;
+      for (int yy = ty; yy < B::TY; yy += 8) {
+         const int j = j0 + yy;
+         if (j >= g.n1) break;
+         const R v = U[((DIM == 3 ? zz + 2 : 0) * B::BY + yy + 2) * B::BX + tx + 2];
+         uout[g.c(i, j, k)] = v;
+         for_each_image(g, i, j, k, [&](long long idx) { uout[idx] = v; });
+      }
+   }
+}
+
+template <class R>
+bool rb_sweep_fusable(const Grid& g)
+{
+   return g.n0 % 2 == 0 && g.n1 % 2 == 0 && (g.dim == 2 || g.n2 % 2 == 0) && g.n0 >= 4 &&
+          g.n1 >= 4 && (g.dim == 2 || g.n2 >= 4);
+}
+
+template <class R, int DIM, bool ZERO>
+static int launch_sweep(const FacOp<R>& op, const Grid& g, const R* f, const R* uin, R* uout,
+                        cudaStream_t s)
+{
+   using B = SweepBox<DIM>;
+   const size_t smem = rb_sweep_smem(op, DIM);
+   static bool attr = false;  // opt in to more than 48 KB once per instantiation
+   if (!attr) {
+      const int most = (int)(sizeof(R) * (size_t)(B::NU + 3 * B::NC));  // f, C and M staged
+      cudaFuncSetAttribute(k_rb_sweep<R, DIM, ZERO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           most);
+      attr = true;
+   }
+   const dim3 grid((g.n0 + B::TX - 1) / B::TX, (g.n1 + B::TY - 1) / B::TY,
+                   DIM == 3 ? (g.n2 + B::TZ - 1) / B::TZ : 1);
+   k_rb_sweep<R, DIM, ZERO><<<grid, dim3(32, 8), smem, s>>>(op, g, f, uin, uout);
+   return launch_status();
+}
+
+template <class R>
+int rb_sweep_fused(const FacOp<R>& op, const Grid& g, const R* f, const R* uin, R* uout,
+                   cudaStream_t s)
+{
+   if (g.dim == 3)
+      return uin ? launch_sweep<R, 3, false>(op, g, f, uin, uout, s)
+                 : launch_sweep<R, 3, true>(op, g, f, uin, uout, s);
+   return uin ? launch_sweep<R, 2, false>(op, g, f, uin, uout, s)
+              : launch_sweep<R, 2, true>(op, g, f, uin, uout, s);
+}
+
 // res = f - A u and part[block] = sum over the block's cells of res^2
 // (fixed grid, fixed order: deterministic with the finishing pass)
 template <class R>
-__global__ void k_residual_part(FacOp<R> op, Grid g, const R* f, const R* u,
-                                R* res, double* part)
+__global__ void k_residual_part(FacOp<R> op, Grid g, const R* __restrict__ f,
+                                const R* __restrict__ u, R* __restrict__ res, double* part)
 {
    __shared__ double sh[32];
    R accr = R(0);  // per-thread sum in R (FP32 in the mixed path)
+#pragma unroll 2
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       int i, j, k;
@@ -162,8 +368,8 @@ __global__ void k_residual_part(FacOp<R> op, Grid g, const R* f, const R* u,
 }
 
 template <class R>
-__global__ void k_residual(FacOp<R> op, Grid g, const R* f, const R* u,
-                           R* res)
+__global__ void k_residual(FacOp<R> op, Grid g, const R* __restrict__ f,
+                           const R* __restrict__ u, R* __restrict__ res)
 {
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
@@ -192,7 +398,7 @@ __global__ void k_phase_set_c(Grid g, const double* phi, double gamma,
 static unsigned nblocks(long long n)
 {
    long long b = (n + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    return (unsigned)(b < 1 ? 1 : b);
 }
 
@@ -201,7 +407,8 @@ int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
                int offset, double* maxres, cudaStream_t s, bool images)
 {
    const long long tot = (long long)((g.n0 + 1) / 2) * g.n1 * g.n2;
-   k_rbgs_color<R><<<nblocks(tot), 256, 0, s>>>(op, g, f, u, offset, maxres, images);
+   k_rbgs_color<R><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(op, g, f, u, offset,
+                                                                 maxres, images);
    return launch_status();
 }
 
@@ -221,7 +428,7 @@ template <class R>
 int residual(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
              R* res, cudaStream_t s)
 {
-   k_residual<R><<<nblocks(g.cells()), 256, 0, s>>>(op, g, f, u, res);
+   k_residual<R><<<(unsigned)((g.cells() + 255) / 256), 256, 0, s>>>(op, g, f, u, res);
    return launch_status();
 }
 
@@ -246,6 +453,12 @@ template int residual_partial<double>(const FacOp<double>&, const Grid&, const d
 template int residual_partial<float>(const FacOp<float>&, const Grid&, const float*,
                                      const float*, float*, double*, int*, cudaStream_t);
 template int fill_ghosts_t<double>(const Grid&, double*, cudaStream_t);
+template bool rb_sweep_fusable<double>(const Grid&);
+template bool rb_sweep_fusable<float>(const Grid&);
+template int rb_sweep_fused<double>(const FacOp<double>&, const Grid&, const double*,
+                                    const double*, double*, cudaStream_t);
+template int rb_sweep_fused<float>(const FacOp<float>&, const Grid&, const float*,
+                                   const float*, float*, cudaStream_t);
 template int fill_ghosts_t<float>(const Grid&, float*, cudaStream_t);
 template int residual<double>(const FacOp<double>&, const Grid&, const double*,
                               const double*, double*, cudaStream_t);
@@ -336,6 +549,21 @@ int ampe_efo_rbgs(const ampe_model_t* m, const double* dface0,
                               c_const, mcell, m_const);
    return rbgs_color(op, make_grid(*m), rhs, u, offset, maxres,
                      (cudaStream_t)stream, false);
+}
+
+int ampe_efo_rbgs_sweep(const ampe_model_t* m, const double* dface0,
+                        const double* dface1, const double* dface2, double d_const,
+                        const double* ccell, double c_const, const double* mcell,
+                        double m_const, const double* rhs, const double* u_in,
+                        double* u_out, void* stream)
+{
+   if (check_model(m) || !rhs || !u_out || u_in == u_out) return AMPE_ERR_INVALID;
+   if (dface0 && (!dface1 || (m->dim == 3 && !dface2))) return AMPE_ERR_INVALID;
+   const Grid g = make_grid(*m);
+   if (!rb_sweep_fusable<double>(g)) return AMPE_ERR_INVALID;
+   FacOp<double> op = make_op(m, dface0, dface1, dface2, d_const, ccell, c_const, mcell,
+                              m_const);
+   return rb_sweep_fused(op, g, rhs, u_in, u_out, (cudaStream_t)stream);
 }
 
 int ampe_efo_residual(const ampe_model_t* m, const double* dface0,

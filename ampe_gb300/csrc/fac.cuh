@@ -28,6 +28,13 @@ int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
                      R* res, double* part, int* nblk, cudaStream_t s);
 template <class R>
 int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s);
+// one red + black sweep in one launch, uin -> uout (ghost images written);
+// uin null: zero initial guess.  Requires even extents (rb_sweep_fusable).
+template <class R>
+bool rb_sweep_fusable(const Grid& g);
+template <class R>
+int rb_sweep_fused(const FacOp<R>& op, const Grid& g, const R* f, const R* uin, R* uout,
+                   cudaStream_t s);
 template <class R>
 int residual(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
              R* res, cudaStream_t s);

@@ -217,7 +217,7 @@ int rhs_fused(const ampe_model_t& m, const Grid& g, const double* phi,
               double* conc_rhs, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    if (quat)
       k_rhs_fused<true><<<(unsigned)b, 256, 0, s>>>(
           m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, phi_rhs, conc_rhs);

@@ -400,11 +400,11 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const float* ogm, double* phi_rhs, double* conc_rhs, cudaStream_t s)
 {
    long long b = (g.cells_ghost() + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    k_phi_to_f32<<<(unsigned)b, 256, 0, s>>>(g, phi, pf);
    launch_status();
    b = (g.cells() + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    if (g.dim == 3)
       k_rhs_mixed<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, ogm,
                                                  phi_rhs, conc_rhs);
@@ -704,7 +704,7 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              float* out, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da, db,
                                           qf ? qf->dq : nullptr);
    launch_status();
@@ -730,7 +730,7 @@ int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                    const double* phi, QuatF32& qf, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    if (g.dim == 3)
       k_quat_cells_f32<3><<<(unsigned)b, 256, 0, s>>>(mp, g, phi, qf.q, qf.ogm, qf.mq);
    else
@@ -744,7 +744,7 @@ int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 {
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    long long b = (tot + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    FacePtrs f;
    for (int d = 0; d < 3; d++) {
       f.fc[d] = D[d];
@@ -764,7 +764,7 @@ int quat_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 {
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    long long b = (tot + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    FacePtrs f;
    for (int d = 0; d < 3; d++) {
       f.fc[d] = fc[d];

@@ -136,7 +136,7 @@ __global__ void k_quat_project(long long N, double* q)
 static unsigned nb(long long n)
 {
    long long b = (n + 255) / 256;
-   if (b > 152 * 32) b = 152 * 32;
+   if (b > kMaxBlocks) b = kMaxBlocks;
    return (unsigned)(b < 1 ? 1 : b);
 }
 

@@ -191,6 +191,8 @@ struct DevLevel {
    Grid g;
    double dx[3];
    R *u = nullptr, *f = nullptr, *r = nullptr, *C = nullptr, *M = nullptr;
+   R* u2 = nullptr;  // second u buffer of the one-launch sweep (ping-pong)
+   bool fused = false;
    R* D[3] = {nullptr, nullptr, nullptr};
    bool hasC = false, hasD = false, hasM = false;
    R cc = 0, dc = 0, mc = 0;
@@ -245,6 +247,11 @@ int fac_create(DevFac<R>& F, const ampe_model_t& m, int nlevels, bool hasD,
       for (int d = 0; d < 3; d++) L.dx[d] = mm.dx[d];
       const long long ng = L.g.cells_ghost();
       L.u = (R*)dalloc<R>(pool, ng, &err);
+      // the one-launch sweep stages halos in shared memory and recomputes the
+      // red halo; on GB300 two colour passes at one thread per cell run
+      // faster for this 7-point operator, so the stepper keeps them
+      L.fused = false;
+      if (L.fused) L.u2 = (R*)dalloc<R>(pool, ng, &err);
       L.f = (R*)dalloc<R>(pool, ng, &err);
       L.r = (R*)dalloc<R>(pool, ng, &err);
       L.hasC = hasC;
@@ -323,11 +330,20 @@ double rms_interior(Ctx& cx, const Grid& g, const R* v)
    return sqrt(ss / (double)g.cells());
 }
 
-// red then black; each colour writes through to the ghost images
+// red then black.  first: the sweep starts from u = 0.  Levels with even
+// extents run the one-launch sweep (u <- u2, pointers swapped); otherwise,
+// and when the residual maxima are wanted, two colour launches in place,
+// each writing through to the ghost images.
 template <class R>
-void rb_sweep(Ctx& cx, DevLevel<R>& L, double* maxres)
+void rb_sweep(Ctx& cx, DevLevel<R>& L, double* maxres, bool first = false)
 {
    FacOp<R> op = L.op();
+   if (L.fused && !maxres) {
+      rb_sweep_fused(op, L.g, L.f, first ? nullptr : L.u, L.u2, cx.s);
+      std::swap(L.u, L.u2);
+      return;
+   }
+   if (first) cudaMemsetAsync(L.u, 0, sizeof(R) * L.g.cells_ghost(), cx.s);
    if (maxres) cudaMemsetAsync(maxres, 0, 2 * sizeof(double), cx.s);
    rbgs_color(op, L.g, L.f, L.u, 0, maxres, cx.s, true);
    rbgs_color(op, L.g, L.f, L.u, 1, maxres ? maxres + 1 : nullptr, cx.s, true);
@@ -338,12 +354,13 @@ void vcycle(Ctx& cx, DevFac<R>& F, int l)
 {
    DevLevel<R>& L = F.lev[l];
    const long long ng = L.g.cells_ghost();
-   cudaMemsetAsync(L.u, 0, sizeof(R) * ng, cx.s);
    if (l == (int)F.lev.size() - 1) {
-      for (int it = 0; it < cx.p->mg_coarse_sweeps; it++) rb_sweep(cx, L, nullptr);
+      if (cx.p->mg_coarse_sweeps < 1) cudaMemsetAsync(L.u, 0, sizeof(R) * ng, cx.s);
+      for (int it = 0; it < cx.p->mg_coarse_sweeps; it++) rb_sweep(cx, L, nullptr, it == 0);
       return;
    }
-   for (int it = 0; it < cx.p->mg_pre; it++) rb_sweep(cx, L, nullptr);
+   if (cx.p->mg_pre < 1) cudaMemsetAsync(L.u, 0, sizeof(R) * ng, cx.s);
+   for (int it = 0; it < cx.p->mg_pre; it++) rb_sweep(cx, L, nullptr, it == 0);
    residual(L.op(), L.g, L.f, L.u, L.r, cx.s);
    DevLevel<R>& C = F.lev[l + 1];
    k_restrict<R><<<map_blocks(C.g.cells()), 256, 0, cx.s>>>(L.g, C.g, L.r, C.f);
@@ -366,22 +383,20 @@ int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const R* r, R* z, double tol)
    launch_status();
    FacOp<R> op = L0.op();
    R* const f_own = L0.f;
-   R* const u_own = L0.u;
    double norm = 0.0;
    int it = 0;
    do {
-      // cycle 0 solves with the initial residual f0 straight into sol (the
-      // initial guess is zero); later cycles correct sol with u from rr
+      // cycle 0 solves with the initial residual f0 (zero initial guess) and
+      // its result becomes sol; later cycles correct sol with u from rr
       L0.f = it == 0 ? F.f0 : F.rr;
-      L0.u = it == 0 ? F.sol : u_own;
       if (mode == 2 && F.lev.size() > 1) {
          vcycle(cx, F, 0);
       } else {
-         cudaMemsetAsync(L0.u, 0, sizeof(R) * ng, cx.s);
+         if (cx.p->rb_sweeps < 1) cudaMemsetAsync(L0.u, 0, sizeof(R) * ng, cx.s);
          int not_conv = 1;
          for (int sw = 0; sw < cx.p->rb_sweeps && not_conv; sw++) {
             const bool early = cx.p->rb_tol >= 0.0;
-            rb_sweep(cx, L0, early ? F.maxres : nullptr);
+            rb_sweep(cx, L0, early ? F.maxres : nullptr, sw == 0);
             if (early) {
                double h[2];
                cudaMemcpyAsync(h, F.maxres, 2 * sizeof(double),
@@ -391,7 +406,9 @@ int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const R* r, R* z, double tol)
             }
          }
       }
-      if (it > 0) {  // ghosts included: u's ghosts are current
+      if (it == 0) {
+         std::swap(F.sol, L0.u);  // the cycle's result buffer becomes sol
+      } else {  // ghosts included: u's ghosts are current
          R* sol = F.sol;
          const R* u = L0.u;
          map(ng, [=] __device__(long long t) { sol[t] += u[t]; }, cx.s);
@@ -404,7 +421,6 @@ int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const R* r, R* z, double tol)
       it++;
    } while (norm > tol && it < cx.p->fac_max_cycles);
    L0.f = f_own;
-   L0.u = u_own;
    k_from_ghosted<R, R><<<map_blocks(g.cells()), 256, 0, cx.s>>>(g, F.sol, z);
    launch_status();
    cx.st->fac_cycles += it;

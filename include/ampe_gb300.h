@@ -248,6 +248,18 @@ int ampe_efo_rbgs(const ampe_model_t* m, const double* dface0,
                   double m_const, const double* rhs, double* u, int offset,
                   double* maxres, void* stream);
 
+/* One whole red-black sweep of EllipticFACOps::smoothErrorByRedBlack
+ * (EllipticFACOps.cc:1067-1230: red cells, then black cells) in a single
+ * launch, reading u_in and writing u_out (interior and periodic ghost
+ * images); u_in NULL starts from u = 0.  The result equals two
+ * ampe_efo_rbgs colour calls with a ghost fill between them.  Requires
+ * even extents (AMPE_ERR_INVALID otherwise) and u_in != u_out. */
+int ampe_efo_rbgs_sweep(const ampe_model_t* m, const double* dface0,
+                        const double* dface1, const double* dface2,
+                        double d_const, const double* ccell, double c_const,
+                        const double* mcell, double m_const, const double* rhs,
+                        const double* u_in, double* u_out, void* stream);
+
 /* EFO_COMPRES* (3d/ellipticfacops.m4:448-575): res = f - A u. */
 int ampe_efo_residual(const ampe_model_t* m, const double* dface0,
                       const double* dface1, const double* dface2,

@@ -301,3 +301,60 @@ def test_phase_set_c(cuda, orc):
     c_d = dev(np.zeros(m.ghost_shape()))
     assert cuda.lib.ampe_phase_fac_set_c(C.byref(m), P(dev(phi)), 0.3, P(c_d), None) == 0
     assert O.rel_l2(host(c_d), c_o) <= TOL
+
+
+def sweep_models():
+    out = []
+    m = configs.dilute2d(64)
+    m.n[1] = 40
+    out.append(("2d_64x40", m))
+    m = configs.calphad3d(12, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 10, 8
+    out.append(("3d_12x10x8", m))
+    m = configs.calphad3d(40, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 18, 22
+    out.append(("3d_40x18x22", m))
+    m = configs.calphad3d(64, seed=3, T_run=1500.0)
+    out.append(("3d_64", m))
+    return out
+
+
+@pytest.mark.parametrize("name,m", sweep_models())
+@pytest.mark.parametrize("vard", [False, True])
+@pytest.mark.parametrize("zero", [False, True])
+def test_rbgs_sweep_one_launch(cuda, orc, name, m, vard, zero):
+    """The one-launch red+black sweep equals two colour calls plus a ghost
+    fill (and the oracle), interior and ghosts, from u or from u = 0."""
+    rng = np.random.default_rng(16)
+    D = [np.ascontiguousarray(-rng.uniform(0.5, 1.5, s)) for s in m.face_shapes()] if vard \
+        else [None] * 3
+    Cc = rnd_ghosted(m, rng, 1.0, 2.0)
+    Mc = rnd_ghosted(m, rng, 0.5, 1.5)
+    f = rnd_ghosted(m, rng, -1, 1)
+    u = np.zeros(m.ghost_shape()) if zero else rnd_ghosted(m, rng, -1, 1)
+    Dd = [None if a is None else dev(a) for a in D]
+    args = [P(a) for a in Dd] + [-0.7, P(dev(Cc)), 0.0, P(dev(Mc)), 0.0, P(dev(f))]
+    u_two = dev(u)
+    for off in (0, 1):
+        assert cuda.lib.ampe_efo_rbgs(C.byref(m), *args, P(u_two), off, None, None) == 0
+        assert cuda.lib.ampe_fill_ghosts(C.byref(m), P(u_two), None) == 0
+    u_out = dev(np.full(m.ghost_shape(), 7.0))
+    u_in = None if zero else dev(u)
+    assert cuda.lib.ampe_efo_rbgs_sweep(C.byref(m), *args, P(u_in), P(u_out), None) == 0
+    a, b = host(u_out), host(u_two)
+    assert np.array_equal(a, b), np.abs(a - b).max()
+    u_o = u.copy()
+    for off in (0, 1):
+        orc.orc_efo_rbgs(C.byref(m), *[O.ptr(x) for x in D], -0.7, O.ptr(Cc), 0.0, O.ptr(Mc), 0.0,
+                         O.ptr(f), O.ptr(u_o), off)
+        orc.orc_fill_ghosts(C.byref(m), O.ptr(u_o))
+    assert O.rel_l2(a, u_o) <= TOL
+
+
+def test_rbgs_sweep_rejects_odd(cuda):
+    m = configs.calphad3d(12, seed=3, T_run=1500.0)
+    m.n[2] = 9
+    x = dev(np.zeros(m.ghost_shape()))
+    y = dev(np.zeros(m.ghost_shape()))
+    assert cuda.lib.ampe_efo_rbgs_sweep(C.byref(m), None, None, None, -1.0, None, 1.0, None, 1.0,
+                                        P(x), P(x), P(y), None) == abi.AMPE_ERR_INVALID
