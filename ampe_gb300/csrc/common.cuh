@@ -85,6 +85,9 @@ template <class F>
 __device__ __forceinline__ void for_each_image(const Grid& g, int i, int j,
                                                int k, F f)
 {
+   if (i >= g.ng && i < g.n0 - g.ng && j >= g.ng && j < g.n1 - g.ng &&
+       (g.dim != 3 || (k >= g.ng && k < g.n2 - g.ng)))
+      return;  // interior cell: no image
    int si[2] = {0, 0}, sj[2] = {0, 0}, sk[2] = {0, 0};
    int ni = 1, nj = 1, nk = 1;
    if (i < g.ng)

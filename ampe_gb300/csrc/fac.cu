@@ -4,6 +4,8 @@
 // cell arrays ghosted (width g.ng), face D arrays ghost-free.
 // Templated on the arithmetic type R so that the mixed-precision
 // preconditioner runs the same code in FP32.
+#include <type_traits>
+
 #include "common.cuh"
 #include "devvec.cuh"
 #include "fac.cuh"
@@ -46,6 +48,92 @@ __device__ __forceinline__ R cell_residual(const FacOp<R>& op, const Grid& g,
    const R C = op.C ? op.C[c] : op.cc;
    if (dudr) *dudr = R(1) / (M * dsum - C);
    return f[c] - M * div - C * uc;
+}
+
+// cell_residual specialised on the dimension and on which coefficients are
+// arrays (HD: face D, HC: cell C, HM: cell M); c = g.c(i,j,k).  Neighbours
+// and upper faces by their constant offsets.  Same expression order as
+// cell_residual.
+template <class R, int DIM, bool HD, bool HC, bool HM>
+__device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
+                                         const R* __restrict__ f, const R* u, int i,
+                                         int j, int k, int c, R* dudr)
+{
+   const R uc = u[c];
+   R div = R(0), dsum = R(0);
+   {
+      const R dxi = op.dxi[0];
+      R Dm = op.dc, Dp = op.dc;
+      if (HD) {
+         const int fi = g.fx(i, j, k);
+         Dm = op.D0[fi];
+         Dp = op.D0[fi + 1];
+      }
+      const R fm = dxi * Dm * (uc - u[c - 1]);
+      const R fp = dxi * Dp * (u[c + 1] - uc);
+      div += dxi * (fp - fm);
+      dsum += dxi * dxi * (Dp + Dm);
+   }
+   {
+      const R dxi = op.dxi[1];
+      R Dm = op.dc, Dp = op.dc;
+      if (HD) {
+         const int fi = g.fy(i, j, k);
+         Dm = op.D1[fi];
+         Dp = op.D1[fi + g.n0];
+      }
+      const R fm = dxi * Dm * (uc - u[c - g.sx]);
+      const R fp = dxi * Dp * (u[c + g.sx] - uc);
+      div += dxi * (fp - fm);
+      dsum += dxi * dxi * (Dp + Dm);
+   }
+   if (DIM == 3) {
+      const R dxi = op.dxi[2];
+      R Dm = op.dc, Dp = op.dc;
+      if (HD) {
+         const int fi = g.fz(i, j, k);
+         Dm = op.D2[fi];
+         Dp = op.D2[fi + g.n0 * g.n1];
+      }
+      const R fm = dxi * Dm * (uc - u[c - g.sy]);
+      const R fp = dxi * Dp * (u[c + g.sy] - uc);
+      div += dxi * (fp - fm);
+      dsum += dxi * dxi * (Dp + Dm);
+   }
+   const R M = HM ? op.M[c] : op.mc;
+   const R C = HC ? op.C[c] : op.cc;
+   if (dudr) *dudr = R(1) / (M * dsum - C);
+   return f[c] - M * div - C * uc;
+}
+
+// call F<DIM, HD, HC, HM>() for the operator's shape
+template <class R, class F>
+void dispatch_op(const FacOp<R>& op, int dim, F&& fn)
+{
+   const bool hd = op.D0 != nullptr, hc = op.C != nullptr, hm = op.M != nullptr;
+#define AMPE_OP_CASE(D, A, B, C_)                                               \
+   if (dim == D && hd == A && hc == B && hm == C_) {                            \
+      fn(std::integral_constant<int, D>(), std::integral_constant<bool, A>(),   \
+         std::integral_constant<bool, B>(), std::integral_constant<bool, C_>()); \
+      return;                                                                  \
+   }
+   AMPE_OP_CASE(3, false, true, false)  // phase block
+   AMPE_OP_CASE(3, true, false, false)  // composition block
+   AMPE_OP_CASE(3, true, false, true)   // quaternion block
+   AMPE_OP_CASE(2, false, true, false)
+   AMPE_OP_CASE(2, true, false, false)
+   AMPE_OP_CASE(2, true, false, true)
+   AMPE_OP_CASE(3, false, false, false)
+   AMPE_OP_CASE(3, false, false, true)
+   AMPE_OP_CASE(3, false, true, true)
+   AMPE_OP_CASE(3, true, true, false)
+   AMPE_OP_CASE(3, true, true, true)
+   AMPE_OP_CASE(2, false, false, false)
+   AMPE_OP_CASE(2, false, false, true)
+   AMPE_OP_CASE(2, false, true, true)
+   AMPE_OP_CASE(2, true, true, false)
+   AMPE_OP_CASE(2, true, true, true)
+#undef AMPE_OP_CASE
 }
 
 __device__ __forceinline__ void atomic_max_nonneg(double* a, double v)
@@ -111,7 +199,7 @@ int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s)
 // to its periodic ghost images, so that no ghost fill is needed between
 // colours (the stepper's smoother); the leaf entry point updates the
 // interior only.
-template <class R>
+template <class R, int DIM, bool HD, bool HC, bool HM>
 __global__ void __launch_bounds__(256)
     k_rbgs_color(FacOp<R> op, Grid g, const R* __restrict__ f, R* u, int offset,
                  double* maxres, bool images)
@@ -129,8 +217,8 @@ __global__ void __launch_bounds__(256)
       const int i = 2 * ih + ((j + k + offset) & 1);
       if (i < g.n0) {
          R dudr;
-         const R r = cell_residual(op, g, f, u, i, j, k, &dudr);
          const int c = g.c(i, j, k);
+         const R r = op_residual<R, DIM, HD, HC, HM>(op, g, f, u, i, j, k, c, &dudr);
          const R un = u[c] + -r * dudr;
          u[c] = un;
          if (images) for_each_image(g, i, j, k, [&](long long idx) { u[idx] = un; });
@@ -348,7 +436,7 @@ int rb_sweep_fused(const FacOp<R>& op, const Grid& g, const R* f, const R* uin, 
 
 // res = f - A u and part[block] = sum over the block's cells of res^2
 // (fixed grid, fixed order: deterministic with the finishing pass)
-template <class R>
+template <class R, int DIM, bool HD, bool HC, bool HM>
 __global__ void k_residual_part(FacOp<R> op, Grid g, const R* __restrict__ f,
                                 const R* __restrict__ u, R* __restrict__ res, double* part)
 {
@@ -359,15 +447,16 @@ __global__ void k_residual_part(FacOp<R> op, Grid g, const R* __restrict__ f,
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       int i, j, k;
       g.ijk(t, i, j, k);
-      const R r = cell_residual(op, g, f, u, i, j, k, (R*)nullptr);
-      res[g.c(i, j, k)] = r;
+      const int c = g.c(i, j, k);
+      const R r = op_residual<R, DIM, HD, HC, HM>(op, g, f, u, i, j, k, c, (R*)nullptr);
+      res[c] = r;
       accr += r * r;
    }
    double acc = block_sum<NoOp>((double)accr, sh);
    if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-template <class R>
+template <class R, int DIM, bool HD, bool HC, bool HM>
 __global__ void k_residual(FacOp<R> op, Grid g, const R* __restrict__ f,
                            const R* __restrict__ u, R* __restrict__ res)
 {
@@ -375,7 +464,8 @@ __global__ void k_residual(FacOp<R> op, Grid g, const R* __restrict__ f,
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       int i, j, k;
       g.ijk(t, i, j, k);
-      res[g.c(i, j, k)] = cell_residual(op, g, f, u, i, j, k, (R*)nullptr);
+      const int c = g.c(i, j, k);
+      res[c] = op_residual<R, DIM, HD, HC, HM>(op, g, f, u, i, j, k, c, (R*)nullptr);
    }
 }
 
@@ -407,8 +497,11 @@ int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
                int offset, double* maxres, cudaStream_t s, bool images)
 {
    const long long tot = (long long)((g.n0 + 1) / 2) * g.n1 * g.n2;
-   k_rbgs_color<R><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(op, g, f, u, offset,
-                                                                 maxres, images);
+   const unsigned nb = (unsigned)((tot + 255) / 256);
+   dispatch_op(op, g.dim, [&](auto D, auto HD, auto HC, auto HM) {
+      k_rbgs_color<R, decltype(D)::value, decltype(HD)::value, decltype(HC)::value,
+                   decltype(HM)::value><<<nb, 256, 0, s>>>(op, g, f, u, offset, maxres, images);
+   });
    return launch_status();
 }
 
@@ -420,7 +513,11 @@ int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
    long long nb = (n + kRedThreads - 1) / kRedThreads;
    const int blocks = (int)(nb < kRedBlocks ? (nb < 1 ? 1 : nb) : kRedBlocks);
    *nblk = blocks;
-   k_residual_part<R><<<blocks, kRedThreads, 0, s>>>(op, g, f, u, res, part);
+   dispatch_op(op, g.dim, [&](auto D, auto HD, auto HC, auto HM) {
+      k_residual_part<R, decltype(D)::value, decltype(HD)::value, decltype(HC)::value,
+                      decltype(HM)::value><<<blocks, kRedThreads, 0, s>>>(op, g, f, u, res,
+                                                                         part);
+   });
    return launch_status();
 }
 
@@ -428,7 +525,11 @@ template <class R>
 int residual(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
              R* res, cudaStream_t s)
 {
-   k_residual<R><<<(unsigned)((g.cells() + 255) / 256), 256, 0, s>>>(op, g, f, u, res);
+   const unsigned nb = (unsigned)((g.cells() + 255) / 256);
+   dispatch_op(op, g.dim, [&](auto D, auto HD, auto HC, auto HM) {
+      k_residual<R, decltype(D)::value, decltype(HD)::value, decltype(HC)::value,
+                 decltype(HM)::value><<<nb, 256, 0, s>>>(op, g, f, u, res);
+   });
    return launch_status();
 }
 
