@@ -103,7 +103,8 @@ __device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
    const R M = HM ? op.M[c] : op.mc;
    const R C = HC ? op.C[c] : op.cc;
    if (dudr) *dudr = R(1) / (M * dsum - C);
-   return f[c] - M * div - C * uc;
+   const R fv = op.f_interior ? f[g.interior(i, j, k)] : f[c];
+   return fv - M * div - C * uc;
 }
 
 // call F<DIM, HD, HC, HM>() for the operator's shape
@@ -427,6 +428,7 @@ template <class R>
 int rb_sweep_fused(const FacOp<R>& op, const Grid& g, const R* f, const R* uin, R* uout,
                    cudaStream_t s)
 {
+   if (op.f_interior) return AMPE_ERR_INVALID;  // stages f with ghosted indexing
    if (g.dim == 3)
       return uin ? launch_sweep<R, 3, false>(op, g, f, uin, uout, s)
                  : launch_sweep<R, 3, true>(op, g, f, uin, uout, s);
@@ -438,7 +440,8 @@ int rb_sweep_fused(const FacOp<R>& op, const Grid& g, const R* f, const R* uin, 
 // (fixed grid, fixed order: deterministic with the finishing pass)
 template <class R, int DIM, bool HD, bool HC, bool HM>
 __global__ void k_residual_part(FacOp<R> op, Grid g, const R* __restrict__ f,
-                                const R* __restrict__ u, R* __restrict__ res, double* part)
+                                const R* __restrict__ u, R* __restrict__ res, double* part,
+                                R* __restrict__ z)
 {
    __shared__ double sh[32];
    R accr = R(0);  // per-thread sum in R (FP32 in the mixed path)
@@ -449,7 +452,8 @@ __global__ void k_residual_part(FacOp<R> op, Grid g, const R* __restrict__ f,
       g.ijk(t, i, j, k);
       const int c = g.c(i, j, k);
       const R r = op_residual<R, DIM, HD, HC, HM>(op, g, f, u, i, j, k, c, (R*)nullptr);
-      res[c] = r;
+      res[t] = r;
+      if (z) z[t] = u[c];
       accr += r * r;
    }
    double acc = block_sum<NoOp>((double)accr, sh);
@@ -505,9 +509,45 @@ int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
    return launch_status();
 }
 
+// coarse cell (ic,jc,kc): w * sum of the residuals of its 2^d children, in
+// the order of k_restrict (z, then y, then x)
+template <class R, int DIM, bool HD, bool HC, bool HM>
+__global__ void k_residual_restrict(FacOp<R> op, Grid gf, Grid gc, const R* __restrict__ f,
+                                    const R* __restrict__ u, R* __restrict__ fc)
+{
+   const R w = DIM == 3 ? R(0.125) : R(0.25);
+   const int dz = DIM == 3 ? 2 : 1;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < gc.cells();
+        t += (long long)gridDim.x * blockDim.x) {
+      int i, j, k;
+      gc.ijk(t, i, j, k);
+      R s = R(0);
+      for (int cz = 0; cz < dz; cz++)
+         for (int b = 0; b < 2; b++)
+            for (int a = 0; a < 2; a++) {
+               const int fi = 2 * i + a, fj = 2 * j + b, fk = dz * k + cz;
+               s += op_residual<R, DIM, HD, HC, HM>(op, gf, f, u, fi, fj, fk,
+                                                    gf.c(fi, fj, fk), (R*)nullptr);
+            }
+      fc[t] = w * s;
+   }
+}
+
+template <class R>
+int residual_restrict(const FacOp<R>& op, const Grid& gf, const Grid& gc, const R* f,
+                      const R* u, R* fc, cudaStream_t s)
+{
+   const unsigned nb = (unsigned)((gc.cells() + 255) / 256);
+   dispatch_op(op, gf.dim, [&](auto D, auto HD, auto HC, auto HM) {
+      k_residual_restrict<R, decltype(D)::value, decltype(HD)::value, decltype(HC)::value,
+                          decltype(HM)::value><<<nb, 256, 0, s>>>(op, gf, gc, f, u, fc);
+   });
+   return launch_status();
+}
+
 template <class R>
 int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
-                     R* res, double* part, int* nblk, cudaStream_t s)
+                     R* res, double* part, int* nblk, R* z, cudaStream_t s)
 {
    const long long n = g.cells();
    long long nb = (n + kRedThreads - 1) / kRedThreads;
@@ -516,7 +556,7 @@ int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
    dispatch_op(op, g.dim, [&](auto D, auto HD, auto HC, auto HM) {
       k_residual_part<R, decltype(D)::value, decltype(HD)::value, decltype(HC)::value,
                       decltype(HM)::value><<<blocks, kRedThreads, 0, s>>>(op, g, f, u, res,
-                                                                         part);
+                                                                         part, z);
    });
    return launch_status();
 }
@@ -549,10 +589,15 @@ template int rbgs_color<double>(const FacOp<double>&, const Grid&,
 template int rbgs_color<float>(const FacOp<float>&, const Grid&, const float*,
                                float*, int, double*, cudaStream_t, bool);
 template int residual_partial<double>(const FacOp<double>&, const Grid&, const double*,
-                                      const double*, double*, double*, int*,
+                                      const double*, double*, double*, int*, double*,
                                       cudaStream_t);
 template int residual_partial<float>(const FacOp<float>&, const Grid&, const float*,
-                                     const float*, float*, double*, int*, cudaStream_t);
+                                     const float*, float*, double*, int*, float*,
+                                     cudaStream_t);
+template int residual_restrict<double>(const FacOp<double>&, const Grid&, const Grid&,
+                                       const double*, const double*, double*, cudaStream_t);
+template int residual_restrict<float>(const FacOp<float>&, const Grid&, const Grid&,
+                                      const float*, const float*, float*, cudaStream_t);
 template int fill_ghosts_t<double>(const Grid&, double*, cudaStream_t);
 template bool rb_sweep_fusable<double>(const Grid&);
 template bool rb_sweep_fusable<float>(const Grid&);

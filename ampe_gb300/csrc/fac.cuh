@@ -17,15 +17,23 @@ struct FacOp {
    const R* M = nullptr;
    R mc = 0;
    R dxi[3] = {0, 0, 0};
+   // the right-hand side f is an interior array (no ghosts: it is only read
+   // at the cell itself); false: ghosted like u (the leaf entry points)
+   bool f_interior = false;
 };
 
 template <class R>
 int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
                int offset, double* maxres, cudaStream_t s, bool images);
-// res = f - A u and per-block sums of res^2 into part (*nblk blocks)
+// res = f - A u (interior layout) and per-block sums of res^2 into part
+// (*nblk blocks); z (optional) receives u's interior values
 template <class R>
 int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
-                     R* res, double* part, int* nblk, cudaStream_t s);
+                     R* res, double* part, int* nblk, R* z, cudaStream_t s);
+// coarse f (interior layout) = cell average of the fine residual f - A u
+template <class R>
+int residual_restrict(const FacOp<R>& op, const Grid& gf, const Grid& gc, const R* f,
+                      const R* u, R* fc, cudaStream_t s);
 template <class R>
 int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s);
 // one red + black sweep in one launch, uin -> uout (ghost images written);

@@ -69,20 +69,6 @@ __global__ void k_from_ghosted(Grid g, const R* src, D* dst)
    }
 }
 
-// dst (ghosted, with ghost images) = interior src, same type
-template <class R>
-__global__ void k_copy_ghosted(Grid g, const R* src, R* dst)
-{
-   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-        t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
-      int i, j, k;
-      g.ijk(t, i, j, k);
-      const R x = src[t];
-      dst[g.c(i, j, k)] = x;
-      for_each_image(g, i, j, k, [&](long long idx) { dst[idx] = x; });
-   }
-}
-
 // cell-average restriction of interior values (2^d children)
 template <class R>
 __global__ void k_restrict(Grid gf, Grid gc, const R* src, R* dst)
@@ -210,6 +196,7 @@ struct DevLevel {
       o.M = hasM ? M : nullptr;
       o.mc = mc;
       for (int d = 0; d < 3; d++) o.dxi[d] = d < g.dim ? R(1.0 / dx[d]) : R(0);
+      o.f_interior = true;  // right-hand sides: interior arrays
       return o;
    }
 };
@@ -217,7 +204,7 @@ struct DevLevel {
 template <class R>
 struct DevFac {
    std::vector<DevLevel<R>> lev;
-   R *f0 = nullptr, *sol = nullptr, *rr = nullptr;
+   R *sol = nullptr, *rr = nullptr;
    double* maxres = nullptr;  // device [2]: red, black
 };
 
@@ -275,7 +262,6 @@ int fac_create(DevFac<R>& F, const ampe_model_t& m, int nlevels, bool hasD,
       for (int d = 0; d < 3; d++) mm.dx[d] *= 2.0;
    }
    const long long ng0 = F.lev[0].g.cells_ghost();
-   F.f0 = (R*)dalloc<R>(pool, ng0, &err);
    F.sol = (R*)dalloc<R>(pool, ng0, &err);
    F.rr = (R*)dalloc<R>(pool, ng0, &err);
    F.maxres = (double*)dalloc<double>(pool, 2, &err);
@@ -361,10 +347,8 @@ void vcycle(Ctx& cx, DevFac<R>& F, int l)
    }
    if (cx.p->mg_pre < 1) cudaMemsetAsync(L.u, 0, sizeof(R) * ng, cx.s);
    for (int it = 0; it < cx.p->mg_pre; it++) rb_sweep(cx, L, nullptr, it == 0);
-   residual(L.op(), L.g, L.f, L.u, L.r, cx.s);
    DevLevel<R>& C = F.lev[l + 1];
-   k_restrict<R><<<map_blocks(C.g.cells()), 256, 0, cx.s>>>(L.g, C.g, L.r, C.f);
-   launch_status();
+   residual_restrict(L.op(), L.g, C.g, L.f, L.u, C.f, cx.s);
    vcycle(cx, F, l + 1);
    k_prolong_add<R><<<map_blocks(L.g.cells()), 256, 0, cx.s>>>(L.g, C.g, C.u, L.u);
    launch_status();
@@ -379,16 +363,15 @@ int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const R* r, R* z, double tol)
    DevLevel<R>& L0 = F.lev[0];
    const Grid g = L0.g;
    const long long ng = g.cells_ghost();
-   k_copy_ghosted<R><<<map_blocks(g.cells()), 256, 0, cx.s>>>(g, r, F.f0);
-   launch_status();
    FacOp<R> op = L0.op();
    R* const f_own = L0.f;
    double norm = 0.0;
    int it = 0;
    do {
-      // cycle 0 solves with the initial residual f0 (zero initial guess) and
-      // its result becomes sol; later cycles correct sol with u from rr
-      L0.f = it == 0 ? F.f0 : F.rr;
+      // cycle 0 solves with the right-hand side r itself (interior layout,
+      // zero initial guess) and its result becomes sol; later cycles correct
+      // sol with u from the residual rr.  Level 0's f is only read.
+      L0.f = it == 0 ? const_cast<R*>(r) : F.rr;
       if (mode == 2 && F.lev.size() > 1) {
          vcycle(cx, F, 0);
       } else {
@@ -413,16 +396,15 @@ int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const R* r, R* z, double tol)
          const R* u = L0.u;
          map(ng, [=] __device__(long long t) { sol[t] += u[t]; }, cx.s);
       }
+      // rr = r - A sol, its norm, and sol's interior into z
       int nblk = 0;
-      residual_partial(op, g, F.f0, F.sol, F.rr, cx.red->part, &nblk, cx.s);
+      residual_partial(op, g, r, F.sol, F.rr, cx.red->part, &nblk, z, cx.s);
       k_finish<<<1, 1024, 0, cx.s>>>(cx.red->part, nblk, cx.red->dres, 0);
       g_launches++;
       norm = sqrt(cx.red->fetch(1)[0] / (double)g.cells());
       it++;
    } while (norm > tol && it < cx.p->fac_max_cycles);
    L0.f = f_own;
-   k_from_ghosted<R, R><<<map_blocks(g.cells()), 256, 0, cx.s>>>(g, F.sol, z);
-   launch_status();
    cx.st->fac_cycles += it;
    return it;
 }
