@@ -34,6 +34,7 @@ __global__ void k_partial(long long n, F f, double* part)
 {
    __shared__ double sh[32];
    double acc = 0.0;
+#pragma unroll 4
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
         t += (long long)gridDim.x * blockDim.x)
       acc += f(t);
@@ -49,6 +50,7 @@ __global__ void k_partial_f(long long n, F f, double* part)
 {
    __shared__ double sh[32];
    float acc = 0.f, comp = 0.f;
+#pragma unroll 4
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
         t += (long long)gridDim.x * blockDim.x) {
       const float y = f(t) - comp;

@@ -445,7 +445,7 @@ __global__ void k_residual_part(FacOp<R> op, Grid g, const R* __restrict__ f,
 {
    __shared__ double sh[32];
    R accr = R(0);  // per-thread sum in R (FP32 in the mixed path)
-#pragma unroll 2
+#pragma unroll 4
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       int i, j, k;

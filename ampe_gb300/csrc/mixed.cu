@@ -283,12 +283,34 @@ MixParams make_mix_params(const ampe_model_t& m)
    p.T0 = (float)m.T0;
    p.gdx = (float)(m.gradT * m.dx[0]);
    p.qfloor = m.quat_floor_type;
+   p.pb = (m.avg_type == 'a' && m.diff_interp == 'p' && m.energy_interp == 'p' &&
+           m.conc_interp == 'p' && m.well_type == 'd' && m.orient_interp1 == 'p' &&
+           m.orient_interp2 == 'p')
+              ? 1
+              : 0;
    return p;
 }
 
 // ---------------------------------------------------------------------------
 // FP32 stencil helpers (DIM known at compile time)
 // ---------------------------------------------------------------------------
+// The functions.f type codes of the model; PB: the common set ('a' face
+// average, 'p' interpolation everywhere, 'd' double well) as compile-time
+// constants, so that the type dispatch folds away.
+template <bool PB>
+struct Types {
+   char avg, diff, energy, conc, well, o1, o2;
+   __device__ __forceinline__ explicit Types(const ampe_model_t& m)
+       : avg(PB ? 'a' : m.avg_type),
+         diff(PB ? 'p' : m.diff_interp),
+         energy(PB ? 'p' : m.energy_interp),
+         conc(PB ? 'p' : m.conc_interp),
+         well(PB ? 'd' : m.well_type),
+         o1(PB ? 'p' : m.orient_interp1),
+         o2(PB ? 'p' : m.orient_interp2)
+   {
+   }
+};
 template <int DIM>
 __device__ __forceinline__ float face_flux_lin(const MixParams& mp, int d,
                                                const float* pf, const Grid& g,
@@ -309,7 +331,7 @@ __device__ __forceinline__ float face_flux_lin(const MixParams& mp, int d,
 }
 
 // face weights (1-h) D_L, h D_S from the phases of the two cells
-template <int DIM>
+template <int DIM, bool PB = false>
 __device__ __forceinline__ void face_diff(const ampe_model_t& m,
                                           const MixParams& mp, const Grid& g,
                                           const double* tfield, const float* pf,
@@ -317,8 +339,9 @@ __device__ __forceinline__ void face_diff(const ampe_model_t& m,
                                           int a1, int a2, int ei, int ej,
                                           int ek, float& DL, float& DS)
 {
-   const float vphi = average_func(pf[lo], pf[up], m.avg_type);
-   const float hphi = interp_func(vphi, m.diff_interp);
+   const Types<PB> ty(m);
+   const float vphi = average_func(pf[lo], pf[up], ty.avg);
+   const float hphi = interp_func(vphi, ty.diff);
    float dlq = mp.Dl, dsq = mp.Ds;
    if (mp.tdep) {
       const float invT =
@@ -351,7 +374,7 @@ __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
       pf[t] = d2f(phi[t]);
 }
 
-template <int DIM>
+template <int DIM, bool PB>
 __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
                             const double* tfield, const float* pf,
                             const float* cl, const float* cs, const float* dF,
@@ -371,24 +394,25 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
          float DLm, DSm, DLp, DSp;
-         face_diff<DIM>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), c, i, j, k, ei,
+         face_diff<DIM, PB>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), c, i, j, k, ei,
                         ej, ek, DLm, DSm);
-         face_diff<DIM>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek,
+         face_diff<DIM, PB>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek,
                         DLp, DSp);
          const long long lo = g.c(i - ei, j - ej, k - ek);
          const float flm = mp.dxi[d] * (DLm * (cl[c] - cl[lo]) + DSm * (cs[c] - cs[lo]));
          const float flp = mp.dxi[d] * (DLp * (cl[up] - cl[c]) + DSp * (cs[up] - cs[c]));
          div += mp.dxi[d] * (flp - flm);
       }
+      const Types<PB> ty(m);
       const float p = pf[c];
-      float r = diff - mp.w * deriv_well_func(p, m.well_type);
+      float r = diff - mp.w * deriv_well_func(p, ty.well);
       if (ogm) {  // orientation term, 3d/quatrhs.m4:481-509
          const float gm = ogm[t];
          const float T = temp_f(m, mp, g, tfield, i, j, k);
-         r = r - mp.misor * T * deriv_interp_func(p, m.orient_interp1) * gm -
-             deriv_interp_func(p, m.orient_interp2) * mp.eq2h * gm * gm;
+         r = r - mp.misor * T * deriv_interp_func(p, ty.o1) * gm -
+             deriv_interp_func(p, ty.o2) * mp.eq2h * gm * gm;
       }
-      r += deriv_interp_func(p, m.energy_interp) * dF[t];
+      r += deriv_interp_func(p, ty.energy) * dF[t];
       phi_rhs[t] = f2d(r * mp.Mphi);
       conc_rhs[t] = f2d(mp.Mc * div);
    }
@@ -405,12 +429,21 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    launch_status();
    b = (g.cells() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
-   if (g.dim == 3)
-      k_rhs_mixed<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, ogm,
-                                                 phi_rhs, conc_rhs);
-   else
-      k_rhs_mixed<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, ogm,
-                                                 phi_rhs, conc_rhs);
+#define AMPE_RHS(D, P)                                                              \
+   k_rhs_mixed<D, P><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, ogm, \
+                                                 phi_rhs, conc_rhs)
+   if (g.dim == 3) {
+      if (mp.pb)
+         AMPE_RHS(3, true);
+      else
+         AMPE_RHS(3, false);
+   } else {
+      if (mp.pb)
+         AMPE_RHS(2, true);
+      else
+         AMPE_RHS(2, false);
+   }
+#undef AMPE_RHS
    return launch_status();
 }
 
@@ -419,6 +452,7 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 // ---------------------------------------------------------------------------
 // pointwise: dphi, and the linearised KKS split (da, db) solving
 //   J [da; db] = [dc - (b - a) h_c'(phi) dphi; 0]
+template <bool PB>
 __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
                            const double* tfield, const float* pf,
                            const float* cl, const float* cs, const float* v,
@@ -431,14 +465,15 @@ __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
       g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
+      const Types<PB> ty(m);
       const float p = pf[c], a = cl[c], b = cs[c];
-      const float h = interp_func(p, m.conc_interp);
+      const float h = interp_func(p, ty.conc);
       const float vp = v[t], vc = v[t + N];
       const float J00 = 1.f - h, J01 = h;
       const float J10 = 1.f / (a * (1.f - a)) + dxi_f(tf, a, 0) * tf.iRT;
       const float J11 = -1.f / (b * (1.f - b)) - dxi_f(tf, b, 1) * tf.iRT;
       const float idet = 1.f / (J00 * J11 - J01 * J10);
-      const float r0 = vc - (b - a) * deriv_interp_func(p, m.conc_interp) * vp;
+      const float r0 = vc - (b - a) * deriv_interp_func(p, ty.conc) * vp;
       const float xa = J11 * r0 * idet, xb = -J10 * r0 * idet;
       dphi[c] = vp;
       da[c] = xa;
@@ -495,7 +530,7 @@ __device__ __forceinline__ float second_deriv_interp_f(float phi, char type)
 }
 
 // out = v - gamma J v
-template <int DIM>
+template <int DIM, bool PB>
 __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
                              const CoefF* tabf, const double* tfield,
                              const float* pf, const float* cl, const float* cs,
@@ -519,13 +554,14 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
          const long long up = g.c(i + ei, j + ej, k + ek);
          const long long lo = g.c(i - ei, j - ej, k - ek);
          float DLm, DSm, DLp, DSp;
-         face_diff<DIM>(m, mp, g, tfield, pf, lo, c, i, j, k, ei, ej, ek, DLm, DSm);
-         face_diff<DIM>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek, DLp,
+         face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, c, i, j, k, ei, ej, ek, DLm, DSm);
+         face_diff<DIM, PB>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek, DLp,
                         DSp);
          const float flm = mp.dxi[d] * (DLm * (da[c] - da[lo]) + DSm * (db[c] - db[lo]));
          const float flp = mp.dxi[d] * (DLp * (da[up] - da[c]) + DSp * (db[up] - db[c]));
          div += mp.dxi[d] * (flp - flm);
       }
+      const Types<PB> ty(m);
       const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
       const float p = pf[c], a = cl[c], b = cs[c], vp = dphi[c];
       // d(dF)/db = -f_S''(b) (a - b), d(dF)/da = muL - muS = 0
@@ -535,14 +571,14 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
       if (ogm) {  // phi-derivative of the orientation term at lagged |grad q|
          const float gm = ogm[t];
          const float T = temp_f(m, mp, g, tfield, i, j, k);
-         orient = (mp.misor * T * second_deriv_interp_f(p, m.orient_interp1) * gm +
-                   second_deriv_interp_f(p, m.orient_interp2) * mp.eq2h * gm * gm) *
+         orient = (mp.misor * T * second_deriv_interp_f(p, ty.o1) * gm +
+                   second_deriv_interp_f(p, ty.o2) * mp.eq2h * gm * gm) *
                   vp;
       }
-      const float jp = mp.Mphi * (diff - mp.w * second_deriv_well_func(p, m.well_type) * vp -
+      const float jp = mp.Mphi * (diff - mp.w * second_deriv_well_func(p, ty.well) * vp -
                                   orient +
-                                  second_deriv_interp_f(p, m.energy_interp) * dF[t] * vp +
-                                  deriv_interp_func(p, m.energy_interp) * ddF);
+                                  second_deriv_interp_f(p, ty.energy) * dF[t] * vp +
+                                  deriv_interp_func(p, ty.energy) * ddF);
       const float jc = mp.Mc * div;
       out[t] = v[t] - gamma * jp;
       out[t + N] = v[t + N] - gamma * jc;
@@ -705,16 +741,30 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 {
    long long b = (g.cells() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
-   k_jv_point<<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da, db,
-                                          qf ? qf->dq : nullptr);
+   float* dq = qf ? qf->dq : nullptr;
+   if (mp.pb)
+      k_jv_point<true><<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da,
+                                                   db, dq);
+   else
+      k_jv_point<false><<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi,
+                                                    da, db, dq);
    launch_status();
    const float* ogm = (qf && m.with_orient) ? qf->ogm : nullptr;
-   if (g.dim == 3)
-      k_jv_stencil<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
-                                                  da, db, v, ogm, (float)gamma, out);
-   else
-      k_jv_stencil<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, dphi,
-                                                  da, db, v, ogm, (float)gamma, out);
+#define AMPE_JV(D, P)                                                                   \
+   k_jv_stencil<D, P><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, \
+                                                  dphi, da, db, v, ogm, (float)gamma, out)
+   if (g.dim == 3) {
+      if (mp.pb)
+         AMPE_JV(3, true);
+      else
+         AMPE_JV(3, false);
+   } else {
+      if (mp.pb)
+         AMPE_JV(2, true);
+      else
+         AMPE_JV(2, false);
+   }
+#undef AMPE_JV
    int rc = launch_status();
    if (qf && !rc) {
       if (g.dim == 3)

@@ -26,6 +26,7 @@ struct MixParams {
    float qfloor2, qmaxi;  // grad floor^2, 1/floor
    float T0, gdx;      // T = T0 (+ gdx (i + 1/2) for a gradient along x)
    char qfloor;        // eval_grad_normi type
+   int pb;             // common type codes ('a', 'p', 'd'): specialised kernels
 };
 
 // FP32 working set of the quaternion equation in the mixed path

@@ -302,6 +302,9 @@ struct Ctx {
    Reducer* red;
    const ampe_step_params_t* p;
    ampe_step_stats_t* st;
+   // optional timing hook around the finest level's smoother sweeps
+   void (*mark)(void* owner, bool begin) = nullptr;
+   void* owner = nullptr;
 };
 
 template <class R>
@@ -346,13 +349,17 @@ void vcycle(Ctx& cx, DevFac<R>& F, int l)
       return;
    }
    if (cx.p->mg_pre < 1) cudaMemsetAsync(L.u, 0, sizeof(R) * ng, cx.s);
+   if (l == 0 && cx.mark) cx.mark(cx.owner, true);
    for (int it = 0; it < cx.p->mg_pre; it++) rb_sweep(cx, L, nullptr, it == 0);
+   if (l == 0 && cx.mark) cx.mark(cx.owner, false);
    DevLevel<R>& C = F.lev[l + 1];
    residual_restrict(L.op(), L.g, C.g, L.f, L.u, C.f, cx.s);
    vcycle(cx, F, l + 1);
    k_prolong_add<R><<<map_blocks(L.g.cells()), 256, 0, cx.s>>>(L.g, C.g, C.u, L.u);
    launch_status();
+   if (l == 0 && cx.mark) cx.mark(cx.owner, true);
    for (int it = 0; it < cx.p->mg_post; it++) rb_sweep(cx, L, nullptr);
+   if (l == 0 && cx.mark) cx.mark(cx.owner, false);
 }
 
 // FACPreconditioner::solveSystem on one level.  r: interior block of the
@@ -460,7 +467,8 @@ struct Stepper {
    double kms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
    long long kcount[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
-   Ctx ctx() { return Ctx{s, &red, &p, &st}; }
+   cudaEvent_t smooth_a = nullptr;  // open KT_SMOOTH interval
+   Ctx ctx();
 };
 
 constexpr int kMaxKrylov = 16;  // Krylov dimension limit of the stepper
@@ -482,9 +490,10 @@ enum {
    KT_JV = 2,
    KT_MLP = 3,
    KT_QUAT = 4,
-   KT_PREC = 5,  // whole preconditioner solve (all blocks)
-   KT_PSET = 6,  // preconditioner setup
-   KT_NKINDS = 7
+   KT_PREC = 5,    // whole preconditioner solve (all blocks)
+   KT_PSET = 6,    // preconditioner setup
+   KT_SMOOTH = 7,  // red-black sweeps on the finest multigrid level
+   KT_NKINDS = 8
 };
 
 static cudaEvent_t prof_event(Stepper& S)
@@ -512,6 +521,32 @@ struct ProfScope {
       }
    }
 };
+
+// Ctx hook: time the finest level's sweeps (KT_SMOOTH) in profiling mode
+static void smooth_mark(void* owner, bool begin)
+{
+   Stepper& S = *(Stepper*)owner;
+   if (!S.prof) return;
+   if (begin) {
+      S.smooth_a = prof_event(S);
+      if (S.smooth_a) cudaEventRecord(S.smooth_a, S.s);
+      return;
+   }
+   cudaEvent_t b = S.smooth_a ? prof_event(S) : nullptr;
+   if (b) {
+      cudaEventRecord(b, S.s);
+      S.pending.push_back({KT_SMOOTH, {S.smooth_a, b}});
+   }
+   S.smooth_a = nullptr;
+}
+
+Ctx Stepper::ctx()
+{
+   Ctx c{s, &red, &p, &st};
+   c.mark = smooth_mark;
+   c.owner = this;
+   return c;
+}
 
 // fold finished event pairs into the totals (stream must be idle)
 static void prof_collect(Stepper& S)
@@ -1004,14 +1039,17 @@ static int bdf_step(Stepper& S, double h, int q)
    const double rtol = S.p.rtol, atol = S.p.atol;
    double* wi = S.wi;
    if (S.p.precision == 1) {
+      // FP32 weights (no FP64 division per element); the FP64 copies used by
+      // the Newton test hold the same values exactly
       float *w32 = S.w32, *wi32 = S.wi32;
+      const float rtf = (float)rtol, atf = (float)atol;
       map(ny, [=] __device__(long long t) {
-         const double e = rtol * fabs(yn[t]) + atol;
-         const double wv = 1.0 / e;
-         w[t] = wv;
-         wi[t] = e;
-         w32[t] = d2f(wv);
-         wi32[t] = d2f(e);
+         const float e = rtf * fabsf(d2f(yn[t])) + atf;
+         const float wv = 1.f / e;
+         w32[t] = wv;
+         wi32[t] = e;
+         w[t] = f2d(wv);
+         wi[t] = f2d(e);
       }, S.s);
    } else {
       map(ny, [=] __device__(long long t) {

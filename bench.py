@@ -45,14 +45,25 @@ RHS_MIXED_BYTES_PER_CELL = 36
 # dphi, dcL, dcS) + stencil pass 44 B (dphi, dcL, dcS, phi, cL, cS, dF, v;
 # write out)
 JV_BYTES_PER_CELL = 76
+# one red-black sweep (two colour launches) on the finest multigrid level,
+# FP32, per cell: phase block u r/w 8 + f 4 + C 4 = 16 B, composition block
+# u r/w 8 + f 4 + D (3 faces) 12 = 24 B; the two blocks alternate: 20 B
+SMOOTH_BYTES_PER_CELL = 20
+SMOOTH_BYTES_PER_CELL_FP64 = 40
 # MLP inference: 2 (3*64 + 64*64 + 64*64 + 64*2) multiply-adds per cell
 MLP_FLOPS_PER_CELL = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
 KERNEL_NAMES = {
     False: {"kks_newton": "k_kks_mixed", "rhs_fused": "k_rhs_mixed",
-            "jv_analytic": "k_jv_point+k_jv_stencil"},
+            "jv_analytic": "k_jv_point+k_jv_stencil",
+            "smooth_fine": "k_rbgs_color<float,3> x2 (finest-level red-black sweep)"},
     True: {"kks_newton": "k_kks_interior", "rhs_fused": "k_rhs_fused<0>",
-           "jv_analytic": "-"},
+           "jv_analytic": "-",
+           "smooth_fine": "k_rbgs_color<double,3> x2 (finest-level red-black sweep)"},
 }
+# profiling-timer kinds of the stepper (ampe_stepper_kernel_time)
+KINDS = ((0, "kks_newton"), (1, "rhs_fused"), (2, "jv_analytic"), (3, "mlp_infer_tc"),
+         (4, "quat_rhs"), (5, "precond_solve"), (6, "precond_setup"), (7, "smooth_fine"))
+SINGLE_KERNELS = ("kks_newton", "rhs_fused", "jv_analytic", "mlp_infer_tc", "smooth_fine")
 ATOL = 1.0e-6
 
 
@@ -73,6 +84,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--only-head", action="store_true",
                     help="time only the headline path (no FP64 / mixed comparison)")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the headline path's timed steps with cudaProfilerStart/"
+                         "Stop (ncu --profile-from-start off captures only them)")
     return ap.parse_args()
 
 
@@ -285,16 +299,20 @@ def timed_path(args, m, phi, c, path, local, mlp=None):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    prof_range = args.profile_range and path == args.path
+    if prof_range:
+        torch.cuda.profiler.start()
     e0.record(stream)
     st = g.advance(args.steps)
     e1.record(stream)
     torch.cuda.synchronize()
+    if prof_range:
+        torch.cuda.profiler.stop()
     clocks.stop()
     ms = e0.elapsed_time(e1)
     launches = L.ampe_stepper_kernel_launches(g._h) - launches0
     kt = {}
-    for kind, name in ((0, "kks_newton"), (1, "rhs_fused"), (2, "jv_analytic"),
-                       (3, "mlp_infer_tc")):
+    for kind, name in KINDS:
         tot, cnt = C.c_double(), C.c_longlong()
         L.ampe_stepper_kernel_time(g._h, kind, C.byref(tot), C.byref(cnt))
         kt[name] = {"ms": tot.value, "launches": cnt.value}
@@ -384,8 +402,10 @@ def run_ours(args):
     kt = res_h["kernels"]
     per_cell = {"kks_newton": KKS_BYTES_PER_CELL if head == "fp64" else KKS_MIXED_BYTES_PER_CELL,
                 "rhs_fused": RHS_BYTES_PER_CELL if head == "fp64" else RHS_MIXED_BYTES_PER_CELL,
-                "jv_analytic": JV_BYTES_PER_CELL}
-    kname = max((k for k in kt if kt[k]["launches"]), key=lambda k: kt[k]["ms"])
+                "jv_analytic": JV_BYTES_PER_CELL,
+                "smooth_fine": SMOOTH_BYTES_PER_CELL_FP64 if head == "fp64"
+                else SMOOTH_BYTES_PER_CELL}
+    kname = max((k for k in SINGLE_KERNELS if kt[k]["launches"]), key=lambda k: kt[k]["ms"])
     tot, cnt = kt[kname]["ms"], kt[kname]["launches"]
     avg_ms = tot / max(cnt, 1)
     if kname == "mlp_infer_tc":

@@ -432,7 +432,9 @@ void* ampe_stepper_stream(void* handle);
  * 1 fused RHS, 2 analytic Jacobian-vector product (mixed path), 3 surrogate
  * inference, 4 quaternion RHS (mobility, face coefficients, divergence),
  * 5 preconditioner solves (all blocks, FAC cycles included), 6
- * preconditioner setups.  Enabling resets the totals. */
+ * preconditioner setups, 7 red-black sweeps on the finest multigrid level
+ * (one interval per pre- or post-smoothing, two colour launches per sweep).
+ * Enabling resets the totals. */
 int ampe_stepper_profile(void* handle, int enable);
 int ampe_stepper_kernel_time(void* handle, int kind, double* total_ms,
                              long long* launches);
