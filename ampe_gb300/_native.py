@@ -58,6 +58,7 @@ _PROTOS = {
     "ampe_stepper_load_y": (I, [P, P, P, I]),
     "ampe_stepper_jv": (I, [P, P, D, P, I]),
     "ampe_stepper_set_quat": (I, [P, P, I]),
+    "ampe_stepper_set_orientation": (I, [P, P, I]),
     "ampe_stepper_get_quat": (I, [P, P, I]),
     "ampe_stepper_size": (C.c_longlong, [P]),
     "ampe_stepper_eval_rhs_full": (I, [P, P, I]),

@@ -79,6 +79,23 @@ def dilute2d(n=256, T=900.0):
     return m
 
 
+def dendrite2d(n=2048, undercooling=0.55, delta=0.02):
+    """dilute2d with the 2D four-fold anisotropic flux (delta = 0.02, qlen 2)
+    at the temperature of a dimensionless undercooling
+    (T_L(c0) - T) / dT0 = undercooling, T_L(c0) = Tm + m c0 with c0 = 0.02 and
+    the freezing range dT0 = |m| c0 (1 - k) / k."""
+    c0, Tm, mliq, k = 0.02, 933.0, -260.0, 0.14
+    T_L = Tm + mliq * c0
+    dT0 = abs(mliq) * c0 * (1.0 - k) / k
+    T = T_L - undercooling * dT0
+    m = dilute2d(n, T=T)
+    m.flux_type = abi.FLUX_ANISOTROPIC
+    m.aniso_eps = delta
+    m.aniso_k = 4
+    m.qlen = 2
+    return m
+
+
 def random_rk(seed, T_check=(1250.0, 1750.0), lim=2.0e4):
     """Two Redlich-Kister coefficients (L0, L1) per phase, convex draws."""
     rng = np.random.default_rng(seed)

@@ -283,6 +283,10 @@ MixParams make_mix_params(const ampe_model_t& m)
    p.T0 = (float)m.T0;
    p.gdx = (float)(m.gradT * m.dx[0]);
    p.qfloor = m.quat_floor_type;
+   p.eps = (float)m.epsilon_phi;
+   p.nu = (float)m.aniso_eps;
+   p.kn = (float)m.aniso_k;
+   p.qlen4 = m.qlen == 4 ? 1 : 0;
    p.pb = (m.avg_type == 'a' && m.diff_interp == 'p' && m.energy_interp == 'p' &&
            m.conc_interp == 'p' && m.well_type == 'd' && m.orient_interp1 == 'p' &&
            m.orient_interp2 == 'p')
@@ -330,6 +334,105 @@ __device__ __forceinline__ float face_flux_lin(const MixParams& mp, int d,
                   (P(i + 1, j) - P(i + 1, j - 1)));
 }
 
+// ---------------------------------------------------------------------------
+// 2D anisotropic flux (anisotropic_gradient_flux, 2d/quatrhs.m4:154-256) in
+// FP32 with its Jacobian.  theta = atan(dpy/dpx) (pi/2 when |dpx| <= 1e-12),
+// orientation phi_o = acos(q0) (2 acos for four-component q),
+// eps(theta) = eps (1 + nu cos k(theta - phi_o)), e' = d eps / d theta:
+//   x faces: F = e^2 dpx - e e' dpy,   y faces: F = e^2 dpy + e e' dpx,
+// and dF/d(dpx), dF/d(dpy) through theta's derivatives
+// (-dpy, dpx) / (dpx^2 + dpy^2).
+// ---------------------------------------------------------------------------
+__global__ void k_aniso_faces_f32(MixParams mp, Grid g, const float* pf, const double* q,
+                                  AnisoF a)
+{
+   const long long nx = g.nfx(), tot = nx + g.nfy();
+   const float fthr = 1.e-12f;
+   const float half_pi = 1.5707963267948966f;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      face_of(g, t, dir, i, j, k);
+      auto P = [&](int x, int y) { return pf[g.c(x, y, 0)]; };
+      float dpx, dpy, qa;
+      if (dir == 0) {
+         dpx = (P(i, j) - P(i - 1, j)) * mp.dxi[0];
+         dpy = 0.25f * (P(i - 1, j + 1) - P(i - 1, j - 1) + P(i, j + 1) - P(i, j - 1)) * mp.dxi[1];
+         qa = 0.5f * (d2f(q[g.c(i - 1, j, 0)]) + d2f(q[g.c(i, j, 0)]));
+      } else {
+         dpx = 0.25f * (P(i + 1, j - 1) - P(i - 1, j - 1) + P(i + 1, j) - P(i - 1, j)) * mp.dxi[0];
+         dpy = (P(i, j) - P(i, j - 1)) * mp.dxi[1];
+         qa = 0.5f * (d2f(q[g.c(i, j - 1, 0)]) + d2f(q[g.c(i, j, 0)]));
+      }
+      const bool steep = fabsf(dpx) > fthr;
+      const float theta = steep ? atanf(dpy / dpx) : half_pi;
+      qa = fminf(1.f, fmaxf(-1.f, qa));
+      const float po = mp.qlen4 ? 2.f * acosf(qa) : acosf(qa);
+      float sn, cs;
+      sincosf(mp.kn * (theta - po), &sn, &cs);
+      const float e = mp.eps * (1.f + mp.nu * cs);
+      const float de = -mp.kn * mp.eps * mp.nu * sn;
+      const float dde = -mp.kn * mp.kn * mp.eps * mp.nu * cs;
+      float tx = 0.f, ty = 0.f;
+      const float r2 = dpx * dpx + dpy * dpy;
+      if (steep && r2 > 0.f) {
+         tx = -dpy / r2;
+         ty = dpx / r2;
+      }
+      float F, JA, JB;
+      if (dir == 0) {
+         F = e * e * dpx - e * de * dpy;
+         const float dFdt = 2.f * e * de * dpx - (de * de + e * dde) * dpy;
+         JA = e * e + dFdt * tx;
+         JB = -e * de + dFdt * ty;
+         const int f = g.fx(i, j, 0);
+         a.F[0][f] = F;
+         a.JA[0][f] = JA;
+         a.JB[0][f] = JB;
+      } else {
+         F = e * e * dpy + e * de * dpx;
+         const float dFdt = 2.f * e * de * dpy + (de * de + e * dde) * dpx;
+         JA = e * de + dFdt * tx;
+         JB = e * e + dFdt * ty;
+         const int f = g.fy(i, j, 0);
+         a.F[1][f] = F;
+         a.JA[1][f] = JA;
+         a.JB[1][f] = JB;
+      }
+   }
+}
+
+int aniso_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                    const float* pf, const double* q, AnisoF& a, cudaStream_t s)
+{
+   (void)m;
+   const long long tot = g.nfx() + g.nfy();
+   long long b = (tot + 255) / 256;
+   if (b > kMaxBlocks) b = kMaxBlocks;
+   k_aniso_faces_f32<<<(unsigned)b, 256, 0, s>>>(mp, g, pf, q, a);
+   return launch_status();
+}
+
+// linearised anisotropic flux on face d whose upper cell is (i, j): the face
+// gradient of dphi (the stencil of the flux) through the face's Jacobian
+__device__ __forceinline__ float aniso_dflux(const MixParams& mp, const AnisoF& a, int d,
+                                             const float* dp, const Grid& g, int i, int j)
+{
+   auto P = [&](int x, int y) { return dp[g.c(x, y, 0)]; };
+   if (d == 0) {
+      const float gx = (P(i, j) - P(i - 1, j)) * mp.dxi[0];
+      const float gy =
+          0.25f * (P(i - 1, j + 1) - P(i - 1, j - 1) + P(i, j + 1) - P(i, j - 1)) * mp.dxi[1];
+      const int f = g.fx(i, j, 0);
+      return a.JA[0][f] * gx + a.JB[0][f] * gy;
+   }
+   const float gx =
+       0.25f * (P(i + 1, j - 1) - P(i - 1, j - 1) + P(i + 1, j) - P(i - 1, j)) * mp.dxi[0];
+   const float gy = (P(i, j) - P(i, j - 1)) * mp.dxi[1];
+   const int f = g.fy(i, j, 0);
+   return a.JA[1][f] * gx + a.JB[1][f] * gy;
+}
+
 // face weights (1-h) D_L, h D_S from the phases of the two cells
 template <int DIM, bool PB = false>
 __device__ __forceinline__ void face_diff(const ampe_model_t& m,
@@ -374,8 +477,8 @@ __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
       pf[t] = d2f(phi[t]);
 }
 
-template <int DIM, bool PB>
-__global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
+template <int DIM, bool PB, bool ANISO>
+__global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
                             const double* tfield, const float* pf,
                             const float* cl, const float* cs, const float* dF,
                             const float* ogm, double* phi_rhs, double* conc_rhs)
@@ -389,8 +492,14 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
 #pragma unroll
       for (int d = 0; d < DIM; d++) {
          const int ei = d == 0, ej = d == 1, ek = d == 2;
-         const float fm = face_flux_lin<DIM>(mp, d, pf, g, i, j, k);
-         const float fp = face_flux_lin<DIM>(mp, d, pf, g, i + ei, j + ej, k + ek);
+         float fm, fp;
+         if (ANISO) {  // 2D: precomputed face fluxes
+            fm = d == 0 ? an.F[0][g.fx(i, j, 0)] : an.F[1][g.fy(i, j, 0)];
+            fp = d == 0 ? an.F[0][g.fx(i + 1, j, 0)] : an.F[1][g.fy(i, j + 1, 0)];
+         } else {
+            fm = face_flux_lin<DIM>(mp, d, pf, g, i, j, k);
+            fp = face_flux_lin<DIM>(mp, d, pf, g, i + ei, j + ej, k + ek);
+         }
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
          float DLm, DSm, DLp, DSp;
@@ -421,7 +530,8 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g,
 int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield, const double* phi, float* pf,
               const float* cl, const float* cs, const float* dF,
-              const float* ogm, double* phi_rhs, double* conc_rhs, cudaStream_t s)
+              const float* ogm, const double* q, AnisoF* an, double* phi_rhs,
+              double* conc_rhs, cudaStream_t s)
 {
    long long b = (g.cells_ghost() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
@@ -429,10 +539,23 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    launch_status();
    b = (g.cells() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
-#define AMPE_RHS(D, P)                                                              \
-   k_rhs_mixed<D, P><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, dF, ogm, \
-                                                 phi_rhs, conc_rhs)
-   if (g.dim == 3) {
+   const bool aniso = m.flux_type == AMPE_FLUX_ANISOTROPIC;
+   if (aniso) {
+      if (g.dim != 2 || !q || !an) return AMPE_ERR_INVALID;
+      aniso_faces_f32(m, mp, g, pf, q, *an, s);
+   }
+   const AnisoF a0 = an ? *an : AnisoF();
+#define AMPE_RHS(D, P)                                                                      \
+   k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, pf, cl, cs, dF, \
+                                                        ogm, phi_rhs, conc_rhs)
+   if (aniso) {
+      if (mp.pb)
+         k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, pf, cl,
+                                                               cs, dF, ogm, phi_rhs, conc_rhs);
+      else
+         k_rhs_mixed<2, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, pf, cl,
+                                                                cs, dF, ogm, phi_rhs, conc_rhs);
+   } else if (g.dim == 3) {
       if (mp.pb)
          AMPE_RHS(3, true);
       else
@@ -530,8 +653,8 @@ __device__ __forceinline__ float second_deriv_interp_f(float phi, char type)
 }
 
 // out = v - gamma J v
-template <int DIM, bool PB>
-__global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
+template <int DIM, bool PB, bool ANISO>
+__global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
                              const CoefF* tabf, const double* tfield,
                              const float* pf, const float* cl, const float* cs,
                              const float* dF, const float* dphi,
@@ -548,8 +671,14 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g,
 #pragma unroll
       for (int d = 0; d < DIM; d++) {
          const int ei = d == 0, ej = d == 1, ek = d == 2;
-         const float fm = face_flux_lin<DIM>(mp, d, dphi, g, i, j, k);
-         const float fp = face_flux_lin<DIM>(mp, d, dphi, g, i + ei, j + ej, k + ek);
+         float fm, fp;
+         if (ANISO) {  // linearised 2D anisotropic flux on the two faces
+            fm = aniso_dflux(mp, an, d, dphi, g, i, j);
+            fp = aniso_dflux(mp, an, d, dphi, g, i + ei, j + ej);
+         } else {
+            fm = face_flux_lin<DIM>(mp, d, dphi, g, i, j, k);
+            fp = face_flux_lin<DIM>(mp, d, dphi, g, i + ei, j + ej, k + ek);
+         }
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
          const long long lo = g.c(i - ei, j - ej, k - ek);
@@ -737,7 +866,7 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf, const double* tfield, const float* pf,
              const float* cl, const float* cs, const float* dF, const float* v,
              double gamma, float* dphi, float* da, float* db, const QuatF32* qf,
-             float* out, cudaStream_t s)
+             const AnisoF* an, float* out, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
@@ -750,10 +879,20 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                                                     da, db, dq);
    launch_status();
    const float* ogm = (qf && m.with_orient) ? qf->ogm : nullptr;
-#define AMPE_JV(D, P)                                                                   \
-   k_jv_stencil<D, P><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, pf, cl, cs, dF, \
-                                                  dphi, da, db, v, ogm, (float)gamma, out)
-   if (g.dim == 3) {
+   const AnisoF a0 = an ? *an : AnisoF();
+#define AMPE_JV(D, P)                                                                          \
+   k_jv_stencil<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tabf, tfield, pf, cl, cs, \
+                                                         dF, dphi, da, db, v, ogm, (float)gamma, \
+                                                         out)
+   if (m.flux_type == AMPE_FLUX_ANISOTROPIC) {
+      if (g.dim != 2 || !an) return AMPE_ERR_INVALID;
+      if (mp.pb)
+         k_jv_stencil<2, true, true><<<(unsigned)b, 256, 0, s>>>(
+             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, v, ogm, (float)gamma, out);
+      else
+         k_jv_stencil<2, false, true><<<(unsigned)b, 256, 0, s>>>(
+             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, v, ogm, (float)gamma, out);
+   } else if (g.dim == 3) {
       if (mp.pb)
          AMPE_JV(3, true);
       else

@@ -27,7 +27,23 @@ struct MixParams {
    float T0, gdx;      // T = T0 (+ gdx (i + 1/2) for a gradient along x)
    char qfloor;        // eval_grad_normi type
    int pb;             // common type codes ('a', 'p', 'd'): specialised kernels
+   // 2D anisotropic phase flux
+   float eps, nu, kn;
+   int qlen4;
 };
+
+// 2D anisotropic phase flux per face and its Jacobian with respect to the
+// face gradient (dphi/dx, dphi/dy): F[d], JA[d] = dF/d(dphi/dx),
+// JB[d] = dF/d(dphi/dy) for x (d = 0) and y (d = 1) faces
+struct AnisoF {
+   float* F[2] = {nullptr, nullptr};
+   float* JA[2] = {nullptr, nullptr};
+   float* JB[2] = {nullptr, nullptr};
+};
+// fill an AnisoF from the FP32 phase copy and the orientation q (component 0,
+// ghosted FP64), 2D only
+int aniso_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                    const float* pf, const double* q, AnisoF& a, cudaStream_t s);
 
 // FP32 working set of the quaternion equation in the mixed path
 struct QuatF32 {
@@ -45,19 +61,21 @@ int kks_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* conc, const float* guess_l, const float* guess_s,
               const float* clr, const float* csr, float* cl, float* cs,
               float* dF, unsigned long long* counters, cudaStream_t s);
+// q: orientation of the 2D anisotropic flux (null otherwise); its face
+// fluxes and Jacobians go to *an for the Jacobian-vector products
 int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield,
               const double* phi, float* pf, const float* cl, const float* cs,
-              const float* dF, const float* ogm, double* phi_rhs,
-              double* conc_rhs, cudaStream_t s);
+              const float* dF, const float* ogm, const double* q, AnisoF* an,
+              double* phi_rhs, double* conc_rhs, cudaStream_t s);
 // out = v - gamma J v; qf (null without quaternions) adds the q rows and
 // the orientation term of the phase row
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf,
              const double* tfield, const float* pf, const float* cl,
              const float* cs, const float* dF, const float* v, double gamma,
-             float* dphi, float* da, float* db, const QuatF32* qf, float* out,
-             cudaStream_t s);
+             float* dphi, float* da, float* db, const QuatF32* qf, const AnisoF* an,
+             float* out, cudaStream_t s);
 // composition preconditioner faces D = -gamma ((1-h) D_L + h D_S), FP32
 int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                    const double* tfield, const float* pf, double gamma,

@@ -453,6 +453,10 @@ struct Stepper {
    double *q_g = nullptr, *q_lag = nullptr, *ogm = nullptr, *mq = nullptr;
    double* fcq[3] = {nullptr, nullptr, nullptr};
    QuatF32 qf32;  // FP32 quaternion working set (mixed path)
+   // orientation of the anisotropic phase flux: qlen ghosted FP64 components
+   // (static; evolve_quat models use the evolving q instead)
+   double* qorient = nullptr;
+   AnisoF an;  // FP32 anisotropic face fluxes and Jacobians (2D mixed path)
    // preconditioner (FP64 or FP32)
    DevFac<double> facp64, facc64, facq64;
    DevFac<float> facp32, facc32, facq32;
@@ -607,7 +611,8 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
       {
          ProfScope ps(S, KT_RHS);
          rhs_mixed(S.m, S.mp, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32,
-                   quat && S.m.with_orient ? S.qf32.ogm : nullptr, out, out + S.N, S.s);
+                   quat && S.m.with_orient ? S.qf32.ogm : nullptr, S.qorient, &S.an, out,
+                   out + S.N, S.s);
       }
       if (quat) {
          ProfScope ps(S, KT_QUAT);
@@ -632,7 +637,9 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
    }
    {
       ProfScope ps(S, KT_RHS);
-      rhs_fused(S.m, S.g, S.phi_g, nullptr, tf, S.tab, S.cl, S.cs, S.dF,
+      const double* qflux = nullptr;
+      if (S.m.flux_type == AMPE_FLUX_ANISOTROPIC) qflux = quat ? S.q_g : S.qorient;
+      rhs_fused(S.m, S.g, S.phi_g, qflux, tf, S.tab, S.cl, S.cs, S.dF,
                 S.phi_lag, quat && S.m.with_orient ? S.ogm : nullptr, out,
                 out + S.N, S.s);
    }
@@ -902,7 +909,7 @@ static void matvec32(Stepper& S, double gamma, const float* v, float* out)
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
    ProfScope ps(S, KT_JV);
    jv_mixed(S.m, S.mp, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma, S.dphi32,
-            S.da32, S.db32, S.nb == 6 ? &S.qf32 : nullptr, out, S.s);
+            S.da32, S.db32, S.nb == 6 ? &S.qf32 : nullptr, &S.an, out, S.s);
 }
 
 // GMRES of the mixed path: the same algorithm as gmres() (left
@@ -1116,7 +1123,12 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    if (p->precond < 0 || p->precond > 2 || p->precision < 0 ||
        p->precision > 1 || p->max_krylov > kMaxKrylov)
       return AMPE_ERR_INVALID;
-   if (m->flux_type == AMPE_FLUX_ANISOTROPIC) return AMPE_ERR_INVALID;
+   if (m->flux_type == AMPE_FLUX_ANISOTROPIC) {
+      if (m->qlen != 2 && m->qlen != 4) return AMPE_ERR_INVALID;
+      if (m->evolve_quat && m->qlen != 4) return AMPE_ERR_INVALID;
+      // the mixed path linearises the 2D anisotropic flux only
+      if (p->precision == 1 && (m->dim != 2 || m->evolve_quat)) return AMPE_ERR_INVALID;
+   }
    if (m->evolve_quat && (m->quat_mobility_type != 'p' || !(m->quat_grad_floor > 0.0)))
       return AMPE_ERR_INVALID;
    if (ampe_device_count() < 1) return AMPE_ERR_NO_DEVICE;
@@ -1151,6 +1163,17 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
       for (int l = 0; l <= p->max_krylov; l++) S->V.push_back(dvec(*S, S->NY, &err));
    }
    S->counters = (unsigned long long*)dalloc<unsigned long long>(S->pool, 2, &err);
+   if (m->flux_type == AMPE_FLUX_ANISOTROPIC && !m->evolve_quat) {
+      S->qorient = dvec(*S, (long long)m->qlen * S->NG, &err);
+      if (p->precision == 1) {
+         for (int d = 0; d < 2; d++) {
+            const long long nf = d == 0 ? S->g.nfx() : S->g.nfy();
+            S->an.F[d] = (float*)dalloc<float>(S->pool, nf, &err);
+            S->an.JA[d] = (float*)dalloc<float>(S->pool, nf, &err);
+            S->an.JB[d] = (float*)dalloc<float>(S->pool, nf, &err);
+         }
+      }
+   }
    if (S->nb == 6) {
       S->q_g = dvec(*S, 4 * S->NG, &err);
       S->q_lag = dvec(*S, 4 * S->NG, &err);
@@ -1205,6 +1228,11 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    // the zero fills of dalloc run on the legacy stream, which does not
    // order with the non-blocking stepper stream: finish them first
    if (!err && cudaDeviceSynchronize() != cudaSuccess) err = AMPE_ERR_CUDA;
+   if (!err && S->qorient) {  // default orientation: angle 0, q = (1, 0, ...)
+      double* q0 = S->qorient;
+      const long long ng = S->NG;
+      map(ng, [=] __device__(long long t) { q0[t] = 1.0; }, S->s);
+   }
    if (!err && S->tab) err = build_thermo_table(*m, S->tab, nt, S->s);
    if (!err && S->tabf) err = build_coef_f(S->tab, S->tabf, nt, S->s);
    if (!err && cudaStreamSynchronize(S->s) != cudaSuccess) err = AMPE_ERR_CUDA;
@@ -1474,6 +1502,20 @@ int ampe_stepper_set_quat(void* h, const double* q, int host)
    cudaMemcpyAsync(S->ynm1 + 2 * S->N, S->yn + 2 * S->N, b4, cudaMemcpyDeviceToDevice,
                    S->s);
    S->hist = 0;
+   if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
+   return AMPE_OK;
+}
+
+int ampe_stepper_set_orientation(void* h, const double* q, int host)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || !q || !S->qorient) return AMPE_ERR_INVALID;
+   const cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+   const size_t bytes = sizeof(double) * (size_t)S->N;
+   for (int c = 0; c < S->m.qlen; c++) {
+      cudaMemcpyAsync(S->tmp, q + c * S->N, bytes, kind, S->s);
+      to_ghosted<double>(S->g, S->tmp, nullptr, 0.0, S->qorient + c * S->NG, S->s);
+   }
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
    return AMPE_OK;
 }

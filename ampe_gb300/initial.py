@@ -74,3 +74,32 @@ def polycrystal_state(n=128, ngrains=8, seed=0, channel=6.0, width=1.5,
     q = np.ascontiguousarray(np.moveaxis(quats[g1], -1, 0))
     c = rng.uniform(clo, chi, size=(n, n, n))
     return phi, c, q
+
+
+def dendrite2d_state(n=2048, nseeds=16, radius=8.0, seed=0, width=3.0, c0=0.02,
+                     noise=1e-3):
+    """2D seeds of the given radius at seeded random centres, each with a
+    random orientation angle theta in [0, pi); every cell takes its nearest
+    seed's angle.  Returns phi, c (1, n, n) and q (2, 1, n, n) =
+    (cos theta, sin theta), the 2-component orientation read by the 2D
+    anisotropic flux (phi_orient = acos q0)."""
+    rng = np.random.default_rng(seed)
+    centers = [tuple(rng.uniform(0, n, size=2)) for _ in range(nseeds)]
+    angles = rng.uniform(0.0, np.pi, size=nseeds)
+    phi = tanh_seed((n, n), centers, [radius] * nseeds, width)
+    ax = np.arange(n) + 0.5
+    yy, xx = np.meshgrid(ax, ax, indexing="ij")
+    best = np.full((n, n), np.inf)
+    theta = np.zeros((n, n))
+    for (cy, cx), a in zip(centers, angles):
+        dy = np.abs(yy - cy)
+        dy = np.minimum(dy, n - dy)
+        dx = np.abs(xx - cx)
+        dx = np.minimum(dx, n - dx)
+        d = dx * dx + dy * dy
+        closer = d < best
+        theta = np.where(closer, a, theta)
+        best = np.where(closer, d, best)
+    c = c0 + rng.uniform(-noise, noise, size=(n, n))
+    q = np.stack([np.cos(theta), np.sin(theta)]).reshape(2, 1, n, n)
+    return phi.reshape(1, n, n), c.reshape(1, n, n), np.ascontiguousarray(q)

@@ -85,6 +85,14 @@ class ImplicitStepper:
         self._keep_q = q
         check(lib.ampe_stepper_set_quat(self._h, _ptr(q), 1), "ampe_stepper_set_quat")
 
+    def set_orientation(self, q):
+        """Static orientation of the anisotropic flux: array (qlen, *interior
+        shape), component-major."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        self._keep_o = q
+        check(lib.ampe_stepper_set_orientation(self._h, _ptr(q), 1),
+              "ampe_stepper_set_orientation")
+
     def get_quat(self):
         q = np.empty(4 * self.n)
         check(lib.ampe_stepper_get_quat(self._h, _ptr(q), 1), "ampe_stepper_get_quat")

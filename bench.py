@@ -70,10 +70,11 @@ ATOL = 1.0e-6
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--workload", default="calphad", choices=["calphad", "poly", "dendrite"])
+    ap.add_argument("--n", type=int, default=0, help="cells per side (0: the workload's)")
     ap.add_argument("--path", default="mixed+surrogate",
                     choices=["fp64", "mixed", "mixed+surrogate"])
     ap.add_argument("--surrogate-samples", type=int, default=1 << 22)
@@ -130,10 +131,11 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
+            time.sleep(0.3)  # let the sampler start before the timed region
         except FileNotFoundError:
             self.proc = None
 
@@ -174,13 +176,56 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def workload(n, seed=3):
+class State:
+    """Initial state of a workload: phi, c and, per model, the evolving
+    quaternions or the static orientation of the anisotropic flux."""
+
+    def __init__(self, phi, c, quat=None, orient=None):
+        self.phi, self.c, self.quat, self.orient = phi, c, quat, orient
+
+    def load(self, stepper):
+        stepper.set_state(self.phi, self.c)
+        if self.quat is not None:
+            stepper.set_quat(self.quat)
+        if self.orient is not None:
+            stepper.set_orientation(self.orient)
+
+
+def default_n(kind):
+    return {"calphad": 256, "poly": 128, "dendrite": 2048}[kind]
+
+
+def workload(n, kind="calphad", seed=3):
+    """calphad: phi + c CALPHAD 3D, T_run + 50 K gradient (the headline);
+    poly: phi + q + c CALPHAD polycrystal 3D at 1500 K, seeded Voronoi grains
+    (8 at 128^3, 64 at 512^3), 6-cell liquid channel; dendrite: 2D dilute KKS,
+    four-fold anisotropic flux (delta 0.02), undercooling 0.55, 16 seeds of
+    radius 8 with random orientation angles."""
     from ampe_gb300 import configs, initial
 
+    if kind == "poly":
+        m = configs.polycrystal3d(n, seed=seed, T=1500.0)
+        ngr = max(8, (n // 128) ** 3 * 8)
+        phi, c, q = initial.polycrystal_state(n, ngrains=ngr, seed=1, channel=6.0)
+        return m, State(phi, c, quat=q)
+    if kind == "dendrite":
+        m = configs.dendrite2d(n)
+        phi, c, q = initial.dendrite2d_state(n, nseeds=16, radius=8.0, seed=seed)
+        return m, State(phi, c, orient=q)
     m = configs.calphad3d(n, seed=seed, T_run=1500.0)
     phi, c = initial.calphad3d_state(n, seed=seed, nseeds=max(2, (n // 32) ** 3 // 2),
                                      radius=max(4.0, n / 20.0))
-    return m, phi, c
+    return m, State(phi, c)
+
+
+WORKLOAD_NAMES = {
+    "calphad": "phi+c CALPHAD implicit step %d^3 (dt=0.1, BDF<=2, Newton-GMRES(5), "
+               "MG-preconditioned FAC blocks, atol %g)",
+    "poly": "phi+q+c CALPHAD polycrystal implicit step %d^3 (dt=0.1, BDF<=2, "
+            "Newton-GMRES(5), MG-preconditioned FAC blocks, atol %g)",
+    "dendrite": "phi+c dilute anisotropic dendrite implicit step %d^2 (dt=0.1, BDF<=2, "
+                "Newton-GMRES(5), MG-preconditioned FAC blocks, atol %g)",
+}
 
 
 def step_params(args, path):
@@ -196,19 +241,20 @@ def cpu_baseline(args, threads=None):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle as O
 
-    n = args.cpu_n
-    m, phi, c = workload(n)
+    n = args.cpu_n if args.workload != "dendrite" else 8 * args.cpu_n
+    m, st0 = workload(n, args.workload)
     p = step_params(args, "fp64")
     s = O.OracleStepper(m, p)
-    s.set_state(phi, c)
+    st0.load(s)
     s.advance(1)  # warm-up (first-touch, BDF1 start)
     steps = 2
     t0 = time.perf_counter()
     rc, st = s.advance(steps)
     dt = time.perf_counter() - t0
     cores = threads or os.cpu_count()
-    return {"value": n ** 3 * steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d^3 level, %d implicit steps (after 1 warm-up), oracle/ C++ FP64" % (n, steps)}
+    return {"value": m.cells() * steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d cells (%s), %d implicit steps (after 1 warm-up), oracle/ C++ FP64"
+                      % (m.cells(), args.workload, steps)}
 
 
 def run_reference(args):
@@ -220,27 +266,27 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle as O
 
-    n = args.cpu_n
-    m, phi, c = workload(n)
+    n = args.cpu_n if args.workload != "dendrite" else 8 * args.cpu_n
+    m, st0 = workload(n, args.workload)
     p = step_params(args, "fp64")
     s = O.OracleStepper(m, p)
-    s.set_state(phi, c)
+    st0.load(s)
     s.advance(max(1, args.warmup))
     t0 = time.perf_counter()
     rc, st = s.advance(args.steps)
     dt = time.perf_counter() - t0
-    v = n ** 3 * args.steps / dt
+    v = m.cells() * args.steps / dt
     out = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "phi+c CALPHAD implicit step, bounded CPU sample %d^3" % n,
-                   "sample_of": "%d^3" % args.n},
+        "config": {"workload": (WORKLOAD_NAMES[args.workload] % (n, ATOL))
+                   + ", bounded CPU sample", "sample_of": "%d cells per side" % args.n},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d^3 level, %d implicit steps, oracle/ C++ FP64 (reference "
+                         "sample": "%d cells, %d implicit steps, oracle/ C++ FP64 (reference "
                                    "sources unbuildable here: no SAMRAI/SUNDIALS/hypre/Thermo4PFM)"
-                                   % (n, args.steps)},
+                                   % (m.cells(), args.steps)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -275,7 +321,7 @@ def train_surrogate(args, m, local):
     return h, info
 
 
-def timed_path(args, m, phi, c, path, local, mlp=None):
+def timed_path(args, m, st0, path, local, mlp=None):
     """Warm up, then time args.steps accepted steps of one path on the device.
     Returns (result dict, final host state, stepper)."""
     import torch
@@ -288,7 +334,7 @@ def timed_path(args, m, phi, c, path, local, mlp=None):
     g = ImplicitStepper(m, step_params(args, path))
     if path == "mixed+surrogate":
         _native.check(L.ampe_stepper_attach_surrogate(g._h, mlp), "attach_surrogate")
-    g.set_state(phi, c)
+    st0.load(g)
     g.advance(args.warmup)
     stream = torch.cuda.ExternalStream(L.ampe_stepper_stream(g._h))
     torch.cuda.synchronize()
@@ -317,7 +363,10 @@ def timed_path(args, m, phi, c, path, local, mlp=None):
         L.ampe_stepper_kernel_time(g._h, kind, C.byref(tot), C.byref(cnt))
         kt[name] = {"ms": tot.value, "launches": cnt.value}
     L.ampe_stepper_profile(g._h, 0)
-    state = g.get_state()
+    state = {"phi": None, "c": None}
+    state["phi"], state["c"] = g.get_state()[:2]
+    if st0.quat is not None:
+        state["q"] = g.get_quat()
     return {"ms": ms, "stats": st, "launches": int(launches), "kernels": kt,
             "clocks": clocks.summary(), "value": N * args.steps / (ms / 1e3)}, state, g
 
@@ -333,7 +382,7 @@ def run_ours(args):
     from ampe_gb300 import _native
 
     L = _native.lib
-    m, phi, c = workload(args.n)
+    m, st0 = workload(args.n, args.workload)
     N = m.cells()
     head = args.path
     mlp, sur_info = None, None
@@ -341,13 +390,13 @@ def run_ours(args):
         mlp, sur_info = train_surrogate(args, m, local)
     if ws > 1:
         dist.barrier()
-    res_h, st_h, g = timed_path(args, m, phi, c, head, local, mlp)
+    res_h, st_h, g = timed_path(args, m, st0, head, local, mlp)
     ms_max, updates = aggregate(res_h["ms"], N * args.steps)
     value = updates / (ms_max / 1e3)
 
     # end to end through the C-ABI, state from pinned host memory each step
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and args.workload == "calphad":
         hp = torch.empty(N, dtype=torch.float64).pin_memory()
         hc = torch.empty(N, dtype=torch.float64).pin_memory()
         L.ampe_stepper_get_state(g._h, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()),
@@ -377,7 +426,7 @@ def run_ours(args):
             continue
         if other == "mixed+surrogate" and mlp is None:
             continue
-        r, st, g2 = timed_path(args, m, phi, c, other, local, mlp)
+        r, st, g2 = timed_path(args, m, st0, other, local, mlp)
         g2.close()
         del g2
         torch.cuda.empty_cache()
@@ -387,12 +436,15 @@ def run_ours(args):
     for name, (r, st) in results.items():
         d = {"value": r["value"], "ms_per_step": r["ms"] / args.steps,
              "kks_iters": r["stats"]["kks_iters"], "kks_fallback": r["stats"]["kks_fallback"],
-             "newton_iters": r["stats"]["newton_iters"], "gmres_iters": r["stats"]["gmres_iters"]}
+             "newton_iters": r["stats"]["newton_iters"], "gmres_iters": r["stats"]["gmres_iters"],
+             "clocks": r["clocks"], "kernels_ms": {k: v["ms"] for k, v in r["kernels"].items()
+                                                   if v["launches"]}}
         if ref is not None and name != "fp64":
             d["speedup_vs_fp64"] = r["value"] / ref[0]["value"]
             d["rel_l2_err_vs_fp64"] = {
-                f: float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
-                for f, a, b in zip(("phi", "c"), st[:2], ref[1][:2])}
+                f: float(np.linalg.norm((st[f] - ref[1][f]).ravel())
+                         / np.linalg.norm(ref[1][f].ravel()))
+                for f in st}
         paths[name] = d
     if mlp is not None:
         L.ampe_mlp_destroy(mlp)
@@ -428,9 +480,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": "phi+c CALPHAD implicit step %d^3 (dt=0.1, BDF<=2, "
-                               "Newton-GMRES(5), MG-preconditioned FAC blocks, atol %g)"
-                               % (args.n, ATOL), "path": head, "cells": N,
+        "config": {"workload": WORKLOAD_NAMES[args.workload] % (args.n, ATOL),
+                   "path": head, "cells": N,
                    "l2": "inputs larger than L2 (state 2 x %d MB)" % (N * 8 // 2 ** 20),
                    "parallelism": "replicas" if ws > 1 else "single"},
         "paths": paths,
@@ -452,6 +503,8 @@ def run_ours(args):
 
 def main():
     args = parse()
+    if args.n <= 0:
+        args.n = default_n(args.workload)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -414,6 +414,12 @@ int ampe_stepper_load_y(void* handle, const double* phi, const double* conc,
  * Accepted steps are projected onto unit quaternions
  * (QuatIntegrator::applyProjection, QuatIntegrator.cc:3911-3940). */
 int ampe_stepper_set_quat(void* handle, const double* q, int host);
+/* Anisotropic flux models without evolve_quat: the static orientation field
+ * read by the phase flux (PhaseFluxStrategyAnisotropy, quat_id of
+ * PhaseFluxStrategy::computeFluxes, PhaseFluxStrategy.h:25-27), qlen
+ * component-major interior arrays; 2D qlen 2 gives phi_o = acos q0.
+ * Default after create: q = (1, 0, ...), angle 0. */
+int ampe_stepper_set_orientation(void* handle, const double* q, int host);
 int ampe_stepper_get_quat(void* handle, double* q, int host);
 /* Length of the stepper's state vector y: 2N, or 6N with quaternions. */
 long long ampe_stepper_size(void* handle);

@@ -112,6 +112,7 @@ void orc_stepper_get_state(void* h, double* phi, double* conc, double* cl,
                            double* cs);
 void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs);
 void orc_stepper_eval_rhs_full(void* h, double* out);
+void orc_stepper_set_orientation(void* h, const double* q);
 long orc_stepper_size(void* h);
 int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats);
 void orc_stepper_jv(void* h, const double* v, double gamma, double* out,

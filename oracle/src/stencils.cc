@@ -463,9 +463,13 @@ void orc_jv_analytic(const ampe_model_t* m, const double* phi,
    orc_fill_ghosts(m, dp.data());
    orc_fill_ghosts(m, da.data());
    orc_fill_ghosts(m, db.data());
-   // phase part: linear flux of dphi + pointwise terms
+   // phase part: linear flux of dphi + pointwise terms.  The product is
+   // defined for the linear (simple, isotropic) fluxes only: for the
+   // anisotropic flux the phase rows are NaN (not available) and the
+   // composition rows are still formed.
+   const bool linear_flux = m->flux_type != AMPE_FLUX_ANISOTROPIC;
    std::vector<double> f0(L.nfx()), f1(L.nfy()), f2(L.dim == 3 ? L.nfz() : 1);
-   orc_phase_flux(m, dp.data(), nullptr, f0.data(), f1.data(), f2.data());
+   if (linear_flux) orc_phase_flux(m, dp.data(), nullptr, f0.data(), f1.data(), f2.data());
    std::vector<double> lap(N);
    ampe_model_t m0 = *m;
    m0.phase_well_scale = 0.0;
@@ -503,7 +507,7 @@ void orc_jv_analytic(const ampe_model_t* m, const double* phi,
                 (lap[t] - m->phase_well_scale * second_deriv_well_func(p, m->well_type) * v[t] +
                  second_deriv_interp_func(p, m->energy_interp) * dF * v[t] +
                  deriv_interp_func(p, m->energy_interp) * ddF);
-            out[t] = v[t] - gamma * jp;
+            out[t] = linear_flux ? v[t] - gamma * jp : std::nan("");
             out[t + N] = v[t + N] - gamma * jc[t];
          }
 }

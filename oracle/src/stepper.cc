@@ -27,6 +27,9 @@ struct OStepper {
    int nb = 2;  // scalar fields in y: phi, c (+ q0..q3)
    long NY = 0; // nb * N
    std::vector<double> q_g, q_lag, ogm, mq, fcq[3], Dq[3];
+   // static orientation field of the anisotropic phase flux (qlen ghosted
+   // components; evolve_quat models use q_g instead)
+   std::vector<double> qorient;
    void* fac_quat = nullptr;
    std::vector<double> phi_g, c_g, cl, cs, clr, csr, temp, phi_lag;
    std::vector<double> cl_nf, cs_nf;  // cL, cS of the last f(y) with fd_flag=0
@@ -93,7 +96,10 @@ void eval_rhs(OStepper& s, const double* y, double* fy, int fd_flag)
          orc_quat_grad_modulus(&s.m, s.q_lag.data(), s.ogm.data());
       }
    }
-   orc_rhs_phase_conc_q(&s.m, s.phi_g.data(), nullptr, temp_ptr(s),
+   const double* qflux = nullptr;
+   if (s.m.flux_type == AMPE_FLUX_ANISOTROPIC)
+      qflux = quat ? s.q_g.data() : s.qorient.data();
+   orc_rhs_phase_conc_q(&s.m, s.phi_g.data(), qflux, temp_ptr(s),
                         s.cl.data(), s.cs.data(), s.phi_lag.data(),
                         quat ? s.ogm.data() : nullptr, fy, fy + s.N);
    if (quat) {
@@ -331,6 +337,11 @@ void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p)
    s->Dc[1].assign(L.nfy(), 0.0);
    s->Dc[2].assign(L.dim == 3 ? L.nfz() : 1, 0.0);
    s->nb = m->evolve_quat ? 6 : 2;
+   if (m->flux_type == AMPE_FLUX_ANISOTROPIC && !m->evolve_quat) {
+      // default orientation: q = (1, 0, ...), angle 0
+      s->qorient.assign((size_t)m->qlen * s->NG, 0.0);
+      std::fill(s->qorient.begin(), s->qorient.begin() + s->NG, 1.0);
+   }
    s->NY = s->nb * s->N;
    s->yn.assign(s->NY, 0.0);
    s->ynm1.assign(s->NY, 0.0);
@@ -401,6 +412,18 @@ void orc_stepper_set_quat(void* h, const double* q)
    if (!s->m.evolve_quat) return;
    std::copy(q, q + 4 * s->N, s->yn.begin() + 2 * s->N);
    std::copy(q, q + 4 * s->N, s->ynm1.begin() + 2 * s->N);
+}
+
+// static orientation (qlen interior components) of the anisotropic flux
+void orc_stepper_set_orientation(void* h, const double* q)
+{
+   OStepper* s = (OStepper*)h;
+   if (s->qorient.empty()) return;
+   std::vector<double> tmp(s->NG);
+   for (int c = 0; c < s->m.qlen; c++) {
+      to_ghosted(*s, q + c * s->N, tmp);
+      std::copy(tmp.begin(), tmp.end(), s->qorient.begin() + c * s->NG);
+   }
 }
 
 void orc_stepper_get_quat(void* h, double* q)

@@ -79,6 +79,7 @@ def lib():
             "orc_quat_face_coef": (None, [MP, P, P, P, P, P, P]),
             "orc_quat_rhs": (None, [MP, P, P, P, P, P, P]),
             "orc_stepper_eval_rhs_full": (None, [P, P]),
+            "orc_stepper_set_orientation": (None, [P, P]),
             "orc_stepper_size": (C.c_long, [P]),
             "orc_rhs_phase_conc_q": (None, [MP, P, P, P, P, P, P, P, P, P]),
             "orc_jv_analytic": (None, [MP, P, P, P, P, D, P]),
@@ -121,6 +122,11 @@ class OracleStepper:
     def set_quat(self, q):
         q = np.ascontiguousarray(q, dtype=np.float64)
         self.L.orc_stepper_set_quat(self.h, ptr(q))
+
+    def set_orientation(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        self._q_keep = q
+        self.L.orc_stepper_set_orientation(self.h, ptr(q))
 
     def get_quat(self):
         q = np.empty((4,) + tuple(self.model.interior_shape()))
