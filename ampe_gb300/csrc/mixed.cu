@@ -120,8 +120,12 @@ __device__ __forceinline__ float driving_force_f32(const CoefF& th, float a,
    float SLa, S1La, S2La, SSb, S1Sb, S2Sb;
    rk_f(th.L[0], ua, SLa, S1La, S2La);
    rk_f(th.L[1], ub, SSb, S1Sb, S2Sb);
+   // ln(a/b) = log1p((a-b)/b) and ln((1-a)/(1-b)) = log1p((b-a)/(1-b)): the
+   // arguments of the logarithms are near one for a ~ b and for dilute
+   // compositions; log1p of the exactly formed difference keeps FP32
+   // relative accuracy there
    const float ideal =
-       th.RT * (a * logf(a / b) + (1.f - a) * logf((1.f - a) / (1.f - b)));
+       th.RT * (a * log1pf((a - b) / b) + (1.f - a) * log1pf((b - a) / (1.f - b)));
    const float fl = a * th.dG[0] + th.GB[0] + a * (1.f - a) * SLa;
    const float fs = b * th.dG[1] + th.GB[1] + b * (1.f - b) * SSb;
    const float xs = th.dG[1] - ub * SSb + b * (1.f - b) * 2.f * S1Sb;
@@ -343,7 +347,7 @@ __device__ __forceinline__ float face_flux_lin(const MixParams& mp, int d,
 // and dF/d(dpx), dF/d(dpy) through theta's derivatives
 // (-dpy, dpx) / (dpx^2 + dpy^2).
 // ---------------------------------------------------------------------------
-__global__ void k_aniso_faces_f32(MixParams mp, Grid g, const float* pf, const double* q,
+__global__ void k_aniso_faces_f32(MixParams mp, Grid g, const double* ph, const double* q,
                                   AnisoF a)
 {
    const long long nx = g.nfx(), tot = nx + g.nfy();
@@ -353,21 +357,22 @@ __global__ void k_aniso_faces_f32(MixParams mp, Grid g, const float* pf, const d
         t += (long long)gridDim.x * blockDim.x) {
       int dir, i, j, k;
       face_of(g, t, dir, i, j, k);
-      auto P = [&](int x, int y) { return pf[g.c(x, y, 0)]; };
-      float dpx, dpy, qa;
+      // neighbour differences of the FP64 phase, rounded once
+      auto D = [&](int x, int y, int x2, int y2) {
+         return d2f(ph[g.c(x, y, 0)] - ph[g.c(x2, y2, 0)]);
+      };
+      float dpx, dpy, po;
       if (dir == 0) {
-         dpx = (P(i, j) - P(i - 1, j)) * mp.dxi[0];
-         dpy = 0.25f * (P(i - 1, j + 1) - P(i - 1, j - 1) + P(i, j + 1) - P(i, j - 1)) * mp.dxi[1];
-         qa = 0.5f * (d2f(q[g.c(i - 1, j, 0)]) + d2f(q[g.c(i, j, 0)]));
+         dpx = D(i, j, i - 1, j) * mp.dxi[0];
+         dpy = 0.25f * (D(i - 1, j + 1, i - 1, j - 1) + D(i, j + 1, i, j - 1)) * mp.dxi[1];
+         po = a.PO[0][g.fx(i, j, 0)];
       } else {
-         dpx = 0.25f * (P(i + 1, j - 1) - P(i - 1, j - 1) + P(i + 1, j) - P(i - 1, j)) * mp.dxi[0];
-         dpy = (P(i, j) - P(i, j - 1)) * mp.dxi[1];
-         qa = 0.5f * (d2f(q[g.c(i, j - 1, 0)]) + d2f(q[g.c(i, j, 0)]));
+         dpx = 0.25f * (D(i + 1, j - 1, i - 1, j - 1) + D(i + 1, j, i - 1, j)) * mp.dxi[0];
+         dpy = D(i, j, i, j - 1) * mp.dxi[1];
+         po = a.PO[1][g.fy(i, j, 0)];
       }
       const bool steep = fabsf(dpx) > fthr;
       const float theta = steep ? atanf(dpy / dpx) : half_pi;
-      qa = fminf(1.f, fmaxf(-1.f, qa));
-      const float po = mp.qlen4 ? 2.f * acosf(qa) : acosf(qa);
       float sn, cs;
       sincosf(mp.kn * (theta - po), &sn, &cs);
       const float e = mp.eps * (1.f + mp.nu * cs);
@@ -402,14 +407,42 @@ __global__ void k_aniso_faces_f32(MixParams mp, Grid g, const float* pf, const d
    }
 }
 
+__global__ void k_aniso_orientation(Grid g, int qlen4, const double* q, AnisoF a)
+{
+   const long long nx = g.nfx(), tot = nx + g.nfy();
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      face_of(g, t, dir, i, j, k);
+      double qa = dir == 0 ? 0.5 * (q[g.c(i - 1, j, 0)] + q[g.c(i, j, 0)])
+                           : 0.5 * (q[g.c(i, j - 1, 0)] + q[g.c(i, j, 0)]);
+      qa = fmin(1.0, fmax(-1.0, qa));
+      const double po = qlen4 ? 2.0 * acos(qa) : acos(qa);
+      if (dir == 0)
+         a.PO[0][g.fx(i, j, 0)] = (float)po;
+      else
+         a.PO[1][g.fy(i, j, 0)] = (float)po;
+   }
+}
+
+int aniso_orientation_f32(const ampe_model_t& m, const Grid& g, const double* q,
+                          AnisoF& a, cudaStream_t s)
+{
+   const long long tot = g.nfx() + g.nfy();
+   long long b = (tot + 255) / 256;
+   if (b > kMaxBlocks) b = kMaxBlocks;
+   k_aniso_orientation<<<(unsigned)b, 256, 0, s>>>(g, m.qlen == 4 ? 1 : 0, q, a);
+   return launch_status();
+}
+
 int aniso_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
-                    const float* pf, const double* q, AnisoF& a, cudaStream_t s)
+                    const double* ph, const double* q, AnisoF& a, cudaStream_t s)
 {
    (void)m;
    const long long tot = g.nfx() + g.nfy();
    long long b = (tot + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
-   k_aniso_faces_f32<<<(unsigned)b, 256, 0, s>>>(mp, g, pf, q, a);
+   k_aniso_faces_f32<<<(unsigned)b, 256, 0, s>>>(mp, g, ph, q, a);
    return launch_status();
 }
 
@@ -431,6 +464,30 @@ __device__ __forceinline__ float aniso_dflux(const MixParams& mp, const AnisoF& 
    const float gy = (P(i, j) - P(i, j - 1)) * mp.dxi[1];
    const int f = g.fy(i, j, 0);
    return a.JA[1][f] * gx + a.JB[1][f] * gy;
+}
+
+// the same flux from the FP64 phase: each neighbour difference is formed in
+// FP64 and rounded once (phi ~ 1 rounded to FP32 first would leave the
+// difference of two rounded numbers: ~6e-8 absolute, about 1e-6 relative to
+// an interface gradient)
+template <int DIM>
+__device__ __forceinline__ float face_flux_lin64(const MixParams& mp, int d,
+                                                 const double* ph, const Grid& g,
+                                                 int i, int j, int k)
+{
+   if (DIM == 3 || !mp.iso) {
+      const int ei = d == 0, ej = d == 1, ek = d == 2;
+      return d2f(ph[g.c(i, j, k)] - ph[g.c(i - ei, j - ej, k - ek)]) * mp.flux_dinv[d];
+   }
+   auto D = [&](int a, int b, int a2, int b2) {
+      return d2f(ph[g.c(a, b, 0)] - ph[g.c(a2, b2, 0)]);
+   };
+   const float dinv = mp.flux_dinv[d];
+   if (d == 0)
+      return dinv * (D(i, j - 1, i - 1, j - 1) + D(i, j, i - 1, j) * 10.f +
+                     D(i, j + 1, i - 1, j + 1));
+   return dinv * (D(i - 1, j, i - 1, j - 1) + D(i, j, i, j - 1) * 10.f +
+                  D(i + 1, j, i + 1, j - 1));
 }
 
 // face weights (1-h) D_L, h D_S from the phases of the two cells
@@ -479,7 +536,7 @@ __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
 
 template <int DIM, bool PB, bool ANISO>
 __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
-                            const double* tfield, const float* pf,
+                            const double* tfield, const double* ph, const float* pf,
                             const float* cl, const float* cs, const float* dF,
                             const float* ogm, double* phi_rhs, double* conc_rhs)
 {
@@ -497,8 +554,8 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
             fm = d == 0 ? an.F[0][g.fx(i, j, 0)] : an.F[1][g.fy(i, j, 0)];
             fp = d == 0 ? an.F[0][g.fx(i + 1, j, 0)] : an.F[1][g.fy(i, j + 1, 0)];
          } else {
-            fm = face_flux_lin<DIM>(mp, d, pf, g, i, j, k);
-            fp = face_flux_lin<DIM>(mp, d, pf, g, i + ei, j + ej, k + ek);
+            fm = face_flux_lin64<DIM>(mp, d, ph, g, i, j, k);
+            fp = face_flux_lin64<DIM>(mp, d, ph, g, i + ei, j + ej, k + ek);
          }
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
@@ -542,19 +599,21 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    const bool aniso = m.flux_type == AMPE_FLUX_ANISOTROPIC;
    if (aniso) {
       if (g.dim != 2 || !q || !an) return AMPE_ERR_INVALID;
-      aniso_faces_f32(m, mp, g, pf, q, *an, s);
+      aniso_faces_f32(m, mp, g, phi, q, *an, s);
    }
    const AnisoF a0 = an ? *an : AnisoF();
 #define AMPE_RHS(D, P)                                                                      \
-   k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, pf, cl, cs, dF, \
-                                                        ogm, phi_rhs, conc_rhs)
+   k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, pf, cl, cs, \
+                                                        dF, ogm, phi_rhs, conc_rhs)
    if (aniso) {
       if (mp.pb)
-         k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, pf, cl,
-                                                               cs, dF, ogm, phi_rhs, conc_rhs);
+         k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, pf,
+                                                               cl, cs, dF, ogm, phi_rhs,
+                                                               conc_rhs);
       else
-         k_rhs_mixed<2, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, pf, cl,
-                                                                cs, dF, ogm, phi_rhs, conc_rhs);
+         k_rhs_mixed<2, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, pf,
+                                                                cl, cs, dF, ogm, phi_rhs,
+                                                                conc_rhs);
    } else if (g.dim == 3) {
       if (mp.pb)
          AMPE_RHS(3, true);

@@ -39,11 +39,17 @@ struct AnisoF {
    float* F[2] = {nullptr, nullptr};
    float* JA[2] = {nullptr, nullptr};
    float* JB[2] = {nullptr, nullptr};
+   float* PO[2] = {nullptr, nullptr};  // orientation angle phi_o per face
 };
-// fill an AnisoF from the FP32 phase copy and the orientation q (component 0,
-// ghosted FP64), 2D only
+// phi_o = acos(qbar) (2 acos for four-component q) per face, in FP64, once
+// per orientation field: acos is ill-conditioned at qbar ~ +-1, where an
+// FP32 qbar would cost up to ~1e-3 rad
+int aniso_orientation_f32(const ampe_model_t& m, const Grid& g, const double* q,
+                          AnisoF& a, cudaStream_t s);
+// fill an AnisoF from the FP64 phase (differences formed in FP64, rounded
+// once) and the orientation q (component 0, ghosted FP64), 2D only
 int aniso_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
-                    const float* pf, const double* q, AnisoF& a, cudaStream_t s);
+                    const double* ph, const double* q, AnisoF& a, cudaStream_t s);
 
 // FP32 working set of the quaternion equation in the mixed path
 struct QuatF32 {

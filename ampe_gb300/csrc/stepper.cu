@@ -1171,6 +1171,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
             S->an.F[d] = (float*)dalloc<float>(S->pool, nf, &err);
             S->an.JA[d] = (float*)dalloc<float>(S->pool, nf, &err);
             S->an.JB[d] = (float*)dalloc<float>(S->pool, nf, &err);
+            S->an.PO[d] = (float*)dalloc<float>(S->pool, nf, &err);
          }
       }
    }
@@ -1232,6 +1233,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
       double* q0 = S->qorient;
       const long long ng = S->NG;
       map(ng, [=] __device__(long long t) { q0[t] = 1.0; }, S->s);
+      if (S->an.PO[0]) aniso_orientation_f32(*m, S->g, S->qorient, S->an, S->s);
    }
    if (!err && S->tab) err = build_thermo_table(*m, S->tab, nt, S->s);
    if (!err && S->tabf) err = build_coef_f(S->tab, S->tabf, nt, S->s);
@@ -1516,6 +1518,7 @@ int ampe_stepper_set_orientation(void* h, const double* q, int host)
       cudaMemcpyAsync(S->tmp, q + c * S->N, bytes, kind, S->s);
       to_ghosted<double>(S->g, S->tmp, nullptr, 0.0, S->qorient + c * S->NG, S->s);
    }
+   if (S->an.PO[0]) aniso_orientation_f32(S->m, S->g, S->qorient, S->an, S->s);
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
    return AMPE_OK;
 }

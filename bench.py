@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--surrogate-samples", type=int, default=1 << 22)
     ap.add_argument("--surrogate-steps", type=int, default=2000)
     ap.add_argument("--precond", type=int, default=2)
+    ap.add_argument("--atol", type=float, default=ATOL,
+                    help="Newton/WRMS absolute tolerance (rtol = atol/100)")
     ap.add_argument("--cpu-n", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -231,7 +233,7 @@ WORKLOAD_NAMES = {
 def step_params(args, path):
     from ampe_gb300 import configs
 
-    return configs.step_params(dt=0.1, precond=args.precond, mg_levels=5, atol=ATOL,
+    return configs.step_params(dt=0.1, precond=args.precond, mg_levels=5, atol=args.atol,
                                precision=0 if path == "fp64" else 1,
                                surrogate=1 if path == "mixed+surrogate" else 0)
 
@@ -281,7 +283,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": (WORKLOAD_NAMES[args.workload] % (n, ATOL))
+        "config": {"workload": (WORKLOAD_NAMES[args.workload] % (n, args.atol))
                    + ", bounded CPU sample", "sample_of": "%d cells per side" % args.n},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "%d cells, %d implicit steps, oracle/ C++ FP64 (reference "
@@ -480,7 +482,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD_NAMES[args.workload] % (args.n, ATOL),
+        "config": {"workload": WORKLOAD_NAMES[args.workload] % (args.n, args.atol),
                    "path": head, "cells": N,
                    "l2": "inputs larger than L2 (state 2 x %d MB)" % (N * 8 // 2 ** 20),
                    "parallelism": "replicas" if ws > 1 else "single"},
