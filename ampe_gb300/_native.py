@@ -35,6 +35,7 @@ _PROTOS = {
     "ampe_phase_concentrations": (I, [MP, P, P, P, P, P, P, P, P, P]),
     "ampe_conc_diffusion": (I, [MP, P, P, P, P, P, P, P, P, P]),
     "ampe_add_flux": (I, [MP, P, P, P, P, P, P, P, P]),
+    "ampe_conc_flux_kks": (I, [MP, P, P, P, P, P, P, P, P, P]),
     "ampe_computerhsconcentration": (I, [MP, P, P, P, P, P]),
     "ampe_rhs_phase_conc": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_efo_rbgs": (I, [MP, P, P, P, D, P, D, P, D, P, P, I, P, P]),

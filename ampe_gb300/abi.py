@@ -16,6 +16,7 @@ NOALLOC_SCRATCH_DOUBLES = 1 << 19
 FLUX_SIMPLE, FLUX_ISOTROPIC, FLUX_ANISOTROPIC = 0, 1, 2
 THERMO_DILUTE, THERMO_CALPHAD = 0, 1
 TEMP_CONSTANT, TEMP_GRADIENT, TEMP_FIELD = 0, 1, 2
+CONC_EBS, CONC_KKS = 0, 1
 MAX_TSEG = 6
 
 
@@ -78,6 +79,8 @@ class Model(C.Structure):
         ("quat_floor_type", C.c_char),
         ("quat_mobility_type", C.c_char),
         ("pad1", C.c_char * 6),
+        ("conc_form", C.c_int),
+        ("pad2", C.c_int),
     ]
 
     def cells(self):

@@ -133,8 +133,9 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
                             const double* quat, const double* tfield,
                             const ThermoCoef* tab, const double* cl,
                             const double* cs, const double* dF,
-                            const double* phid, const double* ogm,
-                            double* phi_rhs, double* conc_rhs)
+                            const double* phid, const double* ogm, const double* conc,
+                            const double* cld, const double* csd, double* phi_rhs,
+                            double* conc_rhs)
 {
    const long long qs = g.cells_ghost();
    const double eq2 = 0.5 * m.epsilon_q * m.epsilon_q;
@@ -189,7 +190,8 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
             const long long up = g.c(a0, a1, a2);
             const long long lo = g.c(a0 - ei, a1 - ej, a2 - ek);
             const double vphi = average_func(phid[lo], phid[up], m.avg_type);
-            const double hphi = interp_func(vphi, m.diff_interp);
+            const bool kksf = m.conc_form == AMPE_CONC_KKS;
+            const double hphi = interp_func(vphi, kksf ? m.energy_interp : m.diff_interp);
             double dlq = m.D_liquid, dsq = m.D_solid;
             if (tdep) {
                const double invT =
@@ -197,6 +199,17 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
                           temperature_at(m, g, tfield, a0, a1, a2));
                dlq = m.D_liquid * exp(-qlR * invT);
                dsq = m.D_solid * exp(-qsR * invT);
+            }
+            if (kksf) {
+               // "kks" form (KKSCompositionRHSStrategy.cc:98-441): D0 grad c +
+               // D0 h'(phibar)(cLbar - cSbar) grad phi, coefficients from the
+               // lagged phi, cL, cS
+               const double d0 = (1.0 - hphi) * dlq + hphi * dsq;
+               const double clb = 0.5 * (cld[up] + cld[lo]);
+               const double csb = 0.5 * (csd[up] + csd[lo]);
+               const double dph = d0 * deriv_interp_func(vphi, m.energy_interp) * (clb - csb);
+               fl[side] = dxi[d] * (d0 * (conc[up] - conc[lo]) + dph * (phi[up] - phi[lo]));
+               continue;
             }
             const double DL = (1.0 - hphi) * dlq, DS = hphi * dsq;
             double f = 0.0;
@@ -213,17 +226,21 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
 int rhs_fused(const ampe_model_t& m, const Grid& g, const double* phi,
               const double* quat, const double* tfield, const ThermoCoef* tab,
               const double* cl, const double* cs, const double* dF,
-              const double* phid, const double* ogm, double* phi_rhs,
+              const double* phid, const double* ogm, const double* conc,
+              const double* cld, const double* csd, double* phi_rhs,
               double* conc_rhs, cudaStream_t s)
 {
+   if (m.conc_form == AMPE_CONC_KKS && (!conc || !cld || !csd)) return AMPE_ERR_INVALID;
    long long b = (g.cells() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
    if (quat)
       k_rhs_fused<true><<<(unsigned)b, 256, 0, s>>>(
-          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, phi_rhs, conc_rhs);
+          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, conc, cld, csd, phi_rhs,
+          conc_rhs);
    else
       k_rhs_fused<false><<<(unsigned)b, 256, 0, s>>>(
-          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, phi_rhs, conc_rhs);
+          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, conc, cld, csd, phi_rhs,
+          conc_rhs);
    return launch_status();
 }
 
@@ -241,6 +258,8 @@ extern "C" int ampe_rhs_phase_conc(const ampe_model_t* m, const double* phi,
       return AMPE_ERR_INVALID;
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC && !quat) return AMPE_ERR_INVALID;
    if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
+   if (m->conc_form == AMPE_CONC_KKS) return AMPE_ERR_INVALID;  // needs c: ampe_conc_flux_kks
    return rhs_fused(*m, make_grid(*m), phi, quat, temp, nullptr, cl, cs,
-                    nullptr, phi, nullptr, phi_rhs, conc_rhs, (cudaStream_t)stream);
+                    nullptr, phi, nullptr, nullptr, nullptr, nullptr, phi_rhs, conc_rhs,
+                    (cudaStream_t)stream);
 }

@@ -14,7 +14,8 @@ int kks_interior(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
 int rhs_fused(const ampe_model_t& m, const Grid& g, const double* phi,
               const double* quat, const double* tfield, const ThermoCoef* tab,
               const double* cl, const double* cs, const double* dF,
-              const double* phid, const double* ogm, double* phi_rhs,
+              const double* phid, const double* ogm, const double* conc,
+              const double* cld, const double* csd, double* phi_rhs,
               double* conc_rhs, cudaStream_t s);
 
 }  // namespace ampe

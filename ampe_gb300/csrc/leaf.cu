@@ -167,6 +167,53 @@ __global__ void k_phase_conc_ghostbox(ampe_model_t m, Grid g,
    }
 }
 
+// "kks" composition flux: concentration_pfmdiffusion (3d/concentrationdiffusion.m4:
+// 14-128, energy interpolation of KKSCompositionRHSStrategy.cc:111), the
+// coupling D0 h'(phibar)(cLbar - cSbar) (KKSCompositionRHSStrategy.cc:
+// 166-310) and concentrationflux (3d/concentrationrhs.m4:14-104), fused
+__global__ void k_conc_flux_kks(ampe_model_t m, Grid g, const double* phi,
+                                const double* temp, const double* conc,
+                                const double* cl, const double* cs, double* f0,
+                                double* f1, double* f2)
+{
+   const double qlR = m.Q_liquid / kGasR, qsR = m.Q_solid / kGasR;
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      const long long nx = g.nfx(), ny = g.nfy();
+      long long r = t;
+      if (r < nx) {
+         dir = 0;
+         g.split(r, g.fd0p, g.fd1, i, j, k);
+      } else if ((r -= nx) < ny) {
+         dir = 1;
+         g.split(r, g.fd0, g.fd1p, i, j, k);
+      } else {
+         r -= ny;
+         dir = 2;
+         g.ijk(r, i, j, k);
+      }
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const long long lo = g.c(i - ei, j - ej, k - ek), up = g.c(i, j, k);
+      const double vphi = average_func(phi[lo], phi[up], m.avg_type);
+      const double hphi = interp_func(vphi, m.energy_interp);
+      const double invT = 2.0 / (temperature_at(m, g, temp, i - ei, j - ej, k - ek) +
+                                 temperature_at(m, g, temp, i, j, k));
+      const double dlq = m.D_liquid * exp(-qlR * invT);
+      const double dsq = m.D_solid * exp(-qsR * invT);
+      const double d0 = (1.0 - hphi) * dlq + hphi * dsq;
+      const double clb = 0.5 * (cl[up] + cl[lo]);
+      const double csb = 0.5 * (cs[up] + cs[lo]);
+      const double dph = d0 * deriv_interp_func(vphi, m.energy_interp) * (clb - csb);
+      const double dinv = 1.0 / m.dx[dir];
+      const double v = dinv * (d0 * (conc[up] - conc[lo]) + dph * (phi[up] - phi[lo]));
+      if (dir == 0) f0[g.fx(i, j, k)] = v;
+      if (dir == 1) f1[g.fy(i, j, k)] = v;
+      if (dir == 2) f2[g.fz(i, j, k)] = v;
+   }
+}
+
 __global__ void k_conc_diffusion(ampe_model_t m, Grid g, const double* phi,
                                  const double* temp, double* dl0, double* dl1,
                                  double* dl2, double* ds0, double* ds1,
@@ -357,6 +404,21 @@ int ampe_conc_diffusion(const ampe_model_t* m, const double* phi,
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    k_conc_diffusion<<<blocks_for(tot), 256, 0, S(stream)>>>(
        *m, g, phi, temp, dl0, dl1, dl2, ds0, ds1, ds2);
+   return launch_status();
+}
+
+int ampe_conc_flux_kks(const ampe_model_t* m, const double* phi, const double* temp,
+                       const double* conc, const double* cl, const double* cs,
+                       double* flux0, double* flux1, double* flux2, void* stream)
+{
+   if (check_model(m) || !phi || !conc || !cl || !cs || !flux0 || !flux1)
+      return AMPE_ERR_INVALID;
+   if (m->dim == 3 && !flux2) return AMPE_ERR_INVALID;
+   if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   k_conc_flux_kks<<<blocks_for(tot), 256, 0, S(stream)>>>(*m, g, phi, temp, conc, cl, cs,
+                                                           flux0, flux1, flux2);
    return launch_status();
 }
 

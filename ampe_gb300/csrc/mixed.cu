@@ -291,6 +291,7 @@ MixParams make_mix_params(const ampe_model_t& m)
    p.nu = (float)m.aniso_eps;
    p.kn = (float)m.aniso_k;
    p.qlen4 = m.qlen == 4 ? 1 : 0;
+   p.kksc = m.conc_form == AMPE_CONC_KKS ? 1 : 0;
    p.pb = (m.avg_type == 'a' && m.diff_interp == 'p' && m.energy_interp == 'p' &&
            m.conc_interp == 'p' && m.well_type == 'd' && m.orient_interp1 == 'p' &&
            m.orient_interp2 == 'p')
@@ -466,6 +467,33 @@ __device__ __forceinline__ float aniso_dflux(const MixParams& mp, const AnisoF& 
    return a.JA[1][f] * gx + a.JB[1][f] * gy;
 }
 
+// "kks" composition form on the face lo|up (KKSCompositionRHSStrategy.cc:
+// 98-441): D0 = (1-h) D_L + h D_S with h = energy_interp(phibar), and the
+// coupling D_phi = D0 h'(phibar)(cLbar - cSbar)
+template <int DIM, bool PB>
+__device__ __forceinline__ void kks_face_coef(const ampe_model_t& m, const MixParams& mp,
+                                              const Grid& g, const double* tfield,
+                                              const float* pf, const float* cl,
+                                              const float* cs, long long lo, long long up,
+                                              int a0, int a1, int a2, int ei, int ej, int ek,
+                                              float& D0, float& Dp)
+{
+   const Types<PB> ty(m);
+   const float vphi = average_func(pf[lo], pf[up], ty.avg);
+   const float h = interp_func(vphi, ty.energy);
+   float dlq = mp.Dl, dsq = mp.Ds;
+   if (mp.tdep) {
+      const float invT =
+          2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
+                        temperature_at(m, g, tfield, a0, a1, a2));
+      dlq = mp.Dl * expf(-mp.qlR * invT);
+      dsq = mp.Ds * expf(-mp.qsR * invT);
+   }
+   D0 = (1.f - h) * dlq + h * dsq;
+   Dp = D0 * deriv_interp_func(vphi, ty.energy) *
+        (0.5f * (cl[up] + cl[lo]) - 0.5f * (cs[up] + cs[lo]));
+}
+
 // the same flux from the FP64 phase: each neighbour difference is formed in
 // FP64 and rounded once (phi ~ 1 rounded to FP32 first would leave the
 // difference of two rounded numbers: ~6e-8 absolute, about 1e-6 relative to
@@ -536,7 +564,8 @@ __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
 
 template <int DIM, bool PB, bool ANISO>
 __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
-                            const double* tfield, const double* ph, const float* pf,
+                            const double* tfield, const double* ph, const double* cc,
+                            const float* pf,
                             const float* cl, const float* cs, const float* dF,
                             const float* ogm, double* phi_rhs, double* conc_rhs)
 {
@@ -559,12 +588,24 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
          }
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
+         const long long lo = g.c(i - ei, j - ej, k - ek);
+         if (mp.kksc) {  // "kks" form: c and phi differences in FP64, rounded once
+            float D0m, Dpm, D0p, Dpp;
+            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, c, i, j, k, ei, ej, ek,
+                                   D0m, Dpm);
+            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, c, up, i + ei, j + ej, k + ek,
+                                   ei, ej, ek, D0p, Dpp);
+            const float flm =
+                mp.dxi[d] * (D0m * d2f(cc[c] - cc[lo]) + Dpm * d2f(ph[c] - ph[lo]));
+            const float flp =
+                mp.dxi[d] * (D0p * d2f(cc[up] - cc[c]) + Dpp * d2f(ph[up] - ph[c]));
+            div += mp.dxi[d] * (flp - flm);
+            continue;
+         }
          float DLm, DSm, DLp, DSp;
-         face_diff<DIM, PB>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), c, i, j, k, ei,
-                        ej, ek, DLm, DSm);
+         face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, c, i, j, k, ei, ej, ek, DLm, DSm);
          face_diff<DIM, PB>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek,
                         DLp, DSp);
-         const long long lo = g.c(i - ei, j - ej, k - ek);
          const float flm = mp.dxi[d] * (DLm * (cl[c] - cl[lo]) + DSm * (cs[c] - cs[lo]));
          const float flp = mp.dxi[d] * (DLp * (cl[up] - cl[c]) + DSp * (cs[up] - cs[c]));
          div += mp.dxi[d] * (flp - flm);
@@ -587,9 +628,10 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
 int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield, const double* phi, float* pf,
               const float* cl, const float* cs, const float* dF,
-              const float* ogm, const double* q, AnisoF* an, double* phi_rhs,
-              double* conc_rhs, cudaStream_t s)
+              const float* ogm, const double* q, AnisoF* an, const double* cc,
+              double* phi_rhs, double* conc_rhs, cudaStream_t s)
 {
+   if (mp.kksc && !cc) return AMPE_ERR_INVALID;
    long long b = (g.cells_ghost() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
    k_phi_to_f32<<<(unsigned)b, 256, 0, s>>>(g, phi, pf);
@@ -603,16 +645,16 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    }
    const AnisoF a0 = an ? *an : AnisoF();
 #define AMPE_RHS(D, P)                                                                      \
-   k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, pf, cl, cs, \
-                                                        dF, ogm, phi_rhs, conc_rhs)
+   k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, cc, pf, cl, \
+                                                        cs, dF, ogm, phi_rhs, conc_rhs)
    if (aniso) {
       if (mp.pb)
-         k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, pf,
-                                                               cl, cs, dF, ogm, phi_rhs,
+         k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, cc,
+                                                               pf, cl, cs, dF, ogm, phi_rhs,
                                                                conc_rhs);
       else
-         k_rhs_mixed<2, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, pf,
-                                                                cl, cs, dF, ogm, phi_rhs,
+         k_rhs_mixed<2, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, cc,
+                                                                pf, cl, cs, dF, ogm, phi_rhs,
                                                                 conc_rhs);
    } else if (g.dim == 3) {
       if (mp.pb)
@@ -638,7 +680,7 @@ template <bool PB>
 __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
                            const double* tfield, const float* pf,
                            const float* cl, const float* cs, const float* v,
-                           float* dphi, float* da, float* db, float* dq)
+                           float* dphi, float* da, float* db, float* dcv, float* dq)
 {
    const long long N = g.cells(), NG = g.cells_ghost();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
@@ -665,6 +707,10 @@ __global__ void k_jv_point(ampe_model_t m, Grid g, const CoefF* tabf,
          da[idx] = xa;
          db[idx] = xb;
       });
+      if (dcv) {  // the c part of v, ghosted ("kks" composition form)
+         dcv[c] = vc;
+         for_each_image(g, i, j, k, [&](long long idx) { dcv[idx] = vc; });
+      }
       if (dq) {
 #pragma unroll
          for (int q = 0; q < 4; q++) {
@@ -717,8 +763,8 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
                              const CoefF* tabf, const double* tfield,
                              const float* pf, const float* cl, const float* cs,
                              const float* dF, const float* dphi,
-                             const float* da, const float* db, const float* v,
-                             const float* ogm, float gamma, float* out)
+                             const float* da, const float* db, const float* dcv,
+                             const float* v, const float* ogm, float gamma, float* out)
 {
    const long long N = g.cells();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N;
@@ -741,6 +787,19 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
          const long long lo = g.c(i - ei, j - ej, k - ek);
+         if (mp.kksc) {  // "kks" form: linear in (c, phi), coefficients held
+            float D0m, Dpm, D0p, Dpp;
+            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, c, i, j, k, ei, ej, ek,
+                                   D0m, Dpm);
+            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, c, up, i + ei, j + ej, k + ek,
+                                   ei, ej, ek, D0p, Dpp);
+            const float flm =
+                mp.dxi[d] * (D0m * (dcv[c] - dcv[lo]) + Dpm * (dphi[c] - dphi[lo]));
+            const float flp =
+                mp.dxi[d] * (D0p * (dcv[up] - dcv[c]) + Dpp * (dphi[up] - dphi[c]));
+            div += mp.dxi[d] * (flp - flm);
+            continue;
+         }
          float DLm, DSm, DLp, DSp;
          face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, c, i, j, k, ei, ej, ek, DLm, DSm);
          face_diff<DIM, PB>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek, DLp,
@@ -848,8 +907,16 @@ __global__ void k_conc_faces_f32(ampe_model_t m, MixParams mp, Grid g,
       face_of(g, t, dir, i, j, k);
       const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
       float DL, DS;
-      face_diff<DIM>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), g.c(i, j, k), i, j, k,
-                     ei, ej, ek, DL, DS);
+      if (mp.kksc) {  // "kks" form: D0 (energy interpolation)
+         float D0, Dp;
+         kks_face_coef<DIM, false>(m, mp, g, tfield, pf, pf, pf, g.c(i - ei, j - ej, k - ek),
+                                   g.c(i, j, k), i, j, k, ei, ej, ek, D0, Dp);
+         DL = D0;
+         DS = 0.f;
+      } else {
+         face_diff<DIM>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), g.c(i, j, k), i, j,
+                        k, ei, ej, ek, DL, DS);
+      }
       const long long fi = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
       f.fc[dir][fi] = -gamma * (DL + DS);
    }
@@ -924,33 +991,36 @@ __global__ void k_jv_quat(ampe_model_t m, MixParams mp, Grid g, const float* pf,
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf, const double* tfield, const float* pf,
              const float* cl, const float* cs, const float* dF, const float* v,
-             double gamma, float* dphi, float* da, float* db, const QuatF32* qf,
-             const AnisoF* an, float* out, cudaStream_t s)
+             double gamma, float* dphi, float* da, float* db, float* dcv,
+             const QuatF32* qf, const AnisoF* an, float* out, cudaStream_t s)
 {
+   if (mp.kksc && !dcv) return AMPE_ERR_INVALID;
    long long b = (g.cells() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
    float* dq = qf ? qf->dq : nullptr;
    if (mp.pb)
       k_jv_point<true><<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da,
-                                                   db, dq);
+                                                   db, mp.kksc ? dcv : nullptr, dq);
    else
       k_jv_point<false><<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi,
-                                                    da, db, dq);
+                                                    da, db, mp.kksc ? dcv : nullptr, dq);
    launch_status();
    const float* ogm = (qf && m.with_orient) ? qf->ogm : nullptr;
    const AnisoF a0 = an ? *an : AnisoF();
 #define AMPE_JV(D, P)                                                                          \
    k_jv_stencil<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tabf, tfield, pf, cl, cs, \
-                                                         dF, dphi, da, db, v, ogm, (float)gamma, \
-                                                         out)
+                                                         dF, dphi, da, db, dcv, v, ogm,          \
+                                                         (float)gamma, out)
    if (m.flux_type == AMPE_FLUX_ANISOTROPIC) {
       if (g.dim != 2 || !an) return AMPE_ERR_INVALID;
       if (mp.pb)
          k_jv_stencil<2, true, true><<<(unsigned)b, 256, 0, s>>>(
-             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, v, ogm, (float)gamma, out);
+             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm, (float)gamma,
+             out);
       else
          k_jv_stencil<2, false, true><<<(unsigned)b, 256, 0, s>>>(
-             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, v, ogm, (float)gamma, out);
+             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm, (float)gamma,
+             out);
    } else if (g.dim == 3) {
       if (mp.pb)
          AMPE_JV(3, true);

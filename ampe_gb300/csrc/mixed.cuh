@@ -30,6 +30,7 @@ struct MixParams {
    // 2D anisotropic phase flux
    float eps, nu, kn;
    int qlen4;
+   int kksc;  // "kks" composition flux form
 };
 
 // 2D anisotropic phase flux per face and its Jacobian with respect to the
@@ -73,15 +74,15 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield,
               const double* phi, float* pf, const float* cl, const float* cs,
               const float* dF, const float* ogm, const double* q, AnisoF* an,
-              double* phi_rhs, double* conc_rhs, cudaStream_t s);
+              const double* cc, double* phi_rhs, double* conc_rhs, cudaStream_t s);
 // out = v - gamma J v; qf (null without quaternions) adds the q rows and
 // the orientation term of the phase row
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf,
              const double* tfield, const float* pf, const float* cl,
              const float* cs, const float* dF, const float* v, double gamma,
-             float* dphi, float* da, float* db, const QuatF32* qf, const AnisoF* an,
-             float* out, cudaStream_t s);
+             float* dphi, float* da, float* db, float* dcv, const QuatF32* qf,
+             const AnisoF* an, float* out, cudaStream_t s);
 // composition preconditioner faces D = -gamma ((1-h) D_L + h D_S), FP32
 int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                    const double* tfield, const float* pf, double gamma,

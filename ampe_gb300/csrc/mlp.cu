@@ -730,8 +730,9 @@ int Mlp::infer(const Grid& g, const double* phi, const double* conc,
          cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
          attr = true;
       }
+      // 42 KB of shared memory and 64 TMEM columns per CTA: five CTAs per SM
       long long tiles = (g.cells() + 127) / 128;
-      int blocks = (int)(tiles < 152 * 4 ? tiles : 152 * 4);
+      int blocks = (int)(tiles < 152 * 5 ? tiles : 152 * 5);
       k_mlp_infer_tc<<<blocks, 128, smem, s>>>(m, g, norm, (const __nv_bfloat16*)packed,
                                                bias_cat, phi, conc, tfield, gl, gs, err);
    } else {

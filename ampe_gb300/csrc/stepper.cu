@@ -154,7 +154,9 @@ __global__ void k_conc_precond_faces(ampe_model_t m, Grid g, const double* phi,
       const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
       const double vphi = average_func(phi[g.c(i - ei, j - ej, k - ek)],
                                        phi[g.c(i, j, k)], m.avg_type);
-      const double hphi = interp_func(vphi, m.diff_interp);
+      // the "kks" composition form's D0 uses the energy interpolation
+      const double hphi = interp_func(
+          vphi, m.conc_form == AMPE_CONC_KKS ? m.energy_interp : m.diff_interp);
       double dlq = m.D_liquid, dsq = m.D_solid;  // exp(0) = 1 exactly
       if (tdep) {
          const double invT = 2.0 / (temperature_at(m, g, tfield, i - ei, j - ej, k - ek) +
@@ -444,7 +446,7 @@ struct Stepper {
    // mixed path (FP32 working copies)
    float *cl32 = nullptr, *cs32 = nullptr, *clr32 = nullptr, *csr32 = nullptr;
    float *dF32 = nullptr, *pf32 = nullptr, *dphi32 = nullptr, *da32 = nullptr,
-         *db32 = nullptr;
+         *db32 = nullptr, *dc32 = nullptr;
    float *guess_l = nullptr, *guess_s = nullptr;  // surrogate initial guess
    Mlp* mlp = nullptr;                            // attached surrogate
    unsigned long long* mcount = nullptr;          // mixed KKS counters [5]
@@ -611,8 +613,8 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
       {
          ProfScope ps(S, KT_RHS);
          rhs_mixed(S.m, S.mp, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32,
-                   quat && S.m.with_orient ? S.qf32.ogm : nullptr, S.qorient, &S.an, out,
-                   out + S.N, S.s);
+                   quat && S.m.with_orient ? S.qf32.ogm : nullptr, S.qorient, &S.an, S.c_g,
+                   out, out + S.N, S.s);
       }
       if (quat) {
          ProfScope ps(S, KT_QUAT);
@@ -640,8 +642,8 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
       const double* qflux = nullptr;
       if (S.m.flux_type == AMPE_FLUX_ANISOTROPIC) qflux = quat ? S.q_g : S.qorient;
       rhs_fused(S.m, S.g, S.phi_g, qflux, tf, S.tab, S.cl, S.cs, S.dF,
-                S.phi_lag, quat && S.m.with_orient ? S.ogm : nullptr, out,
-                out + S.N, S.s);
+                S.phi_lag, quat && S.m.with_orient ? S.ogm : nullptr, S.c_g, S.cl_nf,
+                S.cs_nf, out, out + S.N, S.s);
    }
    if (quat) {
       ProfScope ps(S, KT_QUAT);
@@ -909,7 +911,7 @@ static void matvec32(Stepper& S, double gamma, const float* v, float* out)
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
    ProfScope ps(S, KT_JV);
    jv_mixed(S.m, S.mp, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma, S.dphi32,
-            S.da32, S.db32, S.nb == 6 ? &S.qf32 : nullptr, &S.an, out, S.s);
+            S.da32, S.db32, S.dc32, S.nb == 6 ? &S.qf32 : nullptr, &S.an, out, S.s);
 }
 
 // GMRES of the mixed path: the same algorithm as gmres() (left
@@ -1189,6 +1191,8 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
                         &S->dphi32, &S->da32, &S->db32};
       for (float** q : f32g) *q = (float*)dalloc<float>(S->pool, S->NG, &err);
       S->dF32 = (float*)dalloc<float>(S->pool, S->N, &err);
+      if (m->conc_form == AMPE_CONC_KKS)
+         S->dc32 = (float*)dalloc<float>(S->pool, S->NG, &err);
       S->mcount = (unsigned long long*)dalloc<unsigned long long>(S->pool, 5, &err);
       if (p->surrogate) {
          S->guess_l = (float*)dalloc<float>(S->pool, S->N, &err);

@@ -49,29 +49,38 @@ def polycrystal_state(n=128, ngrains=8, seed=0, channel=6.0, width=1.5,
     """Periodic Voronoi polycrystal: grain interiors solid (phi = 1), a liquid
     channel `channel` cells wide along the grain boundaries, each grain's
     orientation a random unit quaternion (the channel cells take their
-    nearest grain's), c ~ U[clo, chi].  Returns phi, c, q (4, z, y, x)."""
+    nearest grain's), c ~ U[clo, chi].  Returns phi, c, q (4, z, y, x).
+    Built slab by slab along z so that 512^3 levels fit in host memory."""
     rng = np.random.default_rng(seed)
     seeds = rng.uniform(0, n, size=(ngrains, 3))
     quats = random_unit_quaternions(rng, ngrains)
     ax = np.arange(n) + 0.5
-    z, y, x = np.meshgrid(ax, ax, ax, indexing="ij")
-    d1 = np.full((n, n, n), np.inf)
-    d2 = np.full((n, n, n), np.inf)
-    g1 = np.zeros((n, n, n), dtype=np.int64)
-    for g, s in enumerate(seeds):
-        dd = np.zeros((n, n, n))
-        for coord, sc in zip((x, y, z), s):
-            d = np.abs(coord - sc)
-            d = np.minimum(d, n - d)
-            dd += d * d
-        dd = np.sqrt(dd)
-        closer = dd < d1
-        d2 = np.where(closer, d1, np.minimum(d2, dd))
-        g1 = np.where(closer, g, g1)
-        d1 = np.where(closer, dd, d1)
-    dist_gb = 0.5 * (d2 - d1)  # distance to the nearest grain boundary
-    phi = 0.5 * (1.0 + np.tanh((dist_gb - 0.5 * channel) / width))
-    q = np.ascontiguousarray(np.moveaxis(quats[g1], -1, 0))
+    phi = np.empty((n, n, n))
+    q = np.empty((4, n, n, n))
+    y, x = np.meshgrid(ax, ax, indexing="ij")
+    dxy = []
+    for s_ in seeds:  # periodic in-plane squared distances, per seed
+        dx = np.abs(x - s_[0])
+        dx = np.minimum(dx, n - dx)
+        dy = np.abs(y - s_[1])
+        dy = np.minimum(dy, n - dy)
+        dxy.append(dx * dx + dy * dy)
+    for k in range(n):
+        z = ax[k]
+        d1 = np.full((n, n), np.inf)
+        d2 = np.full((n, n), np.inf)
+        g1 = np.zeros((n, n), dtype=np.int64)
+        for g, s_ in enumerate(seeds):
+            dz = abs(z - s_[2])
+            dz = min(dz, n - dz)
+            dd = np.sqrt(dxy[g] + dz * dz)
+            closer = dd < d1
+            d2 = np.where(closer, d1, np.minimum(d2, dd))
+            g1 = np.where(closer, g, g1)
+            d1 = np.where(closer, dd, d1)
+        dist_gb = 0.5 * (d2 - d1)  # distance to the nearest grain boundary
+        phi[k] = 0.5 * (1.0 + np.tanh((dist_gb - 0.5 * channel) / width))
+        q[:, k] = np.moveaxis(quats[g1], -1, 0)
     c = rng.uniform(clo, chi, size=(n, n, n))
     return phi, c, q
 

@@ -80,6 +80,9 @@ def parse():
     ap.add_argument("--surrogate-samples", type=int, default=1 << 22)
     ap.add_argument("--surrogate-steps", type=int, default=2000)
     ap.add_argument("--precond", type=int, default=2)
+    ap.add_argument("--ref-atol", type=float, default=0.0,
+                    help="also run the FP64 path at this tighter tolerance (untimed) and "
+                         "report every path's error against it")
     ap.add_argument("--atol", type=float, default=ATOL,
                     help="Newton/WRMS absolute tolerance (rtol = atol/100)")
     ap.add_argument("--cpu-n", type=int, default=48)
@@ -448,6 +451,27 @@ def run_ours(args):
                          / np.linalg.norm(ref[1][f].ravel()))
                 for f in st}
         paths[name] = d
+    if args.ref_atol > 0.0:
+        # untimed reference: FP64 path at a tighter Newton tolerance; the
+        # error of each path against it compares with its own tolerance error
+        from ampe_gb300.stepper import ImplicitStepper
+        from ampe_gb300 import configs
+
+        pr = configs.step_params(dt=0.1, precond=args.precond, mg_levels=5, atol=args.ref_atol,
+                                 precision=0)
+        gr = ImplicitStepper(m, pr)
+        st0.load(gr)
+        gr.advance(args.warmup + args.steps)
+        refs = {"phi": None, "c": None}
+        refs["phi"], refs["c"] = gr.get_state()[:2]
+        if st0.quat is not None:
+            refs["q"] = gr.get_quat()
+        gr.close()
+        for name, (r, st) in results.items():
+            paths[name]["rel_l2_err_vs_fp64_atol_%g" % args.ref_atol] = {
+                f: float(np.linalg.norm((st[f] - refs[f]).ravel())
+                         / np.linalg.norm(refs[f].ravel()))
+                for f in st}
     if mlp is not None:
         L.ampe_mlp_destroy(mlp)
 

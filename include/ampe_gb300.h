@@ -52,6 +52,13 @@ extern "C" {
 #define AMPE_THERMO_DILUTE 0  /* KKSdiluteBinary */
 #define AMPE_THERMO_CALPHAD 1 /* CALPHADFreeEnergyStrategyBinary */
 
+/* composition flux forms: EBSCompositionRHSStrategy (M_c div((1-h)D_L grad cL
+ * + h D_S grad cS), h = diff_interp) and KKSCompositionRHSStrategy (M_c
+ * div(D0 grad c + D0 h'(phibar)(cLbar - cSbar) grad phi), D0 = (1-h)D_L +
+ * h D_S, h = energy_interp; KKSCompositionRHSStrategy.cc:98-441) */
+#define AMPE_CONC_EBS 0
+#define AMPE_CONC_KKS 1
+
 /* temperature sources */
 #define AMPE_TEMP_CONSTANT 0 /* T = T0 everywhere */
 #define AMPE_TEMP_GRADIENT 1 /* T = T0 + gradT * (i + 0.5) * dx[0], analytic */
@@ -123,6 +130,10 @@ typedef struct ampe_model {
    char quat_floor_type;     /* 'm' max, 's' smooth, 't' tanh (quat.f:1497) */
    char quat_mobility_type;  /* 'p' 1 - pbg(phi) (3d/mobility.m4:13-95) */
    char pad1[6];
+
+   /* ---- composition flux form (QuatModelParameters.cc:203-222 rhs_form) ---- */
+   int conc_form;  /* AMPE_CONC_EBS or AMPE_CONC_KKS */
+   int pad2;
 } ampe_model_t;
 
 /* Integrator / preconditioner controls (QuatIntegrator.cc:278-301,
@@ -204,6 +215,20 @@ int ampe_conc_diffusion(const ampe_model_t* m, const double* phi,
                         const double* temp, double* dl0, double* dl1,
                         double* dl2, double* ds0, double* ds1, double* ds2,
                         void* stream);
+
+/* Composition flux of the "kks" form (AMPE's default rhs_form,
+ * KKSCompositionRHSStrategy.cc:98-441): CONCENTRATION_PFMDIFFUSION
+ * (ConcFort.h, 3d/concentrationdiffusion.m4:14-128; h = energy_interp) for
+ * D0, the coupling D0 h'(phibar)(cLbar - cSbar) of
+ * setDiffCoeffForPhaseOnPatch (:166-310) and CONCENTRATIONFLUX
+ * (ConcFort.h:16, 3d/concentrationrhs.m4:14-104), fused:
+ * flux = (D0 (c_up - c_lo) + D_phi (phi_up - phi_lo)) / dx on every face.
+ * phi, conc, cl, cs ghosted; flux side arrays.  Then
+ * ampe_computerhsconcentration gives c'. */
+int ampe_conc_flux_kks(const ampe_model_t* m, const double* phi,
+                       const double* temp, const double* conc, const double* cl,
+                       const double* cs, double* flux0, double* flux1,
+                       double* flux2, void* stream);
 
 /* Replaces ADD_FLUX (ConcFort.h:139, 3d/flux.m4:15-100) for depth 1:
  * flux_d += D_d * (u_i - u_{i-1}) / dx_d. */

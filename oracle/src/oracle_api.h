@@ -46,6 +46,9 @@ long orc_phase_concentrations(const ampe_model_t* m, const double* temp,
 void orc_conc_diffusion(const ampe_model_t* m, const double* phi,
                         const double* temp, double* dl0, double* dl1,
                         double* dl2, double* ds0, double* ds1, double* ds2);
+void orc_conc_flux_kks(const ampe_model_t* m, const double* phid, const double* cld,
+                       const double* csd, const double* temp, const double* phi,
+                       const double* conc, double* f0, double* f1, double* f2);
 void orc_add_flux(const ampe_model_t* m, const double* u, const double* d0,
                   const double* d1, const double* d2, double* f0, double* f1,
                   double* f2);

@@ -325,6 +325,49 @@ void orc_conc_diffusion(const ampe_model_t* m, const double* phi,
    }
 }
 
+// Composition flux of the "kks" form (KKSCompositionRHSStrategy.cc:98-441):
+// D0 = (1-h) D_L + h D_S with h = energy_interp(phibar) and T-dependent
+// D_L, D_S (concentration_pfmdiffusion, 3d/concentrationdiffusion.m4:
+// 14-128), the coupling D_phi = D0 h'(phibar) (cLbar - cSbar) with
+// arithmetic means of cL, cS over the face (setDiffCoeffForPhaseOnPatch,
+// KKSCompositionRHSStrategy.cc:166-310), and
+// flux = (D0 (c_up - c_lo) + D_phi (phi_up - phi_lo)) / dx
+// (concentrationflux, 3d/concentrationrhs.m4:14-104).  phid, cld, csd give
+// the coefficients (lagged in finite-difference evaluations), phi and conc
+// the differences.
+void orc_conc_flux_kks(const ampe_model_t* m, const double* phid, const double* cld,
+                       const double* csd, const double* temp, const double* phi,
+                       const double* conc, double* f0, double* f1, double* f2)
+{
+   Layout L(*m);
+   const double qlR = m->Q_liquid / kGasR, qsR = m->Q_solid / kGasR;
+   for (int dir = 0; dir < L.dim; dir++) {
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const double dinv = 1.0 / m->dx[dir];
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int k = 0; k < L.n2 + ek; k++)
+         for (int j = 0; j < L.n1 + ej; j++)
+            for (int i = 0; i < L.n0 + ei; i++) {
+               const long lo = L.c(i - ei, j - ej, k - ek), up = L.c(i, j, k);
+               const double vphi = average_func(phid[lo], phid[up], m->avg_type);
+               const double hphi = interp_func(vphi, m->energy_interp);
+               const double invT =
+                   2.0 / (temperature_at(*m, temp, L, i - ei, j - ej, k - ek) +
+                          temperature_at(*m, temp, L, i, j, k));
+               const double dlq = m->D_liquid * std::exp(-qlR * invT);
+               const double dsq = m->D_solid * std::exp(-qsR * invT);
+               const double d0 = (1.0 - hphi) * dlq + hphi * dsq;
+               const double clb = 0.5 * (cld[up] + cld[lo]);
+               const double csb = 0.5 * (csd[up] + csd[lo]);
+               const double dphi = d0 * deriv_interp_func(vphi, m->energy_interp) * (clb - csb);
+               const long f = dir == 0 ? L.fx(i, j, k)
+                                       : (dir == 1 ? L.fy(i, j, k) : L.fz(i, j, k));
+               double* F = dir == 0 ? f0 : (dir == 1 ? f1 : f2);
+               F[f] = dinv * (d0 * (conc[up] - conc[lo]) + dphi * (phi[up] - phi[lo]));
+            }
+   }
+}
+
 // add_flux (2d/flux.m4:11-58, 3d/flux.m4:15-100), depth 1
 void orc_add_flux(const ampe_model_t* m, const double* u, const double* d0,
                   const double* d1, const double* d2, double* f0, double* f1,
@@ -488,6 +531,17 @@ void orc_jv_analytic(const ampe_model_t* m, const double* phi,
                 f1.data(), f2.data());
    orc_add_flux(m, db.data(), s0.data(), s1.data(), s2.data(), f0.data(),
                 f1.data(), f2.data());
+   if (m->conc_form == AMPE_CONC_KKS) {
+      // "kks" form: flux linear in (c, phi) with the coefficients held
+      std::vector<double> dcv(NG);
+      for (int k = 0; k < L.n2; k++)
+         for (int j = 0; j < L.n1; j++)
+            for (int i = 0; i < L.n0; i++)
+               dcv[L.c(i, j, k)] = v[L.interior(i, j, k) + N];
+      orc_fill_ghosts(m, dcv.data());
+      orc_conc_flux_kks(m, phi, cl, cs, nullptr, dp.data(), dcv.data(), f0.data(), f1.data(),
+                        f2.data());
+   }
    std::vector<double> jc(N);
    orc_computerhsconcentration(m, f0.data(), f1.data(), f2.data(), jc.data());
 #pragma omp parallel for collapse(2) schedule(static)

@@ -102,6 +102,15 @@ void eval_rhs(OStepper& s, const double* y, double* fy, int fd_flag)
    orc_rhs_phase_conc_q(&s.m, s.phi_g.data(), qflux, temp_ptr(s),
                         s.cl.data(), s.cs.data(), s.phi_lag.data(),
                         quat ? s.ogm.data() : nullptr, fy, fy + s.N);
+   if (s.m.conc_form == AMPE_CONC_KKS) {
+      // "kks" composition form: coefficients from the lagged phi, cL, cS
+      // (QuatIntegrator.cc:3266-3267), differences of the current phi and c
+      Layout L(s.m);
+      std::vector<double> f0(L.nfx()), f1(L.nfy()), f2(L.dim == 3 ? L.nfz() : 1);
+      orc_conc_flux_kks(&s.m, s.phi_lag.data(), s.cl_nf.data(), s.cs_nf.data(), temp_ptr(s),
+                        s.phi_g.data(), s.c_g.data(), f0.data(), f1.data(), f2.data());
+      orc_computerhsconcentration(&s.m, f0.data(), f1.data(), f2.data(), fy + s.N);
+   }
    if (quat) {
       orc_quat_mobility(&s.m, s.phi_g.data(), s.mq.data());
       orc_quat_face_coef(&s.m, s.phi_g.data(), temp_ptr(s), s.q_lag.data(),
@@ -136,7 +145,9 @@ void precond_setup(OStepper& s, double gamma)
    // composition: D = -gamma (D_L + D_S), C = 1, M = M_c
    std::vector<double> l0(L.nfx()), l1(L.nfy()), l2(L.dim == 3 ? L.nfz() : 1);
    std::vector<double> s0(L.nfx()), s1(L.nfy()), s2(l2.size());
-   orc_conc_diffusion(&s.m, s.phi_lag.data(), temp_ptr(s), l0.data(),
+   ampe_model_t mp = s.m;  // the "kks" form's D0 uses the energy interpolation
+   if (s.m.conc_form == AMPE_CONC_KKS) mp.diff_interp = s.m.energy_interp;
+   orc_conc_diffusion(&mp, s.phi_lag.data(), temp_ptr(s), l0.data(),
                       l1.data(), l2.data(), s0.data(), s1.data(), s2.data());
    for (long f = 0; f < L.nfx(); f++) s.Dc[0][f] = -gamma * (l0[f] + s0[f]);
    for (long f = 0; f < L.nfy(); f++) s.Dc[1][f] = -gamma * (l1[f] + s1[f]);
