@@ -292,6 +292,7 @@ MixParams make_mix_params(const ampe_model_t& m)
    p.kn = (float)m.aniso_k;
    p.qlen4 = m.qlen == 4 ? 1 : 0;
    p.kksc = m.conc_form == AMPE_CONC_KKS ? 1 : 0;
+   p.dq = nullptr;
    p.pb = (m.avg_type == 'a' && m.diff_interp == 'p' && m.energy_interp == 'p' &&
            m.conc_interp == 'p' && m.well_type == 'd' && m.orient_interp1 == 'p' &&
            m.orient_interp2 == 'p')
@@ -470,6 +471,44 @@ __device__ __forceinline__ float aniso_dflux(const MixParams& mp, const AnisoF& 
 // "kks" composition form on the face lo|up (KKSCompositionRHSStrategy.cc:
 // 98-441): D0 = (1-h) D_L + h D_S with h = energy_interp(phibar), and the
 // coupling D_phi = D0 h'(phibar)(cLbar - cSbar)
+// (D_L, D_S) of the face between cells (a0-ei, ...) and (a0, a1, a2):
+// D^0 exp(-Q / (R Tbar)), Tbar the mean of the two cells' temperatures
+__device__ __forceinline__ float2 face_dq(const ampe_model_t& m, const MixParams& mp,
+                                          const Grid& g, const double* tfield, int a0,
+                                          int a1, int a2, int ei, int ej, int ek)
+{
+   const float invT = 2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
+                                    temperature_at(m, g, tfield, a0, a1, a2));
+   return make_float2(mp.Dl * expf(-mp.qlR * invT), mp.Ds * expf(-mp.qsR * invT));
+}
+
+__device__ __forceinline__ float2 face_dq_at(const ampe_model_t& m, const MixParams& mp,
+                                             const Grid& g, const double* tfield, int a0,
+                                             int a1, int a2, int ei, int ej, int ek)
+{
+   if (!mp.tdep) return make_float2(mp.Dl, mp.Ds);
+   if (mp.dq) return mp.dq[ei ? a0 : g.n0 + 1 + a0];
+   return face_dq(m, mp, g, tfield, a0, a1, a2, ei, ej, ek);
+}
+
+__global__ void k_diff_table(ampe_model_t m, MixParams mp, Grid g, float2* dq)
+{
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t <= g.n0)
+      dq[t] = face_dq(m, mp, g, nullptr, t, 0, 0, 1, 0, 0);
+   else if (t < 2 * g.n0 + 1)
+      dq[t] = face_dq(m, mp, g, nullptr, t - g.n0 - 1, 0, 0, 0, 1, 0);
+}
+
+int build_diff_table(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                     float2* dq, cudaStream_t s)
+{
+   if (m.temp_mode == AMPE_TEMP_FIELD || !mp.tdep) return AMPE_ERR_INVALID;
+   const int n = 2 * g.n0 + 1;
+   k_diff_table<<<(n + 127) / 128, 128, 0, s>>>(m, mp, g, dq);
+   return launch_status();
+}
+
 template <int DIM, bool PB>
 __device__ __forceinline__ void kks_face_coef(const ampe_model_t& m, const MixParams& mp,
                                               const Grid& g, const double* tfield,
@@ -481,15 +520,8 @@ __device__ __forceinline__ void kks_face_coef(const ampe_model_t& m, const MixPa
    const Types<PB> ty(m);
    const float vphi = average_func(pf[lo], pf[up], ty.avg);
    const float h = interp_func(vphi, ty.energy);
-   float dlq = mp.Dl, dsq = mp.Ds;
-   if (mp.tdep) {
-      const float invT =
-          2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
-                        temperature_at(m, g, tfield, a0, a1, a2));
-      dlq = mp.Dl * expf(-mp.qlR * invT);
-      dsq = mp.Ds * expf(-mp.qsR * invT);
-   }
-   D0 = (1.f - h) * dlq + h * dsq;
+   const float2 dq = face_dq_at(m, mp, g, tfield, a0, a1, a2, ei, ej, ek);
+   D0 = (1.f - h) * dq.x + h * dq.y;
    Dp = D0 * deriv_interp_func(vphi, ty.energy) *
         (0.5f * (cl[up] + cl[lo]) - 0.5f * (cs[up] + cs[lo]));
 }
@@ -530,16 +562,9 @@ __device__ __forceinline__ void face_diff(const ampe_model_t& m,
    const Types<PB> ty(m);
    const float vphi = average_func(pf[lo], pf[up], ty.avg);
    const float hphi = interp_func(vphi, ty.diff);
-   float dlq = mp.Dl, dsq = mp.Ds;
-   if (mp.tdep) {
-      const float invT =
-          2.f / (float)(temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
-                        temperature_at(m, g, tfield, a0, a1, a2));
-      dlq = mp.Dl * expf(-mp.qlR * invT);
-      dsq = mp.Ds * expf(-mp.qsR * invT);
-   }
-   DL = (1.f - hphi) * dlq;
-   DS = hphi * dsq;
+   const float2 dq = face_dq_at(m, mp, g, tfield, a0, a1, a2, ei, ej, ek);
+   DL = (1.f - hphi) * dq.x;
+   DS = hphi * dq.y;
 }
 
 // temperature of cell (i,j,k) in FP32 (ghost cells take their periodic image)
@@ -562,8 +587,29 @@ __global__ void k_phi_to_f32(Grid g, const double* phi, float* pf)
       pf[t] = d2f(phi[t]);
 }
 
+// weights of the lower (m) and upper (p) face of cell (i,j,k) along d
+__device__ __forceinline__ void face_w(const FaceW& fw, const Grid& g, int d, int i, int j,
+                                       int k, float& Am, float& Bm, float& Ap, float& Bp)
+{
+   int f, step;
+   if (d == 0) {
+      f = g.fx(i, j, k);
+      step = 1;
+   } else if (d == 1) {
+      f = g.fy(i, j, k);
+      step = g.n0;
+   } else {
+      f = g.fz(i, j, k);
+      step = g.n0 * g.n1;
+   }
+   Am = fw.A[d][f];
+   Bm = fw.B[d][f];
+   Ap = fw.A[d][f + step];
+   Bp = fw.B[d][f + step];
+}
+
 template <int DIM, bool PB, bool ANISO>
-__global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
+__global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an, FaceW fw,
                             const double* tfield, const double* ph, const double* cc,
                             const float* pf,
                             const float* cl, const float* cs, const float* dF,
@@ -589,25 +635,16 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
          const long long lo = g.c(i - ei, j - ej, k - ek);
+         float Am, Bm, Ap, Bp;
+         face_w(fw, g, d, i, j, k, Am, Bm, Ap, Bp);
+         float flm, flp;
          if (mp.kksc) {  // "kks" form: c and phi differences in FP64, rounded once
-            float D0m, Dpm, D0p, Dpp;
-            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, c, i, j, k, ei, ej, ek,
-                                   D0m, Dpm);
-            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, c, up, i + ei, j + ej, k + ek,
-                                   ei, ej, ek, D0p, Dpp);
-            const float flm =
-                mp.dxi[d] * (D0m * d2f(cc[c] - cc[lo]) + Dpm * d2f(ph[c] - ph[lo]));
-            const float flp =
-                mp.dxi[d] * (D0p * d2f(cc[up] - cc[c]) + Dpp * d2f(ph[up] - ph[c]));
-            div += mp.dxi[d] * (flp - flm);
-            continue;
+            flm = mp.dxi[d] * (Am * d2f(cc[c] - cc[lo]) + Bm * d2f(ph[c] - ph[lo]));
+            flp = mp.dxi[d] * (Ap * d2f(cc[up] - cc[c]) + Bp * d2f(ph[up] - ph[c]));
+         } else {
+            flm = mp.dxi[d] * (Am * (cl[c] - cl[lo]) + Bm * (cs[c] - cs[lo]));
+            flp = mp.dxi[d] * (Ap * (cl[up] - cl[c]) + Bp * (cs[up] - cs[c]));
          }
-         float DLm, DSm, DLp, DSp;
-         face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, c, i, j, k, ei, ej, ek, DLm, DSm);
-         face_diff<DIM, PB>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek,
-                        DLp, DSp);
-         const float flm = mp.dxi[d] * (DLm * (cl[c] - cl[lo]) + DSm * (cs[c] - cs[lo]));
-         const float flp = mp.dxi[d] * (DLp * (cl[up] - cl[c]) + DSp * (cs[up] - cs[c]));
          div += mp.dxi[d] * (flp - flm);
       }
       const Types<PB> ty(m);
@@ -625,17 +662,58 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
    }
 }
 
+// composition flux weights of every face (EBS: (1-h) D_L, h D_S with h =
+// diff_interp; "kks": D0, D_phi)
+template <int DIM, bool PB>
+__global__ void k_face_weights(ampe_model_t m, MixParams mp, Grid g, const double* tfield,
+                               const float* pf, const float* cl, const float* cs, FaceW fw)
+{
+   const long long tot = g.nfx() + g.nfy() + (DIM == 3 ? g.nfz() : 0);
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      face_of(g, t, dir, i, j, k);
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const long long lo = g.c(i - ei, j - ej, k - ek), up = g.c(i, j, k);
+      float a, b;
+      if (mp.kksc)
+         kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, up, i, j, k, ei, ej, ek, a, b);
+      else
+         face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, up, i, j, k, ei, ej, ek, a, b);
+      const int f = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+      fw.A[dir][f] = a;
+      fw.B[dir][f] = b;
+   }
+}
+
 int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield, const double* phi, float* pf,
               const float* cl, const float* cs, const float* dF,
               const float* ogm, const double* q, AnisoF* an, const double* cc,
-              double* phi_rhs, double* conc_rhs, cudaStream_t s)
+              const FaceW& fw, double* phi_rhs, double* conc_rhs, cudaStream_t s)
 {
    if (mp.kksc && !cc) return AMPE_ERR_INVALID;
    long long b = (g.cells_ghost() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
    k_phi_to_f32<<<(unsigned)b, 256, 0, s>>>(g, phi, pf);
    launch_status();
+   {
+      const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+      long long bf = (tot + 255) / 256;
+      if (bf > kMaxBlocks) bf = kMaxBlocks;
+      if (g.dim == 3) {
+         if (mp.pb)
+            k_face_weights<3, true><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+         else
+            k_face_weights<3, false><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+      } else {
+         if (mp.pb)
+            k_face_weights<2, true><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+         else
+            k_face_weights<2, false><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+      }
+      launch_status();
+   }
    b = (g.cells() + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
    const bool aniso = m.flux_type == AMPE_FLUX_ANISOTROPIC;
@@ -645,17 +723,17 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    }
    const AnisoF a0 = an ? *an : AnisoF();
 #define AMPE_RHS(D, P)                                                                      \
-   k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, cc, pf, cl, \
-                                                        cs, dF, ogm, phi_rhs, conc_rhs)
+   k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tfield, phi, cc, pf, \
+                                                        cl, cs, dF, ogm, phi_rhs, conc_rhs)
    if (aniso) {
       if (mp.pb)
-         k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, cc,
-                                                               pf, cl, cs, dF, ogm, phi_rhs,
-                                                               conc_rhs);
+         k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tfield, phi,
+                                                               cc, pf, cl, cs, dF, ogm,
+                                                               phi_rhs, conc_rhs);
       else
-         k_rhs_mixed<2, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tfield, phi, cc,
-                                                                pf, cl, cs, dF, ogm, phi_rhs,
-                                                                conc_rhs);
+         k_rhs_mixed<2, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tfield, phi,
+                                                                cc, pf, cl, cs, dF, ogm,
+                                                                phi_rhs, conc_rhs);
    } else if (g.dim == 3) {
       if (mp.pb)
          AMPE_RHS(3, true);
@@ -759,7 +837,7 @@ __device__ __forceinline__ float second_deriv_interp_f(float phi, char type)
 
 // out = v - gamma J v
 template <int DIM, bool PB, bool ANISO>
-__global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
+__global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g, AnisoF an, FaceW fw,
                              const CoefF* tabf, const double* tfield,
                              const float* pf, const float* cl, const float* cs,
                              const float* dF, const float* dphi,
@@ -787,25 +865,14 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g, AnisoF an,
          diff += (fp - fm) * mp.dxi[d];
          const long long up = g.c(i + ei, j + ej, k + ek);
          const long long lo = g.c(i - ei, j - ej, k - ek);
-         if (mp.kksc) {  // "kks" form: linear in (c, phi), coefficients held
-            float D0m, Dpm, D0p, Dpp;
-            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, c, i, j, k, ei, ej, ek,
-                                   D0m, Dpm);
-            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, c, up, i + ei, j + ej, k + ek,
-                                   ei, ej, ek, D0p, Dpp);
-            const float flm =
-                mp.dxi[d] * (D0m * (dcv[c] - dcv[lo]) + Dpm * (dphi[c] - dphi[lo]));
-            const float flp =
-                mp.dxi[d] * (D0p * (dcv[up] - dcv[c]) + Dpp * (dphi[up] - dphi[c]));
-            div += mp.dxi[d] * (flp - flm);
-            continue;
-         }
-         float DLm, DSm, DLp, DSp;
-         face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, c, i, j, k, ei, ej, ek, DLm, DSm);
-         face_diff<DIM, PB>(m, mp, g, tfield, pf, c, up, i + ei, j + ej, k + ek, ei, ej, ek, DLp,
-                        DSp);
-         const float flm = mp.dxi[d] * (DLm * (da[c] - da[lo]) + DSm * (db[c] - db[lo]));
-         const float flp = mp.dxi[d] * (DLp * (da[up] - da[c]) + DSp * (db[up] - db[c]));
+         float Am, Bm, Ap, Bp;
+         face_w(fw, g, d, i, j, k, Am, Bm, Ap, Bp);
+         // "kks" form: linear in (c, phi) with the weights held; EBS: in the
+         // linearised split (dcL, dcS)
+         const float* xa = mp.kksc ? dcv : da;
+         const float* xb = mp.kksc ? dphi : db;
+         const float flm = mp.dxi[d] * (Am * (xa[c] - xa[lo]) + Bm * (xb[c] - xb[lo]));
+         const float flp = mp.dxi[d] * (Ap * (xa[up] - xa[c]) + Bp * (xb[up] - xb[c]));
          div += mp.dxi[d] * (flp - flm);
       }
       const Types<PB> ty(m);
@@ -894,31 +961,18 @@ __global__ void k_quat_faces_f32(ampe_model_t m, MixParams mp, Grid g,
    }
 }
 
-// composition preconditioner faces D = -gamma ((1-h) D_L + h D_S) in FP32
-template <int DIM>
-__global__ void k_conc_faces_f32(ampe_model_t m, MixParams mp, Grid g,
-                                 const double* tfield, const float* pf, float gamma,
-                                 FacePtrs f)
+// composition preconditioner faces from the face weights of the last f
+// evaluation: D = -gamma (A + B) for EBS ((1-h) D_L + h D_S), -gamma A for
+// the "kks" form (D0)
+__global__ void k_conc_faces_f32(long long nx, long long ny, long long nz, FaceW fw,
+                                 float gamma, int kksc, FacePtrs f)
 {
-   const long long tot = g.nfx() + g.nfy() + (DIM == 3 ? g.nfz() : 0);
-   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx + ny + nz;
         t += (long long)gridDim.x * blockDim.x) {
-      int dir, i, j, k;
-      face_of(g, t, dir, i, j, k);
-      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
-      float DL, DS;
-      if (mp.kksc) {  // "kks" form: D0 (energy interpolation)
-         float D0, Dp;
-         kks_face_coef<DIM, false>(m, mp, g, tfield, pf, pf, pf, g.c(i - ei, j - ej, k - ek),
-                                   g.c(i, j, k), i, j, k, ei, ej, ek, D0, Dp);
-         DL = D0;
-         DS = 0.f;
-      } else {
-         face_diff<DIM>(m, mp, g, tfield, pf, g.c(i - ei, j - ej, k - ek), g.c(i, j, k), i, j,
-                        k, ei, ej, ek, DL, DS);
-      }
-      const long long fi = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
-      f.fc[dir][fi] = -gamma * (DL + DS);
+      const int dir = t < nx ? 0 : (t < nx + ny ? 1 : 2);
+      const long long fi = t - (dir == 0 ? 0 : (dir == 1 ? nx : nx + ny));
+      const float a = fw.A[dir][fi];
+      f.fc[dir][fi] = kksc ? -gamma * a : -gamma * (a + fw.B[dir][fi]);
    }
 }
 
@@ -992,7 +1046,8 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const CoefF* tabf, const double* tfield, const float* pf,
              const float* cl, const float* cs, const float* dF, const float* v,
              double gamma, float* dphi, float* da, float* db, float* dcv,
-             const QuatF32* qf, const AnisoF* an, float* out, cudaStream_t s)
+             const QuatF32* qf, const AnisoF* an, const FaceW& fw, float* out,
+             cudaStream_t s)
 {
    if (mp.kksc && !dcv) return AMPE_ERR_INVALID;
    long long b = (g.cells() + 255) / 256;
@@ -1008,19 +1063,19 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    const float* ogm = (qf && m.with_orient) ? qf->ogm : nullptr;
    const AnisoF a0 = an ? *an : AnisoF();
 #define AMPE_JV(D, P)                                                                          \
-   k_jv_stencil<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, tabf, tfield, pf, cl, cs, \
+   k_jv_stencil<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tabf, tfield, pf, cl, cs, \
                                                          dF, dphi, da, db, dcv, v, ogm,          \
                                                          (float)gamma, out)
    if (m.flux_type == AMPE_FLUX_ANISOTROPIC) {
       if (g.dim != 2 || !an) return AMPE_ERR_INVALID;
       if (mp.pb)
          k_jv_stencil<2, true, true><<<(unsigned)b, 256, 0, s>>>(
-             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm, (float)gamma,
-             out);
+             m, mp, g, a0, fw, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm,
+             (float)gamma, out);
       else
          k_jv_stencil<2, false, true><<<(unsigned)b, 256, 0, s>>>(
-             m, mp, g, a0, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm, (float)gamma,
-             out);
+             m, mp, g, a0, fw, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm,
+             (float)gamma, out);
    } else if (g.dim == 3) {
       if (mp.pb)
          AMPE_JV(3, true);
@@ -1057,10 +1112,11 @@ int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 }
 
 int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
-                   const double* tfield, const float* pf, double gamma,
-                   float* const D[3], cudaStream_t s)
+                   const FaceW& fw, double gamma, float* const D[3], cudaStream_t s)
 {
-   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   (void)m;
+   const long long nz = g.dim == 3 ? g.nfz() : 0;
+   const long long tot = g.nfx() + g.nfy() + nz;
    long long b = (tot + 255) / 256;
    if (b > kMaxBlocks) b = kMaxBlocks;
    FacePtrs f;
@@ -1068,10 +1124,8 @@ int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
       f.fc[d] = D[d];
       f.dfc[d] = nullptr;
    }
-   if (g.dim == 3)
-      k_conc_faces_f32<3><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, (float)gamma, f);
-   else
-      k_conc_faces_f32<2><<<(unsigned)b, 256, 0, s>>>(m, mp, g, tfield, pf, (float)gamma, f);
+   k_conc_faces_f32<<<(unsigned)b, 256, 0, s>>>(g.nfx(), g.nfy(), nz, fw, (float)gamma,
+                                                mp.kksc, f);
    return launch_status();
 }
 

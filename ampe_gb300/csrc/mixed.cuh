@@ -31,6 +31,20 @@ struct MixParams {
    float eps, nu, kn;
    int qlen4;
    int kksc;  // "kks" composition flux form
+   // T-dependent diffusivities per x index for analytic temperatures:
+   // dq[i] = (D_L, D_S) at x-face i (0..n0, T averaged over cells i-1, i),
+   // dq[n0 + 1 + i] = (D_L, D_S) at cell column i (y and z faces); null
+   // with a stored temperature field or T-independent diffusion
+   const float2* dq;
+};
+
+// composition flux weights per face, computed once per f evaluation and
+// read by the RHS, the Jacobian-vector products and the composition
+// preconditioner: EBS form A = (1-h) D_L, B = h D_S (flux = A grad cL +
+// B grad cS); "kks" form A = D0, B = D_phi (flux = A grad c + B grad phi)
+struct FaceW {
+   float* A[3] = {nullptr, nullptr, nullptr};
+   float* B[3] = {nullptr, nullptr, nullptr};
 };
 
 // 2D anisotropic phase flux per face and its Jacobian with respect to the
@@ -45,6 +59,9 @@ struct AnisoF {
 // phi_o = acos(qbar) (2 acos for four-component q) per face, in FP64, once
 // per orientation field: acos is ill-conditioned at qbar ~ +-1, where an
 // FP32 qbar would cost up to ~1e-3 rad
+// fills mp.dq (2 n0 + 1 entries) for analytic temperatures
+int build_diff_table(const ampe_model_t& m, const MixParams& mp, const Grid& g,
+                     float2* dq, cudaStream_t s);
 int aniso_orientation_f32(const ampe_model_t& m, const Grid& g, const double* q,
                           AnisoF& a, cudaStream_t s);
 // fill an AnisoF from the FP64 phase (differences formed in FP64, rounded
@@ -74,7 +91,8 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const double* tfield,
               const double* phi, float* pf, const float* cl, const float* cs,
               const float* dF, const float* ogm, const double* q, AnisoF* an,
-              const double* cc, double* phi_rhs, double* conc_rhs, cudaStream_t s);
+              const double* cc, const FaceW& fw, double* phi_rhs, double* conc_rhs,
+              cudaStream_t s);
 // out = v - gamma J v; qf (null without quaternions) adds the q rows and
 // the orientation term of the phase row
 int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
@@ -82,11 +100,10 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
              const double* tfield, const float* pf, const float* cl,
              const float* cs, const float* dF, const float* v, double gamma,
              float* dphi, float* da, float* db, float* dcv, const QuatF32* qf,
-             const AnisoF* an, float* out, cudaStream_t s);
+             const AnisoF* an, const FaceW& fw, float* out, cudaStream_t s);
 // composition preconditioner faces D = -gamma ((1-h) D_L + h D_S), FP32
 int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
-                   const double* tfield, const float* pf, double gamma,
-                   float* const D[3], cudaStream_t s);
+                   const FaceW& fw, double gamma, float* const D[3], cudaStream_t s);
 // |grad q| (from qf.q) and M_q(phi) at cells
 int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                    const double* phi, QuatF32& qf, cudaStream_t s);

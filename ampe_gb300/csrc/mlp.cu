@@ -60,6 +60,32 @@ __device__ __forceinline__ void encode_inputs(const MlpNorm& nz, double phi,
    x[2] = (float)((T - nz.t_mid) * nz.t_inv_half);
 }
 
+// the same encoding in FP32 for the inference kernels: no FP64 instruction
+// per cell (the conversions of phi and c run on the integer pipe)
+struct NormF {
+   float t_mid, t_inv_half, T0, gdx;
+   int mode;
+};
+__device__ __forceinline__ NormF norm_f(const MlpNorm& nz, const ampe_model_t& m)
+{
+   return NormF{(float)nz.t_mid, (float)nz.t_inv_half, (float)m.T0, (float)(m.gradT * m.dx[0]),
+                m.temp_mode};
+}
+__device__ __forceinline__ void encode_inputs_f(const NormF& nf, const Grid& g,
+                                                const double* tfield, double phi, double c,
+                                                int i, int j, int k, float* x)
+{
+   float T = nf.T0;
+   if (nf.mode == AMPE_TEMP_GRADIENT) {
+      T = nf.T0 + nf.gdx * ((float)i + 0.5f);
+   } else if (nf.mode == AMPE_TEMP_FIELD) {
+      T = d2f(tfield[g.c(i, j, k)]);
+   }
+   x[0] = 2.f * d2f(phi) - 1.f;
+   x[1] = 2.f * d2f(c) - 1.f;
+   x[2] = (T - nf.t_mid) * nf.t_inv_half;
+}
+
 __device__ __forceinline__ float logit_clip(double c)
 {
    double l = log(c / (1.0 - c));
@@ -429,6 +455,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
    bool ok = true;
    const long long N = g.cells();
    const long long ntiles = (N + 127) / 128;
+   const NormF nfl = norm_f(nz, m);
    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
       const long long t = tile * 128 + tid;
       // ---- inputs ----
@@ -437,7 +464,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
          int i, j, k;
          g.ijk(t, i, j, k);
          const long long c = g.c(i, j, k);
-         encode_inputs(nz, phi[c], conc[c], temperature_at(m, g, tfield, i, j, k), in);
+         encode_inputs_f(nfl, g, tfield, phi[c], conc[c], i, j, k, in);
       }
       {
          __nv_bfloat162 p01 = __floats2bfloat162_rn(in[0], in[1]);
@@ -536,13 +563,14 @@ __global__ void k_mlp_infer_simt(ampe_model_t m, Grid g, MlpNorm nz,
                                  const double* conc, const double* tfield,
                                  float* guess_l, float* guess_s)
 {
+   const NormF nfl = norm_f(nz, m);
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       int i, j, k;
       g.ijk(t, i, j, k);
       const long long c = g.c(i, j, k);
       float x[64], y[64];
-      encode_inputs(nz, phi[c], conc[c], temperature_at(m, g, tfield, i, j, k), x);
+      encode_inputs_f(nfl, g, tfield, phi[c], conc[c], i, j, k, x);
       for (int q = 0; q < 3; q++) x[q] = bf16r(x[q]);
       for (int o = 0; o < 64; o++) {
          float a = bias[o];

@@ -435,6 +435,7 @@ struct Stepper {
    double* dF;                 // interior driving force
    ThermoCoef* tab = nullptr;  // per-x (or single) thermodynamic table
    CoefF* tabf = nullptr;      // its FP32 copy (mixed path)
+   float2* dqtab = nullptr;    // (D_L, D_S) per x index (mixed path, analytic T)
    MixParams mp;               // FP32 constants of the mixed kernels
    unsigned long long* counters;
    // 2N interior vectors
@@ -459,6 +460,7 @@ struct Stepper {
    // (static; evolve_quat models use the evolving q instead)
    double* qorient = nullptr;
    AnisoF an;  // FP32 anisotropic face fluxes and Jacobians (2D mixed path)
+   FaceW fw;   // FP32 composition flux weights per face (mixed path)
    // preconditioner (FP64 or FP32)
    DevFac<double> facp64, facc64, facq64;
    DevFac<float> facp32, facc32, facq32;
@@ -614,7 +616,7 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
          ProfScope ps(S, KT_RHS);
          rhs_mixed(S.m, S.mp, S.g, tf, S.phi_g, S.pf32, S.cl32, S.cs32, S.dF32,
                    quat && S.m.with_orient ? S.qf32.ogm : nullptr, S.qorient, &S.an, S.c_g,
-                   out, out + S.N, S.s);
+                   S.fw, out, out + S.N, S.s);
       }
       if (quat) {
          ProfScope ps(S, KT_QUAT);
@@ -685,7 +687,8 @@ static void conc_precond_faces(Stepper& S, const double* tf, double gamma,
 static void conc_precond_faces(Stepper& S, const double* tf, double gamma,
                                DevLevel<float>& C0)
 {
-   conc_faces_f32(S.m, S.mp, S.g, tf, S.pf32, gamma, C0.D, S.s);
+   (void)tf;
+   conc_faces_f32(S.m, S.mp, S.g, S.fw, gamma, C0.D, S.s);
 }
 
 // D = gamma fc of the quaternion block: FP64 from the lagged q, or FP32 from
@@ -911,7 +914,7 @@ static void matvec32(Stepper& S, double gamma, const float* v, float* out)
    const double* tf = S.m.temp_mode == AMPE_TEMP_FIELD ? S.tfield : nullptr;
    ProfScope ps(S, KT_JV);
    jv_mixed(S.m, S.mp, S.g, S.tabf, tf, S.pf32, S.cl32, S.cs32, S.dF32, v, gamma, S.dphi32,
-            S.da32, S.db32, S.dc32, S.nb == 6 ? &S.qf32 : nullptr, &S.an, out, S.s);
+            S.da32, S.db32, S.dc32, S.nb == 6 ? &S.qf32 : nullptr, &S.an, S.fw, out, S.s);
 }
 
 // GMRES of the mixed path: the same algorithm as gmres() (left
@@ -1193,6 +1196,11 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
       S->dF32 = (float*)dalloc<float>(S->pool, S->N, &err);
       if (m->conc_form == AMPE_CONC_KKS)
          S->dc32 = (float*)dalloc<float>(S->pool, S->NG, &err);
+      const long long nfd[3] = {S->g.nfx(), S->g.nfy(), S->g.dim == 3 ? S->g.nfz() : 0};
+      for (int d = 0; d < S->g.dim; d++) {
+         S->fw.A[d] = (float*)dalloc<float>(S->pool, nfd[d], &err);
+         S->fw.B[d] = (float*)dalloc<float>(S->pool, nfd[d], &err);
+      }
       S->mcount = (unsigned long long*)dalloc<unsigned long long>(S->pool, 5, &err);
       if (p->surrogate) {
          S->guess_l = (float*)dalloc<float>(S->pool, S->N, &err);
@@ -1215,6 +1223,8 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    if (m->temp_mode != AMPE_TEMP_FIELD) {
       S->tab = (ThermoCoef*)dalloc<ThermoCoef>(S->pool, nt, &err);
       if (p->precision == 1) S->tabf = (CoefF*)dalloc<CoefF>(S->pool, nt, &err);
+      if (p->precision == 1 && S->mp.tdep)
+         S->dqtab = (float2*)dalloc<float2>(S->pool, 2LL * m->n[0] + 1, &err);
    }
    const int nl = p->precond == 2 ? std::max(1, p->mg_levels) : 1;
    if (!err && p->precond) {
@@ -1241,6 +1251,10 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    }
    if (!err && S->tab) err = build_thermo_table(*m, S->tab, nt, S->s);
    if (!err && S->tabf) err = build_coef_f(S->tab, S->tabf, nt, S->s);
+   if (!err && S->dqtab) {
+      err = build_diff_table(*m, S->mp, S->g, S->dqtab, S->s);
+      S->mp.dq = S->dqtab;
+   }
    if (!err && cudaStreamSynchronize(S->s) != cudaSuccess) err = AMPE_ERR_CUDA;
    if (err) {
       ampe_stepper_destroy(S);
