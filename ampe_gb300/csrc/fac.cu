@@ -54,12 +54,13 @@ __device__ __forceinline__ R cell_residual(const FacOp<R>& op, const Grid& g,
 // arrays (HD: face D, HC: cell C, HM: cell M); c = g.c(i,j,k).  Neighbours
 // and upper faces by their constant offsets.  Same expression order as
 // cell_residual.
-template <class R, int DIM, bool HD, bool HC, bool HM>
-__device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
-                                         const R* __restrict__ f, const R* u, int i,
-                                         int j, int k, int c, R* dudr)
+// U(index, di, dj, dk) loads u at the neighbour (di, dj, dk) of the cell.
+template <class R, int DIM, bool HD, bool HC, bool HM, class UL>
+__device__ __forceinline__ R op_residual_u(const FacOp<R>& op, const Grid& g,
+                                           const R* __restrict__ f, const UL& U, int i,
+                                           int j, int k, int c, R* dudr)
 {
-   const R uc = u[c];
+   const R uc = U(c, 0, 0, 0);
    R div = R(0), dsum = R(0);
    {
       const R dxi = op.dxi[0];
@@ -69,8 +70,8 @@ __device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
          Dm = op.D0[fi];
          Dp = op.D0[fi + 1];
       }
-      const R fm = dxi * Dm * (uc - u[c - 1]);
-      const R fp = dxi * Dp * (u[c + 1] - uc);
+      const R fm = dxi * Dm * (uc - U(c - 1, -1, 0, 0));
+      const R fp = dxi * Dp * (U(c + 1, 1, 0, 0) - uc);
       div += dxi * (fp - fm);
       dsum += dxi * dxi * (Dp + Dm);
    }
@@ -82,8 +83,8 @@ __device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
          Dm = op.D1[fi];
          Dp = op.D1[fi + g.n0];
       }
-      const R fm = dxi * Dm * (uc - u[c - g.sx]);
-      const R fp = dxi * Dp * (u[c + g.sx] - uc);
+      const R fm = dxi * Dm * (uc - U(c - g.sx, 0, -1, 0));
+      const R fp = dxi * Dp * (U(c + g.sx, 0, 1, 0) - uc);
       div += dxi * (fp - fm);
       dsum += dxi * dxi * (Dp + Dm);
    }
@@ -95,8 +96,8 @@ __device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
          Dm = op.D2[fi];
          Dp = op.D2[fi + g.n0 * g.n1];
       }
-      const R fm = dxi * Dm * (uc - u[c - g.sy]);
-      const R fp = dxi * Dp * (u[c + g.sy] - uc);
+      const R fm = dxi * Dm * (uc - U(c - g.sy, 0, 0, -1));
+      const R fp = dxi * Dp * (U(c + g.sy, 0, 0, 1) - uc);
       div += dxi * (fp - fm);
       dsum += dxi * dxi * (Dp + Dm);
    }
@@ -106,6 +107,37 @@ __device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
    const R fv = op.f_interior ? f[g.interior(i, j, k)] : f[c];
    return fv - M * div - C * uc;
 }
+
+template <class R>
+struct PlainU {
+   const R* u;
+   __device__ __forceinline__ R operator()(int c, int, int, int) const { return u[c]; }
+};
+
+template <class R, int DIM, bool HD, bool HC, bool HM>
+__device__ __forceinline__ R op_residual(const FacOp<R>& op, const Grid& g,
+                                         const R* __restrict__ f, const R* u, int i,
+                                         int j, int k, int c, R* dudr)
+{
+   return op_residual_u<R, DIM, HD, HC, HM>(op, g, f, PlainU<R>{u}, i, j, k, c, dudr);
+}
+
+// u plus the piecewise-constant coarse correction e of the next coarser
+// level (coarse ghosts current), at the cell and, with NB, at its
+// neighbours: the value k_prolong_add would have stored there
+template <class R, bool NB>
+struct ProlongU {
+   const R* u;
+   const R* e;
+   Grid gc;
+   int i, j, k, zs;
+   __device__ __forceinline__ R operator()(int c, int di, int dj, int dk) const
+   {
+      const R v = u[c];
+      if (!NB && (di | dj | dk)) return v;
+      return v + e[gc.c((i + di) >> 1, (j + dj) >> 1, (k + dk) >> zs)];
+   }
+};
 
 // call F<DIM, HD, HC, HM>() for the operator's shape
 template <class R, class F>
@@ -232,6 +264,33 @@ __global__ void __launch_bounds__(256)
          mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
       if ((threadIdx.x & 31) == 0) atomic_max_nonneg(maxres, mr);
    }
+}
+
+// One colour of the first post-smoothing sweep with the prolongation of the
+// coarse correction e fused in (u += e is never stored separately): the red
+// pass reads u + e at the cell and its black neighbours, the black pass at
+// the cell (its red neighbours already hold their final values).  Every
+// value equals the one k_prolong_add followed by k_rbgs_color computes.
+template <class R, int DIM, bool HD, bool HC, bool HM, bool RED>
+__global__ void __launch_bounds__(256)
+    k_rbgs_color_prolong(FacOp<R> op, Grid g, const R* __restrict__ f, R* u,
+                         Grid gc, const R* __restrict__ e)
+{
+   const int nh = (g.n0 + 1) / 2;
+   const long long tot = (long long)nh * g.n1 * g.n2;
+   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+   if (t >= tot) return;
+   int ih, j, k;
+   g.split(t, g.fdh, g.fd1, ih, j, k);
+   const int i = 2 * ih + ((j + k + (RED ? 0 : 1)) & 1);
+   if (i >= g.n0) return;
+   R dudr;
+   const int c = g.c(i, j, k);
+   const ProlongU<R, RED> U{u, e, gc, i, j, k, DIM == 3 ? 1 : 0};
+   const R r = op_residual_u<R, DIM, HD, HC, HM>(op, g, f, U, i, j, k, c, &dudr);
+   const R un = U(c, 0, 0, 0) + -r * dudr;
+   u[c] = un;
+   for_each_image(g, i, j, k, [&](long long idx) { u[idx] = un; });
 }
 
 // ---------------------------------------------------------------------------
@@ -452,7 +511,7 @@ __global__ void k_residual_part(FacOp<R> op, Grid g, const R* __restrict__ f,
       g.ijk(t, i, j, k);
       const int c = g.c(i, j, k);
       const R r = op_residual<R, DIM, HD, HC, HM>(op, g, f, u, i, j, k, c, (R*)nullptr);
-      res[t] = r;
+      if (res) res[t] = r;
       if (z) z[t] = u[c];
       accr += r * r;
    }
@@ -507,6 +566,31 @@ int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
                    decltype(HM)::value><<<nb, 256, 0, s>>>(op, g, f, u, offset, maxres, images);
    });
    return launch_status();
+}
+
+template <class R>
+int rbgs_color_prolong(const FacOp<R>& op, const Grid& g, const R* f, R* u, int offset,
+                       const Grid& gc, const R* e, cudaStream_t s)
+{
+   const long long tot = (long long)((g.n0 + 1) / 2) * g.n1 * g.n2;
+   const unsigned nb = (unsigned)((tot + 255) / 256);
+   const bool hd = op.D0 != nullptr, hc = op.C != nullptr, hm = op.M != nullptr;
+#define AMPE_PROL(D, A, B, C_)                                                          \
+   if (g.dim == D && hd == A && hc == B && hm == C_) {                                   \
+      if (offset == 0)                                                                  \
+         k_rbgs_color_prolong<R, D, A, B, C_, true><<<nb, 256, 0, s>>>(op, g, f, u, gc, e);  \
+      else                                                                              \
+         k_rbgs_color_prolong<R, D, A, B, C_, false><<<nb, 256, 0, s>>>(op, g, f, u, gc, e); \
+      return launch_status();                                                           \
+   }
+   AMPE_PROL(3, false, true, false)  // phase block
+   AMPE_PROL(3, true, false, false)  // composition block
+   AMPE_PROL(3, true, false, true)   // quaternion block
+   AMPE_PROL(2, false, true, false)
+   AMPE_PROL(2, true, false, false)
+   AMPE_PROL(2, true, false, true)
+#undef AMPE_PROL
+   return AMPE_ERR_INVALID;
 }
 
 // coarse cell (ic,jc,kc): w * sum of the residuals of its 2^d children, in
@@ -588,6 +672,11 @@ template int rbgs_color<double>(const FacOp<double>&, const Grid&,
                                 cudaStream_t, bool);
 template int rbgs_color<float>(const FacOp<float>&, const Grid&, const float*,
                                float*, int, double*, cudaStream_t, bool);
+template int rbgs_color_prolong<double>(const FacOp<double>&, const Grid&, const double*,
+                                        double*, int, const Grid&, const double*,
+                                        cudaStream_t);
+template int rbgs_color_prolong<float>(const FacOp<float>&, const Grid&, const float*, float*,
+                                       int, const Grid&, const float*, cudaStream_t);
 template int residual_partial<double>(const FacOp<double>&, const Grid&, const double*,
                                       const double*, double*, double*, int*, double*,
                                       cudaStream_t);

@@ -25,8 +25,15 @@ struct FacOp {
 template <class R>
 int rbgs_color(const FacOp<R>& op, const Grid& g, const R* f, R* u,
                int offset, double* maxres, cudaStream_t s, bool images);
-// res = f - A u (interior layout) and per-block sums of res^2 into part
-// (*nblk blocks); z (optional) receives u's interior values
+// one colour of a sweep on u + P e (e: the next coarser level's correction,
+// ghosts current, P piecewise constant), u updated in place with images:
+// the red (offset 0) then black pass equal k_prolong_add followed by a sweep.
+// Phase, composition and quaternion operator shapes only.
+template <class R>
+int rbgs_color_prolong(const FacOp<R>& op, const Grid& g, const R* f, R* u, int offset,
+                       const Grid& gc, const R* e, cudaStream_t s);
+// res = f - A u (interior layout; optional) and per-block sums of res^2
+// into part (*nblk blocks); z (optional) receives u's interior values
 template <class R>
 int residual_partial(const FacOp<R>& op, const Grid& g, const R* f, const R* u,
                      R* res, double* part, int* nblk, R* z, cudaStream_t s);

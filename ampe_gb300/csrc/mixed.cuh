@@ -79,6 +79,8 @@ struct QuatF32 {
    float* dfc[3] = {nullptr, nullptr, nullptr};  // d fc / d phibar
 };
 MixParams make_mix_params(const ampe_model_t& m);
+// guess_l / guess_s (may be null): surrogate initial guesses (3 FP32
+// iterations from them, then the warm start clr / csr as fallback)
 int kks_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const ThermoCoef* tab, const CoefF* tabf, const double* tfield,
               const double* phi,

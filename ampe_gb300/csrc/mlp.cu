@@ -457,10 +457,11 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
    const long long ntiles = (N + 127) / 128;
    const NormF nfl = norm_f(nz, m);
    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const long long t = tile * 128 + tid;
+      const long long row = tile * 128 + tid;
+      const long long t = row < N ? row : -1;
       // ---- inputs ----
       float in[3] = {0.f, 0.f, 0.f};
-      if (t < N) {
+      if (t >= 0) {
          int i, j, k;
          g.ijk(t, i, j, k);
          const long long c = g.c(i, j, k);
@@ -529,7 +530,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
       uint32_t r[16];
       TMEM_LD_X16(t_row, r);
       tmem_wait_ld();
-      if (t < N) {
+      if (t >= 0) {
          const float y0 = __uint_as_float(r[0]) + S.b[192];
          const float y1 = __uint_as_float(r[1]) + S.b[193];
          guess_l[t] = 1.f / (1.f + __expf(-y0));

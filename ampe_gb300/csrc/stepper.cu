@@ -357,10 +357,21 @@ void vcycle(Ctx& cx, DevFac<R>& F, int l)
    DevLevel<R>& C = F.lev[l + 1];
    residual_restrict(L.op(), L.g, C.g, L.f, L.u, C.f, cx.s);
    vcycle(cx, F, l + 1);
-   k_prolong_add<R><<<map_blocks(L.g.cells()), 256, 0, cx.s>>>(L.g, C.g, C.u, L.u);
-   launch_status();
    if (l == 0 && cx.mark) cx.mark(cx.owner, true);
-   for (int it = 0; it < cx.p->mg_post; it++) rb_sweep(cx, L, nullptr);
+   int it = 0;
+   if (cx.p->mg_post > 0 && !L.fused) {
+      // prolongation fused into the first post-sweep's two colours
+      const FacOp<R> op = L.op();
+      if (rbgs_color_prolong(op, L.g, L.f, L.u, 0, C.g, C.u, cx.s) == AMPE_OK) {
+         rbgs_color_prolong(op, L.g, L.f, L.u, 1, C.g, C.u, cx.s);
+         it = 1;
+      }
+   }
+   if (it == 0) {
+      k_prolong_add<R><<<map_blocks(L.g.cells()), 256, 0, cx.s>>>(L.g, C.g, C.u, L.u);
+      launch_status();
+   }
+   for (; it < cx.p->mg_post; it++) rb_sweep(cx, L, nullptr);
    if (l == 0 && cx.mark) cx.mark(cx.owner, false);
 }
 
@@ -405,13 +416,17 @@ int fac_solve(Ctx& cx, DevFac<R>& F, int mode, const R* r, R* z, double tol)
          const R* u = L0.u;
          map(ng, [=] __device__(long long t) { sol[t] += u[t]; }, cx.s);
       }
-      // rr = r - A sol, its norm, and sol's interior into z
+      // the norm of r - A sol, and sol's interior into z; the residual
+      // itself is stored only when another cycle needs it (most solves end
+      // after one cycle)
       int nblk = 0;
-      residual_partial(op, g, r, F.sol, F.rr, cx.red->part, &nblk, z, cx.s);
+      residual_partial(op, g, r, F.sol, (R*)nullptr, cx.red->part, &nblk, z, cx.s);
       k_finish<<<1, 1024, 0, cx.s>>>(cx.red->part, nblk, cx.red->dres, 0);
       g_launches++;
       norm = sqrt(cx.red->fetch(1)[0] / (double)g.cells());
       it++;
+      if (norm > tol && it < cx.p->fac_max_cycles)
+         residual_partial(op, g, r, F.sol, F.rr, cx.red->part, &nblk, (R*)nullptr, cx.s);
    } while (norm > tol && it < cx.p->fac_max_cycles);
    L0.f = f_own;
    cx.st->fac_cycles += it;
@@ -449,6 +464,11 @@ struct Stepper {
    float *dF32 = nullptr, *pf32 = nullptr, *dphi32 = nullptr, *da32 = nullptr,
          *db32 = nullptr, *dc32 = nullptr;
    float *guess_l = nullptr, *guess_s = nullptr;  // surrogate initial guess
+   // no converged phase concentrations to warm-start from yet (set_state
+   // without cl / cs, until the first accepted step): the surrogate's guess
+   // is used only then, since a converged warm start from the previous step
+   // needs fewer Newton iterations than the network's guess
+   bool cold = true;
    Mlp* mlp = nullptr;                            // attached surrogate
    unsigned long long* mcount = nullptr;          // mixed KKS counters [5]
    // quaternion fields: ghosted q (4 NG) and its lagged copy, the cell
@@ -601,15 +621,15 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
       }
    }
    if (S.p.precision == 1) {
-      if (S.p.surrogate && S.mlp) {
+      const bool sur = S.p.surrogate && S.mlp && S.cold;
+      if (sur) {
          ProfScope ps(S, KT_MLP);
          S.mlp->infer(S.g, S.phi_g, S.c_g, tf, S.guess_l, S.guess_s, true, S.s);
       }
       {
          ProfScope ps(S, KT_KKS);
          kks_mixed(S.m, S.mp, S.g, S.tab, S.tabf, tf, S.phi_g, S.c_g,
-                   (S.p.surrogate && S.mlp) ? S.guess_l : nullptr,
-                   (S.p.surrogate && S.mlp) ? S.guess_s : nullptr, S.clr32, S.csr32,
+                   sur ? S.guess_l : nullptr, sur ? S.guess_s : nullptr, S.clr32, S.csr32,
                    S.cl32, S.cs32, S.dF32, S.mcount, S.s);
       }
       {
@@ -921,7 +941,7 @@ static void matvec32(Stepper& S, double gamma, const float* v, float* out)
 // preconditioning, WRMS scaling, modified Gram-Schmidt) on FP32 Krylov
 // vectors.  Inner products: FP32 products, compensated FP32 sums per thread,
 // FP64 across threads and blocks.  b and the correction x are FP64.
-static int gmres32(Stepper& S, double gamma, const double* b, double* x,
+static int gmres32(Stepper& S, double gamma, const float* bf, double* x,
                    double tol)
 {
    const long long ny = S.NY;
@@ -933,8 +953,6 @@ static int gmres32(Stepper& S, double gamma, const double* b, double* x,
    float* av = S.avf;
    const float* w = S.w32;
    const float* wi = S.wi32;
-   float* bf = S.bf;
-   map(ny, [=] __device__(long long t) { bf[t] = d2f(b[t]); }, S.s);
    precond_solve(S, bf, tmp, tol * sqrtN);
    float* V0 = S.Vf[0];
    double beta = std::sqrt(S.red.sumf(ny, [=] __device__(long long t) {
@@ -1051,8 +1069,8 @@ static int bdf_step(Stepper& S, double h, int q)
    const double rtol = S.p.rtol, atol = S.p.atol;
    double* wi = S.wi;
    if (S.p.precision == 1) {
-      // FP32 weights (no FP64 division per element); the FP64 copies used by
-      // the Newton test hold the same values exactly
+      // FP32 weights (no FP64 division per element); the FP64 copy used by
+      // the Newton test holds the same values exactly
       float *w32 = S.w32, *wi32 = S.wi32;
       const float rtf = (float)rtol, atf = (float)atol;
       map(ny, [=] __device__(long long t) {
@@ -1061,7 +1079,6 @@ static int bdf_step(Stepper& S, double h, int q)
          w32[t] = wv;
          wi32[t] = e;
          w[t] = f2d(wv);
-         wi[t] = f2d(e);
       }, S.s);
    } else {
       map(ny, [=] __device__(long long t) {
@@ -1076,10 +1093,17 @@ static int bdf_step(Stepper& S, double h, int q)
       eval_rhs(S, y, nullptr, 0.0, fy, 0);
       if (it == 0 && S.p.precond) precond_setup(S, gamma);
       const double gm = gamma;
-      map(ny, [=] __device__(long long t) { b[t] = -(y[t] - gm * fy[t] - a[t]); },
-          S.s);
-      const int li = S.p.precision == 1 ? gmres32(S, gamma, b, d, lintol)
-                                        : gmres(S, y, fy, w, gamma, b, d, lintol);
+      int li;
+      if (S.p.precision == 1) {  // the Newton right-hand side straight to FP32
+         float* bf = S.bf;
+         map(ny, [=] __device__(long long t) { bf[t] = d2f(-(y[t] - gm * fy[t] - a[t])); },
+             S.s);
+         li = gmres32(S, gamma, bf, d, lintol);
+      } else {
+         map(ny, [=] __device__(long long t) { b[t] = -(y[t] - gm * fy[t] - a[t]); },
+             S.s);
+         li = gmres(S, y, fy, w, gamma, b, d, lintol);
+      }
       S.st.gmres_iters += li;
       S.st.newton_iters++;
       // y += d and WRMS(d) in one pass
@@ -1318,6 +1342,7 @@ int ampe_stepper_set_state(void* h, const double* phi, const double* conc,
    }
    S->hist = 0;
    S->t = 0.0;
+   S->cold = !(cl && cs);
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
    return AMPE_OK;
 }
@@ -1391,6 +1416,7 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
          break;
       }
       S->hist = retries == 0 ? 1 : 0;
+      S->cold = false;
       swap_ptr(S->ynm1, S->yn);  // ynm1 <- yn
       swap_ptr(S->yn, S->ynew);  // yn <- ynew
       if (S->p.precision == 1) {

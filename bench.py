@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="calphad", choices=["calphad", "poly", "dendrite"])
+    ap.add_argument("--workload", default="calphad", choices=["calphad", "poly", "dendrite", "dilute"])
     ap.add_argument("--n", type=int, default=0, help="cells per side (0: the workload's)")
     ap.add_argument("--path", default="mixed+surrogate",
                     choices=["fp64", "mixed", "mixed+surrogate"])
@@ -197,27 +197,41 @@ class State:
 
 
 def default_n(kind):
-    return {"calphad": 256, "poly": 128, "dendrite": 2048}[kind]
+    return {"calphad": 256, "poly": 128, "dendrite": 2048, "dilute": 256}[kind]
 
 
-def workload(n, kind="calphad", seed=3):
+def workload(n, kind="calphad", seed=3, state=True):
     """calphad: phi + c CALPHAD 3D, T_run + 50 K gradient (the headline);
     poly: phi + q + c CALPHAD polycrystal 3D at 1500 K, seeded Voronoi grains
     (8 at 128^3, 64 at 512^3), 6-cell liquid channel; dendrite: 2D dilute KKS,
     four-fold anisotropic flux (delta 0.02), undercooling 0.55, 16 seeds of
-    radius 8 with random orientation angles."""
+    radius 8 with random orientation angles; dilute: 2D dilute KKS at 900 K,
+    isotropic nine-point flux, one tanh seed of radius 20 (width 3) in
+    c = 0.02 +- 1e-3.  state=False: the model only."""
     from ampe_gb300 import configs, initial
 
+    if kind == "dilute":
+        m = configs.dilute2d(n)
+        if not state:
+            return m, None
+        phi, c = initial.dilute2d_state(n, seed=seed, radius=20.0, width=3.0)
+        return m, State(phi, c)
     if kind == "poly":
         m = configs.polycrystal3d(n, seed=seed, T=1500.0)
+        if not state:
+            return m, None
         ngr = max(8, (n // 128) ** 3 * 8)
         phi, c, q = initial.polycrystal_state(n, ngrains=ngr, seed=1, channel=6.0)
         return m, State(phi, c, quat=q)
     if kind == "dendrite":
         m = configs.dendrite2d(n)
+        if not state:
+            return m, None
         phi, c, q = initial.dendrite2d_state(n, nseeds=16, radius=8.0, seed=seed)
         return m, State(phi, c, orient=q)
     m = configs.calphad3d(n, seed=seed, T_run=1500.0)
+    if not state:
+        return m, None
     phi, c = initial.calphad3d_state(n, seed=seed, nseeds=max(2, (n // 32) ** 3 // 2),
                                      radius=max(4.0, n / 20.0))
     return m, State(phi, c)
@@ -230,6 +244,8 @@ WORKLOAD_NAMES = {
             "Newton-GMRES(5), MG-preconditioned FAC blocks, atol %g)",
     "dendrite": "phi+c dilute anisotropic dendrite implicit step %d^2 (dt=0.1, BDF<=2, "
                 "Newton-GMRES(5), MG-preconditioned FAC blocks, atol %g)",
+    "dilute": "phi+c dilute isotropic implicit step %d^2 (dt=0.1, BDF<=2, "
+              "Newton-GMRES(5), MG-preconditioned FAC blocks, atol %g)",
 }
 
 
@@ -241,12 +257,30 @@ def step_params(args, path):
                                surrogate=1 if path == "mixed+surrogate" else 0)
 
 
+def cpu_sample_n(args):
+    """Side of the CPU sample level: cpu_n^3 in 3D, (8 cpu_n)^2 for the 2D
+    dendrite, the whole level for the small 2D dilute case."""
+    if args.workload == "dilute":
+        return min(args.n, 8 * args.cpu_n)
+    return args.cpu_n if args.workload != "dendrite" else 8 * args.cpu_n
+
+
+def arm_config(args, head=None, ws=1):
+    """The config object of both arms' JSON lines (the workload at full size)."""
+    m, _ = workload(args.n, args.workload, state=False)
+    N = m.cells()
+    return {"workload": WORKLOAD_NAMES[args.workload] % (args.n, args.atol),
+            "path": head or args.path, "cells": N,
+            "l2": "inputs larger than L2 (state 2 x %d MB)" % (N * 8 // 2 ** 20),
+            "parallelism": "replicas" if ws > 1 else "single"}
+
+
 def cpu_baseline(args, threads=None):
     """The oracle on a bounded sample (cpu_n^3 level, same physics)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle as O
 
-    n = args.cpu_n if args.workload != "dendrite" else 8 * args.cpu_n
+    n = cpu_sample_n(args)
     m, st0 = workload(n, args.workload)
     p = step_params(args, "fp64")
     s = O.OracleStepper(m, p)
@@ -271,7 +305,7 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle as O
 
-    n = args.cpu_n if args.workload != "dendrite" else 8 * args.cpu_n
+    n = cpu_sample_n(args)
     m, st0 = workload(n, args.workload)
     p = step_params(args, "fp64")
     s = O.OracleStepper(m, p)
@@ -286,12 +320,12 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": (WORKLOAD_NAMES[args.workload] % (n, args.atol))
-                   + ", bounded CPU sample", "sample_of": "%d cells per side" % args.n},
+        "config": arm_config(args),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d cells, %d implicit steps, oracle/ C++ FP64 (reference "
+                         "sample": "%d^%d level (%d cells) of the same workload, %d implicit "
+                                   "steps per timed run, oracle/ C++ FP64 with OpenMP (reference "
                                    "sources unbuildable here: no SAMRAI/SUNDIALS/hypre/Thermo4PFM)"
-                                   % (m.cells(), args.steps)},
+                                   % (n, m.dim, m.cells(), args.steps)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -339,9 +373,22 @@ def timed_path(args, m, st0, path, local, mlp=None):
     g = ImplicitStepper(m, step_params(args, path))
     if path == "mixed+surrogate":
         _native.check(L.ampe_stepper_attach_surrogate(g._h, mlp), "attach_surrogate")
-    st0.load(g)
-    g.advance(args.warmup)
     stream = torch.cuda.ExternalStream(L.ampe_stepper_stream(g._h))
+    # cold start (no converged phase concentrations yet: the surrogate's
+    # case), timed on its own after one untimed step that loads the modules
+    st0.load(g)
+    g.advance(1)
+    st0.load(g)
+    k0 = g.advance(0)["kks_iters"]
+    c0 = torch.cuda.Event(enable_timing=True)
+    c1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    c0.record(stream)
+    cst = g.advance(1)
+    c1.record(stream)
+    torch.cuda.synchronize()
+    cold = {"ms": c0.elapsed_time(c1), "kks_iters": cst["kks_iters"] - k0}
+    g.advance(max(0, args.warmup - 1))
     torch.cuda.synchronize()
     L.ampe_stepper_profile(g._h, 1)
     launches0 = L.ampe_stepper_kernel_launches(g._h)
@@ -373,7 +420,8 @@ def timed_path(args, m, st0, path, local, mlp=None):
     if st0.quat is not None:
         state["q"] = g.get_quat()
     return {"ms": ms, "stats": st, "launches": int(launches), "kernels": kt,
-            "clocks": clocks.summary(), "value": N * args.steps / (ms / 1e3)}, state, g
+            "clocks": clocks.summary(), "value": N * args.steps / (ms / 1e3),
+            "cold_start_step": cold}, state, g
 
 
 def run_ours(args):
@@ -443,7 +491,8 @@ def run_ours(args):
              "kks_iters": r["stats"]["kks_iters"], "kks_fallback": r["stats"]["kks_fallback"],
              "newton_iters": r["stats"]["newton_iters"], "gmres_iters": r["stats"]["gmres_iters"],
              "clocks": r["clocks"], "kernels_ms": {k: v["ms"] for k, v in r["kernels"].items()
-                                                   if v["launches"]}}
+                                                   if v["launches"]},
+             "cold_start_step": r["cold_start_step"]}
         if ref is not None and name != "fp64":
             d["speedup_vs_fp64"] = r["value"] / ref[0]["value"]
             d["rel_l2_err_vs_fp64"] = {
@@ -506,10 +555,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD_NAMES[args.workload] % (args.n, args.atol),
-                   "path": head, "cells": N,
-                   "l2": "inputs larger than L2 (state 2 x %d MB)" % (N * 8 // 2 ** 20),
-                   "parallelism": "replicas" if ws > 1 else "single"},
+        "config": arm_config(args, head, ws),
         "paths": paths,
         "surrogate": sur_info,
         "roofline": roof,

@@ -1,7 +1,8 @@
 """Surrogate MLP: gradients of the GPU training kernels against the numpy
 oracle, tensor-core (tcgen05) inference against the CUDA-core reference
 kernel and numpy, training on Newton-labelled samples, and the mixed stepper
-with the surrogate initial guess against the FP64 oracle."""
+with the surrogate initial guess against the FP64 oracle; the surrogate is
+evaluated only while no converged warm start exists (a cold start)."""
 import ctypes as C
 
 import numpy as np
@@ -143,4 +144,12 @@ def test_training_and_surrogate_stepper(cuda):
     print("first step KKS iterations: plain", st_cold["kks_iters"], "surrogate", st_warm["kks_iters"],
           "fallbacks", st_warm["kks_fallback"])
     assert st_warm["kks_iters"] < st_cold["kks_iters"]
+    # once a step has converged, its phase concentrations are the warm start
+    # and the network is no longer evaluated
+    kt_mlp = 3
+    assert cuda.lib.ampe_stepper_profile(warm._h, 1) == 0
+    warm.advance(1)
+    t, cnt = C.c_double(), C.c_longlong()
+    assert cuda.lib.ampe_stepper_kernel_time(warm._h, kt_mlp, C.byref(t), C.byref(cnt)) == 0
+    assert cnt.value == 0
     cuda.lib.ampe_mlp_destroy(h)
