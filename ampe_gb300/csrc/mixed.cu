@@ -663,26 +663,37 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an, Fac
 }
 
 // composition flux weights of every face (EBS: (1-h) D_L, h D_S with h =
-// diff_interp; "kks": D0, D_phi)
+// diff_interp; "kks": D0, D_phi).  One thread per point (i, j, k) of the box
+// [0, n0] x [0, n1] x [0, n2] computes the lower x, y and z faces of cell
+// (i, j, k) that exist, sharing the cell's index math and loads.
 template <int DIM, bool PB>
 __global__ void k_face_weights(ampe_model_t m, MixParams mp, Grid g, const double* tfield,
-                               const float* pf, const float* cl, const float* cs, FaceW fw)
+                               const float* __restrict__ pf, const float* __restrict__ cl,
+                               const float* __restrict__ cs, FaceW fw)
 {
-   const long long tot = g.nfx() + g.nfy() + (DIM == 3 ? g.nfz() : 0);
+   const long long tot = (long long)(g.n0 + 1) * (g.n1 + 1) * (DIM == 3 ? g.n2 + 1 : 1);
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
         t += (long long)gridDim.x * blockDim.x) {
-      int dir, i, j, k;
-      face_of(g, t, dir, i, j, k);
-      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
-      const long long lo = g.c(i - ei, j - ej, k - ek), up = g.c(i, j, k);
-      float a, b;
-      if (mp.kksc)
-         kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, up, i, j, k, ei, ej, ek, a, b);
-      else
-         face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, up, i, j, k, ei, ej, ek, a, b);
-      const int f = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
-      fw.A[dir][f] = a;
-      fw.B[dir][f] = b;
+      int i, j, k;
+      g.split(t, g.fd0p, g.fd1p, i, j, k);
+      const long long up = g.c(i, j, k);
+#pragma unroll
+      for (int dir = 0; dir < DIM; dir++) {
+         const bool has = dir == 0 ? (j < g.n1 && k < g.n2)
+                                   : (dir == 1 ? (i < g.n0 && k < g.n2) : (i < g.n0 && j < g.n1));
+         if (!has) continue;
+         const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+         const long long lo = g.c(i - ei, j - ej, k - ek);
+         float a, b;
+         if (mp.kksc)
+            kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, up, i, j, k, ei, ej, ek, a,
+                                   b);
+         else
+            face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, up, i, j, k, ei, ej, ek, a, b);
+         const int f = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+         fw.A[dir][f] = a;
+         fw.B[dir][f] = b;
+      }
    }
 }
 
@@ -698,7 +709,8 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    k_phi_to_f32<<<(unsigned)b, 256, 0, s>>>(g, phi, pf);
    launch_status();
    {
-      const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+      const long long tot =
+          (long long)(g.n0 + 1) * (g.n1 + 1) * (g.dim == 3 ? g.n2 + 1 : 1);
       long long bf = (tot + 255) / 256;
       if (bf > kMaxBlocks) bf = kMaxBlocks;
       if (g.dim == 3) {

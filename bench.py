@@ -39,12 +39,15 @@ RHS_BYTES_PER_CELL = 56  # read phi, phi_lag, cL, cS, dF; write phi', c'
 # mixed path KKS kernel: read phi, c (FP64), cL_ref, cS_ref (FP32); write cL,
 # cS, dF (FP32)
 KKS_MIXED_BYTES_PER_CELL = 36
-# mixed RHS: read phi (FP32 copy), cL, cS, dF (FP32), write phi', c' (FP64)
-RHS_MIXED_BYTES_PER_CELL = 36
-# analytic Jv on FP32 Krylov vectors: point pass 32 B (v, phi, cL, cS; write
-# dphi, dcL, dcS) + stencil pass 44 B (dphi, dcL, dcS, phi, cL, cS, dF, v;
-# write out)
-JV_BYTES_PER_CELL = 76
+# mixed RHS evaluation, three launches: FP32 copy of phi (read 8, write 4),
+# composition face weights (read phi 4, write 2 weights x 3 faces 24), RHS
+# (read phi FP64 8, phi FP32 4, cL, cS 8, dF 4, face weights 24; write phi',
+# c' FP64 16)
+RHS_MIXED_BYTES_PER_CELL = 12 + 28 + 64
+# analytic Jv on FP32 Krylov vectors: point pass 32 B (v 8, phi 4, cL, cS 8;
+# write dphi, dcL, dcS 12) + stencil pass 68 B (dphi, dcL, dcS 12, face
+# weights 24, phi 4, cL, cS 8, dF 4, v 8; write out 8)
+JV_BYTES_PER_CELL = 32 + 68
 # one red-black sweep (two colour launches) on the finest multigrid level,
 # FP32, per cell: phase block u r/w 8 + f 4 + C 4 = 16 B, composition block
 # u r/w 8 + f 4 + D (3 faces) 12 = 24 B; the two blocks alternate: 20 B

@@ -1,0 +1,41 @@
+"""bench.py host logic on CPU: both arms describe the same full-size
+workload (the reference arm times a bounded sample of it), every workload
+builds its model, and the CPU sample sizes stay small."""
+import argparse
+
+import pytest
+
+import bench
+
+
+def _args(workload, n=0, path="mixed+surrogate"):
+    a = argparse.Namespace(workload=workload, n=n, path=path, atol=bench.ATOL, cpu_n=48)
+    if a.n <= 0:
+        a.n = bench.default_n(workload)
+    return a
+
+
+@pytest.mark.parametrize("kind,cells", [("calphad", 256 ** 3), ("poly", 128 ** 3),
+                                        ("dendrite", 2048 ** 2), ("dilute", 256 ** 2)])
+def test_arm_config(kind, cells):
+    a = _args(kind)
+    cfg = bench.arm_config(a)
+    assert cfg["cells"] == cells
+    assert cfg["path"] == "mixed+surrogate"
+    assert cfg["workload"] == bench.WORKLOAD_NAMES[kind] % (a.n, a.atol)
+    # the reference arm reports the same config object
+    assert bench.arm_config(a) == cfg
+
+
+@pytest.mark.parametrize("kind", ["calphad", "poly", "dendrite", "dilute"])
+def test_cpu_sample_bounded(kind):
+    a = _args(kind)
+    n = bench.cpu_sample_n(a)
+    m, _ = bench.workload(n, kind, state=False)
+    assert 0 < m.cells() <= 400_000
+
+
+def test_small_workload_states():
+    for kind, n in (("calphad", 16), ("poly", 16), ("dendrite", 32), ("dilute", 32)):
+        m, st = bench.workload(n, kind)
+        assert st.phi.size == m.cells() and st.c.size == m.cells()
