@@ -50,18 +50,25 @@ RHS_MIXED_BYTES_PER_CELL = 12 + 28 + 64
 JV_BYTES_PER_CELL = 32 + 68
 # one red-black sweep (two colour launches) on the finest multigrid level,
 # FP32, per cell: phase block u r/w 8 + f 4 + C 4 = 16 B, composition block
-# u r/w 8 + f 4 + D (3 faces) 12 = 24 B; the two blocks alternate: 20 B
-SMOOTH_BYTES_PER_CELL = 20
-SMOOTH_BYTES_PER_CELL_FP64 = 40
+# u r/w 8 + f 4 + D (3 faces in 3D, 2 in 2D) 12 / 8 B; the two blocks
+# alternate: 20 B in 3D, 18 B in 2D (twice that in FP64)
+SMOOTH_BYTES_PER_CELL = {3: 20, 2: 18}
+SMOOTH_BYTES_PER_CELL_FP64 = {3: 40, 2: 36}
+# DRAM bytes per cell of one finest-level sweep of the FP32 smoother on the
+# 3D CALPHAD phi + c level, from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) of both colour launches of each block at 224^3:
+# phase block 514.1 MB, composition block 307.8 MB per sweep, mean over the
+# two blocks / 11,239,424 cells; traffic scales with the cells
+SMOOTH_DRAM_BYTES_PER_CELL_MEASURED = 36.56
 # MLP inference: 2 (3*64 + 64*64 + 64*64 + 64*2) multiply-adds per cell
 MLP_FLOPS_PER_CELL = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
 KERNEL_NAMES = {
     False: {"kks_newton": "k_kks_mixed", "rhs_fused": "k_rhs_mixed",
             "jv_analytic": "k_jv_point+k_jv_stencil",
-            "smooth_fine": "k_rbgs_color<float,3> x2 (finest-level red-black sweep)"},
+            "smooth_fine": "k_rbgs_color<float,%d> x2 (finest-level red-black sweep)"},
     True: {"kks_newton": "k_kks_interior", "rhs_fused": "k_rhs_fused<0>",
            "jv_analytic": "-",
-           "smooth_fine": "k_rbgs_color<double,3> x2 (finest-level red-black sweep)"},
+           "smooth_fine": "k_rbgs_color<double,%d> x2 (finest-level red-black sweep)"},
 }
 # profiling-timer kinds of the stepper (ampe_stepper_kernel_time)
 KINDS = ((0, "kks_newton"), (1, "rhs_fused"), (2, "jv_analytic"), (3, "mlp_infer_tc"),
@@ -533,8 +540,8 @@ def run_ours(args):
     per_cell = {"kks_newton": KKS_BYTES_PER_CELL if head == "fp64" else KKS_MIXED_BYTES_PER_CELL,
                 "rhs_fused": RHS_BYTES_PER_CELL if head == "fp64" else RHS_MIXED_BYTES_PER_CELL,
                 "jv_analytic": JV_BYTES_PER_CELL,
-                "smooth_fine": SMOOTH_BYTES_PER_CELL_FP64 if head == "fp64"
-                else SMOOTH_BYTES_PER_CELL}
+                "smooth_fine": SMOOTH_BYTES_PER_CELL_FP64[m.dim] if head == "fp64"
+                else SMOOTH_BYTES_PER_CELL[m.dim]}
     kname = max((k for k in SINGLE_KERNELS if kt[k]["launches"]), key=lambda k: kt[k]["ms"])
     tot, cnt = kt[kname]["ms"], kt[kname]["launches"]
     avg_ms = tot / max(cnt, 1)
@@ -548,10 +555,17 @@ def run_ours(args):
     else:
         nbytes = per_cell[kname] * N
         achieved = nbytes / (avg_ms / 1e3) / 1e9
-        roof = {"bound": "hbm", "kernel": KERNEL_NAMES[head == "fp64"][kname],
+        kn = KERNEL_NAMES[head == "fp64"][kname]
+        traffic = None
+        if (kname == "smooth_fine" and head != "fp64" and args.workload == "calphad"):
+            traffic = SMOOTH_DRAM_BYTES_PER_CELL_MEASURED * N
+        roof = {"bound": "hbm", "kernel": kn % m.dim if "%d" in kn else kn,
                 "achieved": achieved, "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s",
-                "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                 "algorithmic_bytes_per_launch": nbytes}
+        if traffic is not None:
+            roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of both "
+                                      "blocks' colour launches at 224^3, scaled by cells")
     roof.update({"avg_launch_ms": avg_ms, "launches": cnt, "share_of_step": tot / res_h["ms"]})
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
