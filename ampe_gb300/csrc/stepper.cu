@@ -455,6 +455,7 @@ struct Stepper {
    unsigned long long* counters;
    // 2N interior vectors
    double *yn, *ynm1, *ynew, *a, *y, *fy, *b, *d, *w, *wi, *tmp, *av, *fp;
+   double *ysave, *ym1save;  // y_n, y_{n-1} at the start of a step being retried
    std::vector<double*> V;
    // mixed path Krylov vectors (FP32) and FP32 copies of the WRMS weights
    std::vector<float*> Vf;
@@ -1180,8 +1181,8 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
                     &S->csr, &S->cl_nf, &S->cs_nf, &S->phi_lag, &S->tfield};
    for (double** q : gh) *q = dvec(*S, S->NG, &err);
    S->dF = dvec(*S, S->N, &err);
-   double** vv[] = {&S->yn, &S->ynm1, &S->ynew, &S->a,   &S->y,  &S->fy, &S->b,
-                    &S->d,  &S->w,    &S->wi,   &S->tmp, &S->av, &S->fp};
+   double** vv[] = {&S->yn, &S->ynm1, &S->ynew, &S->a,   &S->y,  &S->fy, &S->b,  &S->d,
+                    &S->w,  &S->wi,   &S->tmp,  &S->av, &S->fp, &S->ysave, &S->ym1save};
    for (double** q : vv) *q = dvec(*S, S->NY, &err);
    if (p->precision == 1) {
       for (int l = 0; l <= p->max_krylov; l++)
@@ -1401,15 +1402,35 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
       const int q = S->hist ? std::min(2, S->p.max_order) : 1;
       int fail = bdf_step(*S, hstep, q);
       int retries = 0;
-      while (fail && retries < S->p.max_retries) {
-         retries++;
-         S->st.step_retries++;
-         hstep *= 0.5;
-         fail = bdf_step(*S, hstep, 1);
-         if (fail) continue;
-         cudaMemcpyAsync(S->ynm1, S->yn, b2, cudaMemcpyDeviceToDevice, S->s);
-         cudaMemcpyAsync(S->yn, S->ynew, b2, cudaMemcpyDeviceToDevice, S->s);
-         fail = bdf_step(*S, hstep, 1);
+      if (fail) {
+         // order-1 sub-steps: after each failure halve the sub-step and go
+         // on from the last accepted sub-step until the whole step is
+         // covered; if the retries run out, the step's start is restored
+         cudaMemcpyAsync(S->ysave, S->yn, b2, cudaMemcpyDeviceToDevice, S->s);
+         cudaMemcpyAsync(S->ym1save, S->ynm1, b2, cudaMemcpyDeviceToDevice, S->s);
+         double done = 0.0, hsub = hstep;
+         while (fail && retries < S->p.max_retries) {
+            retries++;
+            S->st.step_retries++;
+            hsub *= 0.5;
+            fail = 0;
+            while (done < hstep * (1.0 - 1e-12)) {
+               const double hh = std::min(hsub, hstep - done);
+               if (bdf_step(*S, hh, 1)) {
+                  fail = 1;
+                  break;
+               }
+               done += hh;
+               if (done < hstep * (1.0 - 1e-12)) {  // accept the sub-step
+                  cudaMemcpyAsync(S->ynm1, S->yn, b2, cudaMemcpyDeviceToDevice, S->s);
+                  cudaMemcpyAsync(S->yn, S->ynew, b2, cudaMemcpyDeviceToDevice, S->s);
+               }
+            }
+         }
+         if (fail) {
+            cudaMemcpyAsync(S->yn, S->ysave, b2, cudaMemcpyDeviceToDevice, S->s);
+            cudaMemcpyAsync(S->ynm1, S->ym1save, b2, cudaMemcpyDeviceToDevice, S->s);
+         }
       }
       if (fail) {
          ret = AMPE_ERR_NOT_CONVERGED;

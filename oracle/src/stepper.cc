@@ -473,17 +473,34 @@ int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
       int q = s->hist ? std::min(2, s->p.max_order) : 1;
       int fail = bdf_step(*s, hstep, q, ynew);
       int retries = 0;
-      while (fail && retries < s->p.max_retries) {
-         // restart at order 1 with half the step, twice
-         retries++;
-         s->st.step_retries++;
-         hstep *= 0.5;
-         std::vector<double> ymid;
-         fail = bdf_step(*s, hstep, 1, ymid);
-         if (fail) continue;
-         s->ynm1 = s->yn;
-         s->yn = ymid;
-         fail = bdf_step(*s, hstep, 1, ynew);
+      if (fail) {
+         // order-1 sub-steps: after each failure halve the sub-step and go
+         // on from the last accepted sub-step until the whole step is
+         // covered; if the retries run out, the step's start is restored
+         const std::vector<double> ysave = s->yn, ym1save = s->ynm1;
+         double done = 0.0, hsub = hstep;
+         while (fail && retries < s->p.max_retries) {
+            retries++;
+            s->st.step_retries++;
+            hsub *= 0.5;
+            fail = 0;
+            while (done < hstep * (1.0 - 1e-12)) {
+               const double hh = std::min(hsub, hstep - done);
+               if (bdf_step(*s, hh, 1, ynew)) {
+                  fail = 1;
+                  break;
+               }
+               done += hh;
+               if (done < hstep * (1.0 - 1e-12)) {  // accept the sub-step
+                  s->ynm1 = s->yn;
+                  s->yn = ynew;
+               }
+            }
+         }
+         if (fail) {
+            s->yn = ysave;
+            s->ynm1 = ym1save;
+         }
       }
       if (fail) {
          ret = 1;
