@@ -451,9 +451,12 @@ long long ampe_stepper_size(void* handle);
 /* f(y_n) for the whole state vector (ampe_stepper_size doubles). */
 int ampe_stepper_eval_rhs_full(void* handle, double* out, int host);
 /* Use a trained surrogate (ampe_mlp_*) for the KKS initial guesses of the
- * mixed path (params surrogate=1): each cell starts from the network's
- * guess and falls back to the previous step's values when 3 FP32 Newton
- * iterations do not converge.  The handle must outlive the stepper. */
+ * mixed path (params surrogate=1) while no converged phase concentrations
+ * exist (after ampe_stepper_set_state without cl / cs, until the first
+ * accepted step): each cell starts from the network's guess and falls back
+ * to the stored values when 3 FP32 Newton iterations do not converge.
+ * Afterwards the previous step's values are the starting point.  The handle
+ * must outlive the stepper. */
 int ampe_stepper_attach_surrogate(void* handle, void* mlp);
 /* Launches of library kernels in this process (launch accounting). */
 long long ampe_stepper_kernel_launches(void* handle);
