@@ -14,8 +14,9 @@ QuatModel::evaluateVolumeSolid).
 The zero-slope 32^3 box is run as its mirror image, a 64^3 periodic level
 (cell-centred zero-slope ghosts are the mirror images of the interior
 cells).  Fixed-step BDF1 with a geometric start-up (the sharp initial
-interface) and T updated per step.  The run takes tens of minutes on a few
-cores: opt-in with AMPE_SLOW_TESTS=1."""
+interface) and T updated per step.  Measured: solid fraction 0.3343 at
+t = 0.3, mean composition drift -4.3e-6 (79 minutes on 8 cores): opt-in
+with AMPE_SLOW_TESTS=1."""
 import json
 import os
 
