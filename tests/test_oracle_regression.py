@@ -11,6 +11,12 @@ diffusion interpolation, molar volume 7.68e-6 (energies x 1e-6 / Vm), T =
 fraction 0.33 +- 0.01 at t = 0.3 (test3d.py:55-62; mean of phi,
 QuatModel::evaluateVolumeSolid).
 
+The deck sets no diffusion_type, so the reference derives composition-
+dependent diffusivities from the database's atomic mobilities
+(MobilityCompositionDiffusionStrategy, QuatModelParameters.cc:238-246);
+this run uses the deck's D_L and D_S, which the deck's comment gives as
+that model's values at 1450 K (3d.input:54).
+
 The zero-slope 32^3 box is run as its mirror image, a 64^3 periodic level
 (cell-centred zero-slope ghosts are the mirror images of the interior
 cells).  Fixed-step BDF1 with a geometric start-up (the sharp initial
