@@ -15,7 +15,7 @@ The deck sets no diffusion_type, so the reference derives composition-
 dependent diffusivities from the database's atomic mobilities
 (MobilityCompositionDiffusionStrategy, QuatModelParameters.cc:238-246);
 this run uses the deck's D_L and D_S, which the deck's comment gives as
-that model's values at 1450 K (3d.input:54).
+that model's values at 1450 K (3d.input:51-53).
 
 The zero-slope 32^3 box is run as its mirror image, a 64^3 periodic level
 (cell-centred zero-slope ghosts are the mirror images of the interior
