@@ -1,0 +1,167 @@
+"""Second, independent restatements (numpy, written from the reference's
+Fortran loops) of stencil kernels that no reference known-answer test
+covers, checked against the oracle's C++ on random fields (CPU):
+gradient_flux (3d/quatrhs.m4:12-66), compute_flux_isotropic
+(2d/quatrhs.m4:106-151), the 2D anisotropic_gradient_flux
+(2d/quatrhs.m4:154-256), concentration_pfmdiffusion_of_temperature
+(3d/concentrationdiffusion.m4:310-428) and add_flux (3d/flux.m4:15-100).
+The GPU leaf kernels are checked against the oracle to 1e-12, so these
+close the chain to the reference's formulas."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from ampe_gb300 import abi, configs
+
+
+def _model2d(flux, n=(14, 11)):
+    m = configs.dilute2d(n[0])
+    m.n[1] = n[1]
+    m.dx[0], m.dx[1] = 0.7, 1.3
+    m.epsilon_phi = 1.7
+    m.flux_type = flux
+    return m
+
+
+def _oracle_flux(orc, m, ph, q=None):
+    fs = [np.zeros(s) for s in m.face_shapes()]
+    orc.orc_phase_flux(C.byref(m), O.ptr(ph), None if q is None else O.ptr(q),
+                       *[O.ptr(f) for f in fs])
+    return fs
+
+
+def test_gradient_flux_3d(orc):
+    m = configs.calphad3d(9, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 7, 6
+    m.dx[0], m.dx[1], m.dx[2] = 0.5, 0.8, 1.1
+    m.epsilon_phi = 0.9
+    rng = np.random.default_rng(4)
+    ph = O.ghosted(m, rng.uniform(0, 1, m.interior_shape()))
+    f0, f1, f2 = _oracle_flux(orc, m, ph)
+    e2 = m.epsilon_phi ** 2
+    P = ph  # [k + 1, j + 1, i + 1]
+    r0 = (P[1:-1, 1:-1, 1:] - P[1:-1, 1:-1, :-1]) * (e2 / m.dx[0])
+    r1 = (P[1:-1, 1:, 1:-1] - P[1:-1, :-1, 1:-1]) * (e2 / m.dx[1])
+    r2 = (P[1:, 1:-1, 1:-1] - P[:-1, 1:-1, 1:-1]) * (e2 / m.dx[2])
+    for a, b in ((f0, r0), (f1, r1), (f2, r2)):
+        assert a.shape == b.shape
+        assert O.rel_l2(a, b) <= 1e-14
+
+
+def test_isotropic_flux_2d(orc):
+    m = _model2d(abi.FLUX_ISOTROPIC)
+    rng = np.random.default_rng(5)
+    ph = O.ghosted(m, rng.uniform(0, 1, m.interior_shape()))
+    f0, f1, _ = _oracle_flux(orc, m, ph)
+    e2 = m.epsilon_phi ** 2
+    P = ph[0]  # [j + 1, i + 1]
+    nx, ny = m.n[0], m.n[1]
+    ax = (1.0 / 12.0) * e2 / m.dx[0]
+    ay = (1.0 / 12.0) * e2 / m.dx[1]
+    r0 = np.empty((ny, nx + 1))
+    for j in range(ny):
+        for i in range(nx + 1):
+            p = lambda a, b: P[b + 1, a + 1]  # noqa: E731
+            r0[j, i] = ax * ((p(i, j - 1) - p(i - 1, j - 1)) + (p(i, j) - p(i - 1, j)) * 10.0
+                             + (p(i, j + 1) - p(i - 1, j + 1)))
+    r1 = np.empty((ny + 1, nx))
+    for j in range(ny + 1):
+        for i in range(nx):
+            p = lambda a, b: P[b + 1, a + 1]  # noqa: E731
+            r1[j, i] = ay * ((p(i - 1, j) - p(i - 1, j - 1)) + (p(i, j) - p(i, j - 1)) * 10.0
+                             + (p(i + 1, j) - p(i + 1, j - 1)))
+    assert O.rel_l2(f0[0], r0) <= 1e-14
+    assert O.rel_l2(f1[0], r1) <= 1e-14
+
+
+@pytest.mark.parametrize("qlen", [2, 4])
+def test_anisotropic_flux_2d(orc, qlen):
+    m = _model2d(abi.FLUX_ANISOTROPIC)
+    m.aniso_eps, m.aniso_k, m.qlen = 0.05, 4, qlen
+    rng = np.random.default_rng(6)
+    ph = O.ghosted(m, rng.uniform(0, 1, m.interior_shape()))
+    g = rng.standard_normal((qlen,) + m.interior_shape())
+    g /= np.linalg.norm(g, axis=0, keepdims=True)
+    q = np.ascontiguousarray(np.stack([O.ghosted(m, x) for x in g]))
+    f0, f1, _ = _oracle_flux(orc, m, ph, q)
+    eps, nu, kn = m.epsilon_phi, m.aniso_eps, m.aniso_k
+    dxi, dyi = 1.0 / m.dx[0], 1.0 / m.dx[1]
+    P = ph[0]
+    Q1 = q[0, 0]
+    nx, ny = m.n[0], m.n[1]
+
+    def p(a, b):
+        return P[b + 1, a + 1]
+
+    def angle(qa, qb):
+        qq = min(1.0, max(-1.0, 0.5 * (qa + qb)))
+        return 2.0 * np.arccos(qq) if qlen == 4 else np.arccos(qq)
+
+    def eps_of(dpx, dpy, ph_o):
+        theta = np.arctan(dpy / dpx) if abs(dpx) > 1e-12 else 0.5 * np.pi
+        et = eps * (1.0 + nu * np.cos(kn * (theta - ph_o)))
+        de = -kn * eps * nu * np.sin(kn * (theta - ph_o))
+        return et, de
+
+    r0 = np.empty((ny, nx + 1))
+    for j in range(ny):
+        for i in range(nx + 1):
+            dpx = (p(i, j) - p(i - 1, j)) * dxi
+            dpy = 0.25 * (p(i - 1, j + 1) - p(i - 1, j - 1) + p(i, j + 1) - p(i, j - 1)) * dyi
+            et, de = eps_of(dpx, dpy, angle(Q1[j + 1, i], Q1[j + 1, i + 1]))
+            r0[j, i] = et * et * dpx - et * de * dpy
+    r1 = np.empty((ny + 1, nx))
+    for j in range(ny + 1):
+        for i in range(nx):
+            dpx = 0.25 * (p(i + 1, j - 1) - p(i - 1, j - 1) + p(i + 1, j) - p(i - 1, j)) * dxi
+            dpy = (p(i, j) - p(i, j - 1)) * dyi
+            et, de = eps_of(dpx, dpy, angle(Q1[j, i + 1], Q1[j + 1, i + 1]))
+            r1[j, i] = et * et * dpy + et * de * dpx
+    assert O.rel_l2(f0[0], r0) <= 1e-12
+    assert O.rel_l2(f1[0], r1) <= 1e-12
+
+
+def _interp(phi, t):
+    if t == b"l":
+        return phi
+    return phi ** 3 * (10.0 - 15.0 * phi + 6.0 * phi ** 2)  # 'p' (pbg)
+
+
+@pytest.mark.parametrize("interp", [b"l", b"p"])
+def test_diffusion_of_temperature_and_add_flux_3d(orc, interp):
+    """concentration_pfmdiffusion_of_temperature
+    (3d/concentrationdiffusion.m4:310-428, arithmetic average) and add_flux
+    (3d/flux.m4:15-100) with a stored temperature field."""
+    m = configs.calphad3d(8, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 7, 6
+    m.dx[0], m.dx[1], m.dx[2] = 0.6, 0.9, 1.2
+    m.temp_mode = abi.TEMP_FIELD
+    m.D_liquid, m.D_solid = 3.0, 0.02
+    m.Q_liquid, m.Q_solid = 2.0e4, 5.0e4
+    m.diff_interp, m.avg_type = interp, b"a"
+    rng = np.random.default_rng(7)
+    phi = O.ghosted(m, rng.uniform(0, 1, m.interior_shape()))
+    temp = O.ghosted(m, rng.uniform(1400, 1600, m.interior_shape()))
+    u = O.ghosted(m, rng.uniform(0.1, 0.6, m.interior_shape()))
+    shapes = m.face_shapes()
+    dl = [np.zeros(s) for s in shapes]
+    ds = [np.zeros(s) for s in shapes]
+    orc.orc_conc_diffusion(C.byref(m), O.ptr(phi), O.ptr(temp), *[O.ptr(a) for a in dl],
+                           *[O.ptr(a) for a in ds])
+    fl = [np.zeros(s) for s in shapes]
+    orc.orc_add_flux(C.byref(m), O.ptr(u), *[O.ptr(a) for a in dl], *[O.ptr(a) for a in fl])
+    R = 8.314472  # KKSdiluteBinary.cc:45, the gas constant the kernels use
+    sl = [np.s_[1:-1, 1:-1, 1:], np.s_[1:-1, 1:, 1:-1], np.s_[1:, 1:-1, 1:-1]]
+    sm = [np.s_[1:-1, 1:-1, :-1], np.s_[1:-1, :-1, 1:-1], np.s_[:-1, 1:-1, 1:-1]]
+    for d in range(3):
+        vphi = 0.5 * (phi[sm[d]] + phi[sl[d]])
+        h = _interp(vphi, interp)
+        invT = 2.0 / (temp[sm[d]] + temp[sl[d]])
+        rl = (1.0 - h) * (m.D_liquid * np.exp(-(m.Q_liquid / R) * invT))
+        rs = h * (m.D_solid * np.exp(-(m.Q_solid / R) * invT))
+        assert O.rel_l2(dl[d], rl) <= 1e-14
+        assert O.rel_l2(ds[d], rs) <= 1e-14
+        rf = (1.0 / m.dx[d]) * (rl * (u[sl[d]] - u[sm[d]]))
+        assert O.rel_l2(fl[d], rf) <= 1e-14
