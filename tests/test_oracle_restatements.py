@@ -4,7 +4,10 @@ covers, checked against the oracle's C++ on random fields (CPU):
 gradient_flux (3d/quatrhs.m4:12-66), compute_flux_isotropic
 (2d/quatrhs.m4:106-151), the 2D anisotropic_gradient_flux
 (2d/quatrhs.m4:154-256), concentration_pfmdiffusion_of_temperature
-(3d/concentrationdiffusion.m4:310-428) and add_flux (3d/flux.m4:15-100).
+(3d/concentrationdiffusion.m4:310-428), add_flux (3d/flux.m4:15-100) and
+the quaternion face coefficients (quatgrad_side, 3d/quatgrad.m4:213-335,
+with compute_face_coef3d, 3d/quatfacops.m4:14-155, for the three gradient
+floor types of fortran/quat.f:1497-1537).
 The GPU leaf kernels are checked against the oracle to 1e-12, so these
 close the chain to the reference's formulas."""
 import ctypes as C
@@ -165,3 +168,89 @@ def test_diffusion_of_temperature_and_add_flux_3d(orc, interp):
         assert O.rel_l2(ds[d], rs) <= 1e-14
         rf = (1.0 / m.dx[d]) * (rl * (u[sl[d]] - u[sm[d]]))
         assert O.rel_l2(fl[d], rf) <= 1e-14
+
+
+def _grad_normi(g2, floor_type, floor):
+    """eval_grad_normi (fortran/quat.f:1497-1537)."""
+    fl2, mx = floor * floor, 1.0 / floor
+    if floor_type == b"m":
+        return np.where(g2 > fl2, g2 ** -0.5, mx)
+    if floor_type == b"s":
+        return (g2 + fl2) ** -0.5
+    gng2 = g2 * mx * mx
+    with np.errstate(divide="ignore", invalid="ignore"):
+        big = np.tanh(mx * np.sqrt(g2)) / np.sqrt(g2)
+    return np.where(gng2 > 0.01, big, mx * (1.0 - gng2 * (5.0 - 2.0 * gng2) / 15.0))
+
+
+@pytest.mark.parametrize("floor_type", [b"m", b"s", b"t"])
+def test_quat_face_coef_3d(orc, floor_type):
+    """quatdiffs + quatgrad_side (3d/quatgrad.m4:213-335) and
+    compute_face_coef3d (3d/quatfacops.m4:14-155) at constant T."""
+    m = configs.polycrystal3d(9, seed=3, T=1500.0)
+    m.n[1], m.n[2] = 8, 7
+    m.dx[0], m.dx[1], m.dx[2] = 0.8, 1.0, 1.3
+    m.quat_floor_type = floor_type
+    rng = np.random.default_rng(8)
+    shp = m.interior_shape()
+    g = np.round(rng.standard_normal((4,) + shp)) + 0.05 * rng.standard_normal((4,) + shp)
+    g /= np.linalg.norm(g, axis=0, keepdims=True)
+    q = np.stack([O.ghosted(m, x) for x in g])  # (4, z, y, x) ghosted
+    phi = O.ghosted(m, rng.uniform(0, 1, shp))
+    fo = [np.zeros(s) for s in m.face_shapes()]
+    orc.orc_quat_face_coef(C.byref(m), O.ptr(phi), None, O.ptr(np.ascontiguousarray(q)),
+                           *[O.ptr(f) for f in fo])
+    nx, ny, nz = m.n[0], m.n[1], m.n[2]
+    dxi, dyi, dzi = 1.0 / m.dx[0], 1.0 / m.dx[1], 1.0 / m.dx[2]
+
+    def Q(c, i, j, k):  # q of component c at cell (i, j, k), ghosts at -1 / n
+        return q[c, k + 1, j + 1, i + 1]
+
+    def dxq(c, i, j, k):
+        return Q(c, i, j, k) - Q(c, i - 1, j, k)
+
+    def dyq(c, i, j, k):
+        return Q(c, i, j, k) - Q(c, i, j - 1, k)
+
+    def dzq(c, i, j, k):
+        return Q(c, i, j, k) - Q(c, i, j, k - 1)
+
+    def coef(pa, pb, g2):
+        pm = 0.5 * (pa + pb)  # arithmetic average
+        p1 = _interp(pm, m.orient_interp1)
+        p2 = _interp(pm, m.orient_interp2)
+        diff = m.misorientation_factor * m.T0 * p1
+        return -_grad_normi(np.array(g2), floor_type, m.quat_grad_floor) * diff \
+            - m.epsilon_q ** 2 * p2
+
+    P = phi
+    rx = np.empty((nz, ny, nx + 1))
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx + 1):
+                g2 = 0.0
+                for c in range(4):
+                    g2 += (dxi * dxq(c, i, j, k)) ** 2
+                for c in range(4):
+                    g2 += (0.25 * dyi * (dyq(c, i - 1, j + 1, k) + dyq(c, i - 1, j, k)
+                                         + dyq(c, i, j + 1, k) + dyq(c, i, j, k))) ** 2
+                for c in range(4):
+                    g2 += (0.25 * dzi * (dzq(c, i - 1, j, k + 1) + dzq(c, i - 1, j, k)
+                                         + dzq(c, i, j, k + 1) + dzq(c, i, j, k))) ** 2
+                rx[k, j, i] = coef(P[k + 1, j + 1, i], P[k + 1, j + 1, i + 1], g2)
+    rz = np.empty((nz + 1, ny, nx))
+    for k in range(nz + 1):
+        for j in range(ny):
+            for i in range(nx):
+                g2 = 0.0
+                for c in range(4):
+                    g2 += (0.25 * dxi * (dxq(c, i + 1, j, k - 1) + dxq(c, i, j, k - 1)
+                                         + dxq(c, i + 1, j, k) + dxq(c, i, j, k))) ** 2
+                for c in range(4):
+                    g2 += (0.25 * dyi * (dyq(c, i, j + 1, k - 1) + dyq(c, i, j, k - 1)
+                                         + dyq(c, i, j + 1, k) + dyq(c, i, j, k))) ** 2
+                for c in range(4):
+                    g2 += (dzi * dzq(c, i, j, k)) ** 2
+                rz[k, j, i] = coef(P[k, j + 1, i + 1], P[k + 1, j + 1, i + 1], g2)
+    assert O.rel_l2(fo[0], rx) <= 1e-13
+    assert O.rel_l2(fo[2], rz) <= 1e-13
