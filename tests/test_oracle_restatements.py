@@ -254,3 +254,42 @@ def test_quat_face_coef_3d(orc, floor_type):
                 rz[k, j, i] = coef(P[k, j + 1, i + 1], P[k + 1, j + 1, i + 1], g2)
     assert O.rel_l2(fo[0], rx) <= 1e-13
     assert O.rel_l2(fo[2], rz) <= 1e-13
+
+
+def _dinterp(phi, t):
+    if t == b"l":
+        return np.ones_like(phi)
+    return 30.0 * phi ** 2 * (1.0 - phi) ** 2  # 'p' (pbg)
+
+
+@pytest.mark.parametrize("orient", [0, 1])
+def test_computerhspbg_3d(orc, orient):
+    """computerhspbg (3d/quatrhs.m4:357-515), double well 'd'
+    (g' = 32 phi (1 - phi)(1 - 2 phi), functions.f:275-302), constant T."""
+    m = configs.calphad3d(8, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 7, 6
+    m.dx[0], m.dx[1], m.dx[2] = 0.6, 0.9, 1.2
+    m.temp_mode = abi.TEMP_CONSTANT
+    m.T0 = 1450.0
+    m.with_orient = orient
+    m.misorientation_factor, m.epsilon_q = 0.3, 0.4
+    m.phase_well_scale = 0.7
+    rng = np.random.default_rng(9)
+    fs = [rng.standard_normal(s) for s in m.face_shapes()]
+    phi = O.ghosted(m, rng.uniform(0, 1, m.interior_shape()))
+    ogm = rng.uniform(0, 2, size=m.interior_shape())
+    out = np.zeros(m.interior_shape())
+    orc.orc_computerhspbg(C.byref(m), *[O.ptr(f) for f in fs], None, O.ptr(phi), O.ptr(ogm),
+                          O.ptr(out))
+    f0, f1, f2 = fs
+    p = phi[1:-1, 1:-1, 1:-1]
+    r = ((f0[:, :, 1:] - f0[:, :, :-1]) * (1.0 / m.dx[0])
+         + (f1[:, 1:, :] - f1[:, :-1, :]) * (1.0 / m.dx[1])
+         + (f2[1:, :, :] - f2[:-1, :, :]) * (1.0 / m.dx[2]))
+    r = r - m.phase_well_scale * (32.0 * p * (1.0 - p) * (1.0 - 2.0 * p))
+    if orient:
+        p1 = _dinterp(p, m.orient_interp1)
+        p2 = _dinterp(p, m.orient_interp2)
+        r = r - m.misorientation_factor * m.T0 * p1 * ogm \
+            - p2 * (0.5 * m.epsilon_q ** 2) * ogm * ogm
+    assert O.rel_l2(out, r) <= 1e-13
