@@ -7,7 +7,9 @@ gradient_flux (3d/quatrhs.m4:12-66), compute_flux_isotropic
 (3d/concentrationdiffusion.m4:310-428), add_flux (3d/flux.m4:15-100) and
 the quaternion face coefficients (quatgrad_side, 3d/quatgrad.m4:213-335,
 with compute_face_coef3d, 3d/quatfacops.m4:14-155, for the three gradient
-floor types of fortran/quat.f:1497-1537).
+floor types of fortran/quat.f:1497-1537), computerhspbg
+(3d/quatrhs.m4:357-515) and one colour of the red-black FAC smoother
+(3d/ellipticfacops.m4:16-177).
 The GPU leaf kernels are checked against the oracle to 1e-12, so these
 close the chain to the reference's formulas."""
 import ctypes as C
@@ -293,3 +295,37 @@ def test_computerhspbg_3d(orc, orient):
         r = r - m.misorientation_factor * m.T0 * p1 * ogm \
             - p2 * (0.5 * m.epsilon_q ** 2) * ogm * ogm
     assert O.rel_l2(out, r) <= 1e-13
+
+
+@pytest.mark.parametrize("offset", [0, 1])
+def test_rbgs_colour_3d(orc, offset):
+    """efo_compfluxvardc3d + efo_rbgswithfluxmaxvardcvarsf3d
+    (3d/ellipticfacops.m4:16-177): one colour of the red-black update with
+    face D, cell C and cell M arrays."""
+    m = configs.calphad3d(8, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 6, 6
+    m.dx[0], m.dx[1], m.dx[2] = 0.6, 0.9, 1.2
+    rng = np.random.default_rng(10)
+    D = [rng.uniform(-2.0, -0.5, s) for s in m.face_shapes()]
+    Cc = O.ghosted(m, rng.uniform(1.0, 2.0, m.interior_shape()))
+    Mc = O.ghosted(m, rng.uniform(0.5, 1.5, m.interior_shape()))
+    f = O.ghosted(m, rng.uniform(-1, 1, m.interior_shape()))
+    u = O.ghosted(m, rng.uniform(-1, 1, m.interior_shape()))
+    uo = u.copy()
+    mr = orc.orc_efo_rbgs(C.byref(m), *[O.ptr(a) for a in D], 0.0, O.ptr(Cc), 0.0, O.ptr(Mc), 0.0,
+                          O.ptr(f), O.ptr(uo), offset)
+    dxi = [1.0 / m.dx[d] for d in range(3)]
+    fx = dxi[0] * D[0] * (u[1:-1, 1:-1, 1:] - u[1:-1, 1:-1, :-1])
+    fy = dxi[1] * D[1] * (u[1:-1, 1:, 1:-1] - u[1:-1, :-1, 1:-1])
+    fz = dxi[2] * D[2] * (u[1:, 1:-1, 1:-1] - u[:-1, 1:-1, 1:-1])
+    Mi, Ci, fi, ui = (a[1:-1, 1:-1, 1:-1] for a in (Mc, Cc, f, u))
+    res = fi - Mi * (dxi[0] * (fx[:, :, 1:] - fx[:, :, :-1]) + dxi[1] * (fy[:, 1:, :] - fy[:, :-1, :])
+                     + dxi[2] * (fz[1:, :, :] - fz[:-1, :, :])) - Ci * ui
+    dudr = 1.0 / (Mi * (dxi[0] ** 2 * (D[0][:, :, 1:] + D[0][:, :, :-1])
+                        + dxi[1] ** 2 * (D[1][:, 1:, :] + D[1][:, :-1, :])
+                        + dxi[2] ** 2 * (D[2][1:, :, :] + D[2][:-1, :, :])) - Ci)
+    k, j, i = np.indices(m.interior_shape())
+    colour = (i + j + k) % 2 == offset
+    expect = np.where(colour, ui - res * dudr, ui)
+    assert O.rel_l2(uo[1:-1, 1:-1, 1:-1], expect) <= 1e-14
+    assert abs(mr - np.abs(res[colour]).max()) <= 1e-12 * max(1.0, mr)
