@@ -8,8 +8,9 @@ gradient_flux (3d/quatrhs.m4:12-66), compute_flux_isotropic
 the quaternion face coefficients (quatgrad_side, 3d/quatgrad.m4:213-335,
 with compute_face_coef3d, 3d/quatfacops.m4:14-155, for the three gradient
 floor types of fortran/quat.f:1497-1537), computerhspbg
-(3d/quatrhs.m4:357-515) and one colour of the red-black FAC smoother
-(3d/ellipticfacops.m4:16-177).
+(3d/quatrhs.m4:357-515), one colour of the red-black FAC smoother
+(3d/ellipticfacops.m4:16-177) and the "kks" composition flux
+(KKSCompositionRHSStrategy.cc:98-441).
 The GPU leaf kernels are checked against the oracle to 1e-12, so these
 close the chain to the reference's formulas."""
 import ctypes as C
@@ -329,3 +330,41 @@ def test_rbgs_colour_3d(orc, offset):
     expect = np.where(colour, ui - res * dudr, ui)
     assert O.rel_l2(uo[1:-1, 1:-1, 1:-1], expect) <= 1e-14
     assert abs(mr - np.abs(res[colour]).max()) <= 1e-12 * max(1.0, mr)
+
+
+def test_kks_form_flux_3d(orc):
+    """The "kks" composition flux: concentration_pfmdiffusion
+    (3d/concentrationdiffusion.m4:14-128), the coupling coefficient of
+    KKSCompositionRHSStrategy::setDiffCoeffForPhaseOnPatch (:280-310) and
+    concentrationflux (3d/concentrationrhs.m4:14-104); coefficients from the
+    lagged (phi, cL, cS), differences of the current (phi, c)."""
+    m = configs.calphad3d(8, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 7, 6
+    m.dx[0], m.dx[1], m.dx[2] = 0.6, 0.9, 1.2
+    m.conc_form = abi.CONC_KKS
+    m.temp_mode = abi.TEMP_FIELD
+    m.D_liquid, m.D_solid, m.Q_liquid, m.Q_solid = 3.0, 0.02, 2.0e4, 5.0e4
+    m.energy_interp, m.avg_type = b"p", b"a"
+    rng = np.random.default_rng(11)
+    shp = m.interior_shape()
+    phid, cld, csd = (O.ghosted(m, rng.uniform(lo, hi, shp))
+                      for lo, hi in ((0, 1), (0.2, 0.5), (0.05, 0.3)))
+    phi, conc = O.ghosted(m, rng.uniform(0, 1, shp)), O.ghosted(m, rng.uniform(0.1, 0.5, shp))
+    temp = O.ghosted(m, rng.uniform(1400, 1600, shp))
+    fo = [np.zeros(s) for s in m.face_shapes()]
+    orc.orc_conc_flux_kks(C.byref(m), O.ptr(phid), O.ptr(cld), O.ptr(csd), O.ptr(temp),
+                          O.ptr(phi), O.ptr(conc), *[O.ptr(f) for f in fo])
+    R = 8.314472
+    sl = [np.s_[1:-1, 1:-1, 1:], np.s_[1:-1, 1:, 1:-1], np.s_[1:, 1:-1, 1:-1]]
+    sm = [np.s_[1:-1, 1:-1, :-1], np.s_[1:-1, :-1, 1:-1], np.s_[:-1, 1:-1, 1:-1]]
+    for d in range(3):
+        vphi = 0.5 * (phid[sm[d]] + phid[sl[d]])
+        h = _interp(vphi, b"p")
+        invT = 2.0 / (temp[sm[d]] + temp[sl[d]])
+        d0 = (1.0 - h) * (m.D_liquid * np.exp(-(m.Q_liquid / R) * invT)) \
+            + h * (m.D_solid * np.exp(-(m.Q_solid / R) * invT))
+        cl = 0.5 * (cld[sl[d]] + cld[sm[d]])
+        cs = 0.5 * (csd[sl[d]] + csd[sm[d]])
+        dphi = d0 * _dinterp(vphi, b"p") * (cl - cs)
+        r = (1.0 / m.dx[d]) * (d0 * (conc[sl[d]] - conc[sm[d]]) + dphi * (phi[sl[d]] - phi[sm[d]]))
+        assert O.rel_l2(fo[d], r) <= 1e-13
