@@ -9,8 +9,10 @@ the quaternion face coefficients (quatgrad_side, 3d/quatgrad.m4:213-335,
 with compute_face_coef3d, 3d/quatfacops.m4:14-155, for the three gradient
 floor types of fortran/quat.f:1497-1537), computerhspbg
 (3d/quatrhs.m4:357-515), one colour of the red-black FAC smoother
-(3d/ellipticfacops.m4:16-177) and the "kks" composition flux
-(KKSCompositionRHSStrategy.cc:98-441).
+(3d/ellipticfacops.m4:16-177), the "kks" composition flux
+(KKSCompositionRHSStrategy.cc:98-441), the quaternion mobility
+(3d/mobility.m4:13-95) and the quaternion right-hand side
+(3d/quatfacops.m4:227-311, 596-657).
 The GPU leaf kernels are checked against the oracle to 1e-12, so these
 close the chain to the reference's formulas."""
 import ctypes as C
@@ -368,3 +370,37 @@ def test_kks_form_flux_3d(orc):
         dphi = d0 * _dinterp(vphi, b"p") * (cl - cs)
         r = (1.0 / m.dx[d]) * (d0 * (conc[sl[d]] - conc[sm[d]]) + dphi * (phi[sl[d]] - phi[sm[d]]))
         assert O.rel_l2(fo[d], r) <= 1e-13
+
+
+def test_quat_mobility_and_rhs_3d(orc):
+    """quatmobility, type 'p' (3d/mobility.m4:13-95), then compute_flux3d +
+    add_quat_op3d (3d/quatfacops.m4:227-311, 596-657): q' = -M_q div(fc grad q)
+    per component."""
+    m = configs.polycrystal3d(8, seed=3, T=1500.0)
+    m.n[1], m.n[2] = 7, 6
+    m.dx[0], m.dx[1], m.dx[2] = 0.8, 1.0, 1.3
+    rng = np.random.default_rng(12)
+    shp = m.interior_shape()
+    phi = O.ghosted(m, rng.uniform(-0.1, 1.1, shp))
+    mq = np.zeros_like(phi)
+    orc.orc_quat_mobility(C.byref(m), O.ptr(phi), O.ptr(mq))
+    pc = np.clip(phi[1:-1, 1:-1, 1:-1], 0.0, 1.0)
+    mq_r = m.min_quat_mobility + (m.quat_mobility - m.min_quat_mobility) * (
+        1.0 - pc ** 3 * (10.0 - 15.0 * pc + 6.0 * pc * pc))
+    assert O.rel_l2(mq[1:-1, 1:-1, 1:-1], mq_r) <= 1e-15
+    g = rng.standard_normal((4,) + shp)
+    g /= np.linalg.norm(g, axis=0, keepdims=True)
+    q = np.ascontiguousarray(np.stack([O.ghosted(m, x) for x in g]))
+    fc = [rng.uniform(-2, -0.1, s) for s in m.face_shapes()]
+    out = np.empty(4 * m.cells())
+    orc.orc_quat_rhs(C.byref(m), *[O.ptr(f) for f in fc], O.ptr(mq), O.ptr(q), O.ptr(out))
+    out = out.reshape((4,) + shp)
+    hi = [1.0 / m.dx[d] for d in range(3)]
+    for c in range(4):
+        Q = q[c]
+        fx = fc[0] * hi[0] * (Q[1:-1, 1:-1, 1:] - Q[1:-1, 1:-1, :-1])
+        fy = fc[1] * hi[1] * (Q[1:-1, 1:, 1:-1] - Q[1:-1, :-1, 1:-1])
+        fz = fc[2] * hi[2] * (Q[1:, 1:-1, 1:-1] - Q[:-1, 1:-1, 1:-1])
+        div = ((fx[:, :, 1:] - fx[:, :, :-1]) * hi[0] + (fy[:, 1:, :] - fy[:, :-1, :]) * hi[1]
+               + (fz[1:, :, :] - fz[:-1, :, :]) * hi[2])
+        assert O.rel_l2(out[c], -mq_r * div) <= 1e-13
