@@ -11,8 +11,9 @@ floor types of fortran/quat.f:1497-1537), computerhspbg
 (3d/quatrhs.m4:357-515), one colour of the red-black FAC smoother
 (3d/ellipticfacops.m4:16-177), the "kks" composition flux
 (KKSCompositionRHSStrategy.cc:98-441), the quaternion mobility
-(3d/mobility.m4:13-95) and the quaternion right-hand side
-(3d/quatfacops.m4:227-311, 596-657).
+(3d/mobility.m4:13-95), the quaternion right-hand side
+(3d/quatfacops.m4:227-311, 596-657) and the CALPHAD driving force
+(CALPHADFreeEnergyStrategyBinary.cc:521-670).
 The GPU leaf kernels are checked against the oracle to 1e-12, so these
 close the chain to the reference's formulas."""
 import ctypes as C
@@ -404,3 +405,40 @@ def test_quat_mobility_and_rhs_3d(orc):
         div = ((fx[:, :, 1:] - fx[:, :, :-1]) * hi[0] + (fy[:, 1:, :] - fy[:, :-1, :]) * hi[1]
                + (fz[1:, :, :] - fz[:-1, :, :]) * hi[2])
         assert O.rel_l2(out[c], -mq_r * div) <= 1e-13
+
+
+def test_calphad_driving_force_3d(orc):
+    """CALPHADFreeEnergyStrategyBinary::addDrivingForce
+    (CALPHADFreeEnergyStrategyBinary.cc:521-670): rhs += h'(phi)
+    [(f_L(cL) - f_A(cA)) - mu_A(cA) (cL - cA)], energies per volume; the
+    free energy and its derivative are the oracle's (pinned on the
+    reference's CALPHAD known-answer tests)."""
+    import json
+    import os
+
+    from ampe_gb300.calphad_db import apply_database
+
+    m = configs.calphad3d(6, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 5, 4
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                           "calphad_AuNi.json")) as f:
+        apply_database(m, json.load(f))
+    m.temp_mode = abi.TEMP_CONSTANT
+    m.T0 = 1420.0
+    m.inv_molar_volume[0], m.inv_molar_volume[1] = 0.11, 0.13
+    rng = np.random.default_rng(13)
+    shp = m.interior_shape()
+    phi = O.ghosted(m, rng.uniform(0, 1, shp))
+    cl = O.ghosted(m, rng.uniform(0.2, 0.4, shp))
+    cs = O.ghosted(m, rng.uniform(0.05, 0.2, shp))
+    rhs = rng.standard_normal(shp)
+    r0 = rhs.copy()
+    orc.orc_add_driving_force(C.byref(m), None, O.ptr(phi), O.ptr(cl), O.ptr(cs), O.ptr(rhs))
+    fe = np.vectorize(lambda c, p: orc.orc_free_energy(C.byref(m), m.T0, c, p))
+    mu = np.vectorize(lambda c: orc.orc_dfdc(C.byref(m), m.T0, c, 1))
+    p, a, b = (x[1:-1, 1:-1, 1:-1] for x in (phi, cl, cs))
+    fl = fe(a, 0) * m.inv_molar_volume[0]
+    fa = fe(b, 1) * m.inv_molar_volume[1]
+    dF = (fl - fa) - mu(b) * m.inv_molar_volume[1] * (a - b)
+    expect = r0 + _dinterp(p, m.energy_interp) * dF
+    assert O.rel_l2(rhs, expect) <= 1e-13
