@@ -2,8 +2,8 @@
 Fortran loops) of stencil kernels that no reference known-answer test
 covers, checked against the oracle's C++ on random fields (CPU):
 gradient_flux (3d/quatrhs.m4:12-66), compute_flux_isotropic
-(2d/quatrhs.m4:106-151), the 2D anisotropic_gradient_flux
-(2d/quatrhs.m4:154-256), concentration_pfmdiffusion_of_temperature
+(2d/quatrhs.m4:106-151), the 2D and 3D anisotropic_gradient_flux
+(2d/quatrhs.m4:154-256, 3d/quatrhs.m4:149-349), concentration_pfmdiffusion_of_temperature
 (3d/concentrationdiffusion.m4:310-428), add_flux (3d/flux.m4:15-100) and
 the quaternion face coefficients (quatgrad_side, 3d/quatgrad.m4:213-335,
 with compute_face_coef3d, 3d/quatfacops.m4:14-155, for the three gradient
@@ -442,3 +442,79 @@ def test_calphad_driving_force_3d(orc):
     dF = (fl - fa) - mu(b) * m.inv_molar_volume[1] * (a - b)
     expect = r0 + _dinterp(p, m.energy_interp) * dF
     assert O.rel_l2(rhs, expect) <= 1e-13
+
+
+def _qmul(a, b):
+    """quatmult4 (fortran/quat.f:867-894)."""
+    return np.array([a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3],
+                     a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2],
+                     a[0] * b[2] + a[2] * b[0] + a[3] * b[1] - a[1] * b[3],
+                     a[0] * b[3] + a[3] * b[0] + a[1] * b[2] - a[2] * b[1]])
+
+
+def _dgamma(q, n):
+    """compute_dgamma (3d/quatrhs.m4:149-178)."""
+    qp = np.array([q[0], -q[1], -q[2], -q[3]])
+    npr = _qmul(q, _qmul(n, qp))
+    n4 = npr[1] ** 4 + npr[2] ** 4 + npr[3] ** 4
+    dg = np.array([0.0, npr[1] * (npr[1] ** 2 - n4), npr[2] * (npr[2] ** 2 - n4),
+                   npr[3] * (npr[3] ** 2 - n4)])
+    return _qmul(qp, _qmul(dg, q)), n4
+
+
+def test_anisotropic_flux_3d(orc):
+    """anisotropic_gradient_flux 3D (3d/quatrhs.m4:180-349): cubic
+    anisotropy through the quaternion rotation of the interface normal."""
+    m = configs.calphad3d(7, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 6, 5
+    m.dx[0], m.dx[1], m.dx[2] = 0.8, 1.0, 1.2
+    m.flux_type = abi.FLUX_ANISOTROPIC
+    m.aniso_eps, m.qlen, m.epsilon_phi = 0.05, 4, 1.3
+    rng = np.random.default_rng(14)
+    shp = m.interior_shape()
+    ph = O.ghosted(m, rng.uniform(0, 1, shp))
+    g = rng.standard_normal((4,) + shp)
+    g /= np.linalg.norm(g, axis=0, keepdims=True)
+    q = np.ascontiguousarray(np.stack([O.ghosted(m, x) for x in g]))
+    fo = _oracle_flux(orc, m, ph, q)
+    eps, e4 = m.epsilon_phi, m.aniso_eps
+    factor = 4.0 * e4 / (1.0 - 3.0 * e4)
+    dxi, dyi, dzi = (1.0 / m.dx[d] for d in range(3))
+    nx, ny, nz = m.n[0], m.n[1], m.n[2]
+
+    def P(i, j, k):
+        return ph[k + 1, j + 1, i + 1]
+
+    def flux(dpx, dpy, dpz, qa, qb, comp):
+        g2 = dpx * dpx + dpy * dpy + dpz * dpz
+        if abs(g2) > 1e-12:
+            nn = np.array([0.0, dpx, dpy, dpz]) / np.sqrt(g2)
+            dg, n4 = _dgamma(0.5 * (qa + qb), nn)
+        else:
+            dg, n4 = np.array([0.0, 0.0, 0.0, 1.0]), 0.0
+        gam = eps * (1.0 - 3.0 * e4) * (1.0 + factor * n4)
+        dp = (dpx, dpy, dpz)[comp - 1]
+        return gam * gam * dp + 16.0 * eps * gam * e4 * np.sqrt(g2) * dg[comp]
+
+    rx = np.empty((nz, ny, nx + 1))
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx + 1):
+                dpx = (P(i, j, k) - P(i - 1, j, k)) * dxi
+                dpy = 0.25 * (P(i - 1, j + 1, k) - P(i - 1, j - 1, k) + P(i, j + 1, k)
+                              - P(i, j - 1, k)) * dyi
+                dpz = 0.25 * (P(i - 1, j, k + 1) - P(i - 1, j, k - 1) + P(i, j, k + 1)
+                              - P(i, j, k - 1)) * dzi
+                rx[k, j, i] = flux(dpx, dpy, dpz, q[:, k + 1, j + 1, i], q[:, k + 1, j + 1, i + 1], 1)
+    rz = np.empty((nz + 1, ny, nx))
+    for k in range(nz + 1):
+        for j in range(ny):
+            for i in range(nx):
+                dpx = 0.25 * (P(i + 1, j, k - 1) - P(i - 1, j, k - 1) + P(i + 1, j, k)
+                              - P(i - 1, j, k)) * dxi
+                dpy = 0.25 * (P(i, j + 1, k - 1) - P(i, j - 1, k - 1) + P(i, j + 1, k)
+                              - P(i, j - 1, k)) * dyi
+                dpz = (P(i, j, k) - P(i, j, k - 1)) * dzi
+                rz[k, j, i] = flux(dpx, dpy, dpz, q[:, k, j + 1, i + 1], q[:, k + 1, j + 1, i + 1], 3)
+    assert O.rel_l2(fo[0], rx) <= 1e-12
+    assert O.rel_l2(fo[2], rz) <= 1e-12
