@@ -8,8 +8,9 @@ gradient_flux (3d/quatrhs.m4:12-66), compute_flux_isotropic
 the quaternion face coefficients (quatgrad_side, 3d/quatgrad.m4:213-335,
 with compute_face_coef3d, 3d/quatfacops.m4:14-155, for the three gradient
 floor types of fortran/quat.f:1497-1537), computerhspbg
-(3d/quatrhs.m4:357-515), one colour of the red-black FAC smoother
-(3d/ellipticfacops.m4:16-177), the "kks" composition flux
+(3d/quatrhs.m4:357-515), one colour of the red-black FAC smoother and
+the FAC residual (3d/ellipticfacops.m4:16-177, 448-511), the phase block's
+C coefficient (PhaseFACOps.cc:101-183), the "kks" composition flux
 (KKSCompositionRHSStrategy.cc:98-441), the quaternion mobility
 (3d/mobility.m4:13-95), the quaternion right-hand side
 (3d/quatfacops.m4:227-311, 596-657) and the CALPHAD driving force
@@ -518,3 +519,37 @@ def test_anisotropic_flux_3d(orc):
                 rz[k, j, i] = flux(dpx, dpy, dpz, q[:, k, j + 1, i + 1], q[:, k + 1, j + 1, i + 1], 3)
     assert O.rel_l2(fo[0], rx) <= 1e-12
     assert O.rel_l2(fo[2], rz) <= 1e-12
+
+
+def test_fac_residual_and_phase_c_3d(orc):
+    """efo_compresvarsca3d (3d/ellipticfacops.m4:448-511) and
+    PhaseFACOps::setCOnPatchPrivate (PhaseFACOps.cc:101-183): C = 1 + gamma M
+    w g''(phi), double well 'd' (g'' = 32 (1 - 6 phi + 6 phi^2),
+    functions.f:304-330)."""
+    m = configs.calphad3d(7, seed=3, T_run=1500.0)
+    m.n[1], m.n[2] = 6, 5
+    m.dx[0], m.dx[1], m.dx[2] = 0.7, 1.0, 1.3
+    m.phase_mobility, m.phase_well_scale = 1.7, 0.4
+    rng = np.random.default_rng(15)
+    shp = m.interior_shape()
+    phi = O.ghosted(m, rng.uniform(0, 1, shp))
+    cc = np.zeros_like(phi)
+    orc.orc_phase_fac_set_c(C.byref(m), O.ptr(phi), 0.3, O.ptr(cc))
+    p = phi[1:-1, 1:-1, 1:-1]
+    c_r = 1.0 + (0.3 * m.phase_mobility) * m.phase_well_scale * (32.0 * (1.0 - 6.0 * p + 6.0 * p * p))
+    assert O.rel_l2(cc[1:-1, 1:-1, 1:-1], c_r) <= 1e-15
+    D = [rng.uniform(-2.0, -0.5, s) for s in m.face_shapes()]
+    Mc = O.ghosted(m, rng.uniform(0.5, 1.5, shp))
+    f = O.ghosted(m, rng.uniform(-1, 1, shp))
+    u = O.ghosted(m, rng.uniform(-1, 1, shp))
+    res = np.zeros_like(u)
+    orc.orc_efo_residual(C.byref(m), *[O.ptr(a) for a in D], 0.0, O.ptr(cc), 0.0, O.ptr(Mc), 0.0,
+                         O.ptr(f), O.ptr(u), O.ptr(res))
+    dxi = [1.0 / m.dx[d] for d in range(3)]
+    fx = dxi[0] * D[0] * (u[1:-1, 1:-1, 1:] - u[1:-1, 1:-1, :-1])
+    fy = dxi[1] * D[1] * (u[1:-1, 1:, 1:-1] - u[1:-1, :-1, 1:-1])
+    fz = dxi[2] * D[2] * (u[1:, 1:-1, 1:-1] - u[:-1, 1:-1, 1:-1])
+    Mi, fi, ui = (a[1:-1, 1:-1, 1:-1] for a in (Mc, f, u))
+    r = fi - Mi * (dxi[0] * (fx[:, :, 1:] - fx[:, :, :-1]) + dxi[1] * (fy[:, 1:, :] - fy[:, :-1, :])
+                   + dxi[2] * (fz[1:, :, :] - fz[:-1, :, :])) - c_r * ui
+    assert O.rel_l2(res[1:-1, 1:-1, 1:-1], r) <= 1e-14
