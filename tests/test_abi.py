@@ -105,3 +105,36 @@ def test_version_string():
     from ampe_gb300 import _native
 
     assert b"sm_103a" in _native.lib.ampe_version()
+
+
+@pytest.mark.parametrize("case", ["krylov", "precision", "aniso3d_mixed", "aniso_qlen",
+                                  "quat_qlen", "quat_mobility", "precond"])
+def test_stepper_rejects_unsupported_combinations(case):
+    """ampe_stepper_create validates the model and the parameters on the
+    host, before it looks for a device."""
+    from ampe_gb300 import _native
+
+    L = _native.lib
+    m = configs.dilute2d(16)
+    p = configs.step_params()
+    if case == "krylov":
+        p.max_krylov = 17  # the Krylov basis is sized for at most 16
+    elif case == "precision":
+        p.precision = 2
+    elif case == "aniso3d_mixed":
+        m = configs.calphad3d(8)
+        m.flux_type, m.qlen = abi.FLUX_ANISOTROPIC, 4
+        p.precision = 1  # the mixed path linearises the 2D anisotropic flux only
+    elif case == "aniso_qlen":
+        m.flux_type, m.qlen = abi.FLUX_ANISOTROPIC, 3
+    elif case == "quat_qlen":
+        m = configs.polycrystal3d(8)
+        m.flux_type, m.qlen = abi.FLUX_ANISOTROPIC, 2
+    elif case == "quat_mobility":
+        m = configs.polycrystal3d(8)
+        m.quat_grad_floor = 0.0
+    elif case == "precond":
+        p.precond = 3
+    h = C.c_void_p()
+    assert L.ampe_stepper_create(C.byref(m), C.byref(p), C.byref(h)) == abi.AMPE_ERR_INVALID
+    assert not h.value
