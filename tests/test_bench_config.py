@@ -39,3 +39,14 @@ def test_small_workload_states():
     for kind, n in (("calphad", 16), ("poly", 16), ("dendrite", 32), ("dilute", 32)):
         m, st = bench.workload(n, kind)
         assert st.phi.size == m.cells() and st.c.size == m.cells()
+
+
+def test_l2_policy():
+    """The 256^3 headline streams its state from HBM (twice the L2); levels
+    whose state fits in L2 are flushed before every timed step."""
+    for kind, n, flush in (("calphad", 256, False), ("poly", 512, False), ("poly", 128, True),
+                           ("dendrite", 2048, True), ("dilute", 256, True)):
+        a = _args(kind, n)
+        m, _ = bench.workload(a.n, kind, state=False)
+        assert bench.flushes_l2(a, m) == flush, (kind, n)
+        assert ("flushed" in bench.arm_config(a)["l2"]) == flush
