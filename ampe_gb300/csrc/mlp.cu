@@ -7,8 +7,9 @@
 // layout, accumulators in tensor memory read back with tcgen05.ld; the bias
 // + SiLU epilogue runs on packed bf16x2 and writes the next layer's operand.
 // Training (forward, backward, Adam) runs in FP32 on the CUDA cores with the
-// weights rounded to BF16 in the forward pass; its FLOPs are small next to
-// one inference pass over a 256^3 level.
+// weights rounded to BF16 in the forward pass; 2000 steps of 4096 samples
+// are about 4e11 FLOP, one to two inference passes over a 256^3 level, and
+// take about 0.6 s once per run.
 //
 // Labels come from the FP64 KKS Newton (kks_newton), started from (c, c).
 #include <cuda_bf16.h>
