@@ -183,6 +183,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def kernel_rooflines(kt, per_cell, N, pk):
+    """Achieved algorithmic bandwidth (GB/s) or tensor rate (TFLOP/s) of every
+    instrumented kernel kind: bytes (or FLOP) per cell x cells x launches over
+    the kind's summed CUDA-event time."""
+    out = {}
+    for k, v in kt.items():
+        if not v["launches"] or v["ms"] <= 0.0:
+            continue
+        sec = v["ms"] / 1e3
+        if k == "mlp_infer_tc":
+            a = MLP_FLOPS_PER_CELL * N * v["launches"] / sec / 1e12
+            out[k] = {"achieved": a, "unit": "TFLOP/s", "frac": a / pk["bf16_tflops"]}
+        elif k in per_cell:
+            a = per_cell[k] * N * v["launches"] / sec / 1e9
+            out[k] = {"achieved": a, "unit": "GB/s", "frac": a / pk["hbm_gbs"],
+                      "bytes_per_cell": per_cell[k]}
+    return out
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -608,6 +627,7 @@ def run_ours(args):
         "paths": paths,
         "surrogate": sur_info,
         "roofline": roof,
+        "kernel_rooflines": kernel_rooflines(kt, per_cell, N, pk),
         "kernels": res_h["kernels"],
         "stats": res_h["stats"],
         "gpu_launches": res_h["launches"],

@@ -50,3 +50,15 @@ def test_l2_policy():
         m, _ = bench.workload(a.n, kind, state=False)
         assert bench.flushes_l2(a, m) == flush, (kind, n)
         assert ("flushed" in bench.arm_config(a)["l2"]) == flush
+
+
+def test_kernel_rooflines():
+    kt = {"kks_newton": {"ms": 2.0, "launches": 4}, "smooth_fine": {"ms": 1.0, "launches": 10},
+          "mlp_infer_tc": {"ms": 0.0, "launches": 0}, "quat_rhs": {"ms": 0.0, "launches": 0},
+          "precond_solve": {"ms": 5.0, "launches": 3}}
+    per_cell = {"kks_newton": 36, "smooth_fine": 20}
+    pk = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+    r = bench.kernel_rooflines(kt, per_cell, 1000000, pk)
+    assert set(r) == {"kks_newton", "smooth_fine"}
+    assert abs(r["kks_newton"]["achieved"] - 36 * 1e6 * 4 / 2e-3 / 1e9) < 1e-9
+    assert abs(r["smooth_fine"]["frac"] - (20 * 1e6 * 10 / 1e-3 / 1e9) / 6800.0) < 1e-12
