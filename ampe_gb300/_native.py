@@ -54,6 +54,8 @@ _PROTOS = {
     "ampe_stepper_set_state": (I, [P, P, P, P, P, P, I]),
     "ampe_stepper_get_state": (I, [P, P, P, P, P, I]),
     "ampe_stepper_advance": (I, [P, I, C.POINTER(abi.StepStats)]),
+    "ampe_stepper_advance_to": (I, [P, D, I, C.POINTER(abi.StepStats)]),
+    "ampe_stepper_set_temperature": (I, [P, D, D]),
     "ampe_stepper_eval_rhs": (I, [P, P, P, I]),
     "ampe_stepper_kernel_launches": (C.c_longlong, [P]),
     "ampe_stepper_load_y": (I, [P, P, P, I]),
@@ -64,6 +66,7 @@ _PROTOS = {
     "ampe_stepper_size": (C.c_longlong, [P]),
     "ampe_stepper_eval_rhs_full": (I, [P, P, I]),
     "ampe_stepper_stream": (P, [P]),
+    "ampe_stepper_set_stream": (I, [P, P]),
     "ampe_stepper_profile": (I, [P, I]),
     "ampe_stepper_kernel_time": (I, [P, I, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "ampe_stepper_attach_surrogate": (I, [P, P]),
@@ -78,6 +81,8 @@ _PROTOS = {
     "ampe_mlp_set_normalization": (I, [P, D, D]),
     "ampe_mlp_infer": (I, [P, MP, P, P, P, P, P, I, P]),
     "ampe_mlp_status": (I, [P]),
+    "ampe_mlp_clear_status": (I, [P]),
+    "ampe_mlp_set_wait_limit": (I, [P, I, I]),
 }
 
 for _name, (_res, _args) in _PROTOS.items():

@@ -80,7 +80,7 @@ class Model(C.Structure):
         ("quat_mobility_type", C.c_char),
         ("pad1", C.c_char * 6),
         ("conc_form", C.c_int),
-        ("pad2", C.c_int),
+        ("ng_side", C.c_int),
     ]
 
     def cells(self):
@@ -98,10 +98,14 @@ class Model(C.Structure):
         return (nz, self.n[1], self.n[0])
 
     def face_shapes(self):
+        """(z, y, x) shapes of the three side arrays, ghost width ng_side
+        (no z ghosts in 2D)."""
+        g = self.ng_side
+        gz = g if self.dim == 3 else 0
         nz = self.n[2] if self.dim == 3 else 1
         nx, ny = self.n[0], self.n[1]
-        s = [(nz, ny, nx + 1), (nz, ny + 1, nx)]
-        s.append((nz + 1, ny, nx) if self.dim == 3 else (1, 1, 1))
+        s = [(nz + 2 * gz, ny + 2 * g, nx + 1 + 2 * g), (nz + 2 * gz, ny + 1 + 2 * g, nx + 2 * g)]
+        s.append((nz + 1 + 2 * gz, ny + 2 * g, nx + 2 * g) if self.dim == 3 else (1, 1, 1))
         return s
 
 
@@ -128,6 +132,9 @@ class StepParams(C.Structure):
         ("precision", C.c_int),
         ("surrogate", C.c_int),
         ("max_retries", C.c_int),
+        ("adaptive", C.c_int),
+        ("h_max", C.c_double),
+        ("h_min", C.c_double),
     ]
 
 
@@ -151,7 +158,8 @@ class StepStats(C.Structure):
             "step_retries",
             "kks_fp64_cells",
         )
-    ] + [("t", C.c_double)]
+    ] + [("t", C.c_double), ("err_test_fails", C.c_longlong), ("h_last", C.c_double),
+         ("h_next", C.c_double), ("q_last", C.c_int), ("q_next", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -6,6 +6,7 @@
 // liquidus_slope and keq).
 #pragma once
 
+#include <atomic>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,6 +28,7 @@ struct Grid {
    // entries (enforced by check_model).
    int dim, n0, n1, n2, ng, gz;
    int sx, sy;  // row and plane pitch of the ghosted layout
+   int gs, gsz;  // ghost width of side (face) arrays, in-plane and along z
    // divisors of the index decompositions: n0, n1, n0+1, n1+1, (n0+1)/2
    FastDiv fd0, fd1, fd0p, fd1p, fdh;
    // linear index t < 2^31 over an (a.d x b.d x *) box -> (i, j, k)
@@ -50,11 +52,27 @@ struct Grid {
       return ((k + gz) * (n1 + 2 * ng) + (j + ng)) * sx + (i + ng);
    }
    AMPE_HD int interior(int i, int j, int k) const { return (k * n1 + j) * n0 + i; }
-   AMPE_HD int fx(int i, int j, int k) const { return (k * n1 + j) * (n0 + 1) + i; }
-   AMPE_HD int fy(int i, int j, int k) const { return (k * (n1 + 1) + j) * n0 + i; }
-   AMPE_HD int fz(int i, int j, int k) const { return (k * n1 + j) * n0 + i; }
+   // side arrays (SAMRAI SideData of ghost width gs): normal d has extent
+   // n_d + 1 + 2 gs along d and n_e + 2 gs along the others (no z ghosts
+   // in 2D)
+   AMPE_HD int fx(int i, int j, int k) const
+   {
+      return ((k + gsz) * (n1 + 2 * gs) + (j + gs)) * (n0 + 1 + 2 * gs) + (i + gs);
+   }
+   AMPE_HD int fy(int i, int j, int k) const
+   {
+      return ((k + gsz) * (n1 + 1 + 2 * gs) + (j + gs)) * (n0 + 2 * gs) + (i + gs);
+   }
+   AMPE_HD int fz(int i, int j, int k) const
+   {
+      return ((k + gsz) * (n1 + 2 * gs) + (j + gs)) * (n0 + 2 * gs) + (i + gs);
+   }
+   // index distance to the next y face (y-side arrays) and z face (z-side)
+   AMPE_HD int fys() const { return n0 + 2 * gs; }
+   AMPE_HD int fzs() const { return (n0 + 2 * gs) * (n1 + 2 * gs); }
    AMPE_HD long long cells() const { return (long long)n0 * n1 * n2; }
    AMPE_HD long long cells_ghost() const { return (long long)sy * (n2 + 2 * gz); }
+   // interior faces of each normal (the faces the kernels compute)
    AMPE_HD long long nfx() const { return (long long)(n0 + 1) * n1 * n2; }
    AMPE_HD long long nfy() const { return (long long)n0 * (n1 + 1) * n2; }
    AMPE_HD long long nfz() const { return (long long)n0 * n1 * (n2 + 1); }
@@ -71,6 +89,8 @@ inline Grid make_grid(const ampe_model_t& m)
    g.gz = m.dim == 3 ? m.ng : 0;
    g.sx = g.n0 + 2 * g.ng;
    g.sy = g.sx * (g.n1 + 2 * g.ng);
+   g.gs = m.ng_side;
+   g.gsz = m.dim == 3 ? m.ng_side : 0;
    g.fd0 = FastDiv((unsigned)g.n0);
    g.fd1 = FastDiv((unsigned)g.n1);
    g.fd0p = FastDiv((unsigned)(g.n0 + 1));
@@ -397,12 +417,26 @@ inline int launch_status()
    cudaError_t e = cudaGetLastError();
    return e == cudaSuccess ? AMPE_OK : AMPE_ERR_CUDA;
 }
-// grid cap of the grid-stride kernels: 32 blocks of 256 per SM.  Threads
-// then loop over several items and set up their per-thread constants once
-// (measured faster than one thread per item for the stencil kernels, whose
-// setup includes FP64 work; the smoother colour and residual kernels run one
-// thread per item instead)
-constexpr long long kMaxBlocks = 152 * 32;
+// multiprocessor count of the current device (queried once per device)
+int device_sms();
+// true on the first call with this flag on the current device: for one-time
+// set-up that applies to one device only (cudaFuncSetAttribute)
+inline bool first_on_device(std::atomic<unsigned long long>& seen)
+{
+   int dev = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess) return true;
+   const unsigned long long bit = 1ull << (dev & 63);
+   return !(seen.fetch_or(bit) & bit);
+}
+// grid cap of the grid-stride kernels: per_sm blocks (32 by default, of 256
+// threads) per SM of the current device.  Threads then loop over several
+// items and set up their per-thread constants once (measured faster than one
+// thread per item for the stencil kernels, whose setup includes FP64 work;
+// the smoother colour and residual kernels run one thread per item instead)
+inline long long max_blocks(int per_sm = 32)
+{
+   return (long long)device_sms() * per_sm;
+}
 inline unsigned grid_for(long long n, int block)
 {
    return (unsigned)((n + block - 1) / block);

@@ -8,7 +8,10 @@
 
 namespace ampe {
 
-constexpr int kRedBlocks = 1216;  // 8 blocks per SM on 152 SMs
+// partial sums of the deterministic two-pass reductions: a fixed count (8
+// per SM of a GB300), so that the summation order, and with it every
+// reduced value, is the same on any device
+constexpr int kRedBlocks = 1216;
 constexpr int kRedThreads = 256;
 
 template <class F>
@@ -82,7 +85,7 @@ __global__ void k_map(long long n, F f)
 inline unsigned map_blocks(long long n)
 {
    long long b = (n + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    return (unsigned)(b < 1 ? 1 : b);
 }
 

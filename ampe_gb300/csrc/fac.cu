@@ -81,7 +81,7 @@ __device__ __forceinline__ R op_residual_u(const FacOp<R>& op, const Grid& g,
       if (HD) {
          const int fi = g.fy(i, j, k);
          Dm = op.D1[fi];
-         Dp = op.D1[fi + g.n0];
+         Dp = op.D1[fi + g.fys()];
       }
       const R fm = dxi * Dm * (uc - U(c - g.sx, 0, -1, 0));
       const R fp = dxi * Dp * (U(c + g.sx, 0, 1, 0) - uc);
@@ -94,7 +94,7 @@ __device__ __forceinline__ R op_residual_u(const FacOp<R>& op, const Grid& g,
       if (HD) {
          const int fi = g.fz(i, j, k);
          Dm = op.D2[fi];
-         Dp = op.D2[fi + g.n0 * g.n1];
+         Dp = op.D2[fi + g.fzs()];
       }
       const R fm = dxi * Dm * (uc - U(c - g.sy, 0, 0, -1));
       const R fp = dxi * Dp * (U(c + g.sy, 0, 0, 1) - uc);
@@ -223,7 +223,7 @@ int fill_ghosts_t(const Grid& g, R* f, cudaStream_t s)
    const long long tot = 2LL * g.gz * SX * SY + (long long)g.n2 * 2 * g.ng * SX +
                          (long long)g.n2 * g.n1 * 2 * g.ng;
    long long b = (tot + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    k_fill_ghosts_gather<R><<<(unsigned)(b < 1 ? 1 : b), 256, 0, s>>>(g, f);
    return launch_status();
 }
@@ -470,12 +470,12 @@ static int launch_sweep(const FacOp<R>& op, const Grid& g, const R* f, const R* 
 {
    using B = SweepBox<DIM>;
    const size_t smem = rb_sweep_smem(op, DIM);
-   static bool attr = false;  // opt in to more than 48 KB once per instantiation
-   if (!attr) {
+   // opt in to more than 48 KB once per instantiation and device
+   static std::atomic<unsigned long long> attr{0};
+   if (first_on_device(attr)) {
       const int most = (int)(sizeof(R) * (size_t)(B::NU + 3 * B::NC));  // f, C and M staged
       cudaFuncSetAttribute(k_rb_sweep<R, DIM, ZERO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            most);
-      attr = true;
    }
    const dim3 grid((g.n0 + B::TX - 1) / B::TX, (g.n1 + B::TY - 1) / B::TY,
                    DIM == 3 ? (g.n2 + B::TZ - 1) / B::TZ : 1);
@@ -551,7 +551,7 @@ __global__ void k_phase_set_c(Grid g, const double* phi, double gamma,
 static unsigned nblocks(long long n)
 {
    long long b = (n + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    return (unsigned)(b < 1 ? 1 : b);
 }
 
@@ -798,6 +798,14 @@ int ampe_efo_rbgs_sweep(const ampe_model_t* m, const double* dface0,
    if (!rb_sweep_fusable<double>(g)) return AMPE_ERR_INVALID;
    FacOp<double> op = make_op(m, dface0, dface1, dface2, d_const, ccell, c_const, mcell,
                               m_const);
+   // the z-marching sweep for the operator shapes of the phase, composition
+   // and quaternion blocks on large 3D levels, else the box sweep
+   ZShape zs;
+   if (sweep_z_ok<double>(g, &zs)) {
+      const int rc = sweep_z(op, g, zs, rhs, u_in, u_out, nullptr, (const double*)nullptr,
+                             (cudaStream_t)stream);
+      if (rc != AMPE_ERR_INVALID) return rc;
+   }
    return rb_sweep_fused(op, g, rhs, u_in, u_out, (cudaStream_t)stream);
 }
 

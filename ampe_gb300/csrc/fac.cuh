@@ -57,6 +57,31 @@ template <class R>
 int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
                 double gamma, R* ccell, cudaStream_t s);
 
+// One red-black sweep of a 3D level in a single z-marching pass (sweep_z.cu):
+// blocks of ty rows x the whole x extent x kz planes, u staged in a ring of
+// kZRingPlanes shared-memory planes, rows stored colour-split with halves
+// hs elements apart.
+constexpr int kZRingPlanes = 6;
+struct ZShape {
+   int ty = 0, kz = 0, nh = 0, hs = 0;
+};
+template <class R>
+inline size_t zsweep_smem_bytes(const ZShape& z)
+{
+   return sizeof(R) * (size_t)kZRingPlanes * (size_t)(z.ty + 4) * 2 * (size_t)z.hs;
+}
+// whether the level takes the single-pass sweep (3D, even extents, at least
+// 2^21 cells, shape fits in shared memory); the chosen shape into *out
+template <class R>
+bool sweep_z_ok(const Grid& g, ZShape* out);
+// uin -> uout (uin != uout; ghost images of uout written).  uin null: start
+// from u = 0.  e non-null: start from uin + P e, e the correction on the
+// next coarser level gc (ghosts current), P piecewise constant.  The result
+// equals two rbgs_color passes (red, black) on the same start.
+template <class R>
+int sweep_z(const FacOp<R>& op, const Grid& g, const ZShape& zs, const R* f, const R* uin,
+            R* uout, const Grid* gc, const R* e, cudaStream_t s);
+
 int fill_ghosts(const Grid& g, double* f, cudaStream_t s);
 long long residual_rms_scratch_doubles(const Grid& g);
 int residual_rms_into(const FacOp<double>& op, const Grid& g, const double* f,

@@ -119,7 +119,7 @@ int kks_interior(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
                  double* dF, unsigned long long* counters, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
-   if (b > 152 * 16) b = 152 * 16;
+   if (b > max_blocks(16)) b = max_blocks(16);
    k_kks_interior<<<(unsigned)b, 256, 0, s>>>(m, g, tab, tfield, phi, conc,
                                               clr, csr, cl, cs, dF, counters);
    return launch_status();
@@ -232,7 +232,7 @@ int rhs_fused(const ampe_model_t& m, const Grid& g, const double* phi,
 {
    if (m.conc_form == AMPE_CONC_KKS && (!conc || !cld || !csd)) return AMPE_ERR_INVALID;
    long long b = (g.cells() + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    if (quat)
       k_rhs_fused<true><<<(unsigned)b, 256, 0, s>>>(
           m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, conc, cld, csd, phi_rhs,

@@ -4,6 +4,7 @@
 // (ghosted cell arrays, ghost-free side arrays) so that a SAMRAI adapter can
 // hand them patch data directly.  The fused hot-path kernels live in
 // fused.cu; these are the drop-in / parity surface.
+#include <atomic>
 #include <cstdio>
 
 #include "common.cuh"
@@ -13,6 +14,24 @@
 namespace ampe {
 
 long long g_launches = 0;
+
+int device_sms()
+{
+   constexpr int kDevs = 64;
+   static std::atomic<int> sms[kDevs];
+   int dev = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevs) dev = -1;
+   if (dev >= 0) {
+      const int v = sms[dev].load(std::memory_order_relaxed);
+      if (v > 0) return v;
+   }
+   int n = 0;
+   if (dev < 0 || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) !=
+                      cudaSuccess || n < 1)
+      return 152;  // no device to ask: the GB300's count (launches fail anyway)
+   sms[dev].store(n, std::memory_order_relaxed);
+   return n;
+}
 
 int check_model(const ampe_model_t* m)
 {
@@ -30,7 +49,11 @@ int check_model(const ampe_model_t* m)
    const long long e0 = m->n[0], e1 = m->n[1], e2 = m->dim == 3 ? m->n[2] : 1;
    const long long gz = m->dim == 3 ? m->ng : 0;
    const long long ghost = (e0 + 2 * m->ng) * (e1 + 2 * m->ng) * (e2 + 2 * gz);
-   const long long faces = (e0 + 1) * e1 * e2 + e0 * (e1 + 1) * e2 + e0 * e1 * (e2 + 1);
+   if (m->ng_side < 0) return AMPE_ERR_INVALID;
+   const long long s = m->ng_side, sz = m->dim == 3 ? s : 0;
+   const long long faces = (e0 + 1 + 2 * s) * (e1 + 2 * s) * (e2 + 2 * sz) +
+                           (e0 + 2 * s) * (e1 + 1 + 2 * s) * (e2 + 2 * sz) +
+                           (e0 + 2 * s) * (e1 + 2 * s) * (e2 + 1 + 2 * sz);
    if (ghost > lim || faces > lim) return AMPE_ERR_TOO_LARGE;
    return AMPE_OK;
 }
@@ -312,7 +335,7 @@ static cudaStream_t S(void* s) { return (cudaStream_t)s; }
 static unsigned blocks_for(long long n)
 {
    long long b = (n + 255) / 256;
-   if (b > 152 * 64) b = 152 * 64;
+   if (b > max_blocks(64)) b = max_blocks(64);
    return (unsigned)(b < 1 ? 1 : b);
 }
 

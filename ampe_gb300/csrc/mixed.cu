@@ -2,12 +2,14 @@
 //
 // The outer Newton residual G(y) = y - gamma f(y) - a, the Krylov vectors,
 // their inner products and the WRMS norms stay FP64 (stepper.cu).  Inside:
-//  k_kks_mixed   per-cell KKS Newton in FP32 (logf, FP32 Redlich-Kister
-//                polynomials); cells whose solution lies within 1e-4 of
-//                c = 0 or 1 get an FP64 Newton polish from the FP32 result
-//                (and an FP64 driving force).  Optional initial guess from
-//                the surrogate MLP; cells not converged within 3 iterations
-//                from it restart from the plain warm start.
+//  k_kks_f32 /   per-cell KKS Newton in FP32 (logf, FP32 Redlich-Kister
+//  k_kks_polish64 polynomials); cells whose solution lies within 1e-4 of
+//                c = 0 or 1 (or that FP32 did not converge) are listed and
+//                get an FP64 Newton polish from the FP32 result (and an FP64
+//                driving force) in a second kernel over the list.  Optional
+//                initial guess from the surrogate MLP; cells not converged
+//                within 3 iterations from it restart from the plain warm
+//                start.
 //  k_rhs_mixed   the fused phase + composition right-hand side in FP32
 //                arithmetic, FP64 in/out.
 //  k_jv_point /  the Jacobian-vector product of f written out analytically
@@ -147,26 +149,31 @@ __device__ __forceinline__ CoefF coef_f_at(const ampe_model_t& m,
    return to_f(thermo_coef(m, temperature_at(m, g, tfield, i, j, k)));
 }
 
-__global__ void k_kks_mixed(ampe_model_t m, MixParams mp, Grid g, const ThermoCoef* tab,
-                            const CoefF* tabf, const double* tfield,
-                            const double* phi, const double* conc,
-                            const float* guess_l, const float* guess_s,
-                            const float* clr, const float* csr, float* cl,
-                            float* cs, float* dF, unsigned long long* counters)
+// FP32 pass over every cell.  Cells whose FP32 Newton converged away from
+// c = 0 and 1 are finished here (cL, cS with images, dF); the others are
+// appended to `list` (interior index t, bit 31 set when the FP32 iterate is
+// converged and is the FP64 start) for k_kks_polish64.  The rare FP64 path
+// stays out of this kernel, so it runs at the FP32 path's register count.
+__global__ void __launch_bounds__(256, 4)
+    k_kks_f32(ampe_model_t m, MixParams mp, Grid g, const CoefF* tabf, const double* tfield,
+              const double* __restrict__ phi, const double* __restrict__ conc,
+              const float* __restrict__ guess_l, const float* __restrict__ guess_s,
+              const float* __restrict__ clr, const float* __restrict__ csr, float* cl,
+              float* cs, float* __restrict__ dF, int* __restrict__ list,
+              unsigned long long* counters)
 {
-   // counters: [0] FP32 iterations, [1] failed cells, [2] FP64-polished
-   //           cells, [3] surrogate fallbacks, [4] FP64 iterations
-   unsigned long long it32 = 0, fails = 0, n64 = 0, nfb = 0, it64 = 0;
+   // counters: [0] FP32 iterations, [3] surrogate fallbacks
+   unsigned long long it32 = 0, nfb = 0;
    const float ivm = mp.ivm;
+   int* const nlist = list + g.cells();
    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
         t < g.cells(); t += (long long)gridDim.x * blockDim.x) {
       int i, j, k;
       g.ijk(t, i, j, k);
-      const long long ci = g.c(i, j, k);
+      const int ci = g.c(i, j, k);
       const CoefF tf = coef_f_at(m, g, tabf, tfield, i, j, k);
-      const double phd = phi[ci], cd = conc[ci];
-      const float h = interp_func(d2f(phd), m.conc_interp);
-      const float c = d2f(cd);
+      const float h = interp_func(d2f(phi[ci]), m.conc_interp);
+      const float c = d2f(conc[ci]);
       float x[2];
       int st = -1;
       if (guess_l) {
@@ -189,50 +196,89 @@ __global__ void k_kks_mixed(ampe_model_t m, MixParams mp, Grid g, const ThermoCo
          st = kks_newton_f32(tf, h, c, x, 12);
          it32 += st > 0 ? st : 12;
       }
-      float a = x[0], b = x[1], dfv;
+      const float a = x[0], b = x[1];
       if (st > 0 && !near_bound(a) && !near_bound(b)) {
-         dfv = driving_force_f32(tf, a, b) * ivm;
+         cl[ci] = a;
+         cs[ci] = b;
+         for_each_image(g, i, j, k, [&](int idx) {
+            cl[idx] = a;
+            cs[idx] = b;
+         });
+         dF[t] = driving_force_f32(tf, a, b) * ivm;
       } else {
-         // FP64 polish from the FP32 iterate near c = 0 or 1 (full FP64
-         // Newton from the warm start if FP32 did not converge)
-         n64++;
-         const ThermoCoef th =
-             tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
-                 : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
-         double xd[2];
-         if (st > 0) {
-            xd[0] = a;
-            xd[1] = b;
-         } else {
-            xd[0] = clr[ci];
-            xd[1] = csr[ci];
+         if (st > 0) {  // the FP32 iterate is the FP64 polish's start
+            cl[ci] = a;
+            cs[ci] = b;
          }
-         const double hd = interp_func(phd, m.conc_interp);
-         const int s64 = kks_newton(th, hd, cd, xd, m.newton_max_its, 1.0e-10);
-         if (s64 < 0) {
-            fails++;
-            it64 += m.newton_max_its;
-         } else {
-            it64 += s64;
-         }
-         a = (float)xd[0];
-         b = (float)xd[1];
-         dfv = (float)driving_force_scaled(m, th, xd[0], xd[1]);
+         const int q = atomicAdd(nlist, 1);
+         list[q] = (int)t | (st > 0 ? (int)0x80000000 : 0);
       }
+   }
+   if (counters) {
+      unsigned long long v[2] = {it32, nfb};
+      const int slot[2] = {0, 3};
+      for (int q = 0; q < 2; q++) {
+         unsigned long long x = v[q];
+         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+         if ((threadIdx.x & 31) == 0 && x) atomicAdd(&counters[slot[q]], x);
+      }
+   }
+}
+
+// FP64 Newton for the listed cells near c = 0 or 1, or not converged in
+// FP32: from the FP32 iterate when it converged, else from the warm start
+// (full FP64 Newton); FP64 driving force.
+__global__ void __launch_bounds__(128)
+    k_kks_polish64(ampe_model_t m, Grid g, const ThermoCoef* tab, const double* tfield,
+                   const double* __restrict__ phi, const double* __restrict__ conc,
+                   const float* __restrict__ clr, const float* __restrict__ csr, float* cl,
+                   float* cs, float* __restrict__ dF, const int* __restrict__ list,
+                   unsigned long long* counters)
+{
+   // counters: [1] failed cells, [2] FP64-polished cells, [4] FP64 iterations
+   unsigned long long fails = 0, n64 = 0, it64 = 0;
+   const int n = list[g.cells()];
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+      const int e = list[q];
+      const int t = e & 0x7fffffff;
+      int i, j, k;
+      g.ijk(t, i, j, k);
+      const int ci = g.c(i, j, k);
+      n64++;
+      const ThermoCoef th = tab ? tab[m.temp_mode == AMPE_TEMP_GRADIENT ? i : 0]
+                                : thermo_coef(m, temperature_at(m, g, tfield, i, j, k));
+      double xd[2];
+      if (e < 0) {
+         xd[0] = cl[ci];
+         xd[1] = cs[ci];
+      } else {
+         xd[0] = clr[ci];
+         xd[1] = csr[ci];
+      }
+      const double hd = interp_func(phi[ci], m.conc_interp);
+      const int s64 = kks_newton(th, hd, conc[ci], xd, m.newton_max_its, 1.0e-10);
+      if (s64 < 0) {
+         fails++;
+         it64 += m.newton_max_its;
+      } else {
+         it64 += s64;
+      }
+      const float a = (float)xd[0], b = (float)xd[1];
       cl[ci] = a;
       cs[ci] = b;
-      for_each_image(g, i, j, k, [&](long long idx) {
+      for_each_image(g, i, j, k, [&](int idx) {
          cl[idx] = a;
          cs[idx] = b;
       });
-      dF[t] = dfv;
+      dF[t] = (float)driving_force_scaled(m, th, xd[0], xd[1]);
    }
    if (counters) {
-      unsigned long long v[5] = {it32, fails, n64, nfb, it64};
-      for (int q = 0; q < 5; q++) {
+      unsigned long long v[3] = {fails, n64, it64};
+      const int slot[3] = {1, 2, 4};
+      for (int q = 0; q < 3; q++) {
          unsigned long long x = v[q];
          for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-         if ((threadIdx.x & 31) == 0 && x) atomicAdd(&counters[q], x);
+         if ((threadIdx.x & 31) == 0 && x) atomicAdd(&counters[slot[q]], x);
       }
    }
 }
@@ -247,13 +293,17 @@ int kks_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const ThermoCoef* tab, const CoefF* tabf, const double* tfield,
               const double* phi, const double* conc, const float* guess_l, const float* guess_s,
               const float* clr, const float* csr, float* cl, float* cs,
-              float* dF, unsigned long long* counters, cudaStream_t s)
+              float* dF, int* list, unsigned long long* counters, cudaStream_t s)
 {
+   cudaMemsetAsync(list + g.cells(), 0, sizeof(int), s);
    long long b = (g.cells() + 255) / 256;
-   if (b > 152 * 16) b = 152 * 16;
-   k_kks_mixed<<<(unsigned)b, 256, 0, s>>>(m, mp, g, tab, tabf, tfield, phi, conc,
-                                           guess_l, guess_s, clr, csr, cl, cs,
-                                           dF, counters);
+   if (b > max_blocks(16)) b = max_blocks(16);
+   k_kks_f32<<<(unsigned)b, 256, 0, s>>>(m, mp, g, tabf, tfield, phi, conc, guess_l, guess_s,
+                                         clr, csr, cl, cs, dF, list, counters);
+   const int rc = launch_status();
+   if (rc) return rc;
+   k_kks_polish64<<<(unsigned)max_blocks(4), 128, 0, s>>>(m, g, tab, tfield, phi, conc, clr,
+                                                          csr, cl, cs, dF, list, counters);
    return launch_status();
 }
 
@@ -432,7 +482,7 @@ int aniso_orientation_f32(const ampe_model_t& m, const Grid& g, const double* q,
 {
    const long long tot = g.nfx() + g.nfy();
    long long b = (tot + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    k_aniso_orientation<<<(unsigned)b, 256, 0, s>>>(g, m.qlen == 4 ? 1 : 0, q, a);
    return launch_status();
 }
@@ -443,7 +493,7 @@ int aniso_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    (void)m;
    const long long tot = g.nfx() + g.nfy();
    long long b = (tot + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    k_aniso_faces_f32<<<(unsigned)b, 256, 0, s>>>(mp, g, ph, q, a);
    return launch_status();
 }
@@ -705,14 +755,14 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 {
    if (mp.kksc && !cc) return AMPE_ERR_INVALID;
    long long b = (g.cells_ghost() + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    k_phi_to_f32<<<(unsigned)b, 256, 0, s>>>(g, phi, pf);
    launch_status();
    {
       const long long tot =
           (long long)(g.n0 + 1) * (g.n1 + 1) * (g.dim == 3 ? g.n2 + 1 : 1);
       long long bf = (tot + 255) / 256;
-      if (bf > kMaxBlocks) bf = kMaxBlocks;
+      if (bf > max_blocks()) bf = max_blocks();
       if (g.dim == 3) {
          if (mp.pb)
             k_face_weights<3, true><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
@@ -727,7 +777,7 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
       launch_status();
    }
    b = (g.cells() + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    const bool aniso = m.flux_type == AMPE_FLUX_ANISOTROPIC;
    if (aniso) {
       if (g.dim != 2 || !q || !an) return AMPE_ERR_INVALID;
@@ -1063,7 +1113,7 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 {
    if (mp.kksc && !dcv) return AMPE_ERR_INVALID;
    long long b = (g.cells() + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    float* dq = qf ? qf->dq : nullptr;
    if (mp.pb)
       k_jv_point<true><<<(unsigned)b, 256, 0, s>>>(m, g, tabf, tfield, pf, cl, cs, v, dphi, da,
@@ -1115,7 +1165,7 @@ int quat_cells_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                    const double* phi, QuatF32& qf, cudaStream_t s)
 {
    long long b = (g.cells() + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    if (g.dim == 3)
       k_quat_cells_f32<3><<<(unsigned)b, 256, 0, s>>>(mp, g, phi, qf.q, qf.ogm, qf.mq);
    else
@@ -1130,7 +1180,7 @@ int conc_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    const long long nz = g.dim == 3 ? g.nfz() : 0;
    const long long tot = g.nfx() + g.nfy() + nz;
    long long b = (tot + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    FacePtrs f;
    for (int d = 0; d < 3; d++) {
       f.fc[d] = D[d];
@@ -1148,7 +1198,7 @@ int quat_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
 {
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    long long b = (tot + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    FacePtrs f;
    for (int d = 0; d < 3; d++) {
       f.fc[d] = fc[d];

@@ -80,13 +80,15 @@ struct QuatF32 {
 };
 MixParams make_mix_params(const ampe_model_t& m);
 // guess_l / guess_s (may be null): surrogate initial guesses (3 FP32
-// iterations from them, then the warm start clr / csr as fallback)
+// iterations from them, then the warm start clr / csr as fallback).
+// list: cells + 1 ints of workspace (the cells for the FP64 polish and
+// their count).
 int kks_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
               const ThermoCoef* tab, const CoefF* tabf, const double* tfield,
               const double* phi,
               const double* conc, const float* guess_l, const float* guess_s,
               const float* clr, const float* csr, float* cl, float* cs,
-              float* dF, unsigned long long* counters, cudaStream_t s);
+              float* dF, int* list, unsigned long long* counters, cudaStream_t s);
 // q: orientation of the 2D anisotropic flux (null otherwise); its face
 // fluxes and Jacobians go to *an for the Jacobian-vector products
 int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,

@@ -6,10 +6,10 @@
 // one thread from shared-memory operands in the canonical no-swizzle K-major
 // layout, accumulators in tensor memory read back with tcgen05.ld; the bias
 // + SiLU epilogue runs on packed bf16x2 and writes the next layer's operand.
-// Training (forward, backward, Adam) runs in FP32 on the CUDA cores with the
-// weights rounded to BF16 in the forward pass; 2000 steps of 4096 samples
-// are about 4e11 FLOP, one to two inference passes over a 256^3 level, and
-// take about 0.6 s once per run.
+// Training runs on the tensor cores too: k_mlp_train_tc does the forward and
+// backward products of one 128-sample tile per CTA with BF16 operands and
+// FP32 accumulators, k_mlp_reduce_adam sums the tiles' gradients and takes
+// the FP32 Adam step of the master weights.
 //
 // Labels come from the FP64 KKS Newton (kks_newton), started from (c, c).
 #include <cuda_bf16.h>
@@ -145,104 +145,14 @@ __device__ __forceinline__ float dsilu(float z)
    return s * (1.f + z * (1.f - s));
 }
 
-// thread per (sample, out)
-__global__ void k_lin_fwd(int B, int K, int N, const float* X, int ldx,
-                          const float* W, const float* b, float* Z, float* A,
-                          int act)
-{
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= B * N) return;
-   const int s = t / N, o = t % N;
-   float acc = b[o];
-   for (int k = 0; k < K; k++) acc += X[s * ldx + k] * bf16r(W[o * K + k]);
-   Z[t] = acc;
-   A[t] = act ? silu(acc) : acc;
-}
-
-// loss 0.5 mean over (sample, 2) of (y - target)^2 ; dY = (y - t) / B
-__global__ void k_loss_grad(int B, const float* Y, const float* target,
-                            float* dY, float* loss_part)
-{
-   __shared__ float sh[256];
-   float acc = 0.f;
-   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * B;
-        t += gridDim.x * blockDim.x) {
-      const float d = Y[t] - target[t];
-      dY[t] = d / (float)B;
-      acc += 0.5f * d * d;
-   }
-   sh[threadIdx.x] = acc;
-   __syncthreads();
-   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-      __syncthreads();
-   }
-   if (threadIdx.x == 0) loss_part[blockIdx.x] = sh[0];
-}
-
-// dX[s][k] = sum_o dZ[s][o] W[o][k]   (thread per (sample, in)); then
-// multiplied by silu'(Zprev) when the previous layer has an activation
-__global__ void k_lin_bwd_data(int B, int K, int N, const float* dZ,
-                               const float* W, const float* Zprev, float* dX)
-{
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= B * K) return;
-   const int s = t / K, k = t % K;
-   float acc = 0.f;
-   for (int o = 0; o < N; o++) acc += dZ[s * N + o] * bf16r(W[o * K + k]);
-   dX[t] = Zprev ? acc * dsilu(Zprev[t]) : acc;
-}
-
-// partial dW[o][k] over a chunk of samples: part[chunk][o*K+k] and db
-__global__ void k_lin_bwd_weight(int B, int K, int N, const float* dZ,
-                                 const float* X, int ldx, int chunk,
-                                 float* partW, float* partb)
-{
-   const int nk = N * (K + 1);
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   const int ch = blockIdx.y;
-   if (t >= nk) return;
-   const int o = t / (K + 1), k = t % (K + 1);
-   const int s0 = ch * chunk, s1 = min(B, s0 + chunk);
-   float acc = 0.f;
-   if (k < K)
-      for (int s = s0; s < s1; s++) acc += dZ[s * N + o] * X[s * ldx + k];
-   else
-      for (int s = s0; s < s1; s++) acc += dZ[s * N + o];
-   if (k < K)
-      partW[(size_t)ch * N * K + o * K + k] = acc;
-   else
-      partb[(size_t)ch * N + o] = acc;
-}
-
-__global__ void k_sum_parts(int n, int nparts, const float* part, float* out)
-{
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= n) return;
-   float acc = 0.f;
-   for (int p = 0; p < nparts; p++) acc += part[(size_t)p * n + t];
-   out[t] = acc;
-}
-
-__global__ void k_adam(int n, float* w, const float* g, float* m1, float* m2,
-                       float lr, float b1, float b2, float eps, float c1,
-                       float c2)
-{
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= n) return;
-   const float gt = g[t];
-   const float a = b1 * m1[t] + (1.f - b1) * gt;
-   const float v = b2 * m2[t] + (1.f - b2) * gt * gt;
-   m1[t] = a;
-   m2[t] = v;
-   w[t] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
-}
-
-// BF16 canonical copies for the tensor-core kernel
+// BF16 canonical copies for the tensor-core kernels: the forward operands
+// W_l [out][in] (K = in) and, for the backward products dX = dZ W, W_l^T
+// [in][out] (K = out) of layers 2-4
 __global__ void k_pack_weights(const float* W1, const float* W2,
                                const float* W3, const float* W4,
                                __nv_bfloat16* p1, __nv_bfloat16* p2,
-                               __nv_bfloat16* p3, __nv_bfloat16* p4)
+                               __nv_bfloat16* p3, __nv_bfloat16* p4,
+                               __nv_bfloat16* p4t, __nv_bfloat16* p3t, __nv_bfloat16* p2t)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    // W1: 64 x 16 (K padded from 3)
@@ -261,6 +171,18 @@ __global__ void k_pack_weights(const float* W1, const float* W2,
       const int r = t / 64, k = t % 64;
       const float v = r < 2 ? W4[r * 64 + k] : 0.f;
       p4[canon_off(r, k, 64) / 2] = __float2bfloat16_rn(v);
+   }
+   // W4^T: 64 (in) x 16 (out padded from 2)
+   if (t < 64 * 16) {
+      const int r = t / 16, k = t % 16;
+      const float v = k < 2 ? W4[k * 64 + r] : 0.f;
+      p4t[canon_off(r, k, 16) / 2] = __float2bfloat16_rn(v);
+   }
+   // W3^T, W2^T: 64 (in) x 64 (out)
+   if (t < 64 * 64) {
+      const int r = t / 64, k = t % 64;
+      p3t[canon_off(r, k, 64) / 2] = __float2bfloat16_rn(W3[k * 64 + r]);
+      p2t[canon_off(r, k, 64) / 2] = __float2bfloat16_rn(W2[k * 64 + r]);
    }
 }
 
@@ -316,10 +238,13 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, int count)
    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
 }
 
-// bounded wait on an mbarrier phase; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+// default bound of the mbarrier waits (try_wait polls)
+constexpr int kWaitLimit = 1 << 22;
+
+// bounded wait on an mbarrier phase; returns false after `limit` polls
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int limit)
 {
-   for (int it = 0; it < (1 << 22); it++) {
+   for (int it = 0; it < limit; it++) {
       uint32_t done;
       asm volatile(
           "{\n\t.reg .pred p;\n\t"
@@ -415,11 +340,15 @@ __device__ __forceinline__ void epilogue64(uint32_t taddr, const float* bias,
    }
 }
 
-// guess_l / guess_s for the interior cells of the grid (interior index t)
+// guess_l / guess_s for the interior cells of the grid (interior index t).
+// wait_limit bounds every mbarrier wait; skip_issue (a test of that error
+// path) makes the issuing thread commit nothing, so the first wait runs out
+// with no MMA in flight, the error flag is set and the tensor memory freed.
 __global__ void __launch_bounds__(128) k_mlp_infer_tc(
     ampe_model_t m, Grid g, MlpNorm nz, const __nv_bfloat16* wpk,
     const float* bias, const double* phi, const double* conc,
-    const double* tfield, float* guess_l, float* guess_s, int* err)
+    const double* tfield, float* guess_l, float* guess_s, int* err, int wait_limit,
+    int skip_issue)
 {
    extern __shared__ __align__(1024) unsigned char smraw[];
    MlpSmem& S = *reinterpret_cast<MlpSmem*>(smraw);
@@ -480,12 +409,12 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
       tc_fence_before();
       __syncthreads();
       // ---- layer 1: [128 x 16] x [64 x 16]^T ----
-      if (tid == 0) {
+      if (tid == 0 && !skip_issue) {
          tc_fence_after();
          umma_f16(tmem, umma_desc(a0, 128, 256), umma_desc(w1, 128, 256), umma_idesc(64), 0);
          umma_commit(mbar);
       }
-      ok = __syncthreads_and(mbar_wait(mbar, phase));
+      ok = __syncthreads_and(mbar_wait(mbar, phase, wait_limit));
       if (!ok) break;
       phase ^= 1;
       tc_fence_after();
@@ -495,7 +424,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
          fence_async_smem();
          tc_fence_before();
          __syncthreads();
-         if (tid == 0) {
+         if (tid == 0 && !skip_issue) {
             tc_fence_after();
             const uint32_t wb = layer == 0 ? w2 : w3;
 #pragma unroll
@@ -504,7 +433,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
                         umma_desc(wb + 256 * s, 128, 1024), umma_idesc(64), s > 0);
             umma_commit(mbar);
          }
-         ok = __syncthreads_and(mbar_wait(mbar, phase));
+         ok = __syncthreads_and(mbar_wait(mbar, phase, wait_limit));
          if (!ok) break;
          phase ^= 1;
          tc_fence_after();
@@ -516,7 +445,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
       fence_async_smem();
       tc_fence_before();
       __syncthreads();
-      if (tid == 0) {
+      if (tid == 0 && !skip_issue) {
          tc_fence_after();
 #pragma unroll
          for (int s = 0; s < 4; s++)
@@ -524,7 +453,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
                      umma_desc(w4 + 256 * s, 128, 1024), umma_idesc(16), s > 0);
          umma_commit(mbar);
       }
-      ok = __syncthreads_and(mbar_wait(mbar, phase));
+      ok = __syncthreads_and(mbar_wait(mbar, phase, wait_limit));
       if (!ok) break;
       phase ^= 1;
       tc_fence_after();
@@ -544,7 +473,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
       // a commit did not arrive in time: flag it, give the MMAs in flight
       // one more bounded wait, then release the tensor memory
       if (tid == 0 && err) atomicExch(err, 1);
-      mbar_wait(mbar, phase);
+      mbar_wait(mbar, phase, wait_limit);
    }
    tc_fence_before();
    __syncthreads();
@@ -553,6 +482,341 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(
       asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                    "r"(kMlpTmemCols));
    }
+}
+
+// ---------------------------------------------------------------------------
+// tensor-core training step: forward and backward of one 128-sample tile per
+// CTA on tcgen05 (BF16 operands, FP32 accumulators in tensor memory)
+//
+// Layer l: Z = X W^T + b, A = silu(Z) (identity for the last layer); loss
+// 1/2 mean over samples of the squared logit errors.  Backward, per layer:
+//   dW_l (| db_l) = dZ_l^T [X_l | 1]   M = 128 (out padded), N = in + ones
+//                                     column (80, or 16 for layer 1),
+//                                     K = 128 samples;
+//   dX_{l-1} = dZ_l W_l                M = 128 samples, N = in, K = out;
+//   dZ_{l-1} = dX_{l-1} silu'(Z_{l-1}) (silu' kept in FP32 in tensor memory).
+// Every operand is stored K-major in the canonical no-swizzle layout, so the
+// backward products read transposed copies written by the forward epilogue
+// (X_l^T) and by the packing kernel (W_l^T).  Each CTA writes its tile's
+// weight and bias gradients as one partial; k_mlp_reduce_adam sums the
+// partials in a fixed order, so a training step is deterministic.
+// ---------------------------------------------------------------------------
+struct __align__(128) TrainSmem {
+   // packed weights, in the order the packing kernel writes them
+   __nv_bfloat16 w1[64 * 16];
+   __nv_bfloat16 w2[64 * 64];
+   __nv_bfloat16 w3[64 * 64];
+   __nv_bfloat16 w4[16 * 64];
+   __nv_bfloat16 w4t[64 * 16];  // [in][out padded to 16]
+   __nv_bfloat16 w3t[64 * 64];  // [in][out]
+   __nv_bfloat16 w2t[64 * 64];
+   __nv_bfloat16 x0[128 * 16];    // inputs, K-major (K = 16: 3 used)
+   __nv_bfloat16 act[128 * 64];   // A operand of the next forward layer
+   __nv_bfloat16 x0t[16 * 128];   // [feature | ones | 0][sample]
+   __nv_bfloat16 at[3][80 * 128]; // [feature 64 | ones | 0 x 15][sample]
+   __nv_bfloat16 dzt[128 * 128];  // [out, rows >= out zero][sample]
+   __nv_bfloat16 dzn[128 * 64];   // [sample][out] (K = 64, or 16 for layer 4)
+   float b[3 * 64 + 2];
+   float red[4];
+   unsigned long long mbar;
+   uint32_t tmem;
+};
+
+constexpr int kTrainTmemCols = 512;  // [0,64) Z / dX, [128,208) dW, [256,448) silu'
+
+#define TMEM_ST_X16(taddr, r)                                                       \
+   asm volatile(                                                                   \
+       "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11," \
+       "%12,%13,%14,%15,%16};" ::"r"(taddr),                                        \
+       "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),  \
+       "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]),         \
+       "r"(r[13]), "r"(r[14]), "r"(r[15]))
+
+__device__ __forceinline__ void tmem_wait_st()
+{
+   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float dsilu_f(float z)
+{
+   const float s = 1.f / (1.f + __expf(-z));
+   return s * (1.f + z * (1.f - s));
+}
+
+__device__ __forceinline__ void st_bf16(__nv_bfloat16* base, int byte_off, float v)
+{
+   *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(base) + byte_off) =
+       __float2bfloat16_rn(v);
+}
+
+// 8 consecutive K values of row `row` (K-major canonical, K-tile Kt) as bf16
+__device__ __forceinline__ void st_bf16x8(__nv_bfloat16* base, int row, int k0, int Kt,
+                                          const float* v)
+{
+   uint4 pk;
+   __nv_bfloat162 p;
+   p = __floats2bfloat162_rn(v[0], v[1]);
+   pk.x = *reinterpret_cast<uint32_t*>(&p);
+   p = __floats2bfloat162_rn(v[2], v[3]);
+   pk.y = *reinterpret_cast<uint32_t*>(&p);
+   p = __floats2bfloat162_rn(v[4], v[5]);
+   pk.z = *reinterpret_cast<uint32_t*>(&p);
+   p = __floats2bfloat162_rn(v[6], v[7]);
+   pk.w = *reinterpret_cast<uint32_t*>(&p);
+   *reinterpret_cast<uint4*>(reinterpret_cast<char*>(base) + canon_off(row, k0, Kt)) = pk;
+}
+
+// partial gradient of one CTA: [W0 b0 W1 b1 W2 b2 W3 b3] as in the master
+// parameter vector; loss partial in part_loss[blockIdx.x]
+__global__ void __launch_bounds__(128, 1) k_mlp_train_tc(
+    const __nv_bfloat16* wpk, const float* bias, const float* x, const float* target, int B,
+    float* partials, int npar, float* part_loss, int* err, int wait_limit, int skip_issue)
+{
+   extern __shared__ __align__(1024) unsigned char smraw[];
+   TrainSmem& S = *reinterpret_cast<TrainSmem*>(smraw);
+   const int tid = threadIdx.x, warp = tid >> 5;
+   const int row = tid;
+   const int s = blockIdx.x * 128 + row;
+   const bool valid = s < B;
+   const float invB = 1.f / (float)B;
+   {
+      const uint4* src = reinterpret_cast<const uint4*>(wpk);
+      uint4* dst = reinterpret_cast<uint4*>(S.w1);
+      const int n16 = (int)((sizeof(S.w1) + sizeof(S.w2) + sizeof(S.w3) + sizeof(S.w4) +
+                             sizeof(S.w4t) + sizeof(S.w3t) + sizeof(S.w2t)) / 16);
+      for (int i = tid; i < n16; i += blockDim.x) dst[i] = src[i];
+      for (int i = tid; i < 3 * 64 + 2; i += blockDim.x) S.b[i] = bias[i];
+      // zero x0, the transposed inputs and dZ^T (their padding stays zero)
+      const uint4 z = make_uint4(0, 0, 0, 0);
+      for (int i = tid; i < (int)(sizeof(S.x0) / 16); i += blockDim.x)
+         reinterpret_cast<uint4*>(S.x0)[i] = z;
+      for (int i = tid; i < (int)(sizeof(S.x0t) / 16); i += blockDim.x)
+         reinterpret_cast<uint4*>(S.x0t)[i] = z;
+      for (int i = tid; i < (int)(sizeof(S.at) / 16); i += blockDim.x)
+         reinterpret_cast<uint4*>(&S.at[0][0])[i] = z;
+      for (int i = tid; i < (int)(sizeof(S.dzt) / 16); i += blockDim.x)
+         reinterpret_cast<uint4*>(S.dzt)[i] = z;
+   }
+   __syncthreads();
+   // inputs (BF16) in both layouts, and the ones rows of the transposed
+   // operands (bias gradients come out of the same products)
+   float in[3] = {0.f, 0.f, 0.f};
+   if (valid)
+      for (int q = 0; q < 3; q++) in[q] = x[4 * (long long)s + q];
+   for (int q = 0; q < 3; q++) {
+      st_bf16(S.x0, canon_off(row, q, 16), in[q]);
+      st_bf16(S.x0t, canon_off(q, row, 128), in[q]);
+   }
+   st_bf16(S.x0t, canon_off(3, row, 128), 1.f);
+   for (int l = 0; l < 3; l++) st_bf16(S.at[l], canon_off(64, row, 128), 1.f);
+   const uint32_t mbar = smem_u32(&S.mbar);
+   if (tid == 0) mbar_init(mbar, 1);
+   if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(&S.tmem)),
+                   "r"(kTrainTmemCols));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+   }
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   fence_async_smem();
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t tmem = S.tmem;
+   const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+   const uint32_t t_acc = tmem + lane_off;           // Z / dX, columns [0, 64)
+   const uint32_t t_dw = tmem + 128 + lane_off;      // dW, columns [128, 208)
+   const uint32_t t_sd = tmem + 256 + lane_off;      // silu', columns [256, 448)
+   const uint32_t ax0 = smem_u32(S.x0), aact = smem_u32(S.act);
+   uint32_t phase = 0;
+   bool ok = true;
+   auto wait_mma = [&]() {
+      ok = __syncthreads_and(mbar_wait(mbar, phase, wait_limit));
+      phase ^= 1;
+      tc_fence_after();
+   };
+   auto issue_begin = [&]() {
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+   };
+   // ---------------- forward ----------------
+   issue_begin();
+   if (tid == 0 && !skip_issue) {
+      tc_fence_after();
+      umma_f16(tmem, umma_desc(ax0, 128, 256), umma_desc(smem_u32(S.w1), 128, 256),
+               umma_idesc(64), 0);
+      umma_commit(mbar);
+   }
+   wait_mma();
+   for (int l = 0; l < 3 && ok; l++) {
+      // epilogue of layer l: Z + b, silu' to tensor memory, A in both layouts
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+         uint32_t r[16];
+         TMEM_LD_X16(t_acc + 16 * q, r);
+         tmem_wait_ld();
+         float a[16];
+         uint32_t d[16];
+#pragma unroll
+         for (int j = 0; j < 16; j++) {
+            const float z = __uint_as_float(r[j]) + S.b[64 * l + 16 * q + j];
+            a[j] = silu_f(z);
+            d[j] = __float_as_uint(dsilu_f(z));
+         }
+         TMEM_ST_X16(t_sd + 64 * l + 16 * q, d);
+         st_bf16x8(S.act, row, 16 * q, 64, a);
+         st_bf16x8(S.act, row, 16 * q + 8, 64, a + 8);
+#pragma unroll
+         for (int j = 0; j < 16; j++) st_bf16(S.at[l], canon_off(16 * q + j, row, 128), a[j]);
+      }
+      tmem_wait_st();
+      issue_begin();
+      if (tid == 0 && !skip_issue) {
+         tc_fence_after();
+         if (l < 2) {
+            const uint32_t wb = smem_u32(l == 0 ? S.w2 : S.w3);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+               umma_f16(tmem, umma_desc(aact + 256 * k, 128, 1024),
+                        umma_desc(wb + 256 * k, 128, 1024), umma_idesc(64), k > 0);
+         } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+               umma_f16(tmem, umma_desc(aact + 256 * k, 128, 1024),
+                        umma_desc(smem_u32(S.w4) + 256 * k, 128, 1024), umma_idesc(16), k > 0);
+         }
+         umma_commit(mbar);
+      }
+      wait_mma();
+   }
+   float lossv = 0.f;
+   if (ok) {
+      // ---------------- loss and dZ of the last layer ----------------
+      uint32_t r[16];
+      TMEM_LD_X16(t_acc, r);
+      tmem_wait_ld();
+      float dz[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) dz[j] = 0.f;
+      if (valid) {
+         for (int o = 0; o < 2; o++) {
+            const float y = __uint_as_float(r[o]) + S.b[192 + o];
+            const float e = y - target[2 * (long long)s + o];
+            lossv += 0.5f * e * e;
+            dz[o] = e * invB;
+         }
+      }
+      st_bf16(S.dzt, canon_off(0, row, 128), dz[0]);
+      st_bf16(S.dzt, canon_off(1, row, 128), dz[1]);
+      st_bf16x8(S.dzn, row, 0, 16, dz);
+      st_bf16x8(S.dzn, row, 8, 16, dz + 8);
+   }
+   // ---------------- backward, layers 4 .. 1 ----------------
+   const int poff[4] = {0, 64 * 3 + 64, 64 * 3 + 64 + 64 * 64 + 64,
+                        64 * 3 + 64 + 2 * (64 * 64 + 64)};
+   float* part = partials + (size_t)blockIdx.x * npar;
+   for (int l = 3; l >= 0 && ok; l--) {
+      const int nout = l == 3 ? 2 : 64;
+      const int nin = l == 0 ? 3 : 64;
+      const int ndw = l == 0 ? 16 : 80;
+      issue_begin();
+      if (tid == 0 && !skip_issue) {
+         tc_fence_after();
+         const uint32_t bt = l == 0 ? smem_u32(S.x0t) : smem_u32(S.at[l - 1]);
+         // dW_l | db_l = dZ^T [X | 1], K = 128 samples
+#pragma unroll
+         for (int k = 0; k < 8; k++)
+            umma_f16(tmem + 128, umma_desc(smem_u32(S.dzt) + 256 * k, 128, 2048),
+                     umma_desc(bt + 256 * k, 128, 2048), umma_idesc(ndw), k > 0);
+         if (l > 0) {  // dX_{l-1} = dZ W
+            if (l == 3) {
+               umma_f16(tmem, umma_desc(smem_u32(S.dzn), 128, 256),
+                        umma_desc(smem_u32(S.w4t), 128, 256), umma_idesc(64), 0);
+            } else {
+               const uint32_t wt = smem_u32(l == 2 ? S.w3t : S.w2t);
+#pragma unroll
+               for (int k = 0; k < 4; k++)
+                  umma_f16(tmem, umma_desc(smem_u32(S.dzn) + 256 * k, 128, 1024),
+                           umma_desc(wt + 256 * k, 128, 1024), umma_idesc(64), k > 0);
+            }
+         }
+         umma_commit(mbar);
+      }
+      wait_mma();
+      if (!ok) break;
+      // weight and bias gradients of this tile: rows 0..nout-1 (warps 0, 1)
+      if (warp < 2) {
+         for (int q = 0; q < ndw / 16; q++) {
+            uint32_t r[16];
+            TMEM_LD_X16(t_dw + 16 * q, r);
+            tmem_wait_ld();
+            if (row < nout) {
+#pragma unroll
+               for (int j = 0; j < 16; j++) {
+                  const int c = 16 * q + j;
+                  const float v = __uint_as_float(r[j]);
+                  if (c < nin)
+                     part[poff[l] + row * nin + c] = v;
+                  else if (c == (l == 0 ? 3 : 64))
+                     part[poff[l] + nout * nin + row] = v;
+               }
+            }
+         }
+      }
+      if (l == 0) break;
+      // dZ_{l-1} = dX_{l-1} silu'(Z_{l-1}) for this row -> dZ^T and dZ
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+         uint32_t r[16], d[16];
+         TMEM_LD_X16(t_acc + 16 * q, r);
+         TMEM_LD_X16(t_sd + 64 * (l - 1) + 16 * q, d);
+         tmem_wait_ld();
+         float dz[16];
+#pragma unroll
+         for (int j = 0; j < 16; j++)
+            dz[j] = valid ? __uint_as_float(r[j]) * __uint_as_float(d[j]) : 0.f;
+#pragma unroll
+         for (int j = 0; j < 16; j++) st_bf16(S.dzt, canon_off(16 * q + j, row, 128), dz[j]);
+         st_bf16x8(S.dzn, row, 16 * q, 64, dz);
+         st_bf16x8(S.dzn, row, 16 * q + 8, 64, dz + 8);
+      }
+   }
+   // loss partial: warp sums, then the four warps in order
+   for (int o = 16; o > 0; o >>= 1) lossv += __shfl_xor_sync(0xffffffffu, lossv, o);
+   if ((tid & 31) == 0) S.red[warp] = lossv;
+   if (!ok) {
+      if (tid == 0 && err) atomicExch(err, 1);
+      mbar_wait(mbar, phase, wait_limit);
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (tid == 0) part_loss[blockIdx.x] = ((S.red[0] + S.red[1]) + S.red[2]) + S.red[3];
+   if (warp == 0) {
+      tc_fence_after();
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                   "r"(kTrainTmemCols));
+   }
+}
+
+// gradient = sum of the CTA partials (fixed order), then one Adam update of
+// the FP32 master weights (lr = 0: the sum only)
+__global__ void k_mlp_reduce_adam(int n, int nparts, const float* partials, float* grads,
+                                  float* w, float* m1, float* m2, float lr, float b1, float b2,
+                                  float eps, float c1, float c2)
+{
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= n) return;
+   float g = 0.f;
+   for (int p = 0; p < nparts; p++) g += partials[(size_t)p * n + t];
+   grads[t] = g;
+   if (lr == 0.f) return;
+   const float a = b1 * m1[t] + (1.f - b1) * g;
+   const float v = b2 * m2[t] + (1.f - b2) * g * g;
+   m1[t] = a;
+   m2[t] = v;
+   w[t] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
 }
 
 // FP32 CUDA-core reference of the same inference (validation / fallback-free
@@ -625,17 +889,14 @@ int Mlp::create(const ampe_model_t& model, int batch_max)
       return AMPE_ERR_CUDA;
    cudaMemset(m1, 0, bytes_w);
    cudaMemset(m2, 0, bytes_w);
-   const size_t pk = sizeof(__nv_bfloat16) * (64 * 16 + 2 * 64 * 64 + 16 * 64);
+   // forward operands W1..W4 and backward operands W4^T, W3^T, W2^T
+   const size_t pk =
+       sizeof(__nv_bfloat16) * (64 * 16 + 2 * 64 * 64 + 16 * 64 + 64 * 16 + 2 * 64 * 64);
    if (cudaMalloc(&packed, pk)) return AMPE_ERR_CUDA;
-   // activations for training: Z and A per layer [batch x 64], dZ, dX
-   const size_t act = sizeof(float) * (size_t)batch * 64;
-   for (int l = 0; l < 4; l++)
-      if (cudaMalloc(&Z[l], act) || cudaMalloc(&A[l], act)) return AMPE_ERR_CUDA;
-   if (cudaMalloc(&dZ, act) || cudaMalloc(&dX, act)) return AMPE_ERR_CUDA;
-   nchunks = (batch + 255) / 256;
-   if (cudaMalloc(&partW, sizeof(float) * (size_t)nchunks * 64 * 64) ||
-       cudaMalloc(&partb, sizeof(float) * (size_t)nchunks * 64) ||
-       cudaMalloc(&losspart, sizeof(float) * 256) || cudaMalloc(&err, sizeof(int)))
+   // one gradient partial and one loss partial per 128-sample tile
+   ntiles = (batch + 127) / 128;
+   if (cudaMalloc(&partials, sizeof(float) * (size_t)ntiles * np) ||
+       cudaMalloc(&losspart, sizeof(float) * (size_t)ntiles) || cudaMalloc(&err, sizeof(int)))
       return AMPE_ERR_CUDA;
    cudaMemset(err, 0, sizeof(int));
    return AMPE_OK;
@@ -643,8 +904,7 @@ int Mlp::create(const ampe_model_t& model, int batch_max)
 
 void Mlp::release()
 {
-   void* ps[] = {params, grads, m1, m2, packed, dZ, dX, partW, partb, losspart, err,
-                 Z[0], Z[1], Z[2], Z[3], A[0], A[1], A[2], A[3], samples_x, samples_t};
+   void* ps[] = {params, grads, m1, m2, packed, partials, losspart, err, samples_x, samples_t};
    for (void* p : ps)
       if (p) cudaFree(p);
 }
@@ -685,8 +945,11 @@ int Mlp::pack(cudaStream_t s)
    __nv_bfloat16* p2 = p1 + 64 * 16;
    __nv_bfloat16* p3 = p2 + 64 * 64;
    __nv_bfloat16* p4 = p3 + 64 * 64;
-   k_pack_weights<<<16, 256, 0, s>>>(W(0), W(1), W(2), W(3), p1, p2, p3, p4);
-   // contiguous biases for the inference kernels
+   __nv_bfloat16* p4t = p4 + 16 * 64;
+   __nv_bfloat16* p3t = p4t + 64 * 16;
+   __nv_bfloat16* p2t = p3t + 64 * 64;
+   k_pack_weights<<<16, 256, 0, s>>>(W(0), W(1), W(2), W(3), p1, p2, p3, p4, p4t, p3t, p2t);
+   // contiguous biases for the inference and training kernels
    if (!bias_cat) cudaMalloc(&bias_cat, sizeof(float) * (3 * 64 + 2));
    for (int l = 0; l < 4; l++)
       cudaMemcpyAsync(bias_cat + 64 * l, b(l), sizeof(float) * kLayerN[l],
@@ -694,59 +957,43 @@ int Mlp::pack(cudaStream_t s)
    return launch_status();
 }
 
-// forward + backward on samples [s0, s0 + B); gradients into grads
-int Mlp::grad(const float* x, const float* target, int B, cudaStream_t s,
-              float* loss_out)
+// one training step on samples x[B][4], target[B][2]: forward and backward
+// on the tensor cores (one CTA per 128 samples), the partials summed into
+// grads and, when lr > 0, one Adam update and the repacked operands
+int Mlp::step_tc(const float* x, const float* target, int B, float lr, cudaStream_t s,
+                 float* loss_out)
 {
-   const float* in = x;
-   int ldx = 4;
-   for (int l = 0; l < 4; l++) {
-      const int K = kLayerK[l], N = kLayerN[l];
-      k_lin_fwd<<<(B * N + 255) / 256, 256, 0, s>>>(B, K, N, in, ldx, W(l), b(l), Z[l],
-                                                    A[l], l < 3);
-      in = A[l];
-      ldx = N;
+   if (B < 1 || B > batch) return AMPE_ERR_INVALID;
+   const int nt = (B + 127) / 128;
+   const int smem = (int)sizeof(TrainSmem) + 1024;
+   static std::atomic<unsigned long long> attr{0};
+   if (first_on_device(attr))
+      cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+   const int np = nparams();
+   k_mlp_train_tc<<<nt, 128, smem, s>>>((const __nv_bfloat16*)packed, bias_cat, x, target, B,
+                                        partials, np, losspart, err, wait_limit, skip_issue);
+   int rc = launch_status();
+   if (rc) return rc;
+   float c1 = 1.f, c2 = 1.f;
+   const float b1 = 0.9f, b2 = 0.999f;
+   if (lr > 0.f) {
+      step++;
+      c1 = 1.f - std::pow(b1, (float)step);
+      c2 = 1.f - std::pow(b2, (float)step);
    }
-   k_loss_grad<<<64, 256, 0, s>>>(B, A[3], target, dZ, losspart);
-   g_launches += 5;
-   float* dcur = dZ;
-   for (int l = 3; l >= 0; l--) {
-      const int K = kLayerK[l], N = kLayerN[l];
-      const float* Xin = l > 0 ? A[l - 1] : x;
-      const int ld = l > 0 ? kLayerN[l - 1] : 4;
-      const int nch = (B + 255) / 256;
-      dim3 gw((N * (K + 1) + 255) / 256, nch);
-      k_lin_bwd_weight<<<gw, 256, 0, s>>>(B, K, N, dcur, Xin, ld, 256, partW, partb);
-      k_sum_parts<<<(N * K + 255) / 256, 256, 0, s>>>(N * K, nch, partW, gW(l));
-      k_sum_parts<<<1, 64, 0, s>>>(N, nch, partb, gb(l));
-      g_launches += 3;
-      if (l > 0) {
-         float* dnext = dcur == dZ ? dX : dZ;
-         k_lin_bwd_data<<<(B * K + 255) / 256, 256, 0, s>>>(B, K, N, dcur, W(l), Z[l - 1],
-                                                            dnext);
-         g_launches++;
-         dcur = dnext;
-      }
-   }
-   if (loss_out) {
-      float h[64];
-      cudaMemcpyAsync(h, losspart, sizeof(h), cudaMemcpyDeviceToHost, s);
-      cudaStreamSynchronize(s);
+   k_mlp_reduce_adam<<<(np + 255) / 256, 256, 0, s>>>(np, nt, partials, grads, params, m1, m2,
+                                                      lr, b1, b2, 1e-8f, c1, c2);
+   rc = launch_status();
+   if (!rc && lr > 0.f) rc = pack(s);
+   if (!rc && loss_out) {
+      std::vector<float> h(nt);
+      cudaMemcpyAsync(h.data(), losspart, sizeof(float) * nt, cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return AMPE_ERR_CUDA;
       double acc = 0;
-      for (int q = 0; q < 64; q++) acc += h[q];
+      for (int q = 0; q < nt; q++) acc += h[q];
       *loss_out = (float)(acc / B);
    }
-   return launch_status();
-}
-
-int Mlp::adam_step(float lr, cudaStream_t s)
-{
-   step++;
-   const float b1 = 0.9f, b2 = 0.999f;
-   const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
-   const int n = nparams();
-   k_adam<<<(n + 255) / 256, 256, 0, s>>>(n, params, grads, m1, m2, lr, b1, b2, 1e-8f, c1, c2);
-   return launch_status();
+   return rc;
 }
 
 int Mlp::infer(const Grid& g, const double* phi, const double* conc,
@@ -755,19 +1002,18 @@ int Mlp::infer(const Grid& g, const double* phi, const double* conc,
 {
    if (tensor) {
       const int smem = (int)sizeof(MlpSmem) + 1024;
-      static bool attr = false;
-      if (!attr) {
+      static std::atomic<unsigned long long> attr{0};
+      if (first_on_device(attr))
          cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-         attr = true;
-      }
       // 42 KB of shared memory and 64 TMEM columns per CTA: five CTAs per SM
       long long tiles = (g.cells() + 127) / 128;
-      int blocks = (int)(tiles < 152 * 5 ? tiles : 152 * 5);
+      int blocks = (int)(tiles < max_blocks(5) ? tiles : max_blocks(5));
       k_mlp_infer_tc<<<blocks, 128, smem, s>>>(m, g, norm, (const __nv_bfloat16*)packed,
-                                               bias_cat, phi, conc, tfield, gl, gs, err);
+                                               bias_cat, phi, conc, tfield, gl, gs, err,
+                                               wait_limit, skip_issue);
    } else {
       long long b = (g.cells() + 127) / 128;
-      if (b > 152 * 16) b = 152 * 16;
+      if (b > max_blocks(16)) b = max_blocks(16);
       k_mlp_infer_simt<<<(unsigned)b, 128, 0, s>>>(m, g, norm, W(0), W(1), W(2), W(3),
                                                    bias_cat, phi, conc, tfield, gl, gs);
    }
@@ -790,7 +1036,7 @@ int Mlp::generate(long long n, uint32_t seed, double tlo, double thi, double clo
    cudaMalloc(&fails, sizeof(*fails));
    cudaMemsetAsync(fails, 0, sizeof(*fails), s);
    long long b = (n + 255) / 256;
-   if (b > 152 * 16) b = 152 * 16;
+   if (b > max_blocks(16)) b = max_blocks(16);
    k_gen_samples<<<(unsigned)b, 256, 0, s>>>(m, norm, seed, n, tlo, thi, clo, chi,
                                              samples_x, samples_t, fails);
    unsigned long long hf = 0;
@@ -864,12 +1110,10 @@ int ampe_mlp_train(void* h, int steps, int batch, float lr0, float* final_loss)
    for (int s = 0; s < steps; s++) {
       const long long off = (long long)(s % nb) * batch;
       const bool last = s == steps - 1;
-      int rc = M->grad(M->samples_x + 4 * off, M->samples_t + 2 * off, batch, nullptr,
-                       last ? &loss : nullptr);
-      if (rc) return rc;
       // cosine decay from lr0 to lr0/20
       const float lr = lr0 * (0.05f + 0.95f * 0.5f * (1.f + std::cos(3.14159265f * s / steps)));
-      rc = M->adam_step(lr, nullptr);
+      const int rc = M->step_tc(M->samples_x + 4 * off, M->samples_t + 2 * off, batch, lr,
+                                nullptr, last ? &loss : nullptr);
       if (rc) return rc;
    }
    int rc = M->pack(nullptr);
@@ -883,7 +1127,7 @@ int ampe_mlp_grad(void* h, const float* x, const float* target, int batch,
 {
    Mlp* M = (Mlp*)h;
    if (!M || !x || !target || batch < 1 || batch > M->batch) return AMPE_ERR_INVALID;
-   int rc = M->grad(x, target, batch, nullptr, loss);
+   int rc = M->step_tc(x, target, batch, 0.f, nullptr, loss);
    if (cudaDeviceSynchronize() != cudaSuccess) return AMPE_ERR_CUDA;
    return rc;
 }
@@ -934,6 +1178,22 @@ int ampe_mlp_infer(void* h, const ampe_model_t* grid, const double* phi,
    for (int d = 0; d < 3; d++) M->m.dx[d] = mm.dx[d];
    return M->infer(make_grid(mm), phi, conc, temp, guess_l, guess_s,
                    tensor_cores != 0, (cudaStream_t)stream);
+}
+
+int ampe_mlp_set_wait_limit(void* h, int wait_limit, int skip_issue)
+{
+   Mlp* M = (Mlp*)h;
+   if (!M || wait_limit < 1) return AMPE_ERR_INVALID;
+   M->wait_limit = wait_limit;
+   M->skip_issue = skip_issue ? 1 : 0;
+   return AMPE_OK;
+}
+
+int ampe_mlp_clear_status(void* h)
+{
+   Mlp* M = (Mlp*)h;
+   if (!M) return AMPE_ERR_INVALID;
+   return cudaMemset(M->err, 0, sizeof(int)) == cudaSuccess ? AMPE_OK : AMPE_ERR_CUDA;
 }
 
 int ampe_mlp_status(void* h)

@@ -25,7 +25,8 @@ double* g_dev_addr[kMaxDevices] = {nullptr};
 
 // Device address of the buffer on the current device; looked up once per
 // device (on its first call, which therefore must not be inside a stream
-// capture).
+// capture) and kept for the life of the process, so it does not survive a
+// cudaDeviceReset of that device.
 int scratch_on_current_device(double** out)
 {
    int dev = -1;

@@ -136,7 +136,7 @@ __global__ void k_quat_project(long long N, double* q)
 static unsigned nb(long long n)
 {
    long long b = (n + 255) / 256;
-   if (b > kMaxBlocks) b = kMaxBlocks;
+   if (b > max_blocks()) b = max_blocks();
    return (unsigned)(b < 1 ? 1 : b);
 }
 

@@ -179,8 +179,11 @@ struct DevLevel {
    Grid g;
    double dx[3];
    R *u = nullptr, *f = nullptr, *r = nullptr, *C = nullptr, *M = nullptr;
-   R* u2 = nullptr;  // second u buffer of the one-launch sweep (ping-pong)
-   bool fused = false;
+   // single-pass z-marching sweep (3D levels that qualify): u -> u2, then
+   // the two pointers swap
+   bool zsweep = false;
+   ZShape zs;
+   R* u2 = nullptr;
    R* D[3] = {nullptr, nullptr, nullptr};
    bool hasC = false, hasD = false, hasM = false;
    R cc = 0, dc = 0, mc = 0;
@@ -236,11 +239,8 @@ int fac_create(DevFac<R>& F, const ampe_model_t& m, int nlevels, bool hasD,
       for (int d = 0; d < 3; d++) L.dx[d] = mm.dx[d];
       const long long ng = L.g.cells_ghost();
       L.u = (R*)dalloc<R>(pool, ng, &err);
-      // the one-launch sweep stages halos in shared memory and recomputes the
-      // red halo; on GB300 two colour passes at one thread per cell run
-      // faster for this 7-point operator, so the stepper keeps them
-      L.fused = false;
-      if (L.fused) L.u2 = (R*)dalloc<R>(pool, ng, &err);
+      L.zsweep = sweep_z_ok<R>(L.g, &L.zs);
+      if (L.zsweep) L.u2 = (R*)dalloc<R>(pool, ng, &err);
       L.f = (R*)dalloc<R>(pool, ng, &err);
       L.r = (R*)dalloc<R>(pool, ng, &err);
       L.hasC = hasC;
@@ -321,16 +321,17 @@ double rms_interior(Ctx& cx, const Grid& g, const R* v)
    return sqrt(ss / (double)g.cells());
 }
 
-// red then black.  first: the sweep starts from u = 0.  Levels with even
-// extents run the one-launch sweep (u <- u2, pointers swapped); otherwise,
-// and when the residual maxima are wanted, two colour launches in place,
-// each writing through to the ghost images.
+// red then black.  first: the sweep starts from u = 0.  Levels that take
+// the single-pass z-marching sweep run it (u -> u2, pointers swapped) unless
+// the residual maxima are wanted; otherwise two colour launches in place,
+// each writing through to the ghost images (the one-launch box sweep
+// k_rb_sweep is reachable only through the leaf entry ampe_efo_rbgs_sweep).
 template <class R>
 void rb_sweep(Ctx& cx, DevLevel<R>& L, double* maxres, bool first = false)
 {
    FacOp<R> op = L.op();
-   if (L.fused && !maxres) {
-      rb_sweep_fused(op, L.g, L.f, first ? nullptr : L.u, L.u2, cx.s);
+   if (L.zsweep && !maxres) {
+      sweep_z(op, L.g, L.zs, L.f, first ? nullptr : L.u, L.u2, nullptr, (const R*)nullptr, cx.s);
       std::swap(L.u, L.u2);
       return;
    }
@@ -359,7 +360,12 @@ void vcycle(Ctx& cx, DevFac<R>& F, int l)
    vcycle(cx, F, l + 1);
    if (l == 0 && cx.mark) cx.mark(cx.owner, true);
    int it = 0;
-   if (cx.p->mg_post > 0 && !L.fused) {
+   if (cx.p->mg_post > 0 && L.zsweep) {
+      // prolongation fused into the first post-sweep (u + P e staged)
+      sweep_z(L.op(), L.g, L.zs, L.f, L.u, L.u2, &C.g, C.u, cx.s);
+      std::swap(L.u, L.u2);
+      it = 1;
+   } else if (cx.p->mg_post > 0) {
       // prolongation fused into the first post-sweep's two colours
       const FacOp<R> op = L.op();
       if (rbgs_color_prolong(op, L.g, L.f, L.u, 0, C.g, C.u, cx.s) == AMPE_OK) {
@@ -442,7 +448,8 @@ struct Stepper {
    Grid g;
    long long N = 0, NG = 0, NY = 0;
    int nb = 2;  // scalar fields in y: phi, c (+ q0..q3 when evolve_quat)
-   cudaStream_t s = nullptr;
+   cudaStream_t s = nullptr;      // the stream every launch and copy goes to
+   cudaStream_t own_s = nullptr;  // the stepper's private stream
    Reducer red;
    std::vector<void*> pool;
    // ghosted FP64 scratch
@@ -472,6 +479,7 @@ struct Stepper {
    bool cold = true;
    Mlp* mlp = nullptr;                            // attached surrogate
    unsigned long long* mcount = nullptr;          // mixed KKS counters [5]
+   int* kks_list = nullptr;  // cells for the FP64 polish (N + 1 ints, mixed path)
    // quaternion fields: ghosted q (4 NG) and its lagged copy, the cell
    // modulus |grad q| of the lagged copy, M_q(phi), face coefficients
    double *q_g = nullptr, *q_lag = nullptr, *ogm = nullptr, *mq = nullptr;
@@ -486,6 +494,15 @@ struct Stepper {
    DevFac<double> facp64, facc64, facq64;
    DevFac<float> facp32, facc32, facq32;
    int hist = 0;
+   // variable-step BDF (params adaptive = 1): y_{n-2}, f(y_n) for the
+   // explicit-Euler predictor of a first step, the sizes of the last two
+   // accepted steps, the next step's size and order, the accepted steps
+   // before an order change is considered, the growth cap of the next step
+   // size, how many back values (y_{n-1}, y_{n-2}) are valid
+   double *ynm2 = nullptr, *fn = nullptr;
+   double h_next = 0.0, h1 = 0.0, h2 = 0.0, eta_max = 1.0e4;
+   int q_next = 1, qwait = 2, nhist = 0;
+   bool fn_valid = false;
    double t = 0.0;
    ampe_step_stats_t st;
    // optional per-kernel CUDA-event timing on the stepper's stream
@@ -631,7 +648,7 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
          ProfScope ps(S, KT_KKS);
          kks_mixed(S.m, S.mp, S.g, S.tab, S.tabf, tf, S.phi_g, S.c_g,
                    sur ? S.guess_l : nullptr, sur ? S.guess_s : nullptr, S.clr32, S.csr32,
-                   S.cl32, S.cs32, S.dF32, S.mcount, S.s);
+                   S.cl32, S.cs32, S.dF32, S.kks_list, S.mcount, S.s);
       }
       {
          ProfScope ps(S, KT_RHS);
@@ -1046,27 +1063,14 @@ static int gmres32(Stepper& S, double gamma, const float* bf, double* x,
    return k;
 }
 
-// one BDF step of size h, order q; result in S.ynew.  0 = converged.
-static int bdf_step(Stepper& S, double h, int q)
+// Newton iteration of one BDF step: y - gamma f(y) = a from the predictor
+// in S.y, convergence test del min(1, crate) <= newton_coef; result in
+// S.ynew.  0 = converged.
+static int bdf_newton(Stepper& S, double gamma, double newton_coef)
 {
    const long long ny = S.NY;
-   double *a = S.a, *y = S.y, *yn = S.yn, *ynm1 = S.ynm1, *w = S.w;
+   double *a = S.a, *y = S.y, *yn = S.yn, *w = S.w;
    double *fy = S.fy, *b = S.b, *d = S.d;
-   double gamma;
-   if (q == 1) {
-      gamma = h;
-      map(ny, [=] __device__(long long t) {
-         a[t] = yn[t];
-         y[t] = yn[t];
-      }, S.s);
-   } else {
-      gamma = 2.0 * h / 3.0;
-      const double third = 1.0 / 3.0;
-      map(ny, [=] __device__(long long t) {
-         a[t] = (4.0 * yn[t] - ynm1[t]) * third;
-         y[t] = 2.0 * yn[t] - ynm1[t];
-      }, S.s);
-   }
    const double rtol = S.p.rtol, atol = S.p.atol;
    double* wi = S.wi;
    if (S.p.precision == 1) {
@@ -1089,7 +1093,7 @@ static int bdf_step(Stepper& S, double h, int q)
       }, S.s);
    }
    double crate = 1.0, delp = 0.0;
-   const double lintol = S.p.lin_coef * S.p.newton_coef;
+   const double lintol = S.p.lin_coef * newton_coef;
    for (int it = 0; it < S.p.max_newton; it++) {
       eval_rhs(S, y, nullptr, 0.0, fy, 0);
       if (it == 0 && S.p.precond) precond_setup(S, gamma);
@@ -1114,7 +1118,7 @@ static int bdf_step(Stepper& S, double h, int q)
          return xv * xv;
       }) / (double)ny);
       if (it > 0) crate = std::max(0.3 * crate, del / delp);
-      const double dcon = del * std::min(1.0, crate) / S.p.newton_coef;
+      const double dcon = del * std::min(1.0, crate) / newton_coef;
       if (dcon <= 1.0) {
          cudaMemcpyAsync(S.ynew, y, sizeof(double) * ny,
                          cudaMemcpyDeviceToDevice, S.s);
@@ -1129,11 +1133,293 @@ static int bdf_step(Stepper& S, double h, int q)
    return 1;
 }
 
+// one fixed-size BDF step of size h, order q (constant-step coefficients,
+// linear-extrapolation predictor); result in S.ynew.  0 = converged.
+static int bdf_step(Stepper& S, double h, int q)
+{
+   const long long ny = S.NY;
+   double *a = S.a, *y = S.y, *yn = S.yn, *ynm1 = S.ynm1;
+   double gamma;
+   if (q == 1) {
+      gamma = h;
+      map(ny, [=] __device__(long long t) {
+         a[t] = yn[t];
+         y[t] = yn[t];
+      }, S.s);
+   } else {
+      gamma = 2.0 * h / 3.0;
+      const double third = 1.0 / 3.0;
+      map(ny, [=] __device__(long long t) {
+         a[t] = (4.0 * yn[t] - ynm1[t]) * third;
+         y[t] = 2.0 * yn[t] - ynm1[t];
+      }, S.s);
+   }
+   return bdf_newton(S, gamma, S.p.newton_coef);
+}
+
 static void swap_ptr(double*& a, double*& b)
 {
    double* t = a;
    a = b;
    b = t;
+}
+
+// KKS warm starts of the next step: the accepted step's phase
+// concentrations (QuatModel::resetRefPhaseConcentrations, QuatModel.cc:5218)
+static void keep_warm_start(Stepper& S)
+{
+   const size_t gb = sizeof(double) * (size_t)S.NG;
+   if (S.p.precision == 1) {
+      const size_t gf = sizeof(float) * (size_t)S.NG;
+      cudaMemcpyAsync(S.clr32, S.cl32, gf, cudaMemcpyDeviceToDevice, S.s);
+      cudaMemcpyAsync(S.csr32, S.cs32, gf, cudaMemcpyDeviceToDevice, S.s);
+   } else {
+      cudaMemcpyAsync(S.clr, S.cl_nf, gb, cudaMemcpyDeviceToDevice, S.s);
+      cudaMemcpyAsync(S.csr, S.cs_nf, gb, cudaMemcpyDeviceToDevice, S.s);
+   }
+}
+
+// Variable-step BDF predictor of the next step (size h, order q, from the
+// accepted history): pred = k0 y_n + k1 y_{n-1} + k2 y_{n-2} + k3 f(y_n).
+// Also the error constant c of the estimate LTE ~ c (y_{n+1} - pred):
+//  - no history: explicit Euler y_n + h f(y_n); the BDF1 error h^2 y''/2
+//    against the predictor's h^2 y'': c = 1/2;
+//  - order 1: linear extrapolation through y_n, y_{n-1}, ratio
+//    w = h / h_{n-1}: c = w / (2w + 1) (1/3 at constant steps);
+//  - order 2: quadratic extrapolation through y_n, y_{n-1}, y_{n-2}; the
+//    variable-coefficient BDF2 error A y3/6 with A = h^3 (1+w)^2 /
+//    (w (1+2w)) against the predictor's P y3/6 with P = h (h+h1)(h+h1+h2)
+//    (y3 the third derivative): c = A / (P + A) (2/11 at constant steps).
+struct Pred {
+   double k0, k1, k2, k3, c;
+};
+static Pred predictor(const Stepper& S, double h, int q)
+{
+   Pred P{1.0, 0.0, 0.0, 0.0, 0.5};
+   if (S.nhist == 0) {
+      P.k3 = h;
+      return P;
+   }
+   const double h1 = S.h1, w = h / h1;
+   if (q == 1) {
+      P.k0 = 1.0 + w;
+      P.k1 = -w;
+      P.c = w / (2.0 * w + 1.0);
+      return P;
+   }
+   const double h2 = S.h2;
+   P.k0 = (h + h1) * (h + h1 + h2) / (h1 * (h1 + h2));
+   P.k1 = -h * (h + h1 + h2) / (h1 * h2);
+   P.k2 = h * (h + h1) / ((h1 + h2) * h2);
+   const double A = h * h * h * (1.0 + w) * (1.0 + w) / (w * (1.0 + 2.0 * w));
+   const double Pp = h * (h + h1) * (h + h1 + h2);
+   P.c = A / (Pp + A);
+   return P;
+}
+
+// WRMS norm (weights S.w) of c0 v0 + c1 v1 (+ c2 v2) (+ c3 v3)
+static double wrms_comb(Stepper& S, const double* v0, double c0, const double* v1, double c1,
+                        const double* v2, double c2, const double* v3, double c3)
+{
+   const double* w = S.w;
+   const double ss = S.red.sum(S.NY, [=] __device__(long long t) {
+      double x = c0 * v0[t] + c1 * v1[t];
+      if (v2) x += c2 * v2[t];
+      if (v3) x += c3 * v3[t];
+      x *= w[t];
+      return x * x;
+   });
+   return std::sqrt(ss / (double)S.NY);
+}
+
+// One accepted step of a variable-step BDF of orders 1 and 2 with CVODE's
+// local error test and step-size / order selection (SUNDIALS CVODE 5.7.0
+// as configured by CVODESolver::initializeCVODE, samrai/CVODESolver.cc:
+// 112-258, and driven in CV_ONE_STEP mode, QuatIntegrator.cc:1571-1596).
+// Its published rules: error test dsm = c ||y_{n+1} - pred||_WRMS <= 1;
+// Newton test del min(1, crate) c <= 0.1; after a step
+// eta = 1 / ((6 dsm)^(1/(q+1)) + 1e-6), and every q+1 steps the order-(q-1)
+// and order-(q+1) candidates (bias 6 and 10); no change below eta 1.5;
+// growth capped at 1e4 on the first step and 10 afterwards, at 1 after a
+// step with failures; after an error-test failure eta = max(0.1, ...), at
+// most 0.2 from the second failure, order 1 from the third, 7 failures at
+// most; after a Newton failure eta = 0.25, 10 failures at most.  The
+// corrector is a variable-coefficient BDF with extrapolation predictors
+// instead of CVODE's Nordsieck array, so the step sequence is this
+// algorithm's, not CVODE's own.  The step ends at t_stop at the latest
+// (when t_stop > t).  0 = accepted, 1 = failed (state unchanged).
+static int adaptive_step(Stepper& S, double t_stop)
+{
+   const long long ny = S.NY;
+   const double hmax = S.p.h_max > 0.0 ? S.p.h_max : 1.0e300;
+   int nef = 0, ncf = 0;
+   for (;;) {
+      int q = std::min(S.q_next, std::min(2, S.p.max_order));
+      if (S.nhist < q) q = S.nhist < 1 ? 1 : S.nhist;
+      double h = std::min(S.h_next, hmax);
+      if (t_stop > S.t && S.t + h > t_stop - 1e-12 * std::fabs(t_stop)) h = t_stop - S.t;
+      if (S.nhist == 0 && !S.fn_valid) {
+         eval_rhs(S, S.yn, nullptr, 0.0, S.fn, 0);
+         S.fn_valid = true;
+      }
+      const Pred P = predictor(S, h, q);
+      double gamma = h, a0 = 1.0, a1 = 0.0;
+      if (q == 2) {
+         const double w = h / S.h1;
+         a0 = (1.0 + w) * (1.0 + w) / (1.0 + 2.0 * w);
+         a1 = -w * w / (1.0 + 2.0 * w);
+         gamma = h * (1.0 + w) / (1.0 + 2.0 * w);
+      }
+      {
+         double *a = S.a, *y = S.y;
+         const double *yn = S.yn, *y1 = S.ynm1, *y2 = S.ynm2, *fn = S.fn;
+         const Pred Q = P;
+         const bool use1 = S.nhist >= 1, use2 = q == 2, usef = S.nhist == 0;
+         map(ny, [=] __device__(long long t) {
+            double pr = Q.k0 * yn[t];
+            if (use1) pr += Q.k1 * y1[t];
+            if (use2) pr += Q.k2 * y2[t];
+            if (usef) pr += Q.k3 * fn[t];
+            y[t] = pr;
+            a[t] = use2 ? a0 * yn[t] + a1 * y1[t] : yn[t];
+         }, S.s);
+      }
+      if (bdf_newton(S, gamma, 0.1 / P.c)) {
+         ncf++;
+         if (ncf >= 10 || h <= S.p.h_min) return 1;
+         S.h_next = h * 0.25;
+         S.eta_max = 1.0;
+         continue;
+      }
+      // local error estimate from the predictor-corrector difference
+      const double dsm =
+          P.c * wrms_comb(S, S.ynew, 1.0, S.yn, -P.k0, S.nhist >= 1 ? S.ynm1 : nullptr, -P.k1,
+                          q == 2 ? S.ynm2 : (S.nhist == 0 ? S.fn : nullptr),
+                          q == 2 ? -P.k2 : -P.k3);
+      if (dsm > 1.0) {
+         nef++;
+         S.st.err_test_fails++;
+         if (nef >= 7 || h <= S.p.h_min) return 1;
+         double eta = 1.0 / (std::pow(6.0 * dsm, 1.0 / (q + 1)) + 1.0e-6);
+         eta = std::max(0.1, eta);
+         if (nef >= 2) eta = std::min(eta, 0.2);
+         if (nef >= 3) S.q_next = 1;
+         S.h_next = h * eta;
+         S.eta_max = 1.0;
+         continue;
+      }
+      // accepted: the next step's size and order
+      double eta = 1.0 / (std::pow(6.0 * dsm, 1.0 / (q + 1)) + 1.0e-6);
+      int qn = q;
+      if (--S.qwait <= 0) {
+         if (q == 2) {  // order 1: h^2 times the second divided difference
+            const double h1 = S.h1;
+            const double ca = 1.0 / (h * (h + h1)), cb = 1.0 / (h1 * (h + h1));
+            const double dsm1 = wrms_comb(S, S.ynew, h * h * ca, S.yn, -h * h * (ca + cb),
+                                          S.ynm1, h * h * cb, nullptr, 0.0);
+            const double em = 1.0 / (std::pow(6.0 * dsm1, 0.5) + 1.0e-6);
+            if (em > eta) {
+               eta = em;
+               qn = 1;
+            }
+         } else if (S.p.max_order >= 2 && S.nhist >= 2) {
+            // order 2: (4/3) h^3 times the third divided difference
+            // y[t_{n+1}, t_n, t_{n-1}, t_{n-2}] = sum_i y_i / prod_{j!=i}(t_i - t_j)
+            const double h1 = S.h1, h2 = S.h2;
+            const double t0 = h, t1 = 0.0, t2 = -h1, t3 = -h1 - h2;
+            const double w0 = 1.0 / ((t0 - t1) * (t0 - t2) * (t0 - t3));
+            const double w1 = 1.0 / ((t1 - t0) * (t1 - t2) * (t1 - t3));
+            const double w2 = 1.0 / ((t2 - t0) * (t2 - t1) * (t2 - t3));
+            const double w3 = 1.0 / ((t3 - t0) * (t3 - t1) * (t3 - t2));
+            const double k = 4.0 / 3.0 * h * h * h;
+            const double dsm2 = wrms_comb(S, S.ynew, k * w0, S.yn, k * w1, S.ynm1, k * w2,
+                                          S.ynm2, k * w3);
+            const double ep = 1.0 / (std::pow(10.0 * dsm2, 1.0 / 3.0) + 1.0e-6);
+            if (ep > eta) {
+               eta = ep;
+               qn = 2;
+            }
+         }
+         S.qwait = qn + 1;
+      }
+      if (eta < 1.5) {
+         eta = 1.0;
+         qn = q;
+      } else {
+         eta = std::min(eta, S.eta_max);
+      }
+      if (nef || ncf) eta = std::min(eta, 1.0);
+      S.eta_max = 10.0;
+      S.h_next = std::min(h * eta, hmax);
+      S.q_next = qn;
+      // history shift: y_{n-2} <- y_{n-1} <- y_n <- y_{n+1}
+      double* old2 = S.ynm2;
+      S.ynm2 = S.ynm1;
+      S.ynm1 = S.yn;
+      S.yn = S.ynew;
+      S.ynew = old2;
+      S.h2 = S.h1;
+      S.h1 = h;
+      S.nhist = std::min(S.nhist + 1, 2);
+      S.fn_valid = false;
+      S.t += h;
+      S.st.h_last = h;
+      S.st.q_last = q;
+      return 0;
+   }
+}
+
+// a new start for the variable-step BDF: first step of size dt, order 1
+static void restart_history(Stepper& S)
+{
+   S.nhist = 0;
+   S.q_next = 1;
+   S.qwait = 2;
+   S.h_next = S.p.dt;
+   S.h1 = S.h2 = 0.0;
+   S.eta_max = 1.0e4;
+   S.fn_valid = false;
+}
+
+// bookkeeping after an accepted step (either mode)
+static void step_accepted(Stepper& S)
+{
+   S.cold = false;
+   keep_warm_start(S);
+   S.st.steps++;
+   if (S.prof) {
+      cudaStreamSynchronize(S.s);
+      prof_collect(S);
+   }
+}
+
+// counters of the KKS kernels and the history into the stats
+static int finish_stats(Stepper& S, ampe_step_stats_t* stats)
+{
+   unsigned long long c[2] = {0, 0}, mc[5] = {0, 0, 0, 0, 0};
+   cudaMemcpyAsync(c, S.counters, sizeof(c), cudaMemcpyDeviceToHost, S.s);
+   if (S.mcount) cudaMemcpyAsync(mc, S.mcount, sizeof(mc), cudaMemcpyDeviceToHost, S.s);
+   if (cudaStreamSynchronize(S.s) != cudaSuccess) return AMPE_ERR_CUDA;
+   S.st.kks_iters = (long long)(c[0] + mc[0] + mc[4]);
+   S.st.kks_fail = (long long)(c[1] + mc[1]);
+   S.st.kks_fp64_cells = (long long)mc[2];
+   S.st.kks_fallback = (long long)mc[3];
+   S.st.t = S.t;
+   S.st.h_next = S.p.adaptive ? S.h_next : S.p.dt;
+   S.st.q_next = S.p.adaptive ? S.q_next : (S.hist ? std::min(2, S.p.max_order) : 1);
+   if (stats) *stats = S.st;
+   return AMPE_OK;
+}
+
+// accepted variable steps until t_stop (if > t) or max_steps
+static int advance_adaptive(Stepper& S, double t_stop, int max_steps)
+{
+   for (int n = 0; n < max_steps; n++) {
+      if (t_stop > S.t && S.t >= t_stop - 1e-12 * std::fabs(t_stop)) break;
+      if (adaptive_step(S, t_stop)) return AMPE_ERR_NOT_CONVERGED;
+      step_accepted(S);
+   }
+   return AMPE_OK;
 }
 
 }  // namespace ampe
@@ -1153,6 +1439,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    if (p->precond < 0 || p->precond > 2 || p->precision < 0 ||
        p->precision > 1 || p->max_krylov > kMaxKrylov)
       return AMPE_ERR_INVALID;
+   if (p->adaptive < 0 || p->adaptive > 1 || p->h_min < 0.0) return AMPE_ERR_INVALID;
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC) {
       if (m->qlen != 2 && m->qlen != 4) return AMPE_ERR_INVALID;
       if (m->evolve_quat && m->qlen != 4) return AMPE_ERR_INVALID;
@@ -1165,6 +1452,8 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    Stepper* S = new (std::nothrow) Stepper;
    if (!S) return AMPE_ERR_INVALID;
    S->m = *m;
+   S->m.ng_side = 0;  // the stepper's own face arrays carry no ghosts
+   m = &S->m;
    S->p = *p;
    S->g = make_grid(*m);
    S->N = S->g.cells();
@@ -1176,6 +1465,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    int err = AMPE_OK;
    if (cudaStreamCreateWithFlags(&S->s, cudaStreamNonBlocking) != cudaSuccess)
       err = AMPE_ERR_CUDA;
+   S->own_s = S->s;
    if (!err) err = S->red.init(S->s);
    double** gh[] = {&S->phi_g, &S->c_g, &S->cl, &S->cs, &S->clr,
                     &S->csr, &S->cl_nf, &S->cs_nf, &S->phi_lag, &S->tfield};
@@ -1184,6 +1474,11 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    double** vv[] = {&S->yn, &S->ynm1, &S->ynew, &S->a,   &S->y,  &S->fy, &S->b,  &S->d,
                     &S->w,  &S->wi,   &S->tmp,  &S->av, &S->fp, &S->ysave, &S->ym1save};
    for (double** q : vv) *q = dvec(*S, S->NY, &err);
+   if (p->adaptive) {
+      S->ynm2 = dvec(*S, S->NY, &err);
+      S->fn = dvec(*S, S->NY, &err);
+   }
+   S->h_next = p->dt;
    if (p->precision == 1) {
       for (int l = 0; l <= p->max_krylov; l++)
          S->Vf.push_back((float*)dalloc<float>(S->pool, S->NY, &err));
@@ -1227,6 +1522,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
          S->fw.B[d] = (float*)dalloc<float>(S->pool, nfd[d], &err);
       }
       S->mcount = (unsigned long long*)dalloc<unsigned long long>(S->pool, 5, &err);
+      S->kks_list = (int*)dalloc<int>(S->pool, S->N + 1, &err);
       if (p->surrogate) {
          S->guess_l = (float*)dalloc<float>(S->pool, S->N, &err);
          S->guess_s = (float*)dalloc<float>(S->pool, S->N, &err);
@@ -1297,7 +1593,7 @@ int ampe_stepper_destroy(void* h)
    for (cudaEvent_t e : S->ev_pool) cudaEventDestroy(e);
    for (void* q : S->pool) cudaFree(q);
    S->red.release();
-   if (S->s) cudaStreamDestroy(S->s);
+   if (S->own_s) cudaStreamDestroy(S->own_s);
    delete S;
    return AMPE_OK;
 }
@@ -1342,6 +1638,7 @@ int ampe_stepper_set_state(void* h, const double* phi, const double* conc,
       to_ghosted<double>(S->g, stage, nullptr, 0.0, S->tfield, S->s);
    }
    S->hist = 0;
+   restart_history(*S);
    S->t = 0.0;
    S->cold = !(cl && cs);
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
@@ -1394,9 +1691,13 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
 {
    Stepper* S = (Stepper*)h;
    if (!S || nsteps < 0) return AMPE_ERR_INVALID;
+   if (S->p.adaptive) {
+      const int rc = advance_adaptive(*S, -1.0e300, nsteps);
+      const int rs = finish_stats(*S, stats);
+      return rc ? rc : rs;
+   }
    int ret = AMPE_OK;
    const size_t b2 = sizeof(double) * (size_t)S->NY;
-   const size_t gb = sizeof(double) * (size_t)S->NG;
    for (int n = 0; n < nsteps; n++) {
       double hstep = S->p.dt;
       const int q = S->hist ? std::min(2, S->p.max_order) : 1;
@@ -1437,36 +1738,48 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
          break;
       }
       S->hist = retries == 0 ? 1 : 0;
-      S->cold = false;
       swap_ptr(S->ynm1, S->yn);  // ynm1 <- yn
       swap_ptr(S->yn, S->ynew);  // yn <- ynew
-      if (S->p.precision == 1) {
-         const size_t gf = sizeof(float) * (size_t)S->NG;
-         cudaMemcpyAsync(S->clr32, S->cl32, gf, cudaMemcpyDeviceToDevice, S->s);
-         cudaMemcpyAsync(S->csr32, S->cs32, gf, cudaMemcpyDeviceToDevice, S->s);
-      } else {
-         cudaMemcpyAsync(S->clr, S->cl_nf, gb, cudaMemcpyDeviceToDevice, S->s);
-         cudaMemcpyAsync(S->csr, S->cs_nf, gb, cudaMemcpyDeviceToDevice, S->s);
-      }
       S->t += S->p.dt;
-      S->st.steps++;
-      if (S->prof) {
-         cudaStreamSynchronize(S->s);
-         prof_collect(*S);
-      }
+      S->st.h_last = S->p.dt;
+      S->st.q_last = q;
+      step_accepted(*S);
    }
-   unsigned long long c[2] = {0, 0}, mc[5] = {0, 0, 0, 0, 0};
-   cudaMemcpyAsync(c, S->counters, sizeof(c), cudaMemcpyDeviceToHost, S->s);
-   if (S->mcount)
-      cudaMemcpyAsync(mc, S->mcount, sizeof(mc), cudaMemcpyDeviceToHost, S->s);
-   if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
-   S->st.kks_iters = (long long)(c[0] + mc[0] + mc[4]);
-   S->st.kks_fail = (long long)(c[1] + mc[1]);
-   S->st.kks_fp64_cells = (long long)mc[2];
-   S->st.kks_fallback = (long long)mc[3];
-   S->st.t = S->t;
-   if (stats) *stats = S->st;
-   return ret;
+   const int rs = finish_stats(*S, stats);
+   return ret ? ret : rs;
+}
+
+int ampe_stepper_advance_to(void* h, double t_stop, int max_steps, ampe_step_stats_t* stats)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || max_steps < 0 || !S->p.adaptive) return AMPE_ERR_INVALID;
+   const int rc = advance_adaptive(*S, t_stop, max_steps);
+   const int rs = finish_stats(*S, stats);
+   return rc ? rc : rs;
+}
+
+int ampe_stepper_set_temperature(void* h, double T0, double gradT)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S || !(T0 > 0.0) || S->m.temp_mode == AMPE_TEMP_FIELD) return AMPE_ERR_INVALID;
+   if (S->m.temp_mode == AMPE_TEMP_CONSTANT && gradT != 0.0) return AMPE_ERR_INVALID;
+   S->m.T0 = T0;
+   S->m.gradT = gradT;
+   const float2* dq = S->mp.dq;
+   S->mp = make_mix_params(S->m);
+   S->mp.dq = dq;
+   const int nt = S->m.temp_mode == AMPE_TEMP_GRADIENT ? S->m.n[0] : 1;
+   int err = AMPE_OK;
+   if (S->tab) err = build_thermo_table(S->m, S->tab, nt, S->s);
+   if (!err && S->tabf) err = build_coef_f(S->tab, S->tabf, nt, S->s);
+   if (!err && S->dqtab) err = build_diff_table(S->m, S->mp, S->g, S->dqtab, S->s);
+   if (S->mlp) {  // the network sees the stepper's temperature field
+      S->mlp->m.T0 = T0;
+      S->mlp->m.gradT = gradT;
+   }
+   S->fn_valid = false;
+   if (!err && cudaStreamSynchronize(S->s) != cudaSuccess) err = AMPE_ERR_CUDA;
+   return err;
 }
 
 long long ampe_stepper_kernel_launches(void* h)
@@ -1486,6 +1799,16 @@ int ampe_stepper_attach_surrogate(void* h, void* mlp)
    M->m.gradT = S->m.gradT;
    for (int d = 0; d < 3; d++) M->m.dx[d] = S->m.dx[d];
    S->mlp = M;
+   return AMPE_OK;
+}
+
+int ampe_stepper_set_stream(void* h, void* stream)
+{
+   Stepper* S = (Stepper*)h;
+   if (!S) return AMPE_ERR_INVALID;
+   if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
+   S->s = stream ? (cudaStream_t)stream : S->own_s;
+   S->red.s = S->s;
    return AMPE_OK;
 }
 
@@ -1569,6 +1892,7 @@ int ampe_stepper_set_quat(void* h, const double* q, int host)
    cudaMemcpyAsync(S->ynm1 + 2 * S->N, S->yn + 2 * S->N, b4, cudaMemcpyDeviceToDevice,
                    S->s);
    S->hist = 0;
+   restart_history(*S);
    if (cudaStreamSynchronize(S->s) != cudaSuccess) return AMPE_ERR_CUDA;
    return AMPE_OK;
 }

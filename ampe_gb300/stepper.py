@@ -127,5 +127,18 @@ class ImplicitStepper:
               "ampe_stepper_advance")
         return st.as_dict()
 
+    def advance_to(self, t_stop, max_steps=1):
+        """Variable steps (params.adaptive = 1) until t_stop or max_steps
+        accepted steps (max_steps = 1: CVODE's one-step mode with a stop
+        time)."""
+        st = abi.StepStats()
+        check(lib.ampe_stepper_advance_to(self._h, float(t_stop), int(max_steps), C.byref(st)),
+              "ampe_stepper_advance_to")
+        return st.as_dict()
+
+    def set_temperature(self, T0, gradT=0.0):
+        check(lib.ampe_stepper_set_temperature(self._h, float(T0), float(gradT)),
+              "ampe_stepper_set_temperature")
+
     def kernel_launches(self):
         return lib.ampe_stepper_kernel_launches(self._h)

@@ -56,19 +56,22 @@ SMOOTH_BYTES_PER_CELL = {3: 20, 2: 18}
 SMOOTH_BYTES_PER_CELL_FP64 = {3: 40, 2: 36}
 # DRAM bytes per cell of one finest-level sweep of the FP32 smoother on the
 # 3D CALPHAD phi + c level, from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) of both colour launches of each block at 224^3:
-# phase block 514.1 MB, composition block 307.8 MB per sweep, mean over the
-# two blocks / 11,239,424 cells; traffic scales with the cells
-SMOOTH_DRAM_BYTES_PER_CELL_MEASURED = 36.56
+# dram__bytes_write.sum) of the sweep launches of both blocks; None until
+# captured for the current kernel
+SMOOTH_DRAM_BYTES_PER_CELL_MEASURED = None
 # MLP inference: 2 (3*64 + 64*64 + 64*64 + 64*2) multiply-adds per cell
 MLP_FLOPS_PER_CELL = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
 KERNEL_NAMES = {
-    False: {"kks_newton": "k_kks_mixed", "rhs_fused": "k_rhs_mixed",
+    False: {"kks_newton": "k_kks_f32+k_kks_polish64", "rhs_fused": "k_rhs_mixed",
             "jv_analytic": "k_jv_point+k_jv_stencil",
-            "smooth_fine": "k_rbgs_color<float,%d> x2 (finest-level red-black sweep)"},
+            "smooth_fine": {3: "k_sweep_z<float> (finest-level red-black sweep, one z-marching "
+                               "launch)",
+                            2: "k_rbgs_color<float,2> x2 (finest-level red-black sweep)"}},
     True: {"kks_newton": "k_kks_interior", "rhs_fused": "k_rhs_fused<0>",
            "jv_analytic": "-",
-           "smooth_fine": "k_rbgs_color<double,%d> x2 (finest-level red-black sweep)"},
+           "smooth_fine": {3: "k_sweep_z<double> (finest-level red-black sweep, one z-marching "
+                              "launch)",
+                           2: "k_rbgs_color<double,2> x2 (finest-level red-black sweep)"}},
 }
 # profiling-timer kinds of the stepper (ampe_stepper_kernel_time)
 KINDS = ((0, "kks_newton"), (1, "rhs_fused"), (2, "jv_analytic"), (3, "mlp_infer_tc"),
@@ -308,9 +311,11 @@ def flushes_l2(args, m):
     return m.cells() * 8 * state_fields(args.workload) < L2_BYTES
 
 
-def arm_config(args, head=None, ws=1):
-    """The config object of both arms' JSON lines (the workload at full size)."""
-    m, _ = workload(args.n, args.workload, state=False)
+def arm_config(args, head=None, ws=1, n=None):
+    """The config object of an arm's JSON line: the workload at side n (the
+    full size by default; the reference arm passes the side it stepped)."""
+    n = args.n if n is None else n
+    m, _ = workload(n, args.workload, state=False)
     N = m.cells()
     mb = N * 8 * state_fields(args.workload) / 2 ** 20
     if flushes_l2(args, m):
@@ -318,9 +323,16 @@ def arm_config(args, head=None, ws=1):
               "state %.1f MB < L2" % (L2_FLUSH_BYTES // 2 ** 20, mb))
     else:
         l2 = "inputs larger than L2 (state %.0f MB)" % mb
-    return {"workload": WORKLOAD_NAMES[args.workload] % (args.n, args.atol),
-            "path": head or args.path, "cells": N, "l2": l2,
+    name = WORKLOAD_NAMES[args.workload] % (n, args.atol)
+    if n != args.n:
+        name += ": %d-cell sample of the %d-cell level" % (N, full_cells(args))
+    return {"workload": name, "path": head or args.path, "cells": N, "l2": l2,
             "parallelism": "replicas" if ws > 1 else "single"}
+
+
+def full_cells(args):
+    m, _ = workload(args.n, args.workload, state=False)
+    return m.cells()
 
 
 def cpu_baseline(args, threads=None):
@@ -334,7 +346,7 @@ def cpu_baseline(args, threads=None):
     s = O.OracleStepper(m, p)
     st0.load(s)
     s.advance(1)  # warm-up (first-touch, BDF1 start)
-    steps = 2
+    steps = 5
     t0 = time.perf_counter()
     rc, st = s.advance(steps)
     dt = time.perf_counter() - t0
@@ -368,7 +380,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": arm_config(args),
+        "config": arm_config(args, n=n),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "%d^%d level (%d cells) of the same workload, %d implicit "
                                    "steps per timed run, oracle/ C++ FP64 with OpenMP (reference "
@@ -438,7 +450,6 @@ def timed_path(args, m, st0, path, local, mlp=None):
     cold = {"ms": c0.elapsed_time(c1), "kks_iters": cst["kks_iters"] - k0}
     g.advance(max(0, args.warmup - 1))
     torch.cuda.synchronize()
-    L.ampe_stepper_profile(g._h, 1)
     launches0 = L.ampe_stepper_kernel_launches(g._h)
     clocks = ClockSampler(local)
     clocks.start()
@@ -470,6 +481,18 @@ def timed_path(args, m, st0, path, local, mlp=None):
         torch.cuda.profiler.stop()
     clocks.stop()
     launches = L.ampe_stepper_kernel_launches(g._h) - launches0
+    # per-kernel CUDA-event times in a separate pass of the same number of
+    # steps (events around every kernel class and a stream synchronisation
+    # per step), so that the timed steps above carry no instrumentation
+    L.ampe_stepper_profile(g._h, 1)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    p0.record(stream)
+    g.advance(args.steps)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    ms_prof = p0.elapsed_time(p1)
     kt = {}
     for kind, name in KINDS:
         tot, cnt = C.c_double(), C.c_longlong()
@@ -480,7 +503,8 @@ def timed_path(args, m, st0, path, local, mlp=None):
     state["phi"], state["c"] = g.get_state()[:2]
     if st0.quat is not None:
         state["q"] = g.get_quat()
-    return {"ms": ms, "stats": st, "launches": int(launches), "kernels": kt,
+    return {"ms": ms, "ms_profiled": ms_prof, "stats": st, "launches": int(launches),
+            "kernels": kt,
             "clocks": clocks.summary(), "value": N * args.steps / (ms / 1e3),
             "cold_start_step": cold}, state, g
 
@@ -571,7 +595,7 @@ def run_ours(args):
                                  precision=0)
         gr = ImplicitStepper(m, pr)
         st0.load(gr)
-        gr.advance(args.warmup + args.steps)
+        gr.advance(args.warmup + 2 * args.steps)  # the timed and the profiled steps
         refs = {"phi": None, "c": None}
         refs["phi"], refs["c"] = gr.get_state()[:2]
         if st0.quat is not None:
@@ -607,17 +631,25 @@ def run_ours(args):
         nbytes = per_cell[kname] * N
         achieved = nbytes / (avg_ms / 1e3) / 1e9
         kn = KERNEL_NAMES[head == "fp64"][kname]
+        if isinstance(kn, dict):
+            kn = kn[m.dim]
         traffic = None
-        if (kname == "smooth_fine" and head != "fp64" and args.workload == "calphad"):
+        if (kname == "smooth_fine" and head != "fp64" and args.workload == "calphad"
+                and SMOOTH_DRAM_BYTES_PER_CELL_MEASURED is not None):
             traffic = SMOOTH_DRAM_BYTES_PER_CELL_MEASURED * N
-        roof = {"bound": "hbm", "kernel": kn % m.dim if "%d" in kn else kn,
+        roof = {"bound": "hbm", "kernel": kn,
                 "achieved": achieved, "peak": pk["hbm_gbs"], "peak_kind": pk_kind, "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                 "algorithmic_bytes_per_launch": nbytes}
         if traffic is not None:
             roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of both "
                                       "blocks' colour launches at 224^3, scaled by cells")
-    roof.update({"avg_launch_ms": avg_ms, "launches": cnt, "share_of_step": tot / res_h["ms"]})
+    roof.update({"avg_launch_ms": avg_ms, "launches": cnt,
+                 "share_of_step": tot / res_h["ms_profiled"],
+                 "timing": "kernel times from a profiled pass of %d further steps (%.2f ms/step "
+                           "with the per-kernel events, %.2f ms/step without)"
+                           % (args.steps, res_h["ms_profiled"] / args.steps,
+                              res_h["ms"] / args.steps)})
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,

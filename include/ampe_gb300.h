@@ -22,10 +22,15 @@
  *     active direction (no z ghosts in 2D); strides sx=1, sy=n0+2ng,
  *     sz=(n0+2ng)*(n1+2ng);
  *   - a side (face) field with normal d is stored like a SAMRAI SideData with
- *     ghost width 0: extent n_d+1 along d, n_e along the others, x fastest;
+ *     ghost width m->ng_side (0 by default): extent n_d+1+2g along d,
+ *     n_e+2g along the others (no z ghosts in 2D), x fastest;
  *   - return value: 0 success, <0 error (AMPE_ERR_*), >0 a count of cells
  *     or cycles that did not converge (never an abort).
- * Nothing here allocates device memory except ampe_stepper_create.
+ * Device memory is allocated only by ampe_stepper_create (the stepper's
+ * whole workspace), ampe_mlp_create (the network and its training buffers)
+ * and ampe_mlp_generate (the sample set); every other entry point works in
+ * the caller's buffers (or, for ampe_efo_residual_rms_noalloc, in one
+ * library-owned static buffer).
  */
 #ifndef AMPE_GB300_H
 #define AMPE_GB300_H
@@ -133,7 +138,12 @@ typedef struct ampe_model {
 
    /* ---- composition flux form (QuatModelParameters.cc:203-222 rhs_form) ---- */
    int conc_form;  /* AMPE_CONC_EBS or AMPE_CONC_KKS */
-   int pad2;
+   /* ghost width of the side (face) arrays the leaf entry points take and
+    * return (SAMRAI SideData ghost width, passed by the reference per array,
+    * e.g. fluxng beside phaseng in GRADIENT_FLUX, QuatFort.h:50-61); 0 by
+    * default.  Only interior faces are read or written.  The stepper keeps
+    * its own face arrays and ignores it. */
+   int ng_side;
 } ampe_model_t;
 
 /* Integrator / preconditioner controls (QuatIntegrator.cc:278-301,
@@ -155,6 +165,14 @@ typedef struct ampe_step_params {
    int precision;      /* 0 FP64, 1 mixed (FP32 preconditioner + Jv) */
    int surrogate;      /* 1: MLP initial guess for the cL,cS Newton */
    int max_retries;    /* step-size halvings after a Newton failure */
+   /* 0: fixed steps of size dt.  1: variable steps chosen by CVODE's local
+    * error test and step-size / order rules (CVODESolver.cc:112-258 with
+    * CVodeSStolerances(rtol, atol), CVodeSetMaxOrd(max_order),
+    * CVodeSetInitStep(dt), CVodeSetMaxStep(h_max), CVodeSetMinStep(h_min);
+    * QuatIntegrator.cc:1571-1596), orders 1 and 2. */
+   int adaptive;
+   double h_max;       /* largest step (<= 0: none) */
+   double h_min;       /* smallest step before a failure is final (>= 0) */
 } ampe_step_params_t;
 
 typedef struct ampe_step_stats {
@@ -162,6 +180,11 @@ typedef struct ampe_step_stats {
        precond_setups, fac_cycles, newton_fail, kks_iters, kks_fallback,
        kks_fail, step_retries, kks_fp64_cells;
    double t;
+   /* variable steps: local error test failures, the last accepted step's
+    * size and order, the next step's size and order */
+   long long err_test_fails;
+   double h_last, h_next;
+   int q_last, q_next;
 } ampe_step_stats_t;
 
 /* ---------------------------------------------------------------------
@@ -278,7 +301,10 @@ int ampe_efo_rbgs(const ampe_model_t* m, const double* dface0,
  * launch, reading u_in and writing u_out (interior and periodic ghost
  * images); u_in NULL starts from u = 0.  The result equals two
  * ampe_efo_rbgs colour calls with a ghost fill between them.  Requires
- * even extents (AMPE_ERR_INVALID otherwise) and u_in != u_out. */
+ * even extents (AMPE_ERR_INVALID otherwise) and u_in != u_out.  3D levels of
+ * at least 2^21 cells with the phase (cell C), composition (face D) or
+ * quaternion (face D, cell M) operator shape take the z-marching sweep that
+ * the stepper's multigrid runs. */
 int ampe_efo_rbgs_sweep(const ampe_model_t* m, const double* dface0,
                         const double* dface1, const double* dface2,
                         double d_const, const double* ccell, double c_const,
@@ -319,7 +345,10 @@ int ampe_efo_residual_rms(const ampe_model_t* m, const double* dface0,
  * fit (ghost box above ~523,000 cells, e.g. 80^3) are refused with
  * AMPE_ERR_TOO_LARGE before any launch.  The first call on a device looks up
  * the buffer's device address (cudaGetSymbolAddress), so make that first call
- * outside any CUDA stream capture.  All calls share the one buffer: calls
+ * outside any CUDA stream capture.  That address is kept for the life of the
+ * process: after cudaDeviceReset (or any other teardown of the device's
+ * primary context) it is stale, so do not call this entry point on a device
+ * that has been reset.  All calls share the one buffer: calls
  * whose work overlaps on the GPU (different streams, or different host
  * threads) race and give wrong norms -- serialise them.  No part of the
  * buffer has to start at zero: each call overwrites what it reads. */
@@ -383,11 +412,16 @@ int ampe_mlp_generate(void* handle, long long n, unsigned seed, double t_lo,
                       double t_hi, double c_lo, double c_hi,
                       long long* newton_failures);
 /* Adam on minibatches of the generated samples (loss: 1/2 mean squared
- * error of the two logits); repacks the BF16 tensor-core operands. */
+ * error of the two logits): each step is one tcgen05 forward + backward
+ * launch (one CTA per 128 samples) and one reduction + FP32 Adam launch;
+ * repacks the BF16 tensor-core operands. */
 int ampe_mlp_train(void* handle, int steps, int batch, float lr,
                    float* final_loss);
 /* gradient of the loss on one batch (x: [batch][4] encoded inputs, target:
- * [batch][2] logits; device pointers) into the handle's gradient buffer. */
+ * [batch][2] logits; device pointers) into the handle's gradient buffer,
+ * formed as the training steps form it: the tensor-core forward and
+ * backward products (BF16 operands, FP32 accumulation; the weight
+ * gradients of the 128-sample tiles summed in a fixed order). */
 int ampe_mlp_grad(void* handle, const float* x, const float* target,
                   int batch, float* loss);
 int ampe_mlp_get(void* handle, float* params, float* grads, int host);
@@ -400,6 +434,12 @@ int ampe_mlp_infer(void* handle, const ampe_model_t* grid, const double* phi,
                    float* guess_s, int tensor_cores, void* stream);
 /* AMPE_OK, or AMPE_ERR_NOT_CONVERGED if a tensor-core wait timed out. */
 int ampe_mlp_status(void* handle);
+int ampe_mlp_clear_status(void* handle);
+/* Bound (polls, >= 1; default 2^22) of the tensor-core kernels' mbarrier
+ * waits.  skip_issue != 0 is a test of the timeout path: the issuing thread
+ * commits no MMA, so each kernel's first wait runs out with nothing in
+ * flight, sets the status and frees its tensor memory. */
+int ampe_mlp_set_wait_limit(void* handle, int wait_limit, int skip_issue);
 
 /* ---------------------------------------------------------------------
  * Implicit stepper (CVODEAbstractFunctions + CVODESolver role,
@@ -417,8 +457,21 @@ int ampe_stepper_set_state(void* handle, const double* phi,
                            const double* cs, const double* temp, int host);
 int ampe_stepper_get_state(void* handle, double* phi, double* conc,
                            double* cl, double* cs, int host);
-/* Advance nsteps accepted steps of size p->dt. */
+/* Advance nsteps accepted steps: of size p->dt, or (p->adaptive) of the
+ * sizes the error control chooses. */
 int ampe_stepper_advance(void* handle, int nsteps, ampe_step_stats_t* stats);
+/* p->adaptive: accepted steps until t reaches t_stop (the last step ends at
+ * t_stop exactly) or max_steps steps were taken; max_steps = 1 is CVODE's
+ * CV_ONE_STEP mode with a stop time, as QuatModel drives it (one internal
+ * step per QuatIntegrator::Advance, QuatIntegrator.cc:2096-2104).  The
+ * history (step sizes, order, back values) carries over between calls. */
+int ampe_stepper_advance_to(void* handle, double t_stop, int max_steps,
+                            ampe_step_stats_t* stats);
+/* Temperature of the following steps (TemperatureStrategy role: a scalar
+ * T0 with an optional x gradient, e.g. T0 + dT/dt t set before each step);
+ * the per-x thermodynamic tables are rebuilt, the BDF history is kept.
+ * Models with temp_mode AMPE_TEMP_FIELD take their field via set_state. */
+int ampe_stepper_set_temperature(void* handle, double T0, double gradT);
 /* Evaluate f(y) of the current state (fd_flag=0 path): outputs interior. */
 int ampe_stepper_eval_rhs(void* handle, double* phi_rhs, double* conc_rhs,
                           int host);
@@ -460,6 +513,14 @@ int ampe_stepper_eval_rhs_full(void* handle, double* out, int host);
 int ampe_stepper_attach_surrogate(void* handle, void* mlp);
 /* Launches of library kernels in this process (launch accounting). */
 long long ampe_stepper_kernel_launches(void* handle);
+/* Run the stepper's work on the caller's stream (cudaStream_t; NULL: back to
+ * the stepper's private stream) from the next call on: every launch and copy
+ * of the following calls is ordered on it, after the caller's earlier work
+ * there (CVODE's callbacks run in the caller's order, samrai/
+ * CVODEAbstractFunctions.h:61-90).  The stepper still waits on that stream
+ * where the Newton / GMRES control reads a reduced value, and it waits for
+ * its previous stream before switching.  The stream must outlive its use. */
+int ampe_stepper_set_stream(void* handle, void* stream);
 /* The stepper's CUDA stream (cudaStream_t), for events around advance. */
 void* ampe_stepper_stream(void* handle);
 /* Per-kernel CUDA-event timing on the stepper stream.  kind: 0 KKS Newton,

@@ -118,6 +118,8 @@ void orc_stepper_eval_rhs_full(void* h, double* out);
 void orc_stepper_set_orientation(void* h, const double* q);
 long orc_stepper_size(void* h);
 int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats);
+int orc_stepper_advance_to(void* h, double t_stop, int max_steps, ampe_step_stats_t* stats);
+void orc_stepper_set_temperature(void* h, double T0, double gradT);
 void orc_stepper_jv(void* h, const double* v, double gamma, double* out,
                     int analytic);
 

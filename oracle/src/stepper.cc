@@ -39,6 +39,12 @@ struct OStepper {
    void* fac_conc = nullptr;
    int nsteps_done = 0;
    int hist = 0;  // 1 when ynm1 is one step of size dt behind yn
+   // variable-step BDF (params adaptive = 1): y_{n-2}, the last two step
+   // sizes, the next step's size and order, steps before an order change
+   // is considered, the growth cap, the number of valid back values
+   std::vector<double> ynm2;
+   double h_next = 0.0, h1 = 0.0, h2 = 0.0, eta_max = 1.0e4;
+   int q_next = 1, qwait = 2, nhist = 0;
    double t = 0.0;
    ampe_step_stats_t st{};
 };
@@ -275,12 +281,55 @@ int gmres(OStepper& s, const double* y, const double* fy, const double* w,
    return k;
 }
 
-// One BDF step of size h and order q from yn (and ynm1 for q=2).
+// Newton iteration of one BDF step, y - gamma f(y) = a, from the predictor
+// in y; convergence test del min(1, crate) <= newton_coef.  0 on
+// convergence (result in ynew), 1 on Newton failure.  w receives the WRMS
+// weights of y_n.
+int bdf_newton(OStepper& s, const std::vector<double>& a, std::vector<double>& y,
+               double gamma, double newton_coef, std::vector<double>& w,
+               std::vector<double>& ynew)
+{
+   const long n2 = s.NY;
+   std::vector<double> fy(n2), b(n2), d(n2);
+   w.resize(n2);
+   #pragma omp parallel for schedule(static)
+   for (long c = 0; c < n2; c++)
+      w[c] = 1.0 / (s.p.rtol * std::fabs(s.yn[c]) + s.p.atol);
+   double crate = 1.0, delp = 0.0;
+   const double lintol = s.p.lin_coef * newton_coef;
+   for (int it = 0; it < s.p.max_newton; it++) {
+      eval_rhs(s, y.data(), fy.data(), 0);
+      if (it == 0 && s.p.precond) precond_setup(s, gamma);
+      for (long c = 0; c < n2; c++) b[c] = -(y[c] - gamma * fy[c] - a[c]);
+      const int li = gmres(s, y.data(), fy.data(), w.data(), gamma, b.data(),
+                           d.data(), lintol);
+      s.st.gmres_iters += li;
+      s.st.newton_iters++;
+      for (long c = 0; c < n2; c++) y[c] += d[c];
+      const double del = wrms(s, d.data(), w.data());
+      if (it > 0) crate = std::max(0.3 * crate, del / delp);
+      const double dcon = del * std::min(1.0, crate) / newton_coef;
+      if (dcon <= 1.0) {
+         ynew = y;
+         // projection of the accepted state (QuatIntegrator::applyProjection,
+         // QuatIntegrator.cc:3911-3940; project3d)
+         if (s.m.evolve_quat) orc_quat_project(s.N, ynew.data() + 2 * s.N);
+         return 0;
+      }
+      if (it >= 1 && del > 2.0 * delp) break;
+      delp = del;
+   }
+   s.st.newton_fail++;
+   return 1;
+}
+
+// One BDF step of size h and order q from yn (and ynm1 for q=2), constant-
+// step coefficients, linear-extrapolation predictor.
 // Returns 0 on convergence, 1 on Newton failure.
 int bdf_step(OStepper& s, double h, int q, std::vector<double>& ynew)
 {
    const long n2 = s.NY;
-   std::vector<double> a(n2), y(n2), fy(n2), b(n2), d(n2), w(n2);
+   std::vector<double> a(n2), y(n2), w;
    double gamma;
    if (q == 1) {
       gamma = h;
@@ -297,35 +346,184 @@ int bdf_step(OStepper& s, double h, int q, std::vector<double>& ynew)
          y[c] = 2.0 * s.yn[c] - s.ynm1[c];
       }
    }
-   #pragma omp parallel for schedule(static)
-   for (long c = 0; c < n2; c++)
-      w[c] = 1.0 / (s.p.rtol * std::fabs(s.yn[c]) + s.p.atol);
-   double crate = 1.0, delp = 0.0;
-   const double lintol = s.p.lin_coef * s.p.newton_coef;
-   for (int it = 0; it < s.p.max_newton; it++) {
-      eval_rhs(s, y.data(), fy.data(), 0);
-      if (it == 0 && s.p.precond) precond_setup(s, gamma);
-      for (long c = 0; c < n2; c++) b[c] = -(y[c] - gamma * fy[c] - a[c]);
-      const int li = gmres(s, y.data(), fy.data(), w.data(), gamma, b.data(),
-                           d.data(), lintol);
-      s.st.gmres_iters += li;
-      s.st.newton_iters++;
-      for (long c = 0; c < n2; c++) y[c] += d[c];
-      const double del = wrms(s, d.data(), w.data());
-      if (it > 0) crate = std::max(0.3 * crate, del / delp);
-      const double dcon = del * std::min(1.0, crate) / s.p.newton_coef;
-      if (dcon <= 1.0) {
-         ynew = y;
-         // projection of the accepted state (QuatIntegrator::applyProjection,
-         // QuatIntegrator.cc:3911-3940; project3d)
-         if (s.m.evolve_quat) orc_quat_project(s.N, ynew.data() + 2 * s.N);
-         return 0;
-      }
-      if (it >= 1 && del > 2.0 * delp) break;
-      delp = del;
+   return bdf_newton(s, a, y, gamma, s.p.newton_coef, w, ynew);
+}
+
+// ---- variable-step BDF of orders 1 and 2 with CVODE's error control ----
+// (the GPU stepper's adaptive mode restated; the rules are SUNDIALS CVODE
+// 5.7.0's published ones: error test dsm = c ||y_{n+1} - pred||_WRMS <= 1,
+// Newton test with 0.1 / c, eta = 1/((6 dsm)^(1/(q+1)) + 1e-6), order
+// candidates every q+1 steps with biases 6 and 10, threshold 1.5, growth
+// caps 1e4 / 10 / 1 after failures, error-test failures eta >= 0.1, <= 0.2
+// from the second, order 1 from the third, 7 at most; Newton failures
+// eta = 0.25, 10 at most.)
+
+// the predictor pred = k0 y_n + k1 y_{n-1} + k2 y_{n-2} + k3 f(y_n) and the
+// error constant c of LTE ~ c (y_{n+1} - pred): explicit Euler without
+// history (c = 1/2); linear extrapolation for order 1 (c = w / (2w+1),
+// w = h / h_{n-1}); quadratic extrapolation for order 2 (c = A / (P + A),
+// A = h^3 (1+w)^2 / (w (1+2w)), P = h (h+h1)(h+h1+h2))
+struct OPred {
+   double k0, k1, k2, k3, c;
+};
+OPred predictor(const OStepper& s, double h, int q)
+{
+   OPred P{1.0, 0.0, 0.0, 0.0, 0.5};
+   if (s.nhist == 0) {
+      P.k3 = h;
+      return P;
    }
-   s.st.newton_fail++;
-   return 1;
+   const double h1 = s.h1, w = h / h1;
+   if (q == 1) {
+      P.k0 = 1.0 + w;
+      P.k1 = -w;
+      P.c = w / (2.0 * w + 1.0);
+      return P;
+   }
+   const double h2 = s.h2;
+   P.k0 = (h + h1) * (h + h1 + h2) / (h1 * (h1 + h2));
+   P.k1 = -h * (h + h1 + h2) / (h1 * h2);
+   P.k2 = h * (h + h1) / ((h1 + h2) * h2);
+   const double A = h * h * h * (1.0 + w) * (1.0 + w) / (w * (1.0 + 2.0 * w));
+   const double Pp = h * (h + h1) * (h + h1 + h2);
+   P.c = A / (Pp + A);
+   return P;
+}
+
+double wrms_comb(const OStepper& s, const std::vector<double>& w, const double* v0,
+                 double c0, const double* v1, double c1, const double* v2, double c2,
+                 const double* v3, double c3)
+{
+   std::vector<double> x(s.NY);
+   for (long t = 0; t < s.NY; t++) {
+      double v = c0 * v0[t] + c1 * v1[t];
+      if (v2) v += c2 * v2[t];
+      if (v3) v += c3 * v3[t];
+      x[t] = v;
+   }
+   return wrms(s, x.data(), w.data());
+}
+
+void restart_history(OStepper& s)
+{
+   s.nhist = 0;
+   s.q_next = 1;
+   s.qwait = 2;
+   s.h_next = s.p.dt;
+   s.h1 = s.h2 = 0.0;
+   s.eta_max = 1.0e4;
+}
+
+// one accepted variable step, not past t_stop (> t); 0 ok, 1 failed
+int adaptive_step(OStepper& s, double t_stop)
+{
+   const long n2 = s.NY;
+   const double hmax = s.p.h_max > 0.0 ? s.p.h_max : 1.0e300;
+   std::vector<double> fn;
+   if (s.nhist == 0) {
+      fn.resize(n2);
+      eval_rhs(s, s.yn.data(), fn.data(), 0);
+   }
+   std::vector<double> a(n2), y(n2), w, ynew;
+   int nef = 0, ncf = 0;
+   for (;;) {
+      int q = std::min(s.q_next, std::min(2, s.p.max_order));
+      if (s.nhist < q) q = s.nhist < 1 ? 1 : s.nhist;
+      double h = std::min(s.h_next, hmax);
+      if (t_stop > s.t && s.t + h > t_stop - 1e-12 * std::fabs(t_stop)) h = t_stop - s.t;
+      const OPred P = predictor(s, h, q);
+      double gamma = h, a0 = 1.0, a1 = 0.0;
+      if (q == 2) {
+         const double wr = h / s.h1;
+         a0 = (1.0 + wr) * (1.0 + wr) / (1.0 + 2.0 * wr);
+         a1 = -wr * wr / (1.0 + 2.0 * wr);
+         gamma = h * (1.0 + wr) / (1.0 + 2.0 * wr);
+      }
+      for (long t = 0; t < n2; t++) {
+         double pr = P.k0 * s.yn[t];
+         if (s.nhist >= 1) pr += P.k1 * s.ynm1[t];
+         if (q == 2) pr += P.k2 * s.ynm2[t];
+         if (s.nhist == 0) pr += P.k3 * fn[t];
+         y[t] = pr;
+         a[t] = q == 2 ? a0 * s.yn[t] + a1 * s.ynm1[t] : s.yn[t];
+      }
+      if (bdf_newton(s, a, y, gamma, 0.1 / P.c, w, ynew)) {
+         ncf++;
+         if (ncf >= 10 || h <= s.p.h_min) return 1;
+         s.h_next = h * 0.25;
+         s.eta_max = 1.0;
+         continue;
+      }
+      const double dsm =
+          P.c * wrms_comb(s, w, ynew.data(), 1.0, s.yn.data(), -P.k0,
+                          s.nhist >= 1 ? s.ynm1.data() : nullptr, -P.k1,
+                          q == 2 ? s.ynm2.data() : (s.nhist == 0 ? fn.data() : nullptr),
+                          q == 2 ? -P.k2 : -P.k3);
+      if (dsm > 1.0) {
+         nef++;
+         s.st.err_test_fails++;
+         if (nef >= 7 || h <= s.p.h_min) return 1;
+         double eta = 1.0 / (std::pow(6.0 * dsm, 1.0 / (q + 1)) + 1.0e-6);
+         eta = std::max(0.1, eta);
+         if (nef >= 2) eta = std::min(eta, 0.2);
+         if (nef >= 3) s.q_next = 1;
+         s.h_next = h * eta;
+         s.eta_max = 1.0;
+         continue;
+      }
+      double eta = 1.0 / (std::pow(6.0 * dsm, 1.0 / (q + 1)) + 1.0e-6);
+      int qn = q;
+      if (--s.qwait <= 0) {
+         if (q == 2) {
+            const double h1 = s.h1;
+            const double ca = 1.0 / (h * (h + h1)), cb = 1.0 / (h1 * (h + h1));
+            const double dsm1 = wrms_comb(s, w, ynew.data(), h * h * ca, s.yn.data(),
+                                          -h * h * (ca + cb), s.ynm1.data(), h * h * cb,
+                                          nullptr, 0.0);
+            const double em = 1.0 / (std::pow(6.0 * dsm1, 0.5) + 1.0e-6);
+            if (em > eta) {
+               eta = em;
+               qn = 1;
+            }
+         } else if (s.p.max_order >= 2 && s.nhist >= 2) {
+            const double h1 = s.h1, h2 = s.h2;
+            const double t0 = h, t1 = 0.0, t2 = -h1, t3 = -h1 - h2;
+            const double w0 = 1.0 / ((t0 - t1) * (t0 - t2) * (t0 - t3));
+            const double w1 = 1.0 / ((t1 - t0) * (t1 - t2) * (t1 - t3));
+            const double w2 = 1.0 / ((t2 - t0) * (t2 - t1) * (t2 - t3));
+            const double w3 = 1.0 / ((t3 - t0) * (t3 - t1) * (t3 - t2));
+            const double k = 4.0 / 3.0 * h * h * h;
+            const double dsm2 = wrms_comb(s, w, ynew.data(), k * w0, s.yn.data(), k * w1,
+                                          s.ynm1.data(), k * w2, s.ynm2.data(), k * w3);
+            const double ep = 1.0 / (std::pow(10.0 * dsm2, 1.0 / 3.0) + 1.0e-6);
+            if (ep > eta) {
+               eta = ep;
+               qn = 2;
+            }
+         }
+         s.qwait = qn + 1;
+      }
+      if (eta < 1.5) {
+         eta = 1.0;
+         qn = q;
+      } else {
+         eta = std::min(eta, s.eta_max);
+      }
+      if (nef || ncf) eta = std::min(eta, 1.0);
+      s.eta_max = 10.0;
+      s.h_next = std::min(h * eta, hmax);
+      s.q_next = qn;
+      s.ynm2.swap(s.ynm1);
+      s.ynm1.swap(s.yn);
+      s.yn.swap(ynew);
+      s.h2 = s.h1;
+      s.h1 = h;
+      s.nhist = std::min(s.nhist + 1, 2);
+      s.t += h;
+      s.st.h_last = h;
+      s.st.q_last = q;
+      return 0;
+   }
 }
 
 }  // namespace
@@ -356,6 +554,8 @@ void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p)
    s->NY = s->nb * s->N;
    s->yn.assign(s->NY, 0.0);
    s->ynm1.assign(s->NY, 0.0);
+   s->ynm2.assign(s->NY, 0.0);
+   s->h_next = p->dt;
    const int nl = p->precond == 2 ? p->mg_levels : 1;
    s->fac_phi = orc_fac_create(m, nl);
    s->fac_conc = orc_fac_create(m, nl);
@@ -402,6 +602,7 @@ void orc_stepper_set_state(void* h, const double* phi, const double* conc,
    s->cl_nf = s->clr;
    s->cs_nf = s->csr;
    s->hist = 0;
+   restart_history(*s);
    if (temp) to_ghosted(*s, temp, s->temp);
    s->nsteps_done = 0;
    s->t = 0.0;
@@ -423,6 +624,8 @@ void orc_stepper_set_quat(void* h, const double* q)
    if (!s->m.evolve_quat) return;
    std::copy(q, q + 4 * s->N, s->yn.begin() + 2 * s->N);
    std::copy(q, q + 4 * s->N, s->ynm1.begin() + 2 * s->N);
+   s->hist = 0;
+   restart_history(*s);
 }
 
 // static orientation (qlen interior components) of the anisotropic flux
@@ -463,9 +666,42 @@ long orc_stepper_size(void* h) { return ((OStepper*)h)->NY; }
 
 // Advance nsteps accepted steps.  Returns 0, or 1 if a step failed after
 // max_retries step-size halvings.
+// variable steps until t_stop (if > t) or max_steps; 0 ok, 1 failed
+static int advance_adaptive(OStepper* s, double t_stop, int max_steps)
+{
+   for (int n = 0; n < max_steps; n++) {
+      if (t_stop > s->t && s->t >= t_stop - 1e-12 * std::fabs(t_stop)) break;
+      if (adaptive_step(*s, t_stop)) return 1;
+      s->clr = s->cl_nf;  // QuatModel::resetRefPhaseConcentrations
+      s->csr = s->cs_nf;
+      s->nsteps_done++;
+      s->st.steps++;
+   }
+   return 0;
+}
+
+int orc_stepper_advance_to(void* h, double t_stop, int max_steps, ampe_step_stats_t* stats)
+{
+   OStepper* s = (OStepper*)h;
+   const int rc = advance_adaptive(s, t_stop, max_steps);
+   s->st.t = s->t;
+   s->st.h_next = s->h_next;
+   s->st.q_next = s->q_next;
+   if (stats) *stats = s->st;
+   return rc;
+}
+
+void orc_stepper_set_temperature(void* h, double T0, double gradT)
+{
+   OStepper* s = (OStepper*)h;
+   s->m.T0 = T0;
+   s->m.gradT = gradT;
+}
+
 int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
 {
    OStepper* s = (OStepper*)h;
+   if (s->p.adaptive) return orc_stepper_advance_to(h, -1.0e300, nsteps, stats);
    std::vector<double> ynew;
    int ret = 0;
    for (int n = 0; n < nsteps; n++) {
@@ -514,8 +750,12 @@ int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
       s->nsteps_done++;
       s->t += s->p.dt;
       s->st.steps++;
+      s->st.h_last = s->p.dt;
+      s->st.q_last = q;
    }
    s->st.t = s->t;
+   s->st.h_next = s->p.dt;
+   s->st.q_next = s->hist ? std::min(2, s->p.max_order) : 1;
    if (stats) *stats = s->st;
    return ret;
 }

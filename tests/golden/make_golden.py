@@ -1,7 +1,8 @@
 """Generate the golden fixtures of this directory from the reference tree.
 
-Run in a container where the AMPE reference sources are mounted (default
-/root/reference, or pass a path).  It reads, as data only:
+Run with the root of an AMPE source tree as the one argument:
+    python tests/golden/make_golden.py <path-to-AMPE-sources>
+It reads, as data only:
   - thermodynamic_data/calphadAuNi.dat       -> calphad_AuNi.json
   - tests/CALPHADbinaryEquilibrium/test.input (temperature, initial guess,
     ExpectedResults)                         -> kats.json["calphad_ceq"]
@@ -23,7 +24,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from ampe_gb300.calphad_db import database_from_text, parse_input_text  # noqa: E402
 
 
-def main(ref="/root/reference"):
+def main(ref):
     with open(os.path.join(ref, "thermodynamic_data/calphadAuNi.dat")) as f:
         db = database_from_text(f.read())
     db["source"] = "thermodynamic_data/calphadAuNi.dat"
@@ -80,4 +81,6 @@ def main(ref="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path-to-AMPE-sources>")
+    main(sys.argv[1])

@@ -71,3 +71,33 @@ def loss_and_grad(params, x, target):
     grads.reverse()
     flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
     return loss, flat
+
+
+def fp16(x):
+    return np.asarray(x, np.float64).astype(np.float16).astype(np.float64)
+
+
+def loss_and_grad_bf16(params, x, target):
+    """The gradient as the tensor-core training kernel forms it: operands of
+    every product rounded to BF16 (inputs, activations, weights, and the
+    back-propagated dZ of each layer), silu'(z) stored in FP16, products and
+    sums accumulated exactly here (FP32 on the GPU); the bias gradients are
+    the sums of the BF16 dZ."""
+    zs, acts = forward(params, x, round_acts=True)
+    y = acts[-1]
+    B = x.shape[0]
+    d = y - target
+    loss = 0.5 * np.sum(d * d) / B
+    dz = d / B
+    layers = unpack(np.asarray(params, np.float64))
+    grads = []
+    for li in range(3, -1, -1):
+        W, b = layers[li]
+        dzb = bf16(dz).astype(np.float64)
+        xin = acts[li]
+        grads.append((dzb.T @ xin, dzb.sum(axis=0)))
+        if li > 0:
+            dz = (dzb @ bf16(W).astype(np.float64)) * fp16(dsilu(zs[li - 1]))
+    grads.reverse()
+    flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
+    return loss, flat

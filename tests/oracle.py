@@ -72,6 +72,8 @@ def lib():
             "orc_stepper_get_state": (None, [P, P, P, P, P]),
             "orc_stepper_eval_rhs": (None, [P, P, P]),
             "orc_stepper_advance": (I, [P, I, C.POINTER(abi.StepStats)]),
+            "orc_stepper_advance_to": (I, [P, D, I, C.POINTER(abi.StepStats)]),
+            "orc_stepper_set_temperature": (None, [P, D, D]),
             "orc_stepper_jv": (None, [P, P, D, P, I]),
             "orc_stepper_set_quat": (None, [P, P]),
             "orc_stepper_get_quat": (None, [P, P]),
@@ -161,6 +163,14 @@ class OracleStepper:
         st = abi.StepStats()
         rc = self.L.orc_stepper_advance(self.h, int(n), C.byref(st))
         return rc, st.as_dict()
+
+    def advance_to(self, t_stop, max_steps=1):
+        st = abi.StepStats()
+        rc = self.L.orc_stepper_advance_to(self.h, float(t_stop), int(max_steps), C.byref(st))
+        return rc, st.as_dict()
+
+    def set_temperature(self, T0, gradT=0.0):
+        self.L.orc_stepper_set_temperature(self.h, float(T0), float(gradT))
 
 
 def ghosted(model, interior):

@@ -1,5 +1,5 @@
-"""bench.py host logic on CPU: both arms describe the same full-size
-workload (the reference arm times a bounded sample of it), every workload
+"""bench.py host logic on CPU: each arm describes the level it stepped
+(the reference arm times a bounded sample of the workload and says so), every workload
 builds its model, and the CPU sample sizes stay small."""
 import argparse
 
@@ -23,8 +23,16 @@ def test_arm_config(kind, cells):
     assert cfg["cells"] == cells
     assert cfg["path"] == "mixed+surrogate"
     assert cfg["workload"] == bench.WORKLOAD_NAMES[kind] % (a.n, a.atol)
-    # the reference arm reports the same config object
-    assert bench.arm_config(a) == cfg
+    # the reference arm reports the level it stepped: the full one, or a
+    # sample of it named as such
+    n = bench.cpu_sample_n(a)
+    ref = bench.arm_config(a, n=n)
+    m, _ = bench.workload(n, kind, state=False)
+    assert ref["cells"] == m.cells()
+    if n != a.n:
+        assert "sample of the %d-cell level" % cells in ref["workload"]
+    else:
+        assert ref == cfg
 
 
 @pytest.mark.parametrize("kind", ["calphad", "poly", "dendrite", "dilute"])

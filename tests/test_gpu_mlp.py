@@ -46,9 +46,54 @@ def test_gradients_match_oracle(cuda):
     assert L.ampe_mlp_grad(h, _p(xd), _p(td), B, C.byref(loss)) == 0
     g = np.empty(npar, np.float32)
     assert L.ampe_mlp_get(h, None, g.ctypes.data, 1) == 0
-    lo, go = MO.loss_and_grad(params.astype(np.float64), x.astype(np.float64), tgt.astype(np.float64))
+    # the tensor-core products round every operand to BF16: against the
+    # oracle that rounds the same operands the gradient agrees to FP32
+    # accumulation (and the odd BF16 rounding flip); against the unrounded
+    # FP64 gradient to BF16 resolution
+    lo, go = MO.loss_and_grad_bf16(params.astype(np.float64), x.astype(np.float64),
+                                   tgt.astype(np.float64))
+    lx, gx = MO.loss_and_grad(params.astype(np.float64), x.astype(np.float64),
+                              tgt.astype(np.float64))
+    e_bf = np.linalg.norm(g - go) / np.linalg.norm(go)
+    e_ex = np.linalg.norm(g - gx) / np.linalg.norm(gx)
+    print("tensor-core gradient: rel L2 %.2e vs the BF16-operand oracle, %.2e vs FP64" % (e_bf, e_ex))
     assert abs(loss.value - lo) <= 1e-5 * lo
-    assert np.linalg.norm(g - go) <= 1e-4 * np.linalg.norm(go)
+    assert e_bf <= 2e-3
+    assert e_ex <= 3e-2
+    L.ampe_mlp_destroy(h)
+
+
+def test_tensor_core_wait_timeout(cuda):
+    """The bounded mbarrier waits of the tcgen05 kernels: with the issue
+    skipped (nothing in flight) a wait of 64 polls runs out, the status
+    reports it, tensor memory is freed, and the next calls succeed."""
+    import torch
+
+    L = cuda.lib
+    m = configs.calphad3d(16, seed=3, T_run=1500.0)
+    h = _mlp(cuda, m, batch=256)
+    phi = O.ghosted(m, np.full(m.interior_shape(), 0.5))
+    c = O.ghosted(m, np.full(m.interior_shape(), 0.4))
+    pd, cd = torch.from_numpy(phi).cuda(), torch.from_numpy(c).cuda()
+    N = m.cells()
+    gl = torch.zeros(N, dtype=torch.float32, device="cuda")
+    gs = torch.zeros(N, dtype=torch.float32, device="cuda")
+    x = torch.zeros((256, 4), dtype=torch.float32, device="cuda")
+    t = torch.zeros((256, 2), dtype=torch.float32, device="cuda")
+    loss = C.c_float()
+    ref = []
+    for skip in (0, 1, 0):
+        assert L.ampe_mlp_set_wait_limit(h, 64 if skip else 1 << 22, skip) == 0
+        assert L.ampe_mlp_clear_status(h) == 0
+        assert L.ampe_mlp_infer(h, C.byref(m), _p(pd), _p(cd), None, _p(gl), _p(gs), 1, None) == 0
+        torch.cuda.synchronize()
+        assert L.ampe_mlp_status(h) == (-3 if skip else 0)
+        assert L.ampe_mlp_clear_status(h) == 0
+        assert L.ampe_mlp_grad(h, _p(x), _p(t), 256, C.byref(loss)) == 0
+        assert L.ampe_mlp_status(h) == (-3 if skip else 0)
+        if not skip:
+            ref.append(gl.cpu().numpy().copy())
+    assert np.array_equal(ref[0], ref[1])
     L.ampe_mlp_destroy(h)
 
 

@@ -1,0 +1,113 @@
+"""The reference's regression case tests/KKScomposition (tests/kkscomposition.py)
+run on the GPU, FP64 and mixed paths, to t = 0.3 with the oracle's step
+sequence.  Checks:
+
+* the reference's own acceptance values: solid fraction 0.33 +- 0.01 at
+  t = 0.3 and the composition integral constant to 1e-4
+  (test3d.py:38-62);
+* the trajectory of the CPU oracle's run of the same case
+  (tests/golden/kkscomposition_oracle.json, written by
+  tests/golden/make_kkscomposition.py): solid fraction and mean
+  composition at every output time, and the final phi and c as 8^3-cell
+  block means -- FP64 within 1e-8, mixed within 1e-5;
+* per-field parity with a live oracle run over the first start-up steps
+  (FP64 within 1e-10, mixed within 1e-6)."""
+import json
+
+import numpy as np
+import pytest
+
+import kkscomposition as K
+import oracle as O
+from ampe_gb300 import abi
+from ampe_gb300._native import AmpeError
+from ampe_gb300.stepper import ImplicitStepper
+
+pytestmark = pytest.mark.gpu
+
+TRAJ_TOL = {0: 1e-8, 1: 1e-5}
+START_TOL = {0: 1e-10, 1: 1e-6}
+
+
+class _Gpu:
+    """ImplicitStepper with the oracle's advance convention (rc, stats)."""
+
+    def __init__(self, m, p):
+        self.s = ImplicitStepper(m, p)
+
+    def set_state(self, *a):
+        self.s.set_state(*a)
+
+    def advance(self, n):
+        try:
+            return 0, self.s.advance(n)
+        except AmpeError as e:
+            if "not converged" not in str(e):
+                raise
+            return abi.AMPE_ERR_NOT_CONVERGED, {}
+
+    def advance_to(self, t_stop, n):
+        return 0, self.s.advance_to(t_stop, n)
+
+    def set_temperature(self, T):
+        self.s.set_temperature(T)
+
+    def get_state(self):
+        return self.s.get_state()
+
+    def close(self):
+        self.s.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kkscomposition_start_parity(cuda, precision):
+    ro = K.run(lambda m, p: O.OracleStepper(m, p), t_stop=3e-5)
+    rg = K.run(lambda m, p: _Gpu(m, p), precision=precision, t_stop=3e-5)
+    assert rg["steps"] == ro["steps"] >= 2
+    for f in ("phi", "c"):
+        err = O.rel_l2(rg[f], ro[f])
+        print("KKScomposition start-up (%d steps) precision %d %s rel L2 %.3e"
+              % (ro["steps"], precision, f, err))
+        assert err <= START_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kkscomposition_regression(cuda, precision):
+    r = K.run(lambda m, p: _Gpu(m, p), precision=precision)
+    solid, drift = r["solid"][-1], r["drift"]
+    print("KKScomposition GPU precision %d: solid fraction %.5f at t = %.4f, drift %.2e, "
+          "%d steps, %d rejected" % (precision, solid, r["t"][-1], drift, r["steps"],
+                                      r["rejected"]))
+    assert abs(r["t"][-1] - 0.3) < 1e-9
+    assert abs(solid - K.SOLID_TARGET) <= K.SOLID_TOL
+    assert abs(drift) < K.DRIFT_TOL
+    with open(K.FIXTURE) as f:
+        gold = json.load(f)
+    assert r["steps"] == gold["steps"] and r["rejected"] == gold["rejected"]
+    tol = TRAJ_TOL[precision]
+    assert np.allclose(r["t"], gold["t"], rtol=0, atol=1e-12)
+    ds = np.max(np.abs(np.array(r["solid"]) - gold["solid"]))
+    dc = np.max(np.abs(np.array(r["cmean"]) - gold["cmean"]))
+    eb = {f: O.rel_l2(K.block_means(r[f], gold["block"]).ravel(), np.array(gold[f + "_blocks"]))
+          for f in ("phi", "c")}
+    print("  vs oracle trajectory: max |d solid| %.2e, max |d cmean| %.2e, block-mean rel L2 "
+          "phi %.2e c %.2e" % (ds, dc, eb["phi"], eb["c"]))
+    assert ds <= tol and dc <= tol
+    assert eb["phi"] <= tol and eb["c"] <= tol
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kkscomposition_deck_tolerances(cuda, precision):
+    """The case integrated as the deck integrates it: variable steps at the
+    deck's atol 1e-4 (rtol 1e-6), one step per call, T set per step.  The
+    reference's acceptance values hold."""
+    r = K.run_adaptive(lambda m, p: _Gpu(m, p), precision=precision)
+    solid, drift = r["solid"][-1], r["drift"]
+    h = np.array(r["h"])
+    print("KKScomposition adaptive precision %d: solid fraction %.5f at t = %.4f, drift %.2e, "
+          "%d steps (h %.2e .. %.2e), %d failures, %d Newton iterations"
+          % (precision, solid, r["t"][-1], drift, r["steps"], h.min(), h.max(), r["rejected"],
+             r["newton_iters"]))
+    assert abs(r["t"][-1] - 0.3) < 1e-9
+    assert abs(solid - K.SOLID_TARGET) <= K.SOLID_TOL
+    assert abs(drift) < K.DRIFT_TOL

@@ -59,6 +59,35 @@ def test_noalloc_matches_scratch_version_twice(cuda, dim):
         assert abs(ra - rb) <= 1e-13 * ra, (call, ra, rb)
 
 
+def test_noalloc_size_limit_edge(cuda):
+    """78^3 (an 80^3 ghost box plus the reduction partials fits in 2^19
+    doubles) matches the scratch version; 79^3 (an 81^3 ghost box does not
+    fit) is refused."""
+    import torch
+
+    L = cuda.lib
+    m = configs.calphad3d(78)
+    assert L.ampe_efo_residual_rms_scratch_doubles(C.byref(m)) <= 1 << 19
+    rng = np.random.default_rng(5)
+    D, Cc, f, u = _fields(m, rng)
+    scratch = torch.empty(L.ampe_efo_residual_rms_scratch_doubles(C.byref(m)),
+                          dtype=torch.float64, device="cuda")
+    a = torch.zeros(1, dtype=torch.float64, device="cuda")
+    b = torch.zeros(1, dtype=torch.float64, device="cuda")
+    args = [*[_p(x) for x in D], 0.0, _p(Cc), 0.0, None, 1.7, _p(f), _p(u)]
+    assert L.ampe_efo_residual_rms(C.byref(m), *args, _p(scratch), _p(a), None) == 0
+    assert L.ampe_efo_residual_rms_noalloc(C.byref(m), *args, _p(b), None) == 0
+    torch.cuda.synchronize()
+    assert float(a[0]) > 0.0 and abs(float(a[0]) - float(b[0])) <= 1e-13 * float(a[0])
+    m79 = configs.calphad3d(79)
+    assert L.ampe_efo_residual_rms_scratch_doubles(C.byref(m79)) > 1 << 19
+    f79 = torch.zeros(int(np.prod(m79.ghost_shape())), dtype=torch.float64, device="cuda")
+    x = torch.zeros(1, dtype=torch.float64, device="cuda")
+    rc = L.ampe_efo_residual_rms_noalloc(C.byref(m79), None, None, None, -1.0, None, 1.0, None,
+                                         1.0, _p(f79), _p(f79), _p(x), None)
+    assert rc == abi.AMPE_ERR_TOO_LARGE
+
+
 def test_noalloc_refuses_levels_beyond_its_buffer(cuda):
     import torch
 
