@@ -58,9 +58,9 @@ int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
                 double gamma, R* ccell, cudaStream_t s);
 
 // One red-black sweep of a 3D level in a single z-marching pass (sweep_z.cu):
-// blocks of ty rows x the whole x extent x kz planes, u staged in a ring of
-// kZRingPlanes shared-memory planes, rows stored colour-split with halves
-// hs elements apart.
+// blocks of ty rows x the whole x extent (one thread per column) x kz
+// planes, u staged in a ring of kZRingPlanes shared-memory planes of
+// (ty + 4) rows of hs (= n0) elements.
 constexpr int kZRingPlanes = 6;
 struct ZShape {
    int ty = 0, kz = 0, nh = 0, hs = 0;
@@ -68,10 +68,11 @@ struct ZShape {
 template <class R>
 inline size_t zsweep_smem_bytes(const ZShape& z)
 {
-   return sizeof(R) * (size_t)kZRingPlanes * (size_t)(z.ty + 4) * 2 * (size_t)z.hs;
+   return sizeof(R) * (size_t)kZRingPlanes * (size_t)(z.ty + 4) * (size_t)z.hs;
 }
-// whether the level takes the single-pass sweep (3D, even extents, at least
-// 2^21 cells, shape fits in shared memory); the chosen shape into *out
+// whether the level takes the single-pass sweep (3D, n0 a multiple of 32 up
+// to 256, even extents, at least 2^21 cells, shape fits in shared memory);
+// the chosen shape into *out
 template <class R>
 bool sweep_z_ok(const Grid& g, ZShape* out);
 // uin -> uout (uin != uout; ghost images of uout written).  uin null: start

@@ -639,7 +639,10 @@ static void eval_rhs(Stepper& S, const double* y, const double* v, double sig,
       }
    }
    if (S.p.precision == 1) {
-      const bool sur = S.p.surrogate && S.mlp && S.cold;
+      // surrogate = 1: the network's guess while no converged warm start
+      // exists (a cold start); 2: for every KKS solve (the warm start is
+      // then only the fallback)
+      const bool sur = S.p.surrogate && S.mlp && (S.cold || S.p.surrogate == 2);
       if (sur) {
          ProfScope ps(S, KT_MLP);
          S.mlp->infer(S.g, S.phi_g, S.c_g, tf, S.guess_l, S.guess_s, true, S.s);
@@ -1440,6 +1443,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
        p->precision > 1 || p->max_krylov > kMaxKrylov)
       return AMPE_ERR_INVALID;
    if (p->adaptive < 0 || p->adaptive > 1 || p->h_min < 0.0) return AMPE_ERR_INVALID;
+   if (p->surrogate < 0 || p->surrogate > 2) return AMPE_ERR_INVALID;
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC) {
       if (m->qlen != 2 && m->qlen != 4) return AMPE_ERR_INVALID;
       if (m->evolve_quat && m->qlen != 4) return AMPE_ERR_INVALID;

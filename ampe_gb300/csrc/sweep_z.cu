@@ -5,23 +5,26 @@
 // 153-172).
 //
 // Two colour passes over the level read every array twice (each pass
-// touches whole cache lines of both colours).  Here each block owns a tile
-// of TY rows (y) x the whole x extent and a chunk of KZ planes (z).  It
-// stages u plane by plane in a shared-memory ring (cp.async, two planes
-// ahead), and at step w updates the red cells of plane w on the tile plus
-// one halo row on each side, then the black cells of plane w-1 on the tile
-// (whose red neighbours at w-2, w-1 and w are final by then), and writes
-// plane w-1 to the output buffer with its periodic ghost images.  The halo
-// rows and the two extra red planes at the chunk ends repeat, on identical
-// inputs, updates that the neighbouring blocks also make, so every block
-// reads only the input u (u_in -> u_out, never in place) and the result is
-// the two colour passes' result: every update evaluates the colour kernel's
-// expression in the same order.  f, C, M and the face coefficients are read
-// from global memory at the cell, once per sweep from DRAM.
+// touches whole cache lines of both colours).  Here a block owns TY rows
+// (y) x the whole x extent (one thread per x column) and a chunk of KZ
+// planes (z).  It stages u plane by plane in a shared-memory ring (cp.async,
+// two planes ahead), and at step w updates the red cells of plane w on its
+// rows plus one halo row on each side, then the black cells of plane w-1 on
+// its rows (whose red neighbours at w-2, w-1 and w are final by then), and
+// writes plane w-1 to the output buffer with its periodic ghost images.
+// The halo rows and the two extra red planes at the chunk ends repeat, on
+// identical inputs, updates that the neighbouring blocks also make, so every
+// block reads only the input u (u_in -> u_out, never in place) and the
+// result is the two colour passes' result: every update evaluates the colour
+// kernel's expression in the same order.  f, C, M and the face coefficients
+// are read from global memory at the cell, once per sweep from DRAM; the
+// coefficient loads of a colour stage are all issued before its first
+// update.
 //
-// The ring stores each row colour-split (red half, black half, padded so
-// that the two halves sit 16 banks apart): an update reads its own value and
-// its six neighbours from consecutive words across the warp.
+// Each thread keeps its x column, its neighbours' columns and the block's
+// rows for the whole kernel, so per cell the index work is a few integer
+// operations; in a warp the even and odd lanes update cells of one colour in
+// adjacent rows, so the row-major ring is read without bank conflicts.
 #include <algorithm>
 #include <cstdint>
 
@@ -33,8 +36,7 @@ namespace ampe {
 namespace {
 
 constexpr int kZRing = kZRingPlanes;  // w-2 .. w+1 in use, w+2, w+3 in flight
-constexpr int kZPrefetch = 2;  // planes loaded ahead of the one needed next
-constexpr int kZThreads = 256;
+constexpr int kZPrefetch = 2;         // planes loaded ahead of the one needed next
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -72,9 +74,6 @@ __device__ __forceinline__ int wrap(int a, int n)
 
 }  // namespace
 
-// MODE 0: sweep from u_in; 1: from u = 0 (u_in unused); 2: from u_in + P e
-// (e the next coarser level's correction, piecewise constant: the first
-// post-smoothing sweep with the prolongation fused in)
 // per-cell coefficients of one update (members the operator shape does not
 // use stay unset)
 template <class R>
@@ -83,84 +82,67 @@ struct Coef {
    R d[6];  // faces x-, x+, y-, y+, z-, z+
 };
 
-// CAPR / CAPB: red / black cells per thread and step (at least
-// (ty+2) nh / 256 and ty nh / 256)
-template <class R, bool HD, bool HC, bool HM, int MODE, int CAPR, int CAPB>
-__global__ void __launch_bounds__(kZThreads, 2)
-    k_sweep_z(FacOp<R> op, Grid g, ZShape zs, const R* __restrict__ f,
+// MODE 0: sweep from u_in; 1: from u = 0 (u_in unused); 2: from u_in + P e
+// (e the next coarser level's correction, piecewise constant: the first
+// post-smoothing sweep with the prolongation fused in).  blockDim.x = n0
+// (<= 256: three blocks per SM).
+template <class R, bool HD, bool HC, bool HM, int MODE, int TY>
+__global__ void __launch_bounds__(256, 3)
+    k_sweep_z(FacOp<R> op, Grid g, int kz, const R* __restrict__ f,
               const R* __restrict__ uin, R* __restrict__ uout, Grid gc,
               const R* __restrict__ e)
 {
+   constexpr int ROWS = TY + 4;
+   constexpr int NRED = (TY + 2) / 2, NBLACK = TY / 2;
    extern __shared__ __align__(16) unsigned char zsm[];
    R* const S = reinterpret_cast<R*>(zsm);
-   const int tid = threadIdx.x;
-   const int j0 = blockIdx.x * zs.ty;
-   const int k0 = blockIdx.y * zs.kz;
-   const int k1 = k0 + zs.kz;
-   const int nh = zs.nh, hs = zs.hs, rs = 2 * zs.hs, rows = zs.ty + 4;
-   const int ps = rows * rs;
+   const int n0 = g.n0, x = threadIdx.x;
+   const int xm = x == 0 ? n0 - 1 : x - 1;
+   const int xp = x == n0 - 1 ? 0 : x + 1;
+   const int j0 = blockIdx.x * TY;
+   const int k0 = blockIdx.y * kz, k1 = k0 + kz;
+   const int ps = ROWS * n0;
+   // wrapped y index of every ring row (the block's rows and two halo rows
+   // on each side), fixed for the whole kernel
+   int jw[ROWS];
+#pragma unroll
+   for (int r = 0; r < ROWS; r++) jw[r] = wrap(j0 - 2 + r, g.n1);
+   const bool xedge = x < g.ng || x >= n0 - g.ng;
    auto slot = [&](int p) { return S + ((p - k0 + 2) % kZRing) * ps; };
+   // ghosted index of this column: plane part and row part
+   auto gplane = [&](int kk) { return (kk + g.gz) * g.sy + g.ng + x; };
+   auto grow = [&](int jj) { return (jj + g.ng) * g.sx; };
 
-   // stage plane p (rows j0-2 .. j0+ty+1, every x) in its ring slot
    auto load_plane = [&](int p) {
-      R* dst = slot(p);
-      const int kw = wrap(p, g.n2);
-      const int n = rows * g.n0;
-      for (int t = tid; t < n; t += kZThreads) {
-         const int r = (int)g.fd0.div((unsigned)t);
-         const int i = t - r * g.n0;
-         const int j = j0 - 2 + r;
-         const int col = (i + j + p) & 1;
-         R* d = dst + r * rs + col * hs + (i >> 1);
+      R* dst = slot(p) + x;
+      const R* src = uin + gplane(wrap(p, g.n2));
+#pragma unroll
+      for (int r = 0; r < ROWS; r++) {
          if (MODE == 1)
-            *d = R(0);
+            dst[r * n0] = R(0);
          else
-            cp_async<sizeof(R)>(d, uin + g.c(i, wrap(j, g.n1), kw));
+            cp_async<sizeof(R)>(dst + r * n0, src + grow(jw[r]));
       }
    };
    // MODE 2: add the coarse correction to the values this thread staged
    auto add_correction = [&](int p) {
-      R* dst = slot(p);
+      R* dst = slot(p) + x;
+      const int kc = wrap(p, g.n2) >> 1;
+#pragma unroll
+      for (int r = 0; r < ROWS; r++)
+         dst[r * n0] = dst[r * n0] + e[gc.c(x >> 1, jw[r] >> 1, kc)];
+   };
+   // this column's cells of colour col in plane p from ring row rlo on sit
+   // at rows rlo + par + 2m, par = 0 or 1 by the column's parity
+   auto par_of = [&](int p, int col, int rlo) { return (x + j0 - 2 + rlo + p + col) & 1; };
+   auto gather = [&](int p, int jj, Coef<R>& cf) {
       const int kw = wrap(p, g.n2);
-      const int n = rows * g.n0;
-      for (int t = tid; t < n; t += kZThreads) {
-         const int r = (int)g.fd0.div((unsigned)t);
-         const int i = t - r * g.n0;
-         const int j = j0 - 2 + r;
-         const int col = (i + j + p) & 1;
-         R* d = dst + r * rs + col * hs + (i >> 1);
-         *d = *d + e[gc.c(i >> 1, wrap(j, g.n1) >> 1, kw >> 1)];
-      }
-   };
-   // cell m of this thread in colour col of plane p on ring rows
-   // [r_lo, r_lo + nr): t = tid + 256 m < nr * nh
-   struct Cell {
-      int r, j, jw, i, hx, q;
-   };
-   auto cell = [&](int p, int col, int r_lo, int t) {
-      Cell e;
-      const int rr = (int)g.fdh.div((unsigned)t);
-      e.hx = t - rr * nh;
-      e.r = r_lo + rr;
-      e.j = j0 - 2 + e.r;
-      e.jw = wrap(e.j, g.n1);
-      e.q = (col + e.j + p) & 1;  // x parity of this colour in the row
-      e.i = 2 * e.hx + e.q;
-      return e;
-   };
-   // the cell's coefficients (f, C, M, face D) from global memory: every
-   // load of a step is issued before any update of the step computes
-   auto gather = [&](int p, int col, int r_lo, int nr, int m, Coef<R>& cf) {
-      const int t = tid + m * kZThreads;
-      if (t >= nr * nh) return;
-      const int kw = wrap(p, g.n2);
-      const Cell e = cell(p, col, r_lo, t);
-      const int c = g.c(e.i, e.jw, kw);
-      cf.f = __ldg(f + (op.f_interior ? g.interior(e.i, e.jw, kw) : c));
+      const int c = gplane(kw) + grow(jj);
+      cf.f = __ldg(f + (op.f_interior ? (kw * g.n1 + jj) * n0 + x : c));
       if (HC) cf.c = __ldg(op.C + c);
       if (HM) cf.m = __ldg(op.M + c);
       if (HD) {
-         const int fx = g.fx(e.i, e.jw, kw), fy = g.fy(e.i, e.jw, kw), fz = g.fz(e.i, e.jw, kw);
+         const int fx = g.fx(x, jj, kw), fy = g.fy(x, jj, kw), fz = g.fz(x, jj, kw);
          cf.d[0] = __ldg(op.D0 + fx);
          cf.d[1] = __ldg(op.D0 + fx + 1);
          cf.d[2] = __ldg(op.D1 + fy);
@@ -169,26 +151,15 @@ __global__ void __launch_bounds__(kZThreads, 2)
          cf.d[5] = __ldg(op.D2 + fz + g.fzs());
       }
    };
-   // update cell m of colour col of plane p from the staged u and its
-   // gathered coefficients
-   auto update = [&](int p, int col, int r_lo, int nr, int m, const Coef<R>& cf) {
-      const int t = tid + m * kZThreads;
-      if (t >= nr * nh) return;
+   auto update = [&](int p, int r, const Coef<R>& cf) {
       R* P = slot(p);
       const R* Pm = slot(p - 1);
       const R* Pp = slot(p + 1);
-      const int oth = (1 - col) * hs;
-      const Cell e = cell(p, col, r_lo, t);
-      const int hx = e.hx, r = e.r;
-      int hm = hx - 1 + e.q;
-      if (hm < 0) hm = nh - 1;
-      int hp = hx + e.q;
-      if (hp == nh) hp = 0;
-      R* own = P + r * rs + col * hs + hx;
-      const R uc = *own;
-      const R uxm = P[r * rs + oth + hm], uxp = P[r * rs + oth + hp];
-      const R uym = P[(r - 1) * rs + oth + hx], uyp = P[(r + 1) * rs + oth + hx];
-      const R uzm = Pm[r * rs + oth + hx], uzp = Pp[r * rs + oth + hx];
+      const int o = r * n0;
+      const R uc = P[o + x];
+      const R uxm = P[o + xm], uxp = P[o + xp];
+      const R uym = P[o - n0 + x], uyp = P[o + n0 + x];
+      const R uzm = Pm[o + x], uzp = Pp[o + x];
       // expression order of op_residual_u (the colour kernel's)
       R div = R(0), dsum = R(0);
       {
@@ -219,20 +190,20 @@ __global__ void __launch_bounds__(kZThreads, 2)
       const R C = HC ? cf.c : op.cc;
       const R dudr = R(1) / (M * dsum - C);
       const R res = cf.f - M * div - C * uc;
-      *own = uc + -res * dudr;
+      P[o + x] = uc + -res * dudr;
    };
    // the block's rows of plane p (final values) -> u_out and its images
    auto store = [&](int p) {
-      const R* P = slot(p);
-      const int n = zs.ty * g.n0;
-      for (int t = tid; t < n; t += kZThreads) {
-         const int rr = (int)g.fd0.div((unsigned)t);
-         const int i = t - rr * g.n0;
-         const int j = j0 + rr;
-         const int col = (i + j + p) & 1;
-         const R v = P[(rr + 2) * rs + col * hs + (i >> 1)];
-         uout[g.c(i, j, p)] = v;
-         for_each_image(g, i, j, p, [&](int idx) { uout[idx] = v; });
+      const R* P = slot(p) + x;
+      R* dst = uout + gplane(p);
+      const bool pedge = p < g.ng || p >= g.n2 - g.ng;
+#pragma unroll
+      for (int r = 2; r < TY + 2; r++) {
+         const int j = j0 + r - 2;
+         const R v = P[r * n0];
+         dst[grow(j)] = v;
+         if (xedge || pedge || j < g.ng || j >= g.n1 - g.ng)
+            for_each_image(g, x, j, p, [&](int idx) { uout[idx] = v; });
       }
    };
 
@@ -243,7 +214,7 @@ __global__ void __launch_bounds__(kZThreads, 2)
          load_plane(next);
          cp_commit();
       }
-      // plane w+1 and all older ones have landed
+      // plane w+1 and all older ones have landed (this thread's copies)
       cp_wait(next - (w + 2));
       if (MODE == 2) {
          // every plane gets its correction once, when it is first needed
@@ -253,24 +224,35 @@ __global__ void __launch_bounds__(kZThreads, 2)
          }
          add_correction(w + 1);
       }
-      // coefficients of both updates of this step (red at w on the tile
-      // and one halo row each side, black at w-1 on the tile)
-      Coef<R> cr[CAPR], cb[CAPB];
+      // red at w on the rows and one halo row each side (ring rows
+      // 1 .. TY+2), black at w-1 on the rows (ring rows 2 .. TY+1)
+      {
+         const int par = par_of(w, 0, 1);
+         Coef<R> cr[NRED];
 #pragma unroll
-      for (int m = 0; m < CAPR; m++) gather(w, 0, 1, zs.ty + 2, m, cr[m]);
-      if (w > k0) {
+         for (int m = 0; m < NRED; m++) {
+            const int r = 1 + 2 * m;
+            gather(w, par ? jw[r + 1] : jw[r], cr[m]);
+         }
+         __syncthreads();
 #pragma unroll
-         for (int m = 0; m < CAPB; m++) gather(w - 1, 1, 2, zs.ty, m, cb[m]);
+         for (int m = 0; m < NRED; m++) update(w, 1 + 2 * m + par, cr[m]);
       }
-      __syncthreads();
-#pragma unroll
-      for (int m = 0; m < CAPR; m++) update(w, 0, 1, zs.ty + 2, m, cr[m]);
-      __syncthreads();
       if (w > k0) {
+         const int par = par_of(w - 1, 1, 2);
+         Coef<R> cb[NBLACK];
 #pragma unroll
-         for (int m = 0; m < CAPB; m++) update(w - 1, 1, 2, zs.ty, m, cb[m]);
+         for (int m = 0; m < NBLACK; m++) {
+            const int r = 2 + 2 * m;
+            gather(w - 1, par ? jw[r + 1] : jw[r], cb[m]);
+         }
+         __syncthreads();
+#pragma unroll
+         for (int m = 0; m < NBLACK; m++) update(w - 1, 2 + 2 * m + par, cb[m]);
          __syncthreads();
          store(w - 1);
+      } else {
+         __syncthreads();
       }
    }
 }
@@ -280,16 +262,15 @@ static ZShape choose_zshape(const Grid& g)
 {
    ZShape zs;
    zs.nh = g.n0 / 2;
-   // colour halves 16 banks apart: hs * sizeof(R) / 4 = 16 (mod 32)
-   const int unit = (int)sizeof(R) / 4;
-   const int mod = 32 / unit, want = 16 / unit;
-   zs.hs = zs.nh + ((want - zs.nh % mod) % mod + mod) % mod;
-   zs.ty = 8;
-   while (zs.ty > 2 && zsweep_smem_bytes<R>(zs) > 112 * 1024) zs.ty /= 2;
-   // planes per block: the most that still give every SM a block, at least
-   // 8 (each chunk stages 4 planes and updates 2 red planes twice)
+   zs.hs = g.n0;  // row stride of the ring (one x column per thread)
+   // 8 rows per block in FP32 (three blocks of <= 74 KB per SM), 4 in FP64
+   // (the coefficients of 8 rows do not fit the register budget)
+   zs.ty = sizeof(R) == 4 ? 8 : 4;
+   if (zsweep_smem_bytes<R>(zs) > 74 * 1024) zs.ty = 4;
+   // planes per block: the most that still give every SM three blocks, at
+   // least 8 (each chunk stages 4 planes and updates 2 red planes twice)
    const int by = g.n1 / zs.ty;
-   const int target = device_sms();
+   const int target = 3 * device_sms();
    int best = g.n2;
    for (int kz = g.n2; kz >= 8; kz--) {
       if (g.n2 % kz) continue;
@@ -304,29 +285,27 @@ template <class R>
 bool sweep_z_ok(const Grid& g, ZShape* out)
 {
    if (g.dim != 3 || g.ng < 1) return false;
-   if (g.n0 % 2 || g.n1 % 2 || g.n2 % 2) return false;
+   if (g.n0 % 32 || g.n0 > 256 || g.n1 % 2 || g.n2 % 2) return false;
    if (g.cells() < (1LL << 21)) return false;  // small levels: colour kernels
    const ZShape zs = choose_zshape<R>(g);
    if (g.n1 % zs.ty || g.n2 % zs.kz || zs.kz < 8) return false;
    if (zsweep_smem_bytes<R>(zs) > 200 * 1024) return false;
-   // the cells per thread and step the kernels are built for
-   if ((zs.ty + 2) * zs.nh > 6 * kZThreads || zs.ty * zs.nh > 4 * kZThreads) return false;
    if (out) *out = zs;
    return true;
 }
 
-template <class R, bool HD, bool HC, bool HM, int MODE, int CAPR, int CAPB>
-static int launch_caps(const FacOp<R>& op, const Grid& g, const ZShape& zs, const R* f,
-                       const R* uin, R* uout, const Grid& gc, const R* e, cudaStream_t s)
+template <class R, bool HD, bool HC, bool HM, int MODE, int TY>
+static int launch_ty(const FacOp<R>& op, const Grid& g, const ZShape& zs, const R* f,
+                     const R* uin, R* uout, const Grid& gc, const R* e, cudaStream_t s)
 {
    const int smem = (int)zsweep_smem_bytes<R>(zs);
    static std::atomic<unsigned long long> attr{0};
    if (first_on_device(attr))
-      cudaFuncSetAttribute(k_sweep_z<R, HD, HC, HM, MODE, CAPR, CAPB>,
+      cudaFuncSetAttribute(k_sweep_z<R, HD, HC, HM, MODE, TY>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-   const dim3 grid(g.n1 / zs.ty, g.n2 / zs.kz);
-   k_sweep_z<R, HD, HC, HM, MODE, CAPR, CAPB>
-       <<<grid, kZThreads, smem, s>>>(op, g, zs, f, uin, uout, gc, e);
+   const dim3 grid(g.n1 / TY, g.n2 / zs.kz);
+   k_sweep_z<R, HD, HC, HM, MODE, TY>
+       <<<grid, g.n0, smem, s>>>(op, g, zs.kz, f, uin, uout, gc, e);
    return launch_status();
 }
 
@@ -334,11 +313,8 @@ template <class R, bool HD, bool HC, bool HM, int MODE>
 static int launch_z(const FacOp<R>& op, const Grid& g, const ZShape& zs, const R* f,
                     const R* uin, R* uout, const Grid& gc, const R* e, cudaStream_t s)
 {
-   const int red = (zs.ty + 2) * zs.nh, black = zs.ty * zs.nh;
-   if (red <= 3 * kZThreads && black <= 2 * kZThreads)
-      return launch_caps<R, HD, HC, HM, MODE, 3, 2>(op, g, zs, f, uin, uout, gc, e, s);
-   if (red <= 6 * kZThreads && black <= 4 * kZThreads)
-      return launch_caps<R, HD, HC, HM, MODE, 6, 4>(op, g, zs, f, uin, uout, gc, e, s);
+   if (zs.ty == 8) return launch_ty<R, HD, HC, HM, MODE, 8>(op, g, zs, f, uin, uout, gc, e, s);
+   if (zs.ty == 4) return launch_ty<R, HD, HC, HM, MODE, 4>(op, g, zs, f, uin, uout, gc, e, s);
    return AMPE_ERR_INVALID;
 }
 

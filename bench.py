@@ -103,6 +103,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--only-head", action="store_true",
                     help="time only the headline path (no FP64 / mixed comparison)")
+    ap.add_argument("--surrogate-study-steps", type=int, default=200,
+                    help="steps of the surrogate study (0: skip): from the cold initial state, "
+                         "the plain warm start against the network's guess on cold starts "
+                         "and for every KKS solve")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket the headline path's timed steps with cudaProfilerStart/"
                          "Stop (ncu --profile-from-start off captures only them)")
@@ -326,7 +330,10 @@ def arm_config(args, head=None, ws=1, n=None):
     name = WORKLOAD_NAMES[args.workload] % (n, args.atol)
     if n != args.n:
         name += ": %d-cell sample of the %d-cell level" % (N, full_cells(args))
-    return {"workload": name, "path": head or args.path, "cells": N, "l2": l2,
+    path = head or args.path
+    if path == "mixed+surrogate":
+        path = "mixed+surrogate (network on cold starts; warm steps start from the previous step)"
+    return {"workload": name, "path": path, "cells": N, "l2": l2,
             "parallelism": "replicas" if ws > 1 else "single"}
 
 
@@ -509,6 +516,50 @@ def timed_path(args, m, st0, path, local, mlp=None):
             "cold_start_step": cold}, state, g
 
 
+def surrogate_study(args, m, st0, mlp):
+    """Newton iterations per cell and KKS solve, surrogate fallback rate and
+    wall time of args.surrogate_study_steps steps from the cold initial
+    state, for the mixed path with the plain warm start (the previous
+    step's phase concentrations, QuatModel.cc:5218-5231), with the network's
+    guess on cold starts only, and with the network's guess for every KKS
+    solve (the warm start then only the fallback)."""
+    import torch
+
+    from ampe_gb300 import _native, configs
+    from ampe_gb300.stepper import ImplicitStepper
+
+    L = _native.lib
+    n = args.surrogate_study_steps
+    out = {"steps": n, "cells": m.cells(),
+           "start": "the workload's initial state without phase concentrations (cold)"}
+    for name, mode in (("warm_start", 0), ("surrogate_cold_start", 1),
+                       ("surrogate_every_solve", 2)):
+        p = configs.step_params(dt=0.1, precond=args.precond, mg_levels=5, atol=args.atol,
+                                precision=1, surrogate=mode)
+        g = ImplicitStepper(m, p)
+        if mode:
+            _native.check(L.ampe_stepper_attach_surrogate(g._h, mlp), "attach_surrogate")
+        stream = torch.cuda.ExternalStream(L.ampe_stepper_stream(g._h))
+        st0.load(g)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st = g.advance(n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        solves = m.cells() * st["rhs_evals"]
+        out[name] = {"wall_s": e0.elapsed_time(e1) / 1e3,
+                     "kks_newton_iters_per_cell_solve": st["kks_iters"] / solves,
+                     "fallback_rate": st["kks_fallback"] / solves,
+                     "kks_failed_cells": st["kks_fail"], "rhs_evals": st["rhs_evals"],
+                     "newton_iters": st["newton_iters"]}
+        g.close()
+        del g
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -606,6 +657,9 @@ def run_ours(args):
                 f: float(np.linalg.norm((st[f] - refs[f]).ravel())
                          / np.linalg.norm(refs[f].ravel()))
                 for f in st}
+    study = None
+    if mlp is not None and args.surrogate_study_steps > 0 and args.workload == "calphad":
+        study = surrogate_study(args, m, st0, mlp)
     if mlp is not None:
         L.ampe_mlp_destroy(mlp)
 
@@ -650,6 +704,15 @@ def run_ours(args):
                            "with the per-kernel events, %.2f ms/step without)"
                            % (args.steps, res_h["ms_profiled"] / args.steps,
                               res_h["ms"] / args.steps)})
+    if sur_info is not None:
+        # whether the network ran inside the timed steps: it is evaluated only
+        # while no converged warm start exists (a cold start)
+        sur_info["inferences_in_timed_steps"] = kt["mlp_infer_tc"]["launches"]
+        if not kt["mlp_infer_tc"]["launches"]:
+            sur_info["timed_steps"] = (
+                "the network is not evaluated in the timed (warm) steps: the previous step's "
+                "phase concentrations start the KKS Newton in fewer iterations than its guess; "
+                "it starts cold steps only (cold_start_step, surrogate_study)")
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -658,6 +721,7 @@ def run_ours(args):
         "config": arm_config(args, head, ws),
         "paths": paths,
         "surrogate": sur_info,
+        "surrogate_study": study,
         "roofline": roof,
         "kernel_rooflines": kernel_rooflines(kt, per_cell, N, pk),
         "kernels": res_h["kernels"],

@@ -163,7 +163,8 @@ typedef struct ampe_step_params {
    int mg_levels;      /* multigrid levels incl. the fine one */
    int mg_pre, mg_post, mg_coarse_sweeps;
    int precision;      /* 0 FP64, 1 mixed (FP32 preconditioner + Jv) */
-   int surrogate;      /* 1: MLP initial guess for the cL,cS Newton */
+   int surrogate;      /* MLP initial guess for the cL,cS Newton: 1 on cold
+                        * starts only, 2 for every solve (0: none) */
    int max_retries;    /* step-size halvings after a Newton failure */
    /* 0: fixed steps of size dt.  1: variable steps chosen by CVODE's local
     * error test and step-size / order rules (CVODESolver.cc:112-258 with
