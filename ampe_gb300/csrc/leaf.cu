@@ -294,18 +294,21 @@ __global__ void k_add_flux(ampe_model_t m, Grid g, const double* u,
       if (r < nx) {
          int i, j, k;
          g.split(r, g.fd0p, g.fd1, i, j, k);
-         f0[r] = f0[r] + (1.0 / m.dx[0]) * d0[r] *
+         const int f = g.fx(i, j, k);
+         f0[f] = f0[f] + (1.0 / m.dx[0]) * d0[f] *
                              (u[g.c(i, j, k)] - u[g.c(i - 1, j, k)]);
       } else if ((r -= nx) < ny) {
          int i, j, k;
          g.split(r, g.fd0, g.fd1p, i, j, k);
-         f1[r] = f1[r] + (1.0 / m.dx[1]) * d1[r] *
+         const int f = g.fy(i, j, k);
+         f1[f] = f1[f] + (1.0 / m.dx[1]) * d1[f] *
                              (u[g.c(i, j, k)] - u[g.c(i, j - 1, k)]);
       } else {
          r -= ny;
          int i, j, k;
          g.ijk(r, i, j, k);
-         f2[r] = f2[r] + (1.0 / m.dx[2]) * d2[r] *
+         const int f = g.fz(i, j, k);
+         f2[f] = f2[f] + (1.0 / m.dx[2]) * d2[f] *
                              (u[g.c(i, j, k)] - u[g.c(i, j, k - 1)]);
       }
    }
@@ -324,6 +327,120 @@ __global__ void k_rhs_conc(ampe_model_t m, Grid g, const double* f0,
                  dyi * (f1[g.fy(i, j + 1, k)] - f1[g.fy(i, j, k)]);
       if (g.dim == 3) s = s + dzi * (f2[g.fz(i, j, k + 1)] - f2[g.fz(i, j, k)]);
       rhs[t] = m.conc_mobility * s;
+   }
+}
+
+// ADDCONCENTRATIONFLUXFROMGRADT (3d/concentrationrhs.m4:460-535,
+// 2d/concentrationrhs.m4:369-437): the thermal-diffusion part of the flux,
+// flux_d -= (1/dx_d) Mq_d ((T_i - T_{i-1}) / Tbar), Tbar the face average of
+// T (average_func, avg_type)
+__global__ void k_flux_grad_t(ampe_model_t m, Grid g, const double* T, const double* q0,
+                              const double* q1, const double* q2, double* f0, double* f1,
+                              double* f2)
+{
+   const long long nx = g.nfx(), ny = g.nfy();
+   const long long nz = g.dim == 3 ? g.nfz() : 0;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx + ny + nz;
+        t += (long long)gridDim.x * blockDim.x) {
+      long long r = t;
+      int i, j, k, dir;
+      if (r < nx) {
+         g.split(r, g.fd0p, g.fd1, i, j, k);
+         dir = 0;
+      } else if ((r -= nx) < ny) {
+         g.split(r, g.fd0, g.fd1p, i, j, k);
+         dir = 1;
+      } else {
+         g.ijk(r - ny, i, j, k);
+         dir = 2;
+      }
+      const int c = g.c(i, j, k);
+      const int cm = dir == 0 ? g.c(i - 1, j, k) : (dir == 1 ? g.c(i, j - 1, k) : g.c(i, j, k - 1));
+      const double sideT = average_func(T[cm], T[c], m.avg_type);
+      const double dxi = 1.0 / m.dx[dir];
+      double* F = dir == 0 ? f0 : (dir == 1 ? f1 : f2);
+      const double* Q = dir == 0 ? q0 : (dir == 1 ? q1 : q2);
+      const int f = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+      F[f] = F[f] - dxi * Q[f] * ((T[c] - T[cm]) / sideT);
+   }
+}
+
+// ADDCONCENTRATIONFLUXFROMANTITRAPPING for one composition
+// (3d/concentrationrhs.m4:537-700, 2d/concentrationrhs.m4:439-527): on faces
+// where |grad phi| > 1e-8, flux += alpha (dphi_n / |grad phi|) (cLbar -
+// cSbar) dphidt_bar, the normal difference across the face and the
+// tangential ones as the mean of the two cells' centred differences, in the
+// reference's order of terms
+__global__ void k_flux_antitrapping(ampe_model_t m, Grid g, const double* P,
+                                    const double* cl, const double* cs, const double* dpdt,
+                                    double alpha, double* f0, double* f1, double* f2)
+{
+   const long long nx = g.nfx(), ny = g.nfy();
+   const long long nz = g.dim == 3 ? g.nfz() : 0;
+   const double dxi = 1.0 / m.dx[0], dyi = 1.0 / m.dx[1];
+   const double dzi = g.dim == 3 ? 1.0 / m.dx[2] : 0.0;
+   const double tol = (double)1.e-8f;  // a default-real constant in the reference
+   const double tol2 = tol * tol;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx + ny + nz;
+        t += (long long)gridDim.x * blockDim.x) {
+      long long r = t;
+      int i, j, k, dir;
+      if (r < nx) {
+         g.split(r, g.fd0p, g.fd1, i, j, k);
+         dir = 0;
+      } else if ((r -= nx) < ny) {
+         g.split(r, g.fd0, g.fd1p, i, j, k);
+         dir = 1;
+      } else {
+         g.ijk(r - ny, i, j, k);
+         dir = 2;
+      }
+      auto p = [&](int a, int b, int cc) { return P[g.c(a, b, cc)]; };
+      double gx, gy, gz = 0.0, gn;
+      int cm;
+      if (dir == 0) {
+         gx = dxi * (p(i, j, k) - p(i - 1, j, k));
+         if (g.dim == 3) {
+            gy = dyi * 0.25 * (p(i, j + 1, k) - p(i, j - 1, k) + p(i - 1, j + 1, k) -
+                               p(i - 1, j - 1, k));
+            gz = dzi * 0.25 * (p(i, j, k + 1) - p(i, j, k - 1) + p(i - 1, j, k + 1) -
+                               p(i - 1, j, k - 1));
+         } else {
+            gy = dyi * 0.25 * (p(i - 1, j + 1, k) - p(i - 1, j - 1, k) + p(i, j + 1, k) -
+                               p(i, j - 1, k));
+         }
+         gn = gx;
+         cm = g.c(i - 1, j, k);
+      } else if (dir == 1) {
+         gy = dyi * (p(i, j, k) - p(i, j - 1, k));
+         gx = dxi * 0.25 * (p(i + 1, j - 1, k) - p(i - 1, j - 1, k) + p(i + 1, j, k) -
+                            p(i - 1, j, k));
+         if (g.dim == 3)
+            gz = dzi * 0.25 * (p(i, j - 1, k + 1) - p(i, j - 1, k - 1) + p(i, j, k + 1) -
+                               p(i, j, k - 1));
+         gn = gy;
+         cm = g.c(i, j - 1, k);
+      } else {
+         gz = dzi * (p(i, j, k) - p(i, j, k - 1));
+         gx = dxi * 0.25 * (p(i + 1, j, k - 1) - p(i - 1, j, k - 1) + p(i + 1, j, k) -
+                            p(i - 1, j, k));
+         gy = dyi * 0.25 * (p(i, j + 1, k - 1) - p(i, j - 1, k - 1) + p(i, j + 1, k) -
+                            p(i, j - 1, k));
+         gn = gz;
+         cm = g.c(i, j, k - 1);
+      }
+      double g2 = gx * gx + gy * gy;
+      if (g.dim == 3) g2 = g2 + gz * gz;
+      if (fabs(g2) > tol2) {
+         const int c = g.c(i, j, k);
+         const double dn = sqrt(g2);
+         const double dt = 0.5 * (dpdt[cm] + dpdt[c]);
+         const double acl = 0.5 * (cl[cm] + cl[c]);
+         const double aca = 0.5 * (cs[cm] + cs[c]);
+         double* F = dir == 0 ? f0 : (dir == 1 ? f1 : f2);
+         const int f = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+         F[f] = F[f] + alpha * (gn / dn) * (acl - aca) * dt;
+      }
    }
 }
 
@@ -442,6 +559,34 @@ int ampe_conc_flux_kks(const ampe_model_t* m, const double* phi, const double* t
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    k_conc_flux_kks<<<blocks_for(tot), 256, 0, S(stream)>>>(*m, g, phi, temp, conc, cl, cs,
                                                            flux0, flux1, flux2);
+   return launch_status();
+}
+
+int ampe_add_flux_from_grad_t(const ampe_model_t* m, const double* temp, const double* mq0,
+                              const double* mq1, const double* mq2, double* flux0,
+                              double* flux1, double* flux2, void* stream)
+{
+   if (check_model(m) || !temp || !mq0 || !mq1 || !flux0 || !flux1) return AMPE_ERR_INVALID;
+   if (m->dim == 3 && (!mq2 || !flux2)) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   k_flux_grad_t<<<blocks_for(tot), 256, 0, S(stream)>>>(*m, g, temp, mq0, mq1, mq2, flux0,
+                                                         flux1, flux2);
+   return launch_status();
+}
+
+int ampe_add_flux_from_antitrapping(const ampe_model_t* m, const double* phi,
+                                    const double* cl, const double* cs, const double* dphidt,
+                                    double alpha, double* flux0, double* flux1,
+                                    double* flux2, void* stream)
+{
+   if (check_model(m) || !phi || !cl || !cs || !dphidt || !flux0 || !flux1)
+      return AMPE_ERR_INVALID;
+   if (m->dim == 3 && !flux2) return AMPE_ERR_INVALID;
+   Grid g = make_grid(*m);
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   k_flux_antitrapping<<<blocks_for(tot), 256, 0, S(stream)>>>(*m, g, phi, cl, cs, dphidt,
+                                                               alpha, flux0, flux1, flux2);
    return launch_status();
 }
 

@@ -260,6 +260,31 @@ int ampe_add_flux(const ampe_model_t* m, const double* u, const double* d0,
                   const double* d1, const double* d2, double* flux0,
                   double* flux1, double* flux2, void* stream);
 
+/* Replaces ADDCONCENTRATIONFLUXFROMGRADT (3d/concentrationrhs.m4:460-535,
+ * 2d:369-437; EBSCompositionRHSStrategyWithGradT::addFluxFromGradTonPatch,
+ * EBSCompositionRHSStrategyWithGradT.cc:488-525, called by
+ * QuatIntegrator::evaluateConcentrationRHS, QuatIntegrator.cc:2604-2607):
+ * flux_d -= Mq_d (T_i - T_{i-1}) / (dx_d Tbar), Tbar = average_func of the
+ * two cells (avg_type).  temp ghosted; mq0..2 side arrays (the thermal-
+ * diffusion mobility of the strategy); flux side arrays, updated. */
+int ampe_add_flux_from_grad_t(const ampe_model_t* m, const double* temp,
+                              const double* mq0, const double* mq1,
+                              const double* mq2, double* flux0, double* flux1,
+                              double* flux2, void* stream);
+
+/* Replaces ADDCONCENTRATIONFLUXFROMANTITRAPPING for one composition
+ * (3d/concentrationrhs.m4:537-700, 2d:439-527;
+ * EBSCompositionRHSStrategy::addFluxFromAntitrappingonPatch,
+ * EBSCompositionRHSStrategy.cc:441-520, QuatIntegrator.cc:2608-2612): on
+ * faces with |grad phi| > 1e-8, flux += alpha (dphi_n / |grad phi|)
+ * (cLbar - cSbar) dphidt_bar.  phi, cl, cs, dphidt ghosted (corner ghosts
+ * filled); flux side arrays, updated. */
+int ampe_add_flux_from_antitrapping(const ampe_model_t* m, const double* phi,
+                                    const double* cl, const double* cs,
+                                    const double* dphidt, double alpha,
+                                    double* flux0, double* flux1,
+                                    double* flux2, void* stream);
+
 /* Replaces COMPUTERHSCONCENTRATION (ConcFort.h:419,
  * 3d/concentrationrhs.m4:412-456): rhs = M_c div(flux). */
 int ampe_computerhsconcentration(const ampe_model_t* m, const double* flux0,

@@ -102,6 +102,12 @@ void orc_fac_set_operator(void* h, const double* d0, const double* d1,
 int orc_fac_solve(void* h, const ampe_step_params_t* p, int mode,
                   const double* f, double* u, double tol, double* res);
 
+void orc_add_flux_from_grad_t(const ampe_model_t* m, const double* T, const double* q0,
+                              const double* q1, const double* q2, double* f0, double* f1,
+                              double* f2);
+void orc_add_flux_from_antitrapping(const ampe_model_t* m, const double* phase,
+                                    const double* cl, const double* ca, const double* dphidt,
+                                    double alpha, double* f0, double* f1, double* f2);
 /* implicit stepper */
 void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p);
 void orc_stepper_destroy(void* h);

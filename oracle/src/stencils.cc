@@ -566,4 +566,109 @@ void orc_jv_analytic(const ampe_model_t* m, const double* phi,
          }
 }
 
+
+// addconcentrationfluxfromgradt (3d/concentrationrhs.m4:460-535,
+// 2d/concentrationrhs.m4:369-437): loops of the reference, one face
+// direction after the other
+void orc_add_flux_from_grad_t(const ampe_model_t* m, const double* T, const double* q0,
+                              const double* q1, const double* q2, double* f0, double* f1,
+                              double* f2)
+{
+   Layout L(*m);
+   const double dxinv = 1.0 / m->dx[0], dyinv = 1.0 / m->dx[1];
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i <= L.n0; i++) {
+            const double sideT = average_func(T[L.c(i - 1, j, k)], T[L.c(i, j, k)], m->avg_type);
+            const long f = L.fx(i, j, k);
+            f0[f] = f0[f] - dxinv * q0[f] * ((T[L.c(i, j, k)] - T[L.c(i - 1, j, k)]) / sideT);
+         }
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j <= L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            const double sideT = average_func(T[L.c(i, j - 1, k)], T[L.c(i, j, k)], m->avg_type);
+            const long f = L.fy(i, j, k);
+            f1[f] = f1[f] - dyinv * q1[f] * ((T[L.c(i, j, k)] - T[L.c(i, j - 1, k)]) / sideT);
+         }
+   if (L.dim == 3) {
+      const double dzinv = 1.0 / m->dx[2];
+      for (int k = 0; k <= L.n2; k++)
+         for (int j = 0; j < L.n1; j++)
+            for (int i = 0; i < L.n0; i++) {
+               const double sideT =
+                   average_func(T[L.c(i, j, k - 1)], T[L.c(i, j, k)], m->avg_type);
+               const long f = L.fz(i, j, k);
+               f2[f] = f2[f] - dzinv * q2[f] * ((T[L.c(i, j, k)] - T[L.c(i, j, k - 1)]) / sideT);
+            }
+   }
+}
+
+// addconcentrationfluxfromantitrapping, one composition
+// (3d/concentrationrhs.m4:537-700, 2d/concentrationrhs.m4:439-527)
+void orc_add_flux_from_antitrapping(const ampe_model_t* m, const double* phase,
+                                    const double* cl, const double* ca, const double* dphidt,
+                                    double alpha, double* f0, double* f1, double* f2)
+{
+   Layout L(*m);
+   const bool d3 = L.dim == 3;
+   const double tol = (double)1.e-8f, tol2 = tol * tol;
+   const double dxinv = 1.0 / m->dx[0], dyinv = 1.0 / m->dx[1];
+   const double dzinv = d3 ? 1.0 / m->dx[2] : 0.0;
+   auto P = [&](int i, int j, int k) { return phase[L.c(i, j, k)]; };
+   auto add = [&](double* F, long f, long cm, long c, double dn, double d2) {
+      if (std::fabs(d2) > tol2) {
+         const double dphin = std::sqrt(d2);
+         const double dpdt = 0.5 * (dphidt[cm] + dphidt[c]);
+         const double acl = 0.5 * (cl[cm] + cl[c]);
+         const double aca = 0.5 * (ca[cm] + ca[c]);
+         F[f] = F[f] + alpha * (dn / dphin) * (acl - aca) * dpdt;
+      }
+   };
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i <= L.n0; i++) {
+            const double dphix = dxinv * (P(i, j, k) - P(i - 1, j, k));
+            double dphiy, dphiz = 0.0;
+            if (d3) {
+               dphiy = dyinv * 0.25 * (P(i, j + 1, k) - P(i, j - 1, k) + P(i - 1, j + 1, k) -
+                                       P(i - 1, j - 1, k));
+               dphiz = dzinv * 0.25 * (P(i, j, k + 1) - P(i, j, k - 1) + P(i - 1, j, k + 1) -
+                                       P(i - 1, j, k - 1));
+            } else {
+               dphiy = dyinv * 0.25 * (P(i - 1, j + 1, k) - P(i - 1, j - 1, k) + P(i, j + 1, k) -
+                                       P(i, j - 1, k));
+            }
+            const double d2 = d3 ? dphix * dphix + dphiy * dphiy + dphiz * dphiz
+                                 : dphix * dphix + dphiy * dphiy;
+            add(f0, L.fx(i, j, k), L.c(i - 1, j, k), L.c(i, j, k), dphix, d2);
+         }
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j <= L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            const double dphiy = dyinv * (P(i, j, k) - P(i, j - 1, k));
+            const double dphix = dxinv * 0.25 * (P(i + 1, j - 1, k) - P(i - 1, j - 1, k) +
+                                                  P(i + 1, j, k) - P(i - 1, j, k));
+            double dphiz = 0.0;
+            if (d3)
+               dphiz = dzinv * 0.25 * (P(i, j - 1, k + 1) - P(i, j - 1, k - 1) + P(i, j, k + 1) -
+                                       P(i, j, k - 1));
+            const double d2 = d3 ? dphix * dphix + dphiy * dphiy + dphiz * dphiz
+                                 : dphix * dphix + dphiy * dphiy;
+            add(f1, L.fy(i, j, k), L.c(i, j - 1, k), L.c(i, j, k), dphiy, d2);
+         }
+   if (d3) {
+      for (int k = 0; k <= L.n2; k++)
+         for (int j = 0; j < L.n1; j++)
+            for (int i = 0; i < L.n0; i++) {
+               const double dphiz = dzinv * (P(i, j, k) - P(i, j, k - 1));
+               const double dphix = dxinv * 0.25 * (P(i + 1, j, k - 1) - P(i - 1, j, k - 1) +
+                                                     P(i + 1, j, k) - P(i - 1, j, k));
+               const double dphiy = dyinv * 0.25 * (P(i, j + 1, k - 1) - P(i, j - 1, k - 1) +
+                                                     P(i, j + 1, k) - P(i, j - 1, k));
+               const double d2 = dphix * dphix + dphiy * dphiy + dphiz * dphiz;
+               add(f2, L.fz(i, j, k), L.c(i, j, k - 1), L.c(i, j, k), dphiz, d2);
+            }
+   }
+}
+
 }  // extern "C"

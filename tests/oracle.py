@@ -56,6 +56,8 @@ def lib():
             "orc_conc_diffusion": (None, [MP, P, P, P, P, P, P, P, P]),
             "orc_add_flux": (None, [MP, P, P, P, P, P, P, P]),
             "orc_computerhsconcentration": (None, [MP, P, P, P, P]),
+            "orc_add_flux_from_grad_t": (None, [MP, P, P, P, P, P, P, P]),
+            "orc_add_flux_from_antitrapping": (None, [MP, P, P, P, P, D, P, P, P]),
             "orc_conc_flux_kks": (None, [MP, P, P, P, P, P, P, P, P, P]),
             "orc_rhs_phase_conc": (None, [MP, P, P, P, P, P, P, P, P]),
             "orc_efo_rbgs": (D, [MP, P, P, P, D, P, D, P, D, P, P, I]),

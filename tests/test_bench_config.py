@@ -9,7 +9,7 @@ import bench
 
 
 def _args(workload, n=0, path="mixed+surrogate"):
-    a = argparse.Namespace(workload=workload, n=n, path=path, atol=bench.ATOL, cpu_n=48)
+    a = argparse.Namespace(workload=workload, n=n, path=path, atol=bench.ATOL, cpu_n=80)
     if a.n <= 0:
         a.n = bench.default_n(workload)
     return a
@@ -40,7 +40,7 @@ def test_cpu_sample_bounded(kind):
     a = _args(kind)
     n = bench.cpu_sample_n(a)
     m, _ = bench.workload(n, kind, state=False)
-    assert 0 < m.cells() <= 400_000
+    assert 0 < m.cells() <= 600_000
 
 
 def test_small_workload_states():
