@@ -38,6 +38,7 @@ _PROTOS = {
     "ampe_conc_flux_kks": (I, [MP, P, P, P, P, P, P, P, P, P]),
     "ampe_computerhsconcentration": (I, [MP, P, P, P, P, P]),
     "ampe_add_flux_from_grad_t": (I, [MP, P, P, P, P, P, P, P, P]),
+    "ampe_kim_mobility": (I, [MP, P, P, P, D, D, D, P, P]),
     "ampe_add_flux_from_antitrapping": (I, [MP, P, P, P, P, D, P, P, P, P]),
     "ampe_rhs_phase_conc": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_efo_rbgs": (I, [MP, P, P, P, D, P, D, P, D, P, P, I, P, P]),

@@ -444,6 +444,34 @@ __global__ void k_flux_antitrapping(ampe_model_t m, Grid g, const double* P,
    }
 }
 
+// KimMobilityStrategyInfMob::evaluateMobility (KimMobilityStrategyInfMob.cc:
+// 49-80) for a binary alloy, per cell of the ghost box
+// (KimMobilityStrategy::update, KimMobilityStrategy.cc:204-300):
+// M_phi = factor / zeta, zeta = (cL - cS)^2 f_L''(cL) / D_L(T) x 1e-6 / Vm,
+// D_L(T) = D0 exp(-Q0 / (R T)), factor = 16 w / (3 eps^2 a2)
+// (kks_mobility_factor, KKStools.cc:13-30)
+__global__ void k_kim_mobility(ampe_model_t m, Grid g, const double* tfield, const double* cl,
+                               const double* cs, double factor, double D0, double Q0,
+                               double ivm, double* mob)
+{
+   const int SX = g.n0 + 2 * g.ng, SY = g.n1 + 2 * g.ng;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.cells_ghost();
+        t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % SX) - g.ng;
+      const int j = (int)((t / SX) % SY) - g.ng;
+      const int k = (int)(t / ((long long)SX * SY)) - g.gz;
+      const double T = temperature_at(m, g, tfield, i, j, k);
+      const ThermoCoef th = thermo_coef(m, T);
+      const double a = cl[t], b = cs[t];
+      const double d2f = th.RT / (a * (1.0 - a)) + dxi_of(th, a, 0);
+      const double DL = D0 * exp(-Q0 / (kGasR * T));
+      double zeta = (a - b) * d2f * (a - b);
+      zeta = zeta / DL;
+      zeta *= ivm;
+      mob[t] = factor / zeta;
+   }
+}
+
 }  // namespace ampe
 
 using namespace ampe;
@@ -572,6 +600,29 @@ int ampe_add_flux_from_grad_t(const ampe_model_t* m, const double* temp, const d
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    k_flux_grad_t<<<blocks_for(tot), 256, 0, S(stream)>>>(*m, g, temp, mq0, mq1, mq2, flux0,
                                                          flux1, flux2);
+   return launch_status();
+}
+
+int ampe_kim_mobility(const ampe_model_t* m, const double* temp, const double* cl,
+                      const double* cs, double D0, double Q0, double molar_volume,
+                      double* mobility, void* stream)
+{
+   if (check_model(m) || !cl || !cs || !mobility || !(molar_volume > 0.0) || !(D0 > 0.0))
+      return AMPE_ERR_INVALID;
+   if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
+   double a2;
+   if (m->energy_interp == 'p')
+      a2 = 47.0 / 60.0;
+   else if (m->energy_interp == 'h')
+      a2 = 0.5;
+   else
+      return AMPE_ERR_INVALID;  // kks_mobility_factor: other types refused
+   if (!(m->epsilon_phi > 0.0)) return AMPE_ERR_INVALID;
+   const double factor =
+       16.0 * m->phase_well_scale / (3.0 * m->epsilon_phi * m->epsilon_phi * a2);
+   Grid g = make_grid(*m);
+   k_kim_mobility<<<blocks_for(g.cells_ghost()), 256, 0, S(stream)>>>(
+       *m, g, temp, cl, cs, factor, D0, Q0, 1.0e-6 / molar_volume, mobility);
    return launch_status();
 }
 

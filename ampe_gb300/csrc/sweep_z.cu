@@ -85,15 +85,18 @@ struct Coef {
 // MODE 0: sweep from u_in; 1: from u = 0 (u_in unused); 2: from u_in + P e
 // (e the next coarser level's correction, piecewise constant: the first
 // post-smoothing sweep with the prolongation fused in).  blockDim.x = n0
-// (<= 256: three blocks per SM).
+// (<= 256).
 template <class R, bool HD, bool HC, bool HM, int MODE, int TY>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 2)
     k_sweep_z(FacOp<R> op, Grid g, int kz, const R* __restrict__ f,
               const R* __restrict__ uin, R* __restrict__ uout, Grid gc,
               const R* __restrict__ e)
 {
    constexpr int ROWS = TY + 4;
    constexpr int NRED = (TY + 2) / 2, NBLACK = TY / 2;
+   // software-pipelined coefficient loads where they fit the registers (the
+   // phase operator: f and C per cell)
+   constexpr bool PIPE = !HD;
    extern __shared__ __align__(16) unsigned char zsm[];
    R* const S = reinterpret_cast<R*>(zsm);
    const int n0 = g.n0, x = threadIdx.x;
@@ -207,8 +210,31 @@ __global__ void __launch_bounds__(256, 3)
       }
    };
 
+   // the coefficients of one step: red at w on the rows and one halo row
+   // each side (ring rows 1 .. TY+2), black at w-1 on the rows (ring rows
+   // 2 .. TY+1)
+   auto gather_step = [&](int w, Coef<R>* cr, Coef<R>* cb) {
+      const int pr = par_of(w, 0, 1);
+#pragma unroll
+      for (int m = 0; m < NRED; m++) {
+         const int r = 1 + 2 * m;
+         gather(w, pr ? jw[r + 1] : jw[r], cr[m]);
+      }
+      if (w > k0) {
+         const int pb = par_of(w - 1, 1, 2);
+#pragma unroll
+         for (int m = 0; m < NBLACK; m++) {
+            const int r = 2 + 2 * m;
+            gather(w - 1, pb ? jw[r + 1] : jw[r], cb[m]);
+         }
+      }
+   };
    int next = k0 - 2;  // next plane to stage
-   for (int w = k0 - 1; w <= k1; w++) {
+   // one step; with PIPE the coefficients of step w come in cur (gathered
+   // during step w-1) and those of step w+1 are gathered into nxt before
+   // this step's last barrier, so their loads overlap the store and the next
+   // step's wait
+   auto step = [&](int w, Coef<R>* cr, Coef<R>* cb, Coef<R>* nr, Coef<R>* nb) {
       const int want = min(w + 1 + kZPrefetch, k1 + 1);
       for (; next <= want; next++) {
          load_plane(next);
@@ -224,36 +250,33 @@ __global__ void __launch_bounds__(256, 3)
          }
          add_correction(w + 1);
       }
-      // red at w on the rows and one halo row each side (ring rows
-      // 1 .. TY+2), black at w-1 on the rows (ring rows 2 .. TY+1)
-      {
-         const int par = par_of(w, 0, 1);
-         Coef<R> cr[NRED];
+      if (!PIPE) gather_step(w, cr, cb);
+      __syncthreads();
+      const int pr = par_of(w, 0, 1);
 #pragma unroll
-         for (int m = 0; m < NRED; m++) {
-            const int r = 1 + 2 * m;
-            gather(w, par ? jw[r + 1] : jw[r], cr[m]);
-         }
-         __syncthreads();
-#pragma unroll
-         for (int m = 0; m < NRED; m++) update(w, 1 + 2 * m + par, cr[m]);
-      }
+      for (int m = 0; m < NRED; m++) update(w, 1 + 2 * m + pr, cr[m]);
+      __syncthreads();
       if (w > k0) {
-         const int par = par_of(w - 1, 1, 2);
-         Coef<R> cb[NBLACK];
+         const int pb = par_of(w - 1, 1, 2);
 #pragma unroll
-         for (int m = 0; m < NBLACK; m++) {
-            const int r = 2 + 2 * m;
-            gather(w - 1, par ? jw[r + 1] : jw[r], cb[m]);
-         }
-         __syncthreads();
-#pragma unroll
-         for (int m = 0; m < NBLACK; m++) update(w - 1, 2 + 2 * m + par, cb[m]);
+         for (int m = 0; m < NBLACK; m++) update(w - 1, 2 + 2 * m + pb, cb[m]);
+      }
+      if (PIPE && w < k1) gather_step(w + 1, nr, nb);
+      if (w > k0) {
          __syncthreads();
          store(w - 1);
-      } else {
-         __syncthreads();
       }
+   };
+   if constexpr (PIPE) {
+      Coef<R> ar[NRED], ab[NBLACK], br[NRED], bb[NBLACK];
+      gather_step(k0 - 1, ar, ab);
+      for (int w = k0 - 1; w <= k1; w += 2) {
+         step(w, ar, ab, br, bb);
+         if (w + 1 <= k1) step(w + 1, br, bb, ar, ab);
+      }
+   } else {
+      Coef<R> cr[NRED], cb[NBLACK];
+      for (int w = k0 - 1; w <= k1; w++) step(w, cr, cb, cr, cb);
    }
 }
 
@@ -263,14 +286,14 @@ static ZShape choose_zshape(const Grid& g)
    ZShape zs;
    zs.nh = g.n0 / 2;
    zs.hs = g.n0;  // row stride of the ring (one x column per thread)
-   // 8 rows per block in FP32 (three blocks of <= 74 KB per SM), 4 in FP64
-   // (the coefficients of 8 rows do not fit the register budget)
+   // 8 rows per block in FP32 (<= 74 KB of ring per block), 4 in FP64 (the
+   // coefficients of 8 rows do not fit the register budget)
    zs.ty = sizeof(R) == 4 ? 8 : 4;
    if (zsweep_smem_bytes<R>(zs) > 74 * 1024) zs.ty = 4;
-   // planes per block: the most that still give every SM three blocks, at
+   // planes per block: the most that still give every SM two blocks, at
    // least 8 (each chunk stages 4 planes and updates 2 red planes twice)
    const int by = g.n1 / zs.ty;
-   const int target = 3 * device_sms();
+   const int target = 2 * device_sms();
    int best = g.n2;
    for (int kz = g.n2; kz >= 8; kz--) {
       if (g.n2 % kz) continue;

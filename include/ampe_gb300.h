@@ -285,6 +285,23 @@ int ampe_add_flux_from_antitrapping(const ampe_model_t* m, const double* phi,
                                     double* flux0, double* flux1,
                                     double* flux2, void* stream);
 
+/* Phase mobility of the Kim model with infinite interface mobility,
+ * binary alloy (KimMobilityStrategyInfMob::evaluateMobility,
+ * KimMobilityStrategyInfMob.cc:49-80, on every cell of the ghost box as
+ * KimMobilityStrategy::update, KimMobilityStrategy.cc:204-300, with the
+ * zeta of the liquid phase computed, i.e. no zeta factor given):
+ * M = factor / zeta, zeta = (cL - cS)^2 f_L''(cL) / (D0 exp(-Q0/(R T)))
+ * x 1e-6 / molar_volume, factor = 16 w / (3 eps^2 a2), a2 = 47/60 for
+ * energy_interp 'p', 1/2 for 'h' (kks_mobility_factor, KKStools.cc:13-30;
+ * other types AMPE_ERR_INVALID).  cl, cs, temp (AMPE_TEMP_FIELD only) and
+ * mobility ghosted.  The finite-mobility variant
+ * (KimMobilityStrategyFiniteMob.cc) is the constant mu / (3 sqrt(2) xi),
+ * xi = eps / sqrt(16 w). */
+int ampe_kim_mobility(const ampe_model_t* m, const double* temp,
+                      const double* cl, const double* cs, double D0,
+                      double Q0, double molar_volume, double* mobility,
+                      void* stream);
+
 /* Replaces COMPUTERHSCONCENTRATION (ConcFort.h:419,
  * 3d/concentrationrhs.m4:412-456): rhs = M_c div(flux). */
 int ampe_computerhsconcentration(const ampe_model_t* m, const double* flux0,

@@ -108,6 +108,9 @@ void orc_add_flux_from_grad_t(const ampe_model_t* m, const double* T, const doub
 void orc_add_flux_from_antitrapping(const ampe_model_t* m, const double* phase,
                                     const double* cl, const double* ca, const double* dphidt,
                                     double alpha, double* f0, double* f1, double* f2);
+void orc_kim_mobility(const ampe_model_t* m, const double* tfield, const double* cl,
+                      const double* cs, double factor, double D0, double Q0, double mv,
+                      double* mob);
 /* implicit stepper */
 void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p);
 void orc_stepper_destroy(void* h);

@@ -671,4 +671,26 @@ void orc_add_flux_from_antitrapping(const ampe_model_t* m, const double* phase,
    }
 }
 
+// KimMobilityStrategyInfMob::evaluateMobility (KimMobilityStrategyInfMob.cc:
+// 49-80) with kks_mobility_factor (KKStools.cc:13-30), binary, over the
+// ghost box (KimMobilityStrategy.cc:204-300); factor given by the caller
+void orc_kim_mobility(const ampe_model_t* m, const double* tfield, const double* cl,
+                      const double* cs, double factor, double D0, double Q0, double mv,
+                      double* mob)
+{
+   Layout L(*m);
+   for (int k = -L.gz; k < L.n2 + L.gz; k++)
+      for (int j = -L.ng; j < L.n1 + L.ng; j++)
+         for (int i = -L.ng; i < L.n0 + L.ng; i++) {
+            const long c = L.c(i, j, k);
+            const double T = temperature_at(*m, tfield, L, i, j, k);
+            const double d2f = d2fdc2(thermo_at(*m, T), cl[c], 0);
+            const double DL = D0 * std::exp(-Q0 / (kGasR * T));
+            double zeta = (cl[c] - cs[c]) * d2f * (cl[c] - cs[c]);
+            zeta = zeta / DL;
+            zeta *= 1.e-6 / mv;
+            mob[c] = factor / zeta;
+         }
+}
+
 }  // extern "C"

@@ -113,3 +113,32 @@ def test_flux_terms(cuda, orc, dim, ng_side):
         a = _interior(ms, fd[d][1].cpu().numpy())
         assert O.rel_l2(a, fo[d]) <= TOL
         assert not np.array_equal(a, f[d])
+
+
+@pytest.mark.parametrize("interp", [b"p", b"h"])
+def test_kim_mobility(cuda, orc, interp):
+    """Kim phase mobility (ampe_kim_mobility; KimMobilityStrategyInfMob.cc:
+    49-80) over the ghost box against the oracle, 3D CALPHAD with the x
+    temperature gradient."""
+    import torch
+
+    keep = []
+    m = _model(3)
+    m.energy_interp = interp
+    rng = np.random.default_rng(9)
+    shp = m.interior_shape()
+    cl = O.ghosted(m, rng.uniform(0.3, 0.5, shp))
+    cs = O.ghosted(m, rng.uniform(0.1, 0.25, shp))
+    a2 = 47.0 / 60.0 if interp == b"p" else 0.5
+    factor = 16 * m.phase_well_scale / (3 * m.epsilon_phi ** 2 * a2)
+    mo = np.zeros_like(cl)
+    orc.orc_kim_mobility(C.byref(m), None, O.ptr(cl), O.ptr(cs), factor, 2.5, 4.0e4, 7.68e-6,
+                         O.ptr(mo))
+    pm, tm = _dev(np.zeros_like(cl), keep)
+    assert cuda.lib.ampe_kim_mobility(C.byref(m), None, _dev(cl, keep)[0], _dev(cs, keep)[0],
+                                      2.5, 4.0e4, 7.68e-6, pm, None) == 0
+    torch.cuda.synchronize()
+    assert O.rel_l2(tm.cpu().numpy(), mo) <= TOL
+    m.energy_interp = b"l"
+    assert cuda.lib.ampe_kim_mobility(C.byref(m), None, _dev(cl, keep)[0], _dev(cs, keep)[0],
+                                      2.5, 4.0e4, 7.68e-6, pm, None) == abi.AMPE_ERR_INVALID
