@@ -24,6 +24,7 @@ D = C.c_double
 I = C.c_int
 MP = C.POINTER(abi.Model)
 SP = C.POINTER(abi.StepParams)
+MOB = C.POINTER(abi.Mobility)
 
 _PROTOS = {
     "ampe_version": (C.c_char_p, []),
@@ -39,6 +40,7 @@ _PROTOS = {
     "ampe_computerhsconcentration": (I, [MP, P, P, P, P, P]),
     "ampe_add_flux_from_grad_t": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_kim_mobility": (I, [MP, P, P, P, D, D, D, P, P]),
+    "ampe_conc_diffusion_mobility": (I, [MP, MOB] + [P] * 17),
     "ampe_add_flux_from_antitrapping": (I, [MP, P, P, P, P, D, P, P, P, P]),
     "ampe_rhs_phase_conc": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_efo_rbgs": (I, [MP, P, P, P, D, P, D, P, D, P, P, I, P, P]),

@@ -29,6 +29,14 @@ class GTerm(C.Structure):
     ]
 
 
+class Mobility(C.Structure):
+    """ampe_mobility_t: CALPHAD atomic mobilities of a binary alloy,
+    q[species][phase][qA|qB] = (a0, a1, a2, a3) and
+    qq[species][phase][n] = (a0, a1) of q<n>AB (phase 0 liquid, 1 solid)."""
+
+    _fields_ = [("q", C.c_double * 4 * 2 * 2 * 2), ("qq", C.c_double * 2 * 4 * 2 * 2)]
+
+
 class Model(C.Structure):
     """ampe_model_t."""
 

@@ -74,7 +74,45 @@ def database_from_text(text):
             db["species"][sp][ph] = seg
     for ph, key in (("L", "LmixPhaseL"), ("S", "LmixPhaseA")):
         db["Lmix"][ph] = {k: v for k, v in tree.get(key, {}).items()}
+    if "MobilityParameters" in tree:
+        db["mobility"] = mobility_from_tree(tree["MobilityParameters"])
     return db
+
+
+def mobility_from_tree(node):
+    """The MobilityParameters block (CALPHADMobility::initialize,
+    CALPHADMobility.cc:17-150; CompositionStrategyMobilities.cc:36-90) as
+    {'0'|'1' (species): {'L'|'S' (phase): {'qA': [...], 'qB': [...],
+    'q0AB': [...], ...}}}; keys absent from the block are absent here."""
+    out = {}
+    for s in ("0", "1"):
+        sp = node["Species" + s]
+        out[s] = {}
+        for ph, key in (("L", "PhaseL"), ("S", "PhaseA")):
+            out[s][ph] = {k: list(v) for k, v in sp[key].items()}
+    return out
+
+
+def mobility_struct(mob):
+    """abi.Mobility from mobility_from_tree's dict: qA/qB take 2 or 4
+    values (a0, a1[, a2, a3]); q<n>AB default to (0, 1) as in the
+    reference."""
+    mb = abi.Mobility()
+    for si, s in enumerate(("0", "1")):
+        for pi, ph in enumerate(("L", "S")):
+            d = mob[s][ph]
+            for ii, k in enumerate(("qA", "qB")):
+                v = list(d[k])
+                if len(v) not in (2, 4):
+                    raise ValueError("%s of species %s, phase %s: %d values" % (k, s, ph, len(v)))
+                v = v + [0.0] * (4 - len(v))
+                for c in range(4):
+                    mb.q[si][pi][ii][c] = v[c]
+            for n in range(4):
+                v = d.get("q%dAB" % n, [0.0, 1.0])
+                mb.qq[si][pi][n][0] = v[0]
+                mb.qq[si][pi][n][1] = v[1]
+    return mb
 
 
 def gterm_from_segments(seg):

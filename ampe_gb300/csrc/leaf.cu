@@ -472,6 +472,93 @@ __global__ void k_kim_mobility(ampe_model_t m, Grid g, const double* tfield, con
    }
 }
 
+// Q_i(T) and the interaction terms of one species' mobility in one phase
+// (CALPHADMobility.h getQ, getQQ0..3)
+__device__ __forceinline__ double mob_q(const double* a, double T)
+{
+   return a[0] + kGasR * T * log(a[1]) + a[2] * T * log(T) + a[3] / T;
+}
+
+__device__ __forceinline__ double mob_qq(const double* a, double T)
+{
+   return a[0] + kGasR * T * log(a[1]);
+}
+
+// atomic mobility of species s in phase p at composition (c0, c1 = 1 - c0)
+// (CALPHADMobility::getAtomicMobility and getDeltaG, binary form)
+__device__ __forceinline__ double atomic_mobility(const ampe_mobility_t& mb, int s, int p,
+                                                  double c0, double c1, double T)
+{
+   const double dc = c0 - c1;
+   const double dG =
+       c0 * mob_q(mb.q[s][p][0], T) + c1 * mob_q(mb.q[s][p][1], T) +
+       c0 * c1 *
+           (mob_qq(mb.qq[s][p][0], T) +
+            dc * (mob_qq(mb.qq[s][p][1], T) +
+                  dc * (mob_qq(mb.qq[s][p][2], T) + dc * mob_qq(mb.qq[s][p][3], T))));
+   const double rtinv = 1.0 / (kGasR * T);
+   return exp(dG * rtinv) * rtinv;
+}
+
+// D_p = (mobility matrix) x (free-energy curvature), 1x1 for a binary
+// (computeLocalDiffusionMatrixL/A with computeDiffusionMobilityBinaryPhase)
+__device__ __forceinline__ double phase_diffusion(const ampe_model_t& m,
+                                                  const ampe_mobility_t& mb, int p, double c,
+                                                  double T)
+{
+   const double c1 = 1.0 - c;
+   const double m0 = atomic_mobility(mb, 0, p, c, c1, T);
+   const double m1 = atomic_mobility(mb, 1, p, c, c1, T);
+   const double mm = c * m1 + c1 * m0;
+   const double mob = c * c1 * mm * 1.e12;
+   const ThermoCoef th = thermo_coef(m, T);
+   const double d2f = th.RT / (c * (1.0 - c)) + dxi_of(th, c, p);
+   return mob * d2f;
+}
+
+__global__ void k_conc_diffusion_mobility(ampe_model_t m, ampe_mobility_t mb, Grid g,
+                                          const double* phi, const double* temp,
+                                          const double* cl, const double* cs, double* dl0,
+                                          double* dl1, double* dl2, double* ds0, double* ds1,
+                                          double* ds2, double* el0, double* el1, double* el2,
+                                          double* es0, double* es1, double* es2)
+{
+   const long long nx = g.nfx(), ny = g.nfy();
+   const long long nz = g.dim == 3 ? g.nfz() : 0;
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx + ny + nz;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      long long r = t;
+      if (r < nx) {
+         dir = 0;
+         g.split(r, g.fd0p, g.fd1, i, j, k);
+      } else if ((r -= nx) < ny) {
+         dir = 1;
+         g.split(r, g.fd0, g.fd1p, i, j, k);
+      } else {
+         r -= ny;
+         dir = 2;
+         g.ijk(r, i, j, k);
+      }
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const long long lo = g.c(i - ei, j - ej, k - ek), hi = g.c(i, j, k);
+      const double T = 0.5 * (temperature_at(m, g, temp, i, j, k) +
+                              temperature_at(m, g, temp, i - ei, j - ej, k - ek));
+      const double DL = phase_diffusion(m, mb, 0, 0.5 * (cl[hi] + cl[lo]), T);
+      const double DS = phase_diffusion(m, mb, 1, 0.5 * (cs[hi] + cs[lo]), T);
+      const double hphi = interp_func(average_func(phi[hi], phi[lo], m.avg_type), m.diff_interp);
+      const long long f = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+      double* DLo = dir == 0 ? dl0 : (dir == 1 ? dl1 : dl2);
+      double* DSo = dir == 0 ? ds0 : (dir == 1 ? ds1 : ds2);
+      double* ELo = dir == 0 ? el0 : (dir == 1 ? el1 : el2);
+      double* ESo = dir == 0 ? es0 : (dir == 1 ? es1 : es2);
+      DLo[f] = (1.0 - hphi) * DL;
+      DSo[f] = hphi * DS;
+      if (ELo) ELo[f] = DL;
+      if (ESo) ESo[f] = DS;
+   }
+}
+
 }  // namespace ampe
 
 using namespace ampe;
@@ -623,6 +710,33 @@ int ampe_kim_mobility(const ampe_model_t* m, const double* temp, const double* c
    Grid g = make_grid(*m);
    k_kim_mobility<<<blocks_for(g.cells_ghost()), 256, 0, S(stream)>>>(
        *m, g, temp, cl, cs, factor, D0, Q0, 1.0e-6 / molar_volume, mobility);
+   return launch_status();
+}
+
+int ampe_conc_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* mob,
+                                 const double* phi, const double* temp,
+                                 const double* cl, const double* cs, double* dl0,
+                                 double* dl1, double* dl2, double* ds0, double* ds1,
+                                 double* ds2, double* coef_l0, double* coef_l1,
+                                 double* coef_l2, double* coef_s0, double* coef_s1,
+                                 double* coef_s2, void* stream)
+{
+   if (check_model(m) || !mob || !phi || !cl || !cs || !dl0 || !dl1 || !ds0 || !ds1)
+      return AMPE_ERR_INVALID;
+   if (m->dim == 3 && (!dl2 || !ds2)) return AMPE_ERR_INVALID;
+   if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
+   for (int s = 0; s < 2; s++)
+      for (int p = 0; p < 2; p++) {
+         for (int i = 0; i < 2; i++)
+            if (!(mob->q[s][p][i][1] > 0.0)) return AMPE_ERR_INVALID;  // ln(a1)
+         for (int n = 0; n < 4; n++)
+            if (!(mob->qq[s][p][n][1] > 0.0)) return AMPE_ERR_INVALID;
+      }
+   Grid g = make_grid(*m);
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
+   k_conc_diffusion_mobility<<<blocks_for(tot), 256, 0, S(stream)>>>(
+       *m, *mob, g, phi, temp, cl, cs, dl0, dl1, dl2, ds0, ds1, ds2, coef_l0, coef_l1,
+       coef_l2, coef_s0, coef_s1, coef_s2);
    return launch_status();
 }
 

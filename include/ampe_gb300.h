@@ -302,6 +302,42 @@ int ampe_kim_mobility(const ampe_model_t* m, const double* temp,
                       double Q0, double molar_volume, double* mobility,
                       void* stream);
 
+/* CALPHAD atomic mobilities of a binary alloy, one set per species and phase
+ * (CALPHADMobility::initialize, CALPHADMobility.cc:17-150: the
+ * MobilityParameters block of a thermodynamic database).  For species s in
+ * phase p (0 liquid "PhaseL", 1 solid "PhaseA"):
+ *   q[s][p][i]  = (a0, a1, a2, a3) of qA (i = 0) and qB (i = 1):
+ *                 Q_i(T) = a0 + R T ln(a1) + a2 T ln(T) + a3 / T
+ *                 (a2 = a3 = 0 when the database gives two values);
+ *   qq[s][p][n] = (a0, a1) of q<n>AB, n = 0..3: a0 + R T ln(a1), (0, 1)
+ *                 when absent. */
+typedef struct ampe_mobility {
+   double q[2][2][2][4];
+   double qq[2][2][4][2];
+} ampe_mobility_t;
+
+/* Composition-dependent diffusion from atomic mobilities, binary alloy
+ * (MobilityCompositionDiffusionStrategy::setDiffusion,
+ * MobilityCompositionDiffusionStrategy.cc:83-611, with
+ * computeDiffusionMobilityBinaryPhase, CALPHADMobility.cc:196-215): on every
+ * interior face, with T, cL and cS the arithmetic means of the two cells,
+ *   D_p = c(1-c) (c M_1 + (1-c) M_0) 1e12 * f_p''(c)   (c = cL or cS),
+ *   M_s = exp(dG_s / (R T)) / (R T),
+ *   dG_s = c Q_A + (1-c) Q_B + c (1-c) sum_n q_n (2c-1)^n,
+ * f_p'' the phase's free-energy curvature in J/mol, and
+ *   dl = (1 - h) D_L,  ds = h D_S,  h = diff_interp(avg_type(phi, phi')).
+ * Optional coef_l0..2, coef_s0..2 (may be NULL) receive D_L and D_S
+ * themselves (the reference's diffusion_coeff side data).  Cell fields
+ * ghosted with m->ng, side fields with m->ng_side; temp is read only for
+ * AMPE_TEMP_FIELD. */
+int ampe_conc_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* mob,
+                                 const double* phi, const double* temp,
+                                 const double* cl, const double* cs, double* dl0,
+                                 double* dl1, double* dl2, double* ds0, double* ds1,
+                                 double* ds2, double* coef_l0, double* coef_l1,
+                                 double* coef_l2, double* coef_s0, double* coef_s1,
+                                 double* coef_s2, void* stream);
+
 /* Replaces COMPUTERHSCONCENTRATION (ConcFort.h:419,
  * 3d/concentrationrhs.m4:412-456): rhs = M_c div(flux). */
 int ampe_computerhsconcentration(const ampe_model_t* m, const double* flux0,

@@ -111,6 +111,14 @@ void orc_add_flux_from_antitrapping(const ampe_model_t* m, const double* phase,
 void orc_kim_mobility(const ampe_model_t* m, const double* tfield, const double* cl,
                       const double* cs, double factor, double D0, double Q0, double mv,
                       double* mob);
+double orc_phase_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* mb, int p,
+                                    double c, double T);
+void orc_conc_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* mb,
+                                 const double* phi, const double* temp, const double* cl,
+                                 const double* cs, double* dl0, double* dl1, double* dl2,
+                                 double* ds0, double* ds1, double* ds2, double* el0,
+                                 double* el1, double* el2, double* es0, double* es1,
+                                 double* es2);
 /* implicit stepper */
 void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p);
 void orc_stepper_destroy(void* h);

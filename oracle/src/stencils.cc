@@ -693,4 +693,83 @@ void orc_kim_mobility(const ampe_model_t* m, const double* tfield, const double*
          }
 }
 
+
+// Composition-dependent diffusion from CALPHAD atomic mobilities, binary
+// (MobilityCompositionDiffusionStrategy.cc:180-611 setDiffCoeffInEachPhase-
+// OnPatch and setPFMDiffOnPatch; mobility matrix of
+// computeDiffusionMobilityBinaryPhase, CALPHADMobility.cc:196-215; atomic
+// mobility and dG of CALPHADMobility.h:70-115 and .cc:152-162; the
+// diffusion matrix is the mobility times the J/mol free-energy curvature,
+// computeLocalDiffusionMatrixL/A, .cc:46-80).
+static double orc_mob_q(const double* a, double T)
+{
+   return a[0] + kGasR * T * std::log(a[1]) + a[2] * T * std::log(T) + a[3] / T;
+}
+
+static double orc_mob_qq(const double* a, double T)
+{
+   return a[0] + kGasR * T * std::log(a[1]);
+}
+
+static double orc_atomic_mobility(const ampe_mobility_t& mb, int s, int p, double c0,
+                                  double c1, double T)
+{
+   const double dc = c0 - c1;
+   const double dG =
+       c0 * orc_mob_q(mb.q[s][p][0], T) + c1 * orc_mob_q(mb.q[s][p][1], T) +
+       c0 * c1 *
+           (orc_mob_qq(mb.qq[s][p][0], T) +
+            dc * (orc_mob_qq(mb.qq[s][p][1], T) +
+                  dc * (orc_mob_qq(mb.qq[s][p][2], T) + dc * orc_mob_qq(mb.qq[s][p][3], T))));
+   const double rtinv = 1.0 / (kGasR * T);
+   return std::exp(dG * rtinv) * rtinv;
+}
+
+double orc_phase_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* mb, int p,
+                                    double c, double T)
+{
+   const double c1 = 1.0 - c;
+   const double m0 = orc_atomic_mobility(*mb, 0, p, c, c1, T);
+   const double m1 = orc_atomic_mobility(*mb, 1, p, c, c1, T);
+   const double mm = c * m1 + c1 * m0;
+   return c * c1 * mm * 1.e12 * d2fdc2(thermo_at(*m, T), c, p);
+}
+
+void orc_conc_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* mb,
+                                 const double* phi, const double* temp, const double* cl,
+                                 const double* cs, double* dl0, double* dl1, double* dl2,
+                                 double* ds0, double* ds1, double* ds2, double* el0,
+                                 double* el1, double* el2, double* es0, double* es1,
+                                 double* es2)
+{
+   Layout L(*m);
+   for (int dir = 0; dir < L.dim; dir++) {
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      double* DL = dir == 0 ? dl0 : (dir == 1 ? dl1 : dl2);
+      double* DS = dir == 0 ? ds0 : (dir == 1 ? ds1 : ds2);
+      double* EL = dir == 0 ? el0 : (dir == 1 ? el1 : el2);
+      double* ES = dir == 0 ? es0 : (dir == 1 ? es1 : es2);
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int k = 0; k < L.n2 + ek; k++)
+         for (int j = 0; j < L.n1 + ej; j++)
+            for (int i = 0; i < L.n0 + ei; i++) {
+               const long hi = L.c(i, j, k), lo = L.c(i - ei, j - ej, k - ek);
+               const double T = 0.5 * (temperature_at(*m, temp, L, i, j, k) +
+                                       temperature_at(*m, temp, L, i - ei, j - ej, k - ek));
+               const double dlc = orc_phase_diffusion_mobility(m, mb, 0,
+                                                               0.5 * (cl[hi] + cl[lo]), T);
+               const double dsc = orc_phase_diffusion_mobility(m, mb, 1,
+                                                               0.5 * (cs[hi] + cs[lo]), T);
+               const double hphi =
+                   interp_func(average_func(phi[hi], phi[lo], m->avg_type), m->diff_interp);
+               const long f = dir == 0 ? L.fx(i, j, k)
+                                       : (dir == 1 ? L.fy(i, j, k) : L.fz(i, j, k));
+               DL[f] = (1.0 - hphi) * dlc;
+               DS[f] = hphi * dsc;
+               if (EL) EL[f] = dlc;
+               if (ES) ES[f] = dsc;
+            }
+   }
+}
+
 }  // extern "C"

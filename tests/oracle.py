@@ -58,6 +58,8 @@ def lib():
             "orc_computerhsconcentration": (None, [MP, P, P, P, P]),
             "orc_add_flux_from_grad_t": (None, [MP, P, P, P, P, P, P, P]),
             "orc_kim_mobility": (None, [MP, P, P, P, D, D, D, D, P]),
+            "orc_phase_diffusion_mobility": (D, [MP, C.POINTER(abi.Mobility), I, D, D]),
+            "orc_conc_diffusion_mobility": (None, [MP, C.POINTER(abi.Mobility)] + [P] * 16),
             "orc_add_flux_from_antitrapping": (None, [MP, P, P, P, P, D, P, P, P]),
             "orc_conc_flux_kks": (None, [MP, P, P, P, P, P, P, P, P, P]),
             "orc_rhs_phase_conc": (None, [MP, P, P, P, P, P, P, P, P]),

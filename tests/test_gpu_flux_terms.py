@@ -142,3 +142,61 @@ def test_kim_mobility(cuda, orc, interp):
     m.energy_interp = b"l"
     assert cuda.lib.ampe_kim_mobility(C.byref(m), None, _dev(cl, keep)[0], _dev(cs, keep)[0],
                                       2.5, 4.0e4, 7.68e-6, pm, None) == abi.AMPE_ERR_INVALID
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("ng_side", [0, 1])
+def test_mobility_diffusion(cuda, orc, dim, ng_side):
+    """Composition-dependent diffusion from the AuNi atomic mobilities
+    (ampe_conc_diffusion_mobility; MobilityCompositionDiffusionStrategy.cc:
+    180-611) against the oracle: the weighted face coefficients and the
+    per-phase ones, side arrays with 0 and 1 ghost (ghost faces untouched)."""
+    import json
+    import os
+
+    import torch
+
+    from ampe_gb300 import calphad_db
+
+    keep = []
+    m = _model(dim)
+    with open(os.path.join(os.path.dirname(__file__), "golden", "calphad_AuNi.json")) as f:
+        db = json.load(f)
+    calphad_db.apply_database(m, db)
+    m.T0, m.gradT = 1450.0, 5.0
+    m.temp_mode = abi.TEMP_GRADIENT
+    mb = calphad_db.mobility_struct(db["mobility"])
+    ms = abi.Model.from_buffer_copy(m)
+    ms.ng_side = ng_side
+    rng = np.random.default_rng(12)
+    shp = m.interior_shape()
+    phi = O.ghosted(m, rng.uniform(0, 1, shp))
+    cl = O.ghosted(m, rng.uniform(0.05, 0.5, shp))
+    cs = O.ghosted(m, rng.uniform(0.02, 0.3, shp))
+    faces = m.face_shapes()
+    zero = [np.zeros(faces[d]) if d < dim else np.zeros((1, 1, 1)) for d in range(3)]
+    out = [[x.copy() for x in zero] for _ in range(4)]
+    orc.orc_conc_diffusion_mobility(C.byref(m), C.byref(mb), O.ptr(phi), None, O.ptr(cl),
+                                    O.ptr(cs), *[O.ptr(a) for grp in out for a in grp])
+    # interiors start at the sentinel too, so every face written is checked
+    plain = [np.full(faces[d], SENTINEL) if d < dim else None for d in range(3)]
+    dev = [_sides(m, ms, plain, keep) for _ in range(4)]
+    assert cuda.lib.ampe_conc_diffusion_mobility(
+        C.byref(ms), C.byref(mb), _dev(phi, keep)[0], None, _dev(cl, keep)[0],
+        _dev(cs, keep)[0], *[p for grp in dev for p, _ in grp], None) == 0
+    torch.cuda.synchronize()
+    for q in range(4):
+        for d in range(dim):
+            a = dev[q][d][1].cpu().numpy()
+            assert O.rel_l2(_interior(ms, a), out[q][d]) <= TOL
+            if ng_side:
+                b = a.copy()
+                gz = ng_side if dim == 3 else 0
+                b[gz:b.shape[0] - gz, ng_side:b.shape[1] - ng_side,
+                  ng_side:b.shape[2] - ng_side] = SENTINEL
+                assert np.all(b == SENTINEL)
+    bad = abi.Mobility.from_buffer_copy(mb)
+    bad.qq[0][0][2][1] = 0.0  # ln(0): refused
+    assert cuda.lib.ampe_conc_diffusion_mobility(
+        C.byref(ms), C.byref(bad), _dev(phi, keep)[0], None, _dev(cl, keep)[0],
+        _dev(cs, keep)[0], *[p for grp in dev for p, _ in grp], None) == abi.AMPE_ERR_INVALID
