@@ -41,6 +41,11 @@ _PROTOS = {
     "ampe_add_flux_from_grad_t": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_kim_mobility": (I, [MP, P, P, P, D, D, D, P, P]),
     "ampe_conc_diffusion_mobility": (I, [MP, MOB] + [P] * 17),
+    "ampe_quat_symm_table": (I, [P, P]),
+    "ampe_quat_symm_rotation": (I, [MP, P, P, P, P, P]),
+    "ampe_quat_fundamental": (I, [MP, P, P]),
+    "ampe_quat_diffs_symm": (I, [MP, P, P, P, P, P, P, P, P]),
+    "ampe_quat_grad_side_symm": (I, [MP] + [P] * 16),
     "ampe_add_flux_from_antitrapping": (I, [MP, P, P, P, P, D, P, P, P, P]),
     "ampe_rhs_phase_conc": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_efo_rbgs": (I, [MP, P, P, P, D, P, D, P, D, P, P, I, P, P]),

@@ -469,6 +469,46 @@ int ampe_quat_rhs(const ampe_model_t* m, const double* fc0, const double* fc1,
                   const double* fc2, const double* mq, const double* q,
                   double* out, void* stream);
 
+/* Symmetry-aware orientation (cubic symmetry, 3D, qlen 4), the path of
+ * QuatModel::computeSymmetryRotations and makeQuatFundamental
+ * (QuatModel.cc:4978-5105) and of the symmetric differences and side
+ * gradients.  Side arrays (int rotation indices, depth-4 differences and
+ * gradients, component-major) have ghost width m->ng_side >= 1: the
+ * rotations and differences cover the faces of the interior plus one
+ * transverse ghost layer, as the reference's loops do.  Rotation indices
+ * are 1-based into the 48 unit quaternions of quat.f setqr (quat.f:
+ * 165-288), negative for the conjugate.  Products and norms are evaluated
+ * without fused multiply-add, in the reference's order. */
+
+/* The 48 rotations (qr: 48 x 4, w x y z) and each one's conjugate index
+ * (1-based), as the kernels use them (host only). */
+int ampe_quat_symm_table(double* qr, int* conj);
+/* QUAT_SYMM_ROTATION (3d/quatrotation.m4:12-91) with quatfindsymm4
+ * (quat.f:73-163): for every face, the rotation r minimising
+ * |q_lo r / |q_lo r| - q_hi / |q_hi||^2, searched from the index already in
+ * rot (0 or out of range: 1), ending at the first rotation within
+ * (2 sin(pi/16))^2.  rot0..2 in/out. */
+int ampe_quat_symm_rotation(const ampe_model_t* m, const double* q, int* rot0,
+                            int* rot1, int* rot2, void* stream);
+/* QUAT_FUNDAMENTAL (3d/quatrotation.m4:93-147): every interior q replaced
+ * by its rotation closest to the identity (search from rotation 1). */
+int ampe_quat_fundamental(const ampe_model_t* m, double* q, void* stream);
+/* QUATDIFFS_SYMM (3d/quatdiffs.m4:131-219): diff = q_hi - q_lo r(rot) on the
+ * faces of QUAT_SYMM_ROTATION.  An index out of range gives NaN. */
+int ampe_quat_diffs_symm(const ampe_model_t* m, const double* q, const int* rot0,
+                         const int* rot1, const int* rot2, double* diff0,
+                         double* diff1, double* diff2, void* stream);
+/* QUATGRAD_SIDE_SYMM (3d/quatgrad.m4:376-679) on interior faces:
+ * grad_<c>_<d>side, component c of grad q on the faces of normal d. */
+int ampe_quat_grad_side_symm(const ampe_model_t* m, const double* diff0,
+                             const double* diff1, const double* diff2,
+                             const int* rot0, const int* rot1, const int* rot2,
+                             double* grad_x_xside, double* grad_y_xside,
+                             double* grad_z_xside, double* grad_x_yside,
+                             double* grad_y_yside, double* grad_z_yside,
+                             double* grad_x_zside, double* grad_y_zside,
+                             double* grad_z_zside, void* stream);
+
 /* PhaseFACOps::setCOnPatchPrivate (PhaseFACOps.cc:101-183):
  * C = 1 + gamma M_phi w g''(phi) on interior cells (ghost width m->ng). */
 int ampe_phase_fac_set_c(const ampe_model_t* m, const double* phi,

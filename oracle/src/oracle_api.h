@@ -119,6 +119,20 @@ void orc_conc_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* m
                                  double* ds0, double* ds1, double* ds2, double* el0,
                                  double* el1, double* el2, double* es0, double* es1,
                                  double* es2);
+/* symmetry-aware orientation (cubic, qlen 4; side arrays of ghost width m->ng_side) */
+void orc_quat_symm_table(double* qr, int* conj);
+int orc_quat_find_symm(const double* q1, const double* q2, int iq, double* q2p);
+void orc_quat_symm_rotation(const ampe_model_t* m, const double* q, int* rot0, int* rot1,
+                            int* rot2);
+void orc_quat_fundamental(const ampe_model_t* m, double* q);
+void orc_quat_diffs_symm(const ampe_model_t* m, const double* q, const int* rot0,
+                         const int* rot1, const int* rot2, double* diff0, double* diff1,
+                         double* diff2);
+void orc_quat_grad_side_symm(const ampe_model_t* m, const double* diff0, const double* diff1,
+                             const double* diff2, const int* rot0, const int* rot1,
+                             const int* rot2, double* gxx, double* gyx, double* gzx,
+                             double* gxy, double* gyy, double* gzy, double* gxz, double* gyz,
+                             double* gzz);
 /* implicit stepper */
 void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p);
 void orc_stepper_destroy(void* h);

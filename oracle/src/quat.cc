@@ -183,3 +183,270 @@ void orc_quat_project(long ncells, double* q)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Symmetry-aware orientation, cubic symmetry, qlen 4 (quat.f:73-341,
+// 3d/quatrotation.m4:12-147, 3d/quatdiffs.m4:131-219, 3d/quatgrad.m4:
+// 376-679).  Side arrays here carry the ghost width m->ng_side (>= 1).
+// ---------------------------------------------------------------------------
+namespace {
+
+// setqr (quat.f:165-288): the 48 rotations, (w, x, y, z) before quatset's
+// normalisation, and the conjugate table
+const double kQR[48][4] = {
+    {1, 0, 0, 0},   {0, 1, 0, 0},   {0, 0, 1, 0},   {0, 0, 0, 1},   {-1, 0, 0, 0},
+    {0, -1, 0, 0},  {0, 0, -1, 0},  {0, 0, 0, -1},  {1, 1, 0, 0},   {1, 0, 1, 0},
+    {1, 0, 0, 1},   {0, 1, 1, 0},   {0, 1, 0, 1},   {0, 0, 1, 1},   {-1, 1, 0, 0},
+    {-1, 0, 1, 0},  {-1, 0, 0, 1},  {0, -1, 1, 0},  {0, -1, 0, 1},  {0, 0, -1, 1},
+    {1, -1, 0, 0},  {1, 0, -1, 0},  {1, 0, 0, -1},  {0, 1, -1, 0},  {0, 1, 0, -1},
+    {0, 0, 1, -1},  {-1, -1, 0, 0}, {-1, 0, -1, 0}, {-1, 0, 0, -1}, {0, -1, -1, 0},
+    {0, -1, 0, -1}, {0, 0, -1, -1}, {1, 1, 1, 1},   {-1, 1, 1, 1},  {1, -1, 1, 1},
+    {1, 1, -1, 1},  {1, 1, 1, -1},  {-1, -1, 1, 1}, {-1, 1, -1, 1}, {-1, 1, 1, -1},
+    {1, -1, -1, 1}, {1, -1, 1, -1}, {1, 1, -1, -1}, {1, -1, -1, -1}, {-1, 1, -1, -1},
+    {-1, -1, 1, -1}, {-1, -1, -1, 1}, {-1, -1, -1, -1}};
+const int kConj[48] = {1,  6,  7,  8,  5,  2,  3,  4,  21, 22, 23, 30, 31, 32, 27, 28,
+                       29, 24, 25, 26, 9,  10, 11, 18, 19, 20, 15, 16, 17, 12, 13, 14,
+                       44, 48, 43, 42, 41, 45, 46, 47, 37, 36, 35, 33, 38, 39, 40, 34};
+
+void qnorm4(double* q)
+{
+   const double m = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+   double minv = 0.0;
+   if (!(m < 1.e-15)) minv = 1.0 / m;
+   for (int c = 0; c < 4; c++) q[c] = q[c] * minv;
+}
+
+struct Rotations {
+   double qr[48][4];
+   double thr;
+   Rotations()
+   {
+      for (int a = 0; a < 48; a++) {
+         for (int c = 0; c < 4; c++) qr[a][c] = kQR[a][c];
+         qnorm4(qr[a]);
+      }
+      const double pi = std::acos(-1.0);
+      const double t = 2.0 * std::sin(pi / 16.0);
+      thr = t * t;
+   }
+};
+
+const Rotations& rotations()
+{
+   static const Rotations R;
+   return R;
+}
+
+void qmult4(const double* a, const double* b, double* q)
+{
+   q[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+   q[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+   q[2] = a[0] * b[2] + a[2] * b[0] + a[3] * b[1] - a[1] * b[3];
+   q[3] = a[0] * b[3] + a[3] * b[0] + a[1] * b[2] - a[2] * b[1];
+}
+
+double qdiffsq4(const double* q1, const double* q2)
+{
+   double a[4], b[4], d[4];
+   std::memcpy(a, q1, sizeof(a));
+   std::memcpy(b, q2, sizeof(b));
+   qnorm4(a);
+   qnorm4(b);
+   for (int c = 0; c < 4; c++) d[c] = b[c] - a[c];
+   return d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3];
+}
+
+// quatsymmrotate4; false where the reference stops (index out of range)
+bool symm_rotate(const double* q, int iq, double* qp)
+{
+   if (iq == 0 || iq > 48 || iq < -48) return false;
+   if (iq < 0) iq = kConj[-iq - 1];
+   if (iq == 1)
+      std::memcpy(qp, q, 4 * sizeof(double));
+   else
+      qmult4(q, rotations().qr[iq - 1], qp);
+   return true;
+}
+
+// quatfindsymm4
+void find_symm(const double* q1, const double* q2, int& iq, double* q2p)
+{
+   const Rotations& R = rotations();
+   if (iq == 0 || iq > 48 || iq < -48) iq = 1;
+   if (iq < 0) iq = kConj[-iq - 1];
+   if (iq == 1)
+      std::memcpy(q2p, q2, 4 * sizeof(double));
+   else
+      qmult4(q2, R.qr[iq - 1], q2p);
+   double dsq = qdiffsq4(q1, q2p);
+   if (dsq <= R.thr) return;
+   double min_dsq = dsq, min_q[4];
+   int min_iq = iq;
+   std::memcpy(min_q, q2p, sizeof(min_q));
+   for (int nn = 1; nn <= 48; nn++) {
+      if (nn == iq) continue;
+      if (nn == 1)
+         std::memcpy(q2p, q2, 4 * sizeof(double));
+      else
+         qmult4(q2, R.qr[nn - 1], q2p);
+      dsq = qdiffsq4(q1, q2p);
+      if (dsq < min_dsq) {
+         min_dsq = dsq;
+         min_iq = nn;
+         std::memcpy(min_q, q2p, sizeof(min_q));
+      }
+      if (dsq <= R.thr) break;
+   }
+   std::memcpy(q2p, min_q, sizeof(min_q));
+   iq = min_iq;
+}
+
+// SIDE3d<d>(lo, hi, g) layout of the side arrays
+struct SideLayout {
+   int n0, n1, n2, g;
+   long ext(int d, int a) const
+   {
+      const int n = a == 0 ? n0 : (a == 1 ? n1 : n2);
+      return n + 2 * g + (a == d);
+   }
+   long size(int d) const { return ext(d, 0) * ext(d, 1) * ext(d, 2); }
+   long at(int d, int i, int j, int k) const
+   {
+      return ((long)(k + g) * ext(d, 1) + (j + g)) * ext(d, 0) + (i + g);
+   }
+};
+
+}  // namespace
+
+extern "C" {
+
+void orc_quat_symm_table(double* qr, int* conj)
+{
+   for (int a = 0; a < 48; a++) {
+      for (int c = 0; c < 4; c++) qr[4 * a + c] = rotations().qr[a][c];
+      conj[a] = kConj[a];
+   }
+}
+
+// quatfindsymm4 for one pair (iq in/out), for tests of the search itself
+int orc_quat_find_symm(const double* q1, const double* q2, int iq, double* q2p)
+{
+   find_symm(q1, q2, iq, q2p);
+   return iq;
+}
+
+void orc_quat_symm_rotation(const ampe_model_t* m, const double* q, int* rot0, int* rot1,
+                            int* rot2)
+{
+   Layout L(*m);
+   const SideLayout S{L.n0, L.n1, L.n2, m->ng_side};
+   const long qs = L.cells_ghost();
+   int* rot[3] = {rot0, rot1, rot2};
+   for (int d = 0; d < 3; d++) {
+      const int ei = d == 0, ej = d == 1, ek = d == 2;
+      for (int k = -1 + ek; k <= L.n2; k++)
+         for (int j = -1 + ej; j <= L.n1; j++)
+            for (int i = -1 + ei; i <= L.n0; i++) {
+               double q1[4], q2[4], q2p[4];
+               for (int c = 0; c < 4; c++) {
+                  q1[c] = q[c * qs + L.c(i, j, k)];
+                  q2[c] = q[c * qs + L.c(i - ei, j - ej, k - ek)];
+               }
+               int& iq = rot[d][S.at(d, i, j, k)];
+               find_symm(q1, q2, iq, q2p);
+            }
+   }
+}
+
+void orc_quat_fundamental(const ampe_model_t* m, double* q)
+{
+   Layout L(*m);
+   const long qs = L.cells_ghost();
+   double q1[4] = {1.0, 0.0, 0.0, 0.0};
+   qnorm4(q1);
+   for (int k = 0; k < L.n2; k++)
+      for (int j = 0; j < L.n1; j++)
+         for (int i = 0; i < L.n0; i++) {
+            double q2[4], q2p[4];
+            for (int c = 0; c < 4; c++) q2[c] = q[c * qs + L.c(i, j, k)];
+            int iq = 1;
+            find_symm(q1, q2, iq, q2p);
+            for (int c = 0; c < 4; c++) q[c * qs + L.c(i, j, k)] = q2p[c];
+         }
+}
+
+void orc_quat_diffs_symm(const ampe_model_t* m, const double* q, const int* rot0,
+                         const int* rot1, const int* rot2, double* diff0, double* diff1,
+                         double* diff2)
+{
+   Layout L(*m);
+   const SideLayout S{L.n0, L.n1, L.n2, m->ng_side};
+   const long qs = L.cells_ghost();
+   const int* rot[3] = {rot0, rot1, rot2};
+   double* diff[3] = {diff0, diff1, diff2};
+   for (int d = 0; d < 3; d++) {
+      const int ei = d == 0, ej = d == 1, ek = d == 2;
+      const long ss = S.size(d);
+      for (int k = -1 + ek; k <= L.n2; k++)
+         for (int j = -1 + ej; j <= L.n1; j++)
+            for (int i = -1 + ei; i <= L.n0; i++) {
+               double q2[4], q2p[4];
+               for (int c = 0; c < 4; c++) q2[c] = q[c * qs + L.c(i - ei, j - ej, k - ek)];
+               const long f = S.at(d, i, j, k);
+               if (!symm_rotate(q2, rot[d][f], q2p))
+                  for (int c = 0; c < 4; c++) q2p[c] = std::nan("");
+               for (int c = 0; c < 4; c++)
+                  diff[d][c * ss + f] = q[c * qs + L.c(i, j, k)] - q2p[c];
+            }
+   }
+}
+
+void orc_quat_grad_side_symm(const ampe_model_t* m, const double* diff0, const double* diff1,
+                             const double* diff2, const int* rot0, const int* rot1,
+                             const int* rot2, double* gxx, double* gyx, double* gzx,
+                             double* gxy, double* gyy, double* gzy, double* gxz, double* gyz,
+                             double* gzz)
+{
+   Layout L(*m);
+   const SideLayout S{L.n0, L.n1, L.n2, m->ng_side};
+   const double dinv[3] = {1.0 / m->dx[0], 1.0 / m->dx[1], 1.0 / m->dx[2]};
+   const double p25[3] = {0.25 * dinv[0], 0.25 * dinv[1], 0.25 * dinv[2]};
+   const double* diff[3] = {diff0, diff1, diff2};
+   const int* rot[3] = {rot0, rot1, rot2};
+   double* grad[3][3] = {{gxx, gyx, gzx}, {gxy, gyy, gzy}, {gxz, gyz, gzz}};  // [side][comp]
+   for (int d = 0; d < 3; d++) {
+      const int ld[3] = {d == 0, d == 1, d == 2};
+      const long sd = S.size(d);
+      for (int k = 0; k < L.n2 + ld[2]; k++)
+         for (int j = 0; j < L.n1 + ld[1]; j++)
+            for (int i = 0; i < L.n0 + ld[0]; i++) {
+               const long f = S.at(d, i, j, k);
+               for (int c = 0; c < 4; c++) grad[d][d][c * sd + f] = dinv[d] * diff[d][c * sd + f];
+               for (int e = 0; e < 3; e++) {
+                  if (e == d) continue;
+                  const int ue[3] = {e == 0, e == 1, e == 2};
+                  const long se = S.size(e);
+                  // d1 = diff_e at (cell + e), d2 = diff_e at (cell + e - d),
+                  // d3 = diff_e at (cell - d)
+                  const long f1 = S.at(e, i + ue[0], j + ue[1], k + ue[2]);
+                  const long f2 = S.at(e, i + ue[0] - ld[0], j + ue[1] - ld[1], k + ue[2] - ld[2]);
+                  const long f3 = S.at(e, i - ld[0], j - ld[1], k - ld[2]);
+                  const long fo = S.at(e, i, j, k);
+                  double d1[4], d2[4], d1p[4], d2p[4], d4[4], d4p[4];
+                  for (int c = 0; c < 4; c++) {
+                     d1[c] = diff[e][c * se + f1];
+                     d2[c] = diff[e][c * se + f2];
+                  }
+                  bool ok = symm_rotate(d1, -rot[e][f1], d1p);
+                  ok = symm_rotate(d2, -rot[e][f2], d2p) && ok;
+                  for (int c = 0; c < 4; c++) d4[c] = d2p[c] + diff[e][c * se + f3];
+                  ok = symm_rotate(d4, rot[d][f], d4p) && ok;
+                  for (int c = 0; c < 4; c++)
+                     grad[d][e][c * sd + f] =
+                         ok ? p25[e] * (d4p[c] + d1p[c] + diff[e][c * se + fo]) : std::nan("");
+               }
+            }
+   }
+}
+
+}  // extern "C"

@@ -60,6 +60,12 @@ def lib():
             "orc_kim_mobility": (None, [MP, P, P, P, D, D, D, D, P]),
             "orc_phase_diffusion_mobility": (D, [MP, C.POINTER(abi.Mobility), I, D, D]),
             "orc_conc_diffusion_mobility": (None, [MP, C.POINTER(abi.Mobility)] + [P] * 16),
+            "orc_quat_symm_table": (None, [P, P]),
+            "orc_quat_find_symm": (I, [P, P, I, P]),
+            "orc_quat_symm_rotation": (None, [MP, P, P, P, P]),
+            "orc_quat_fundamental": (None, [MP, P]),
+            "orc_quat_diffs_symm": (None, [MP] + [P] * 7),
+            "orc_quat_grad_side_symm": (None, [MP] + [P] * 15),
             "orc_add_flux_from_antitrapping": (None, [MP, P, P, P, P, D, P, P, P]),
             "orc_conc_flux_kks": (None, [MP, P, P, P, P, P, P, P, P, P]),
             "orc_rhs_phase_conc": (None, [MP, P, P, P, P, P, P, P, P]),
