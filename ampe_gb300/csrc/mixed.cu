@@ -477,6 +477,159 @@ __global__ void k_aniso_orientation(Grid g, int qlen4, const double* q, AnisoF a
    }
 }
 
+// ---------------------------------------------------------------------------
+// 3D anisotropic flux (anisotropic_gradient_flux, 3d/quatrhs.m4:180-355,
+// with compute_dgamma, 3d/quatrhs.m4:149-177) in FP32, and its gradient with
+// respect to the face gradient g of phi by forward-mode differentiation:
+// every quantity carries its value and its three partial derivatives.
+//   n = g/|g|, n' = q n q*, n4 = sum n'_i^4,
+//   dg = q* (n'_i (n'_i^2 - n4))_i q,
+//   gamma = eps (1 - 3 e4)(1 + 4 e4/(1 - 3 e4) n4),
+//   F_d = gamma^2 g_d + 16 eps gamma e4 |g| dg_d,
+// q the (unnormalised) face mean of the orientation quaternion; below
+// |g|^2 = 1e-12 the reference's constant dg and n4 = 0 are used.
+// ---------------------------------------------------------------------------
+struct Dual3 {
+   float v, d[3];
+};
+
+__device__ __forceinline__ Dual3 dconst(float v) { return {v, {0.f, 0.f, 0.f}}; }
+__device__ __forceinline__ Dual3 operator+(const Dual3& a, const Dual3& b)
+{
+   return {a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2]}};
+}
+__device__ __forceinline__ Dual3 operator-(const Dual3& a, const Dual3& b)
+{
+   return {a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2]}};
+}
+__device__ __forceinline__ Dual3 operator*(const Dual3& a, const Dual3& b)
+{
+   return {a.v * b.v,
+           {a.d[0] * b.v + a.v * b.d[0], a.d[1] * b.v + a.v * b.d[1],
+            a.d[2] * b.v + a.v * b.d[2]}};
+}
+__device__ __forceinline__ Dual3 operator*(float a, const Dual3& b)
+{
+   return {a * b.v, {a * b.d[0], a * b.d[1], a * b.d[2]}};
+}
+__device__ __forceinline__ Dual3 dsqrt(const Dual3& a)
+{
+   const float r = sqrtf(a.v);
+   const float h = r > 0.f ? 0.5f / r : 0.f;  // zero at a flat face: the term it scales is zero
+   return {r, {h * a.d[0], h * a.d[1], h * a.d[2]}};
+}
+__device__ __forceinline__ Dual3 drcp(const Dual3& a)
+{
+   const float r = 1.f / a.v, r2 = -r * r;
+   return {r, {r2 * a.d[0], r2 * a.d[1], r2 * a.d[2]}};
+}
+
+// quaternion product on Dual3 components (quatmult4 order)
+__device__ __forceinline__ void dqmul(const Dual3* a, const Dual3* b, Dual3* q)
+{
+   q[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+   q[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+   q[2] = a[0] * b[2] + a[2] * b[0] + a[3] * b[1] - a[1] * b[3];
+   q[3] = a[0] * b[3] + a[3] * b[0] + a[1] * b[2] - a[2] * b[1];
+}
+
+// F and dF/dg on face dir from the face gradient gv (values) and the face
+// quaternion qf
+__device__ __forceinline__ Dual3 aniso3d_flux(const MixParams& mp, int dir, const float* gv,
+                                              const float* qf)
+{
+   const float eps = mp.eps, e4 = mp.nu;
+   const float factor = 4.f * e4 / (1.f - 3.f * e4);
+   Dual3 gd[3];
+   for (int a = 0; a < 3; a++) {
+      gd[a] = dconst(gv[a]);
+      gd[a].d[a] = 1.f;
+   }
+   const Dual3 gphi2 = gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2];
+   Dual3 dg[4], n4;
+   if (fabsf(gphi2.v) > 1.e-12f) {
+      const Dual3 nni = drcp(dsqrt(gphi2));
+      const Dual3 n[4] = {dconst(0.f), gd[0] * nni, gd[1] * nni, gd[2] * nni};
+      const Dual3 q[4] = {dconst(qf[0]), dconst(qf[1]), dconst(qf[2]), dconst(qf[3])};
+      const Dual3 qp[4] = {q[0], dconst(-qf[1]), dconst(-qf[2]), dconst(-qf[3])};
+      Dual3 tmp[4], np[4];
+      dqmul(n, qp, tmp);
+      dqmul(q, tmp, np);
+      const Dual3 p1 = np[1] * np[1], p2 = np[2] * np[2], p3 = np[3] * np[3];
+      n4 = p1 * p1 + p2 * p2 + p3 * p3;
+      const Dual3 dd[4] = {dconst(0.f), np[1] * (p1 - n4), np[2] * (p2 - n4),
+                           np[3] * (p3 - n4)};
+      dqmul(dd, q, tmp);
+      dqmul(qp, tmp, dg);
+   } else {
+      dg[0] = dg[1] = dconst(0.f);
+      dg[2] = dconst(dir == 2 ? 1.f : 0.f);
+      dg[3] = dconst(dir == 2 ? 0.f : 1.f);
+      n4 = dconst(0.f);
+   }
+   const Dual3 gamma = (eps * (1.f - 3.f * e4)) * (dconst(1.f) + factor * n4);
+   return gamma * gamma * gd[dir] + (16.f * eps * e4) * (gamma * dsqrt(gphi2) * dg[dir + 1]);
+}
+
+// face gradient of a cell field on face dir whose upper cell is (i, j, k),
+// the stencil of the 3D anisotropic flux; D(a, b) = field(a) - field(b)
+template <class DF>
+__device__ __forceinline__ void aniso3d_face_grad(const MixParams& mp, const Grid& g, int dir,
+                                                  int i, int j, int k, DF D, float* gv)
+{
+   auto C = [&](int a, int b, int c) { return g.c(a, b, c); };
+   if (dir == 0) {
+      gv[0] = D(C(i, j, k), C(i - 1, j, k)) * mp.dxi[0];
+      gv[1] = 0.25f * (D(C(i - 1, j + 1, k), C(i - 1, j - 1, k)) +
+                       D(C(i, j + 1, k), C(i, j - 1, k))) * mp.dxi[1];
+      gv[2] = 0.25f * (D(C(i - 1, j, k + 1), C(i - 1, j, k - 1)) +
+                       D(C(i, j, k + 1), C(i, j, k - 1))) * mp.dxi[2];
+   } else if (dir == 1) {
+      gv[0] = 0.25f * (D(C(i + 1, j - 1, k), C(i - 1, j - 1, k)) +
+                       D(C(i + 1, j, k), C(i - 1, j, k))) * mp.dxi[0];
+      gv[1] = D(C(i, j, k), C(i, j - 1, k)) * mp.dxi[1];
+      gv[2] = 0.25f * (D(C(i, j - 1, k + 1), C(i, j - 1, k - 1)) +
+                       D(C(i, j, k + 1), C(i, j, k - 1))) * mp.dxi[2];
+   } else {
+      gv[0] = 0.25f * (D(C(i + 1, j, k - 1), C(i - 1, j, k - 1)) +
+                       D(C(i + 1, j, k), C(i - 1, j, k))) * mp.dxi[0];
+      gv[1] = 0.25f * (D(C(i, j + 1, k - 1), C(i, j - 1, k - 1)) +
+                       D(C(i, j + 1, k), C(i, j - 1, k))) * mp.dxi[1];
+      gv[2] = D(C(i, j, k), C(i, j, k - 1)) * mp.dxi[2];
+   }
+}
+
+__device__ __forceinline__ long long face_index(const Grid& g, int dir, int i, int j, int k)
+{
+   return dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));
+}
+
+__global__ void k_aniso3d_faces_f32(MixParams mp, Grid g, const double* ph, const double* q,
+                                    AnisoF a)
+{
+   const long long tot = g.nfx() + g.nfy() + g.nfz();
+   const long long qs = g.cells_ghost();
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+        t += (long long)gridDim.x * blockDim.x) {
+      int dir, i, j, k;
+      face_of(g, t, dir, i, j, k);
+      float gv[3];
+      // neighbour differences of the FP64 phase, rounded once
+      aniso3d_face_grad(mp, g, dir, i, j, k,
+                        [&](long long u, long long l) { return d2f(ph[u] - ph[l]); }, gv);
+      const int ei = dir == 0, ej = dir == 1, ek = dir == 2;
+      const long long lo = g.c(i - ei, j - ej, k - ek), up = g.c(i, j, k);
+      float qf[4];
+      for (int c = 0; c < 4; c++) qf[c] = d2f(0.5 * (q[c * qs + lo] + q[c * qs + up]));
+      const Dual3 F = aniso3d_flux(mp, dir, gv, qf);
+      const long long f = face_index(g, dir, i, j, k);
+      a.F[dir][f] = F.v;
+      a.JA[dir][f] = F.d[0];
+      a.JB[dir][f] = F.d[1];
+      a.JC[dir][f] = F.d[2];
+   }
+}
+
 int aniso_orientation_f32(const ampe_model_t& m, const Grid& g, const double* q,
                           AnisoF& a, cudaStream_t s)
 {
@@ -491,11 +644,26 @@ int aniso_faces_f32(const ampe_model_t& m, const MixParams& mp, const Grid& g,
                     const double* ph, const double* q, AnisoF& a, cudaStream_t s)
 {
    (void)m;
-   const long long tot = g.nfx() + g.nfy();
+   const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    long long b = (tot + 255) / 256;
    if (b > max_blocks()) b = max_blocks();
-   k_aniso_faces_f32<<<(unsigned)b, 256, 0, s>>>(mp, g, ph, q, a);
+   if (g.dim == 3)
+      k_aniso3d_faces_f32<<<(unsigned)b, 256, 0, s>>>(mp, g, ph, q, a);
+   else
+      k_aniso_faces_f32<<<(unsigned)b, 256, 0, s>>>(mp, g, ph, q, a);
    return launch_status();
+}
+
+// linearised 3D anisotropic flux on face d whose upper cell is (i, j, k)
+__device__ __forceinline__ float aniso3d_dflux(const MixParams& mp, const AnisoF& a, int d,
+                                               const float* dp, const Grid& g, int i, int j,
+                                               int k)
+{
+   float gv[3];
+   aniso3d_face_grad(mp, g, d, i, j, k, [&](long long u, long long l) { return dp[u] - dp[l]; },
+                     gv);
+   const long long f = face_index(g, d, i, j, k);
+   return a.JA[d][f] * gv[0] + a.JB[d][f] * gv[1] + a.JC[d][f] * gv[2];
 }
 
 // linearised anisotropic flux on face d whose upper cell is (i, j): the face
@@ -675,9 +843,9 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an, Fac
       for (int d = 0; d < DIM; d++) {
          const int ei = d == 0, ej = d == 1, ek = d == 2;
          float fm, fp;
-         if (ANISO) {  // 2D: precomputed face fluxes
-            fm = d == 0 ? an.F[0][g.fx(i, j, 0)] : an.F[1][g.fy(i, j, 0)];
-            fp = d == 0 ? an.F[0][g.fx(i + 1, j, 0)] : an.F[1][g.fy(i, j + 1, 0)];
+         if (ANISO) {  // precomputed face fluxes
+            fm = an.F[d][face_index(g, d, i, j, k)];
+            fp = an.F[d][face_index(g, d, i + ei, j + ej, k + ek)];
          } else {
             fm = face_flux_lin64<DIM>(mp, d, ph, g, i, j, k);
             fp = face_flux_lin64<DIM>(mp, d, ph, g, i + ei, j + ej, k + ek);
@@ -780,14 +948,23 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    if (b > max_blocks()) b = max_blocks();
    const bool aniso = m.flux_type == AMPE_FLUX_ANISOTROPIC;
    if (aniso) {
-      if (g.dim != 2 || !q || !an) return AMPE_ERR_INVALID;
+      if (!q || !an) return AMPE_ERR_INVALID;
       aniso_faces_f32(m, mp, g, phi, q, *an, s);
    }
    const AnisoF a0 = an ? *an : AnisoF();
 #define AMPE_RHS(D, P)                                                                      \
    k_rhs_mixed<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tfield, phi, cc, pf, \
                                                         cl, cs, dF, ogm, phi_rhs, conc_rhs)
-   if (aniso) {
+   if (aniso && g.dim == 3) {
+      if (mp.pb)
+         k_rhs_mixed<3, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tfield, phi,
+                                                               cc, pf, cl, cs, dF, ogm,
+                                                               phi_rhs, conc_rhs);
+      else
+         k_rhs_mixed<3, false, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tfield, phi,
+                                                                cc, pf, cl, cs, dF, ogm,
+                                                                phi_rhs, conc_rhs);
+   } else if (aniso) {
       if (mp.pb)
          k_rhs_mixed<2, true, true><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tfield, phi,
                                                                cc, pf, cl, cs, dF, ogm,
@@ -917,7 +1094,10 @@ __global__ void k_jv_stencil(ampe_model_t m, MixParams mp, Grid g, AnisoF an, Fa
       for (int d = 0; d < DIM; d++) {
          const int ei = d == 0, ej = d == 1, ek = d == 2;
          float fm, fp;
-         if (ANISO) {  // linearised 2D anisotropic flux on the two faces
+         if (ANISO && DIM == 3) {  // linearised anisotropic flux on the two faces
+            fm = aniso3d_dflux(mp, an, d, dphi, g, i, j, k);
+            fp = aniso3d_dflux(mp, an, d, dphi, g, i + ei, j + ej, k + ek);
+         } else if (ANISO) {
             fm = aniso_dflux(mp, an, d, dphi, g, i, j);
             fp = aniso_dflux(mp, an, d, dphi, g, i + ei, j + ej);
          } else {
@@ -1128,8 +1308,18 @@ int jv_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
    k_jv_stencil<D, P, false><<<(unsigned)b, 256, 0, s>>>(m, mp, g, a0, fw, tabf, tfield, pf, cl, cs, \
                                                          dF, dphi, da, db, dcv, v, ogm,          \
                                                          (float)gamma, out)
-   if (m.flux_type == AMPE_FLUX_ANISOTROPIC) {
-      if (g.dim != 2 || !an) return AMPE_ERR_INVALID;
+   if (m.flux_type == AMPE_FLUX_ANISOTROPIC && g.dim == 3) {
+      if (!an) return AMPE_ERR_INVALID;
+      if (mp.pb)
+         k_jv_stencil<3, true, true><<<(unsigned)b, 256, 0, s>>>(
+             m, mp, g, a0, fw, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm,
+             (float)gamma, out);
+      else
+         k_jv_stencil<3, false, true><<<(unsigned)b, 256, 0, s>>>(
+             m, mp, g, a0, fw, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm,
+             (float)gamma, out);
+   } else if (m.flux_type == AMPE_FLUX_ANISOTROPIC) {
+      if (!an) return AMPE_ERR_INVALID;
       if (mp.pb)
          k_jv_stencil<2, true, true><<<(unsigned)b, 256, 0, s>>>(
              m, mp, g, a0, fw, tabf, tfield, pf, cl, cs, dF, dphi, da, db, dcv, v, ogm,

@@ -50,11 +50,15 @@ struct FaceW {
 // 2D anisotropic phase flux per face and its Jacobian with respect to the
 // face gradient (dphi/dx, dphi/dy): F[d], JA[d] = dF/d(dphi/dx),
 // JB[d] = dF/d(dphi/dy) for x (d = 0) and y (d = 1) faces
+// anisotropic phase flux per face (normal d) at the last f evaluation and
+// its derivatives with respect to the face gradient of phi: JA = dF/dgx,
+// JB = dF/dgy, JC = dF/dgz (3D)
 struct AnisoF {
-   float* F[2] = {nullptr, nullptr};
-   float* JA[2] = {nullptr, nullptr};
-   float* JB[2] = {nullptr, nullptr};
-   float* PO[2] = {nullptr, nullptr};  // orientation angle phi_o per face
+   float* F[3] = {nullptr, nullptr, nullptr};
+   float* JA[3] = {nullptr, nullptr, nullptr};
+   float* JB[3] = {nullptr, nullptr, nullptr};
+   float* JC[3] = {nullptr, nullptr, nullptr};
+   float* PO[2] = {nullptr, nullptr};  // 2D: orientation angle phi_o per face
 };
 // phi_o = acos(qbar) (2 acos for four-component q) per face, in FP64, once
 // per orientation field: acos is ill-conditioned at qbar ~ +-1, where an

@@ -1447,8 +1447,9 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC) {
       if (m->qlen != 2 && m->qlen != 4) return AMPE_ERR_INVALID;
       if (m->evolve_quat && m->qlen != 4) return AMPE_ERR_INVALID;
-      // the mixed path linearises the 2D anisotropic flux only
-      if (p->precision == 1 && (m->dim != 2 || m->evolve_quat)) return AMPE_ERR_INVALID;
+      // the mixed path linearises the anisotropic flux for a static
+      // orientation field (no evolve_quat)
+      if (p->precision == 1 && m->evolve_quat) return AMPE_ERR_INVALID;
    }
    if (m->evolve_quat && (m->quat_mobility_type != 'p' || !(m->quat_grad_floor > 0.0)))
       return AMPE_ERR_INVALID;
@@ -1495,12 +1496,15 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC && !m->evolve_quat) {
       S->qorient = dvec(*S, (long long)m->qlen * S->NG, &err);
       if (p->precision == 1) {
-         for (int d = 0; d < 2; d++) {
-            const long long nf = d == 0 ? S->g.nfx() : S->g.nfy();
+         for (int d = 0; d < m->dim; d++) {
+            const long long nf = d == 0 ? S->g.nfx() : (d == 1 ? S->g.nfy() : S->g.nfz());
             S->an.F[d] = (float*)dalloc<float>(S->pool, nf, &err);
             S->an.JA[d] = (float*)dalloc<float>(S->pool, nf, &err);
             S->an.JB[d] = (float*)dalloc<float>(S->pool, nf, &err);
-            S->an.PO[d] = (float*)dalloc<float>(S->pool, nf, &err);
+            if (m->dim == 3)
+               S->an.JC[d] = (float*)dalloc<float>(S->pool, nf, &err);
+            else
+               S->an.PO[d] = (float*)dalloc<float>(S->pool, nf, &err);
          }
       }
    }

@@ -7,7 +7,12 @@ product (linearised anisotropic flux) within 1e-3 of the oracle's FP64
 finite-difference product where the flux is differentiable at the FD scale
 (interface region), within 5e-2 on the whole level, composition rows within
 1e-5 of the oracle's analytic product; mixed steps within 2e-6 of the FP64
-oracle."""
+oracle.  3D cubic anisotropy (anisotropic_gradient_flux, 3d/quatrhs.m4:
+180-355) with a static two-grain orientation field: FP64 steps as above,
+the mixed path (FP32 flux, Jacobian by forward-mode differentiation) within
+2e-6 of the oracle and its phase-row product within 1e-3 of the FD product
+around the interfaces; an evolving orientation is refused by the mixed
+path."""
 import numpy as np
 import pytest
 
@@ -126,12 +131,94 @@ def test_mixed_steps(cuda):
     assert max(errs) <= 2e-6
 
 
-def test_mixed_3d_aniso_rejected(cuda):
+def case3d(n=20):
+    """3D CALPHAD with the cubic anisotropic flux (eps4 = 0.05), two seeds and
+    a static orientation field of two grains split along x."""
+    from ampe_gb300 import abi
+
+    m = configs.calphad3d(n, seed=3, T_run=1500.0)
+    m.flux_type = abi.FLUX_ANISOTROPIC
+    m.qlen = 4
+    m.aniso_eps = 0.05
+    phi, c = initial.calphad3d_state(n, seed=2, nseeds=2, radius=5.0)
+    rng = np.random.default_rng(13)
+    qa = rng.standard_normal(4)
+    qb = rng.standard_normal(4)
+    qa /= np.linalg.norm(qa)
+    qb /= np.linalg.norm(qb)
+    x = np.arange(n)
+    q = np.where((x < n // 2)[None, None, None, :], qa[:, None, None, None],
+                 qb[:, None, None, None]) * np.ones((4, n, n, n))
+    return m, phi, c, np.ascontiguousarray(q)
+
+
+def test_fp64_steps_3d(cuda):
+    m, phi, c, q = case3d()
+    p = configs.step_params(dt=0.1, precond=2, mg_levels=3, atol=1e-6)
+    o = O.OracleStepper(m, p)
+    o.set_state(phi, c)
+    o.set_orientation(q)
+    rc, so = o.advance(3)
+    assert rc == 0
+    g = ImplicitStepper(m, p)
+    g.set_state(phi, c)
+    g.set_orientation(q)
+    sg = g.advance(3)
+    for k in ("steps", "newton_iters", "gmres_iters", "rhs_evals", "precond_solves"):
+        assert sg[k] == so[k], (k, sg[k], so[k])
+    for a, b in zip(g.get_state(), o.get_state()):
+        assert O.rel_l2(a, b) <= 1e-10
+
+
+def test_mixed_3d_steps_and_jv(cuda):
+    """The mixed path with the FP32 3D anisotropic flux and its forward-mode
+    Jacobian: steps within 2e-6 of the FP64 oracle; the Jacobian-vector
+    product's phase rows within 1e-3 of the oracle's FP64 finite-difference
+    product around the interfaces."""
+    m, phi, c, q = case3d()
+    p64 = configs.step_params(dt=0.1, precond=2, mg_levels=3, atol=1e-6)
+    o = O.OracleStepper(m, p64)
+    o.set_state(phi, c)
+    o.set_orientation(q)
+    rc, so = o.advance(4)
+    assert rc == 0
+    pm = configs.step_params(dt=0.1, precond=2, mg_levels=3, atol=1e-6, precision=1)
+    g = ImplicitStepper(m, pm)
+    g.set_state(phi, c)
+    g.set_orientation(q)
+    sg = g.advance(4)
+    assert sg["steps"] == 4 and sg["kks_fail"] == 0
+    errs = [O.rel_l2(a, b) for a, b in zip(g.get_state()[:2], o.get_state()[:2])]
+    print("mixed 3D aniso vs FP64 oracle rel L2 (phi, c):", errs, sg)
+    assert max(errs) <= 2e-6
+    ph, cc, cl, cs = o.get_state()
+    o.set_state(ph, cc, cl, cs)
+    o.set_orientation(q)
+    g.set_state(ph, cc, cl, cs)
+    v = np.random.default_rng(22).standard_normal(2 * m.cells()) * 1e-3
+    fd = o.jv(v, 0.1, 0)
+    an = g.jv(v, 0.1)
+    N = m.cells()
+    p3 = ph
+    gr = np.sqrt(sum((0.5 * (np.roll(p3, -1, a) - np.roll(p3, 1, a))) ** 2 for a in range(3)))
+    lo = gr.copy()
+    for a in range(3):
+        for sh in (-1, 1):
+            lo = np.minimum(lo, np.roll(gr, sh, a))
+    mask = (lo > 1e-3).ravel()
+    assert mask.sum() > 100
+    err_if = O.rel_l2(an[:N][mask] - v[:N][mask], fd[:N][mask] - v[:N][mask])
+    print("3D aniso Jv phase rows, interface: %.2e" % err_if)
+    assert err_if <= 1e-3
+
+
+def test_mixed_aniso_evolving_orientation_rejected(cuda):
     m = configs.calphad3d(16, seed=3, T_run=1500.0)
     from ampe_gb300 import abi
     m.flux_type = abi.FLUX_ANISOTROPIC
     m.qlen = 4
     m.aniso_eps = 0.05
+    m.evolve_quat = 1
     from ampe_gb300._native import AmpeError
     with pytest.raises(AmpeError):
         ImplicitStepper(m, configs.step_params(precision=1))
