@@ -41,6 +41,11 @@ _PROTOS = {
     "ampe_add_flux_from_grad_t": (I, [MP, P, P, P, P, P, P, P, P]),
     "ampe_kim_mobility": (I, [MP, P, P, P, D, D, D, P, P]),
     "ampe_conc_diffusion_mobility": (I, [MP, MOB] + [P] * 17),
+    "ampe_fac2_work_doubles": (C.c_longlong, [C.POINTER(abi.Fac2)]),
+    "ampe_fac2_composite_residual": (I, [C.POINTER(abi.Fac2), C.POINTER(abi.Fac2Level),
+                                         C.POINTER(abi.Fac2Level)] + [P] * 8 + [P, P]),
+    "ampe_fac2_solve": (I, [C.POINTER(abi.Fac2), C.POINTER(abi.Fac2Level),
+                            C.POINTER(abi.Fac2Level), P, P, P, P, I, D, P, P, P]),
     "ampe_quat_symm_table": (I, [P, P]),
     "ampe_quat_symm_rotation": (I, [MP, P, P, P, P, P]),
     "ampe_quat_fundamental": (I, [MP, P, P]),

@@ -117,6 +117,32 @@ class Model(C.Structure):
         return s
 
 
+class Fac2(C.Structure):
+    """ampe_fac2_t: a periodic coarse level and one fine box refined by 2."""
+
+    _fields_ = [("coarse", Model), ("lo", C.c_int * 3), ("nbox", C.c_int * 3),
+                ("ng_fine", C.c_int), ("level_dx", C.c_int), ("presweeps", C.c_int),
+                ("postsweeps", C.c_int), ("coarse_sweeps", C.c_int),
+                ("d_const", C.c_double), ("c_const", C.c_double), ("m_const", C.c_double)]
+
+    def fine_model(self):
+        """The fine level as a Model: n = 2 nbox, dx / 2, ng = ng_fine."""
+        f = Model.from_buffer_copy(self.coarse)
+        for d in range(3):
+            f.n[d] = 2 * self.nbox[d]
+            f.dx[d] = 0.5 * self.coarse.dx[d]
+        f.ng = self.ng_fine
+        f.ng_side = 0
+        return f
+
+
+class Fac2Level(C.Structure):
+    """ampe_fac2_level_t: face D (3), cell C and M of one level (NULL:
+    the constants of ampe_fac2_t)."""
+
+    _fields_ = [("D", C.c_void_p * 3), ("C", C.c_void_p), ("M", C.c_void_p)]
+
+
 class StepParams(C.Structure):
     """ampe_step_params_t."""
 

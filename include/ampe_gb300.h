@@ -440,6 +440,68 @@ int ampe_efo_residual_rms_noalloc(const ampe_model_t* m, const double* dface0,
                                   const double* u, double* rms, void* stream);
 
 /* ---------------------------------------------------------------------
+ * Two-level composite FAC (AMR): a periodic coarse level and one fine box
+ * refined by 2 in every direction, for  A u = M div(D grad u) - C u = f
+ * (EllipticFACOps with FACPreconditioner's default recursive cycle,
+ * samrai/FACPreconditioner.cc:267-464, EllipticFACOps.cc:948-1758 and
+ * 1947-2029; ellipticfacops.m4 efo_compfluxvardc3d, efo_compresvarsca3d,
+ * efo_rbgswithfluxmax*, efo_ewingfixfluxvardc3d):
+ *   - fine ghost cells from the coarse level by constant refinement, the
+ *     coarse-fine face fluxes by Ewing's correction (weights 2/3 and 1/3
+ *     with the reference's single-precision 1/3);
+ *   - coarse faces on the fine box's boundary take the mean of the four
+ *     fine face fluxes, coarse cells under the box the mean of the fine
+ *     solution / residual (volume-weighted averages);
+ *   - a cycle: presweeps red-black sweeps on the fine level (flux form),
+ *     the fine residual restricted into the coarse right-hand side,
+ *     coarse_sweeps sweeps on the coarse level, the coarse error prolonged
+ *     (constant) and added, postsweeps fine sweeps;
+ *   - the norm: RMS of the composite residual weighted by cell volume,
+ *     coarse cells under the box weight 0.
+ * The reference computes face fluxes and the Ewing correction with the
+ * level-0 spacing on every level (EllipticFACOps.cc:1253,1961: the grid
+ * geometry's dx) and the divergence and smoother with the level's own
+ * spacing; level_dx = 0 reproduces that, level_dx = 1 uses each level's own
+ * spacing throughout (the consistent operator).
+ * Arrays (device): coarse cells ghosted with coarse.ng, fine cells with
+ * ng_fine, face coefficients ghost-free (D0, D1, D2 per level; NULL:
+ * d_const); C and M cell arrays or NULL (c_const, m_const).  3D only. */
+typedef struct ampe_fac2 {
+   ampe_model_t coarse; /* dim 3, n, ng >= 1, dx */
+   int lo[3];           /* fine box lower corner (coarse cells) */
+   int nbox[3];         /* fine box size in coarse cells (>= 2 each) */
+   int ng_fine;         /* ghost width of fine cell arrays (>= 1) */
+   int level_dx;        /* 0: reference spacing rule, 1: per-level spacing */
+   int presweeps, postsweeps, coarse_sweeps;
+   double d_const, c_const, m_const;
+} ampe_fac2_t;
+
+typedef struct ampe_fac2_level {
+   const double* D[3]; /* face coefficients (NULL: d_const) */
+   const double* C;    /* cell (NULL: c_const) */
+   const double* M;    /* cell (NULL: m_const) */
+} ampe_fac2_level_t;
+
+/* doubles of workspace ampe_fac2_solve and ampe_fac2_composite_residual
+ * need */
+long long ampe_fac2_work_doubles(const ampe_fac2_t* p);
+/* composite residual r = f - A u on both levels (computeFullCompositeResidual,
+ * FACPreconditioner.cc:661-683): also restricts u_f into the coarse cells
+ * under the box.  norm (host, may be NULL): the weighted RMS. */
+int ampe_fac2_composite_residual(const ampe_fac2_t* p, const ampe_fac2_level_t* coarse,
+                                 const ampe_fac2_level_t* fine, const double* fc,
+                                 const double* ff, double* uc, double* uf, double* rc,
+                                 double* rf, double* work, double* norm, void* stream);
+/* FAC iterations (solveSystem, FACPreconditioner.cc:267-420): at most
+ * max_cycles, stopping once the norm is <= tol.  norms (host, max_cycles+1
+ * entries): the norm before the first cycle and after each one.  Returns
+ * the number of cycles taken (>= 0) or an AMPE_ERR_*. */
+int ampe_fac2_solve(const ampe_fac2_t* p, const ampe_fac2_level_t* coarse,
+                    const ampe_fac2_level_t* fine, const double* fc, const double* ff,
+                    double* uc, double* uf, int max_cycles, double tol, double* work,
+                    double* norms, void* stream);
+
+/* ---------------------------------------------------------------------
  * Quaternion orientation kernels (evolve_quat models).  q is 4 ghosted
  * cell fields back to back (CellData depth 4), ghosts filled.
  * ------------------------------------------------------------------- */

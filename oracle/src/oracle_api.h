@@ -133,6 +133,15 @@ void orc_quat_grad_side_symm(const ampe_model_t* m, const double* diff0, const d
                              const int* rot2, double* gxx, double* gyx, double* gzx,
                              double* gxy, double* gyy, double* gzy, double* gxz, double* gyz,
                              double* gzz);
+/* two-level composite FAC */
+long long orc_fac2_work_doubles(const ampe_fac2_t* p);
+double orc_fac2_composite_residual(const ampe_fac2_t* p, const ampe_fac2_level_t* lc,
+                                   const ampe_fac2_level_t* lf, const double* fc,
+                                   const double* ff, double* uc, double* uf, double* rc,
+                                   double* rf);
+int orc_fac2_solve(const ampe_fac2_t* p, const ampe_fac2_level_t* lc,
+                   const ampe_fac2_level_t* lf, const double* fc, const double* ff,
+                   double* uc, double* uf, int max_cycles, double tol, double* norms);
 /* implicit stepper */
 void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p);
 void orc_stepper_destroy(void* h);

@@ -107,7 +107,7 @@ def test_version_string():
     assert b"sm_103a" in _native.lib.ampe_version()
 
 
-@pytest.mark.parametrize("case", ["krylov", "precision", "aniso3d_mixed", "aniso_qlen",
+@pytest.mark.parametrize("case", ["krylov", "precision", "aniso_evolving_mixed", "aniso_qlen",
                                   "quat_qlen", "quat_mobility", "precond"])
 def test_stepper_rejects_unsupported_combinations(case):
     """ampe_stepper_create validates the model and the parameters on the
@@ -121,10 +121,10 @@ def test_stepper_rejects_unsupported_combinations(case):
         p.max_krylov = 17  # the Krylov basis is sized for at most 16
     elif case == "precision":
         p.precision = 2
-    elif case == "aniso3d_mixed":
-        m = configs.calphad3d(8)
+    elif case == "aniso_evolving_mixed":
+        m = configs.polycrystal3d(8)
         m.flux_type, m.qlen = abi.FLUX_ANISOTROPIC, 4
-        p.precision = 1  # the mixed path linearises the 2D anisotropic flux only
+        p.precision = 1  # the mixed path linearises the flux for a static orientation only
     elif case == "aniso_qlen":
         m.flux_type, m.qlen = abi.FLUX_ANISOTROPIC, 3
     elif case == "quat_qlen":
