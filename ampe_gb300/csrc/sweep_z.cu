@@ -87,7 +87,7 @@ struct Coef {
 // post-smoothing sweep with the prolongation fused in).  blockDim.x = n0
 // (<= 256).
 template <class R, bool HD, bool HC, bool HM, int MODE, int TY>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2)
     k_sweep_z(FacOp<R> op, Grid g, int kz, const R* __restrict__ f,
               const R* __restrict__ uin, R* __restrict__ uout, Grid gc,
               const R* __restrict__ e)
@@ -97,6 +97,18 @@ __global__ void __launch_bounds__(256, 2)
    // software-pipelined coefficient loads where they fit the registers (the
    // phase operator: f and C per cell)
    constexpr bool PIPE = !HD;
+   // FP32 (the mixed path's preconditioner): the update in its Jacobi form
+   // with an approximate reciprocal; FP64 keeps the colour kernel's
+   // expression order and rounding
+   constexpr bool FAST = sizeof(R) == 4;
+   float w2[3] = {0.f, 0.f, 0.f}, dsum_c = 0.f;
+   if constexpr (FAST) {
+      for (int d = 0; d < 3; d++) w2[d] = (float)op.dxi[d] * (float)op.dxi[d];
+      if constexpr (!HD) {
+         for (int d = 0; d < 3; d++) w2[d] *= (float)op.dc;
+         dsum_c = 2.f * (w2[0] + w2[1] + w2[2]);
+      }
+   }
    extern __shared__ __align__(16) unsigned char zsm[];
    R* const S = reinterpret_cast<R*>(zsm);
    const int n0 = g.n0, x = threadIdx.x;
@@ -163,6 +175,29 @@ __global__ void __launch_bounds__(256, 2)
       const R uxm = P[o + xm], uxp = P[o + xp];
       const R uym = P[o - n0 + x], uyp = P[o + n0 + x];
       const R uzm = Pm[o + x], uzp = Pp[o + x];
+      if constexpr (FAST) {
+         // u <- (M nb - f) / (M dsum - C): the same update, with
+         // nb = sum_d dxi_d^2 (D- u- + D+ u+), dsum = sum_d dxi_d^2 (D- + D+)
+         (void)uc;
+         float nb, dsum;
+         if constexpr (HD) {
+            nb = w2[0] * (cf.d[0] * uxm + cf.d[1] * uxp);
+            nb = fmaf(w2[1], cf.d[2] * uym + cf.d[3] * uyp, nb);
+            nb = fmaf(w2[2], cf.d[4] * uzm + cf.d[5] * uzp, nb);
+            dsum = w2[0] * (cf.d[0] + cf.d[1]);
+            dsum = fmaf(w2[1], cf.d[2] + cf.d[3], dsum);
+            dsum = fmaf(w2[2], cf.d[4] + cf.d[5], dsum);
+         } else {
+            nb = w2[0] * (uxm + uxp);
+            nb = fmaf(w2[1], uym + uyp, nb);
+            nb = fmaf(w2[2], uzm + uzp, nb);
+            dsum = dsum_c;
+         }
+         const float M = HM ? cf.m : op.mc;
+         const float C = HC ? cf.c : op.cc;
+         P[o + x] = __fdividef(fmaf(M, nb, -cf.f), fmaf(M, dsum, -C));
+         return;
+      }
       // expression order of op_residual_u (the colour kernel's)
       R div = R(0), dsum = R(0);
       {
@@ -234,12 +269,14 @@ __global__ void __launch_bounds__(256, 2)
    // during step w-1) and those of step w+1 are gathered into nxt before
    // this step's last barrier, so their loads overlap the store and the next
    // step's wait
+   // Two barriers per step.  The first makes plane w+1 (every thread's
+   // copies) and the previous step's black updates visible; only then is
+   // plane w+2+kZPrefetch-1 issued, into the slot of plane w-3, which the
+   // previous step's black updates were the last to read.  The second
+   // orders the red updates of plane w before the black ones of plane w-1.
+   // Each thread updates and stores only its own column, so the store of
+   // plane w-1 needs no barrier.
    auto step = [&](int w, Coef<R>* cr, Coef<R>* cb, Coef<R>* nr, Coef<R>* nb) {
-      const int want = min(w + 1 + kZPrefetch, k1 + 1);
-      for (; next <= want; next++) {
-         load_plane(next);
-         cp_commit();
-      }
       // plane w+1 and all older ones have landed (this thread's copies)
       cp_wait(next - (w + 2));
       if (MODE == 2) {
@@ -252,6 +289,11 @@ __global__ void __launch_bounds__(256, 2)
       }
       if (!PIPE) gather_step(w, cr, cb);
       __syncthreads();
+      const int want = min(w + 1 + kZPrefetch, k1 + 1);
+      for (; next <= want; next++) {
+         load_plane(next);
+         cp_commit();
+      }
       const int pr = par_of(w, 0, 1);
 #pragma unroll
       for (int m = 0; m < NRED; m++) update(w, 1 + 2 * m + pr, cr[m]);
@@ -262,11 +304,13 @@ __global__ void __launch_bounds__(256, 2)
          for (int m = 0; m < NBLACK; m++) update(w - 1, 2 + 2 * m + pb, cb[m]);
       }
       if (PIPE && w < k1) gather_step(w + 1, nr, nb);
-      if (w > k0) {
-         __syncthreads();
-         store(w - 1);
-      }
+      if (w > k0) store(w - 1);
    };
+   // prologue: the planes the first step reads (k0-2 .. k0) and one ahead
+   for (; next <= min(k0 + 1, k1 + 1); next++) {
+      load_plane(next);
+      cp_commit();
+   }
    if constexpr (PIPE) {
       Coef<R> ar[NRED], ab[NBLACK], br[NRED], bb[NBLACK];
       gather_step(k0 - 1, ar, ab);
