@@ -43,7 +43,7 @@ _PROTOS = {
     "ampe_conc_diffusion_mobility": (I, [MP, MOB] + [P] * 17),
     "ampe_fac2_work_doubles": (C.c_longlong, [C.POINTER(abi.Fac2)]),
     "ampe_fac2_composite_residual": (I, [C.POINTER(abi.Fac2), C.POINTER(abi.Fac2Level),
-                                         C.POINTER(abi.Fac2Level)] + [P] * 8 + [P, P]),
+                                         C.POINTER(abi.Fac2Level)] + [P] * 9),
     "ampe_fac2_solve": (I, [C.POINTER(abi.Fac2), C.POINTER(abi.Fac2Level),
                             C.POINTER(abi.Fac2Level), P, P, P, P, I, D, P, P, P]),
     "ampe_quat_symm_table": (I, [P, P]),

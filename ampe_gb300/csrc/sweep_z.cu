@@ -87,7 +87,7 @@ struct Coef {
 // post-smoothing sweep with the prolongation fused in).  blockDim.x = n0
 // (<= 256).
 template <class R, bool HD, bool HC, bool HM, int MODE, int TY>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
     k_sweep_z(FacOp<R> op, Grid g, int kz, const R* __restrict__ f,
               const R* __restrict__ uin, R* __restrict__ uout, Grid gc,
               const R* __restrict__ e)
@@ -98,8 +98,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2)
    // phase operator: f and C per cell)
    constexpr bool PIPE = !HD;
    // FP32 (the mixed path's preconditioner): the update in its Jacobi form
-   // with an approximate reciprocal; FP64 keeps the colour kernel's
-   // expression order and rounding
+   // with an approximate reciprocal, three blocks per SM for the cell-C
+   // operator (the face-D operators keep two: their coefficients need the
+   // registers); FP64 keeps the colour kernel's expression order and rounding
    constexpr bool FAST = sizeof(R) == 4;
    float w2[3] = {0.f, 0.f, 0.f}, dsum_c = 0.f;
    if constexpr (FAST) {
