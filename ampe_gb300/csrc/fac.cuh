@@ -62,13 +62,16 @@ int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
 // planes, u staged in a ring of kZRingPlanes shared-memory planes of
 // (ty + 4) rows of hs (= n0) elements.
 constexpr int kZRingPlanes = 6;
+constexpr int kZRowStride = 256;  // ring row stride (n0 <= 256)
 struct ZShape {
    int ty = 0, kz = 0, nh = 0, hs = 0;
 };
 template <class R>
 inline size_t zsweep_smem_bytes(const ZShape& z)
 {
-   return sizeof(R) * (size_t)kZRingPlanes * (size_t)(z.ty + 4) * (size_t)z.hs;
+   // the ring, then three int row-offset tables of ty + 4 entries
+   return sizeof(R) * (size_t)kZRingPlanes * (size_t)(z.ty + 4) * (size_t)z.hs +
+          3 * sizeof(int) * (size_t)(z.ty + 4);
 }
 // whether the level takes the single-pass sweep (3D, n0 a multiple of 32 up
 // to 256, even extents, at least 2^21 cells, shape fits in shared memory);

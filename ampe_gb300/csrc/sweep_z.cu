@@ -85,7 +85,11 @@ struct Coef {
 // MODE 0: sweep from u_in; 1: from u = 0 (u_in unused); 2: from u_in + P e
 // (e the next coarser level's correction, piecewise constant: the first
 // post-smoothing sweep with the prolongation fused in).  blockDim.x = n0
-// (<= 256).
+// (<= 256).  The ring's rows are kZRowStride elements apart whatever n0,
+// so every shared-memory access of a cell update has a constant offset from
+// one of a few per-step base pointers; the row offsets of the global arrays
+// (which depend on the block's wrapped rows) sit in three small tables
+// after the ring.
 template <class R, bool HD, bool HC, bool HM, int MODE, int TY>
 __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
     k_sweep_z(FacOp<R> op, Grid g, int kz, const R* __restrict__ f,
@@ -93,6 +97,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
               const R* __restrict__ e)
 {
    constexpr int ROWS = TY + 4;
+   constexpr int HS = kZRowStride, PS = ROWS * HS;
    constexpr int NRED = (TY + 2) / 2, NBLACK = TY / 2;
    // software-pipelined coefficient loads where they fit the registers (the
    // phase operator: f and C per cell)
@@ -112,52 +117,59 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
    }
    extern __shared__ __align__(16) unsigned char zsm[];
    R* const S = reinterpret_cast<R*>(zsm);
+   // per ring row: ghosted row offset (u, C, the output), interior row
+   // offset (f) and the coarse level's ghosted row offset (MODE 2)
+   int* const rowg = reinterpret_cast<int*>(zsm + sizeof(R) * kZRing * PS);
+   int* const rowf = rowg + ROWS;
+   int* const rowe = rowf + ROWS;
    const int n0 = g.n0, x = threadIdx.x;
-   const int xm = x == 0 ? n0 - 1 : x - 1;
-   const int xp = x == n0 - 1 ? 0 : x + 1;
+   const int dxm = x == 0 ? n0 - 1 : -1;  // offsets of the periodic x neighbours
+   const int dxp = x == n0 - 1 ? 1 - n0 : 1;
    const int j0 = blockIdx.x * TY;
    const int k0 = blockIdx.y * kz, k1 = k0 + kz;
-   const int ps = ROWS * n0;
-   // wrapped y index of every ring row (the block's rows and two halo rows
-   // on each side), fixed for the whole kernel
-   int jw[ROWS];
-#pragma unroll
-   for (int r = 0; r < ROWS; r++) jw[r] = wrap(j0 - 2 + r, g.n1);
+   if (x < ROWS) {
+      const int jj = wrap(j0 - 2 + x, g.n1);
+      rowg[x] = (jj + g.ng) * g.sx;
+      rowf[x] = jj * n0;
+      rowe[x] = MODE == 2 ? ((jj >> 1) + gc.ng) * gc.sx : 0;
+   }
+   __syncthreads();
    const bool xedge = x < g.ng || x >= n0 - g.ng;
-   auto slot = [&](int p) { return S + ((p - k0 + 2) % kZRing) * ps; };
-   // ghosted index of this column: plane part and row part
+   // ring slot of plane p (p >= k0 - 2), this column
+   auto slot_of = [&](int p) { return (p - k0 + 2) % kZRing; };
+   auto colp = [&](int sl) { return S + sl * PS + x; };
+   // ghosted offset of this column in plane kk
    auto gplane = [&](int kk) { return (kk + g.gz) * g.sy + g.ng + x; };
-   auto grow = [&](int jj) { return (jj + g.ng) * g.sx; };
 
    auto load_plane = [&](int p) {
-      R* dst = slot(p) + x;
+      R* dst = colp(slot_of(p));
       const R* src = uin + gplane(wrap(p, g.n2));
 #pragma unroll
       for (int r = 0; r < ROWS; r++) {
          if (MODE == 1)
-            dst[r * n0] = R(0);
+            dst[r * HS] = R(0);
          else
-            cp_async<sizeof(R)>(dst + r * n0, src + grow(jw[r]));
+            cp_async<sizeof(R)>(dst + r * HS, src + rowg[r]);
       }
    };
    // MODE 2: add the coarse correction to the values this thread staged
    auto add_correction = [&](int p) {
-      R* dst = slot(p) + x;
-      const int kc = wrap(p, g.n2) >> 1;
+      R* dst = colp(slot_of(p));
+      const R* ep = e + (((wrap(p, g.n2) >> 1) + gc.gz) * gc.sy + gc.ng + (x >> 1));
 #pragma unroll
-      for (int r = 0; r < ROWS; r++)
-         dst[r * n0] = dst[r * n0] + e[gc.c(x >> 1, jw[r] >> 1, kc)];
+      for (int r = 0; r < ROWS; r++) dst[r * HS] = dst[r * HS] + ep[rowe[r]];
    };
    // this column's cells of colour col in plane p from ring row rlo on sit
    // at rows rlo + par + 2m, par = 0 or 1 by the column's parity
    auto par_of = [&](int p, int col, int rlo) { return (x + j0 - 2 + rlo + p + col) & 1; };
-   auto gather = [&](int p, int jj, Coef<R>& cf) {
-      const int kw = wrap(p, g.n2);
-      const int c = gplane(kw) + grow(jj);
-      cf.f = __ldg(f + (op.f_interior ? (kw * g.n1 + jj) * n0 + x : c));
+   // coefficients of ring row rr of plane p
+   auto gather = [&](int kw, int cplane, int fplane, int rr, Coef<R>& cf) {
+      const int c = cplane + rowg[rr];
+      cf.f = __ldg(f + (op.f_interior ? fplane + rowf[rr] : c));
       if (HC) cf.c = __ldg(op.C + c);
       if (HM) cf.m = __ldg(op.M + c);
       if (HD) {
+         const int jj = wrap(j0 - 2 + rr, g.n1);
          const int fx = g.fx(x, jj, kw), fy = g.fy(x, jj, kw), fz = g.fz(x, jj, kw);
          cf.d[0] = __ldg(op.D0 + fx);
          cf.d[1] = __ldg(op.D0 + fx + 1);
@@ -167,15 +179,14 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
          cf.d[5] = __ldg(op.D2 + fz + g.fzs());
       }
    };
-   auto update = [&](int p, int r, const Coef<R>& cf) {
-      R* P = slot(p);
-      const R* Pm = slot(p - 1);
-      const R* Pp = slot(p + 1);
-      const int o = r * n0;
-      const R uc = P[o + x];
-      const R uxm = P[o + xm], uxp = P[o + xp];
-      const R uym = P[o - n0 + x], uyp = P[o + n0 + x];
-      const R uzm = Pm[o + x], uzp = Pp[o + x];
+   // one update at ring row offset o (a compile-time multiple of HS) from
+   // the column bases of its plane (P), the x neighbours' (P + dxm, P + dxp)
+   // and the planes below and above (Pm, Pp)
+   auto update = [&](R* P, const R* Pm, const R* Pp, int o, const Coef<R>& cf) {
+      const R uc = P[o];
+      const R uxm = P[o + dxm], uxp = P[o + dxp];
+      const R uym = P[o - HS], uyp = P[o + HS];
+      const R uzm = Pm[o], uzp = Pp[o];
       if constexpr (FAST) {
          // u <- (M nb - f) / (M dsum - C): the same update, with
          // nb = sum_d dxi_d^2 (D- u- + D+ u+), dsum = sum_d dxi_d^2 (D- + D+)
@@ -196,7 +207,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
          }
          const float M = HM ? cf.m : op.mc;
          const float C = HC ? cf.c : op.cc;
-         P[o + x] = __fdividef(fmaf(M, nb, -cf.f), fmaf(M, dsum, -C));
+         P[o] = __fdividef(fmaf(M, nb, -cf.f), fmaf(M, dsum, -C));
          return;
       }
       // expression order of op_residual_u (the colour kernel's)
@@ -229,18 +240,18 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
       const R C = HC ? cf.c : op.cc;
       const R dudr = R(1) / (M * dsum - C);
       const R res = cf.f - M * div - C * uc;
-      P[o + x] = uc + -res * dudr;
+      P[o] = uc + -res * dudr;
    };
-   // the block's rows of plane p (final values) -> u_out and its images
-   auto store = [&](int p) {
-      const R* P = slot(p) + x;
-      R* dst = uout + gplane(p);
+   // the block's rows of plane p (final values, column base P) -> u_out
+   // and its images
+   auto store = [&](int p, const R* P) {
+      const int dbase = gplane(p);
       const bool pedge = p < g.ng || p >= g.n2 - g.ng;
 #pragma unroll
       for (int r = 2; r < TY + 2; r++) {
          const int j = j0 + r - 2;
-         const R v = P[r * n0];
-         dst[grow(j)] = v;
+         const R v = P[r * HS];
+         uout[dbase + rowg[r]] = v;
          if (xedge || pedge || j < g.ng || j >= g.n1 - g.ng)
             for_each_image(g, x, j, p, [&](int idx) { uout[idx] = v; });
       }
@@ -250,29 +261,28 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
    // each side (ring rows 1 .. TY+2), black at w-1 on the rows (ring rows
    // 2 .. TY+1)
    auto gather_step = [&](int w, Coef<R>* cr, Coef<R>* cb) {
-      const int pr = par_of(w, 0, 1);
+      {
+         const int kw = wrap(w, g.n2);
+         const int cpl = gplane(kw), fpl = kw * g.n1 * n0 + x;
+         const int pr = par_of(w, 0, 1);
 #pragma unroll
-      for (int m = 0; m < NRED; m++) {
-         const int r = 1 + 2 * m;
-         gather(w, pr ? jw[r + 1] : jw[r], cr[m]);
+         for (int m = 0; m < NRED; m++) gather(kw, cpl, fpl, 1 + 2 * m + pr, cr[m]);
       }
       if (w > k0) {
+         const int kw = wrap(w - 1, g.n2);
+         const int cpl = gplane(kw), fpl = kw * g.n1 * n0 + x;
          const int pb = par_of(w - 1, 1, 2);
 #pragma unroll
-         for (int m = 0; m < NBLACK; m++) {
-            const int r = 2 + 2 * m;
-            gather(w - 1, pb ? jw[r + 1] : jw[r], cb[m]);
-         }
+         for (int m = 0; m < NBLACK; m++) gather(kw, cpl, fpl, 2 + 2 * m + pb, cb[m]);
       }
    };
    int next = k0 - 2;  // next plane to stage
-   // one step; with PIPE the coefficients of step w come in cur (gathered
-   // during step w-1) and those of step w+1 are gathered into nxt before
-   // this step's last barrier, so their loads overlap the store and the next
-   // step's wait
-   // Two barriers per step.  The first makes plane w+1 (every thread's
-   // copies) and the previous step's black updates visible; only then is
-   // plane w+2+kZPrefetch-1 issued, into the slot of plane w-3, which the
+   // One step; with PIPE the coefficients of step w come in cur (gathered
+   // during step w-1) and those of step w+1 are gathered into nxt after
+   // this step's updates, so their loads overlap the store and the next
+   // step's wait.  Two barriers per step.  The first makes plane w+1
+   // (every thread's copies) and the previous step's black updates visible;
+   // only then is plane w+3 issued, into the slot of plane w-3, which the
    // previous step's black updates were the last to read.  The second
    // orders the red updates of plane w before the black ones of plane w-1.
    // Each thread updates and stores only its own column, so the store of
@@ -295,17 +305,32 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
          load_plane(next);
          cp_commit();
       }
-      const int pr = par_of(w, 0, 1);
+      // slots of planes w-2 .. w+1
+      const int s0 = slot_of(w);
+      const int sm1 = s0 == 0 ? kZRing - 1 : s0 - 1;
+      const int sm2 = sm1 == 0 ? kZRing - 1 : sm1 - 1;
+      const int sp1 = s0 == kZRing - 1 ? 0 : s0 + 1;
+      R* const Pw = colp(s0);
+      R* const Pw1 = colp(sm1);
+      {
+         const int pr = par_of(w, 0, 1);
+         R* const P = Pw + pr * HS;
+         const R* const Pm = Pw1 + pr * HS;
+         const R* const Pp = colp(sp1) + pr * HS;
 #pragma unroll
-      for (int m = 0; m < NRED; m++) update(w, 1 + 2 * m + pr, cr[m]);
+         for (int m = 0; m < NRED; m++) update(P, Pm, Pp, (1 + 2 * m) * HS, cr[m]);
+      }
       __syncthreads();
       if (w > k0) {
          const int pb = par_of(w - 1, 1, 2);
+         R* const P = Pw1 + pb * HS;
+         const R* const Pm = colp(sm2) + pb * HS;
+         const R* const Pp = Pw + pb * HS;
 #pragma unroll
-         for (int m = 0; m < NBLACK; m++) update(w - 1, 2 + 2 * m + pb, cb[m]);
+         for (int m = 0; m < NBLACK; m++) update(P, Pm, Pp, (2 + 2 * m) * HS, cb[m]);
       }
       if (PIPE && w < k1) gather_step(w + 1, nr, nb);
-      if (w > k0) store(w - 1);
+      if (w > k0) store(w - 1, Pw1);
    };
    // prologue: the planes the first step reads (k0-2 .. k0) and one ahead
    for (; next <= min(k0 + 1, k1 + 1); next++) {
@@ -330,7 +355,7 @@ static ZShape choose_zshape(const Grid& g)
 {
    ZShape zs;
    zs.nh = g.n0 / 2;
-   zs.hs = g.n0;  // row stride of the ring (one x column per thread)
+   zs.hs = kZRowStride;  // row stride of the ring (one x column per thread)
    // 8 rows per block in FP32 (<= 74 KB of ring per block), 4 in FP64 (the
    // coefficients of 8 rows do not fit the register budget)
    zs.ty = sizeof(R) == 4 ? 8 : 4;
