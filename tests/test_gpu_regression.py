@@ -13,6 +13,7 @@ sequence.  Checks:
 * per-field parity with a live oracle run over the first start-up steps
   (FP64 within 1e-10, mixed within 1e-6)."""
 import json
+import os
 
 import numpy as np
 import pytest
@@ -71,9 +72,18 @@ def test_kkscomposition_start_parity(cuda, precision):
         assert err <= START_TOL[precision]
 
 
+_RUNS = {}
+
+
+def _gpu_run(precision):
+    if precision not in _RUNS:
+        _RUNS[precision] = K.run(lambda m, p: _Gpu(m, p), precision=precision)
+    return _RUNS[precision]
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_kkscomposition_regression(cuda, precision):
-    r = K.run(lambda m, p: _Gpu(m, p), precision=precision)
+    r = _gpu_run(precision)
     solid, drift = r["solid"][-1], r["drift"]
     print("KKScomposition GPU precision %d: solid fraction %.5f at t = %.4f, drift %.2e, "
           "%d steps, %d rejected" % (precision, solid, r["t"][-1], drift, r["steps"],
@@ -81,6 +91,15 @@ def test_kkscomposition_regression(cuda, precision):
     assert abs(r["t"][-1] - 0.3) < 1e-9
     assert abs(solid - K.SOLID_TARGET) <= K.SOLID_TOL
     assert abs(drift) < K.DRIFT_TOL
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kkscomposition_trajectory_vs_oracle(cuda, precision):
+    """The GPU run against the oracle's run of the same case (the committed
+    trajectory fixture, tests/golden/make_kkscomposition.py)."""
+    if not os.path.exists(K.FIXTURE):
+        pytest.skip("oracle trajectory fixture not generated")
+    r = _gpu_run(precision)
     with open(K.FIXTURE) as f:
         gold = json.load(f)
     assert r["steps"] == gold["steps"] and r["rejected"] == gold["rejected"]
