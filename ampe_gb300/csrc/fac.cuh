@@ -69,9 +69,7 @@ struct ZShape {
 template <class R>
 inline size_t zsweep_smem_bytes(const ZShape& z)
 {
-   // the ring, then three int row-offset tables of ty + 4 entries
-   return sizeof(R) * (size_t)kZRingPlanes * (size_t)(z.ty + 4) * (size_t)z.hs +
-          3 * sizeof(int) * (size_t)(z.ty + 4);
+   return sizeof(R) * (size_t)kZRingPlanes * (size_t)(z.ty + 4) * (size_t)z.hs;
 }
 // whether the level takes the single-pass sweep (3D, n0 a multiple of 32 up
 // to 256, even extents, at least 2^21 cells, shape fits in shared memory);

@@ -87,11 +87,9 @@ struct Coef {
 // post-smoothing sweep with the prolongation fused in).  blockDim.x = n0
 // (<= 256).  The ring's rows are kZRowStride elements apart whatever n0,
 // so every shared-memory access of a cell update has a constant offset from
-// one of a few per-step base pointers; the row offsets of the global arrays
-// (which depend on the block's wrapped rows) sit in three small tables
-// after the ring.
+// one of a few per-step base pointers.
 template <class R, bool HD, bool HC, bool HM, int MODE, int TY>
-__global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD && MODE != 2) ? 3 : 2)
     k_sweep_z(FacOp<R> op, Grid g, int kz, const R* __restrict__ f,
               const R* __restrict__ uin, R* __restrict__ uout, Grid gc,
               const R* __restrict__ e)
@@ -117,23 +115,17 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
    }
    extern __shared__ __align__(16) unsigned char zsm[];
    R* const S = reinterpret_cast<R*>(zsm);
-   // per ring row: ghosted row offset (u, C, the output), interior row
-   // offset (f) and the coarse level's ghosted row offset (MODE 2)
-   int* const rowg = reinterpret_cast<int*>(zsm + sizeof(R) * kZRing * PS);
-   int* const rowf = rowg + ROWS;
-   int* const rowe = rowf + ROWS;
    const int n0 = g.n0, x = threadIdx.x;
    const int dxm = x == 0 ? n0 - 1 : -1;  // offsets of the periodic x neighbours
    const int dxp = x == n0 - 1 ? 1 - n0 : 1;
    const int j0 = blockIdx.x * TY;
    const int k0 = blockIdx.y * kz, k1 = k0 + kz;
-   if (x < ROWS) {
-      const int jj = wrap(j0 - 2 + x, g.n1);
-      rowg[x] = (jj + g.ng) * g.sx;
-      rowf[x] = jj * n0;
-      rowe[x] = MODE == 2 ? ((jj >> 1) + gc.ng) * gc.sx : 0;
-   }
-   __syncthreads();
+   // wrapped y index of ring row r (the block's rows and two halo rows on
+   // each side) and its ghosted row offset, formed where they are used (a
+   // few integer operations, no registers held and no load in front of the
+   // load that needs them)
+   auto jw = [&](int r) { return wrap(j0 - 2 + r, g.n1); };
+   auto rowg = [&](int r) { return (jw(r) + g.ng) * g.sx; };
    const bool xedge = x < g.ng || x >= n0 - g.ng;
    // ring slot of plane p (p >= k0 - 2), this column
    auto slot_of = [&](int p) { return (p - k0 + 2) % kZRing; };
@@ -149,7 +141,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
          if (MODE == 1)
             dst[r * HS] = R(0);
          else
-            cp_async<sizeof(R)>(dst + r * HS, src + rowg[r]);
+            cp_async<sizeof(R)>(dst + r * HS, src + rowg(r));
       }
    };
    // MODE 2: add the coarse correction to the values this thread staged
@@ -157,19 +149,19 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
       R* dst = colp(slot_of(p));
       const R* ep = e + (((wrap(p, g.n2) >> 1) + gc.gz) * gc.sy + gc.ng + (x >> 1));
 #pragma unroll
-      for (int r = 0; r < ROWS; r++) dst[r * HS] = dst[r * HS] + ep[rowe[r]];
+      for (int r = 0; r < ROWS; r++)
+         dst[r * HS] = dst[r * HS] + ep[((jw(r) >> 1) + gc.ng) * gc.sx];
    };
    // this column's cells of colour col in plane p from ring row rlo on sit
    // at rows rlo + par + 2m, par = 0 or 1 by the column's parity
    auto par_of = [&](int p, int col, int rlo) { return (x + j0 - 2 + rlo + p + col) & 1; };
    // coefficients of ring row rr of plane p
-   auto gather = [&](int kw, int cplane, int fplane, int rr, Coef<R>& cf) {
-      const int c = cplane + rowg[rr];
-      cf.f = __ldg(f + (op.f_interior ? fplane + rowf[rr] : c));
+   auto gather = [&](int kw, int cplane, int fplane, int jj, Coef<R>& cf) {
+      const int c = cplane + (jj + g.ng) * g.sx;
+      cf.f = __ldg(f + (op.f_interior ? fplane + jj * n0 : c));
       if (HC) cf.c = __ldg(op.C + c);
       if (HM) cf.m = __ldg(op.M + c);
       if (HD) {
-         const int jj = wrap(j0 - 2 + rr, g.n1);
          const int fx = g.fx(x, jj, kw), fy = g.fy(x, jj, kw), fz = g.fz(x, jj, kw);
          cf.d[0] = __ldg(op.D0 + fx);
          cf.d[1] = __ldg(op.D0 + fx + 1);
@@ -251,7 +243,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
       for (int r = 2; r < TY + 2; r++) {
          const int j = j0 + r - 2;
          const R v = P[r * HS];
-         uout[dbase + rowg[r]] = v;
+         uout[dbase + (j + g.ng) * g.sx] = v;
          if (xedge || pedge || j < g.ng || j >= g.n1 - g.ng)
             for_each_image(g, x, j, p, [&](int idx) { uout[idx] = v; });
       }
@@ -266,14 +258,20 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD) ? 3 : 2)
          const int cpl = gplane(kw), fpl = kw * g.n1 * n0 + x;
          const int pr = par_of(w, 0, 1);
 #pragma unroll
-         for (int m = 0; m < NRED; m++) gather(kw, cpl, fpl, 1 + 2 * m + pr, cr[m]);
+         for (int m = 0; m < NRED; m++) {
+            const int r = 1 + 2 * m;
+            gather(kw, cpl, fpl, jw(r + pr), cr[m]);
+         }
       }
       if (w > k0) {
          const int kw = wrap(w - 1, g.n2);
          const int cpl = gplane(kw), fpl = kw * g.n1 * n0 + x;
          const int pb = par_of(w - 1, 1, 2);
 #pragma unroll
-         for (int m = 0; m < NBLACK; m++) gather(kw, cpl, fpl, 2 + 2 * m + pb, cb[m]);
+         for (int m = 0; m < NBLACK; m++) {
+            const int r = 2 + 2 * m;
+            gather(kw, cpl, fpl, jw(r + pb), cb[m]);
+         }
       }
    };
    int next = k0 - 2;  // next plane to stage
