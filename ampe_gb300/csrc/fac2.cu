@@ -369,12 +369,9 @@ int setup(Fac2& F, const ampe_fac2_t* p, const ampe_fac2_level_t* lc, const ampe
    }
    F.dvc = mc.dx[0] * mc.dx[1] * mc.dx[2];
    F.dvf = mf.dx[0] * mf.dx[1] * mf.dx[2];
-   // the sum of the weights, in the order the CPU check sums them
-   double den = 0.0;
-   for (long long t = 0; t < F.gf.cells(); t++) den += F.dvf;
+   // the sum of the weights: fine cells, and coarse cells outside the box
    const long long under = (long long)p->nbox[0] * p->nbox[1] * p->nbox[2];
-   for (long long t = 0; t < F.gc.cells() - under; t++) den += F.dvc;
-   F.den = den;
+   F.den = (double)F.gf.cells() * F.dvf + (double)(F.gc.cells() - under) * F.dvc;
    return AMPE_OK;
 }
 

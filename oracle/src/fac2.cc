@@ -267,13 +267,13 @@ double composite_residual(const Two& T, const double* fcr, const double* ffr, do
    Layout Lc(T.c.m), Lf(T.f.m);
    const double dvf = T.f.m.dx[0] * T.f.m.dx[1] * T.f.m.dx[2];
    const double dvc = T.c.m.dx[0] * T.c.m.dx[1] * T.c.m.dx[2];
-   double num = 0.0, den = 0.0;
+   double num = 0.0;
+   long ncoarse = 0;
    for (int k = 0; k < Lf.n2; k++)
       for (int j = 0; j < Lf.n1; j++)
          for (int i = 0; i < Lf.n0; i++) {
             const double v = rf[Lf.c(i, j, k)];
             num += dvf * v * v;
-            den += dvf;
          }
    const ampe_fac2_t& p = *T.p;
    for (int k = 0; k < Lc.n2; k++)
@@ -285,8 +285,9 @@ double composite_residual(const Two& T, const double* fcr, const double* ffr, do
             if (under) continue;
             const double v = rc[Lc.c(i, j, k)];
             num += dvc * v * v;
-            den += dvc;
+            ncoarse++;
          }
+   const double den = (double)Lf.cells() * dvf + (double)ncoarse * dvc;
    return std::sqrt(num / den);
 }
 
