@@ -1429,6 +1429,57 @@ static int advance_adaptive(Stepper& S, double t_stop, int max_steps)
 
 using namespace ampe;
 
+// Host <-> device copies of the state for callers that hand the fields in
+// and out every step.  Pinned host memory is mapped into the device's
+// address space (unified addressing); there a grid of 16-byte loads and
+// stores over the host link moves the data faster than one copy engine, so
+// mapped buffers are copied by a kernel and anything else (pageable memory,
+// a buffer not mapped) by cudaMemcpyAsync.
+static const double* mapped_host(const double* p)
+{
+   cudaPointerAttributes a;
+   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+      cudaGetLastError();  // an unregistered pointer: clear the query's error
+      return nullptr;
+   }
+   if (a.type == cudaMemoryTypeHost && a.devicePointer)
+      return static_cast<const double*>(a.devicePointer);
+   return nullptr;
+}
+
+__global__ void k_copy_f64(const double* __restrict__ src, double* __restrict__ dst,
+                           long long n)
+{
+   const long long n2 = n / 2;
+   const double2* s2 = reinterpret_cast<const double2*>(src);
+   double2* d2 = reinterpret_cast<double2*>(dst);
+   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n2;
+        t += (long long)gridDim.x * blockDim.x)
+      d2[t] = s2[t];
+   if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+}
+
+// copy n doubles between the host and the device on stream s (host -> device
+// if to_device); the kernel path needs both pointers 16-byte aligned
+static int copy_host(double* dst, const double* src, long long n, bool to_device, cudaStream_t s)
+{
+   const double* hp = to_device ? src : dst;
+   const double* mp = mapped_host(hp);
+   const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
+   if (mp && aligned && n >= 2) {
+      const double* from = to_device ? mp : src;
+      double* to = to_device ? dst : const_cast<double*>(mp);
+      k_copy_f64<<<(unsigned)max_blocks(8), 256, 0, s>>>(from, to, n);
+      g_launches++;
+      return cudaGetLastError() == cudaSuccess ? AMPE_OK : AMPE_ERR_CUDA;
+   }
+   return cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n,
+                          to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s) ==
+                  cudaSuccess
+              ? AMPE_OK
+              : AMPE_ERR_CUDA;
+}
+
 extern "C" {
 
 int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
@@ -1660,8 +1711,13 @@ int ampe_stepper_get_state(void* h, double* phi, double* conc, double* cl,
    if (!S) return AMPE_ERR_INVALID;
    const cudaMemcpyKind kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
    const size_t bytes = sizeof(double) * (size_t)S->N;
-   if (phi) cudaMemcpyAsync(phi, S->yn, bytes, kind, S->s);
-   if (conc) cudaMemcpyAsync(conc, S->yn + S->N, bytes, kind, S->s);
+   if (host) {
+      if (phi && copy_host(phi, S->yn, S->N, false, S->s)) return AMPE_ERR_CUDA;
+      if (conc && copy_host(conc, S->yn + S->N, S->N, false, S->s)) return AMPE_ERR_CUDA;
+   } else {
+      if (phi) cudaMemcpyAsync(phi, S->yn, bytes, kind, S->s);
+      if (conc) cudaMemcpyAsync(conc, S->yn + S->N, bytes, kind, S->s);
+   }
    if (cl || cs) {
       if (S->p.precision == 1) {
          k_from_ghosted<float, double><<<map_blocks(S->N), 256, 0, S->s>>>(S->g, S->clr32,
@@ -1954,6 +2010,12 @@ int ampe_stepper_load_y(void* h, const double* phi, const double* conc,
    if (!S || !phi || !conc) return AMPE_ERR_INVALID;
    const cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
    const size_t bytes = sizeof(double) * (size_t)S->N;
+   if (host) {
+      if (copy_host(S->yn, phi, S->N, true, S->s) ||
+          copy_host(S->yn + S->N, conc, S->N, true, S->s))
+         return AMPE_ERR_CUDA;
+      return AMPE_OK;
+   }
    cudaMemcpyAsync(S->yn, phi, bytes, kind, S->s);
    cudaMemcpyAsync(S->yn + S->N, conc, bytes, kind, S->s);
    return cudaGetLastError() == cudaSuccess ? AMPE_OK : AMPE_ERR_CUDA;

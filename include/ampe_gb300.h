@@ -664,7 +664,11 @@ int ampe_stepper_jv(void* handle, const double* v, double gamma, double* out,
                     int host);
 /* Replace the current state y_n (phi, conc interior arrays) keeping the BDF
  * history and the Newton warm starts: for callers that own the fields in
- * host memory and hand them in every step (a SAMRAI patch adapter). */
+ * host memory and hand them in every step (a SAMRAI patch adapter).
+ * host != 0 here and in ampe_stepper_get_state: pinned host buffers that
+ * the device can address (cudaHostAlloc / cudaHostRegister under unified
+ * addressing) are copied by a kernel over the host link, other host memory
+ * by cudaMemcpyAsync; both on the stepper's stream. */
 int ampe_stepper_load_y(void* handle, const double* phi, const double* conc,
                         int host);
 /* evolve_quat models: the orientation part of y_n, 4N doubles (component-
