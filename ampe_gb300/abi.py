@@ -17,6 +17,7 @@ FLUX_SIMPLE, FLUX_ISOTROPIC, FLUX_ANISOTROPIC = 0, 1, 2
 THERMO_DILUTE, THERMO_CALPHAD = 0, 1
 TEMP_CONSTANT, TEMP_GRADIENT, TEMP_FIELD = 0, 1, 2
 CONC_EBS, CONC_KKS = 0, 1
+DIFF_ARRHENIUS, DIFF_MOBILITY = 0, 1
 MAX_TSEG = 6
 
 
@@ -89,6 +90,9 @@ class Model(C.Structure):
         ("pad1", C.c_char * 6),
         ("conc_form", C.c_int),
         ("ng_side", C.c_int),
+        ("conc_diffusion", C.c_int),
+        ("pad2", C.c_int),
+        ("mobility", Mobility),
     ]
 
     def cells(self):

@@ -134,7 +134,9 @@ def gterm_from_segments(seg):
 
 
 def apply_database(model, db):
-    """Set model.g and model.L from a database dict (see database_from_text)."""
+    """Set model.g and model.L (and model.mobility when the database has a
+    MobilityParameters block) from a database dict (see database_from_text).
+    Which diffusivities the model uses stays model.conc_diffusion's choice."""
     model.thermo = abi.THERMO_CALPHAD
     for si, sp in enumerate(("A", "B")):
         for pi, ph in enumerate(("L", "S")):
@@ -145,6 +147,8 @@ def apply_database(model, db):
             v = lm.get("L%d" % k, [0.0, 0.0])
             model.L[pi][k][0] = v[0]
             model.L[pi][k][1] = v[1] if len(v) > 1 else 0.0
+    if "mobility" in db:
+        model.mobility = mobility_struct(db["mobility"])
     return model
 
 

@@ -318,6 +318,50 @@ __device__ __forceinline__ R dxi_of(const ThermoCoef& th, R c, int p)
    return -R(2) * S - R(4) * u * S1 + R(4) * c * (R(1) - c) * S2;
 }
 
+// Q_i(T) and the interaction terms of one species' mobility in one phase
+// (CALPHADMobility.h getQ, getQQ0..3)
+__device__ __forceinline__ double mob_q(const double* a, double T)
+{
+   return a[0] + kGasR * T * log(a[1]) + a[2] * T * log(T) + a[3] / T;
+}
+
+__device__ __forceinline__ double mob_qq(const double* a, double T)
+{
+   return a[0] + kGasR * T * log(a[1]);
+}
+
+// atomic mobility of species s in phase p at composition (c0, c1 = 1 - c0)
+// (CALPHADMobility::getAtomicMobility and getDeltaG, binary form)
+__device__ __forceinline__ double atomic_mobility(const ampe_mobility_t& mb, int s, int p,
+                                                  double c0, double c1, double T)
+{
+   const double dc = c0 - c1;
+   const double dG =
+       c0 * mob_q(mb.q[s][p][0], T) + c1 * mob_q(mb.q[s][p][1], T) +
+       c0 * c1 *
+           (mob_qq(mb.qq[s][p][0], T) +
+            dc * (mob_qq(mb.qq[s][p][1], T) +
+                  dc * (mob_qq(mb.qq[s][p][2], T) + dc * mob_qq(mb.qq[s][p][3], T))));
+   const double rtinv = 1.0 / (kGasR * T);
+   return exp(dG * rtinv) * rtinv;
+}
+
+// D_p = (mobility matrix) x (free-energy curvature), 1x1 for a binary
+// (computeLocalDiffusionMatrixL/A with computeDiffusionMobilityBinaryPhase)
+__device__ __forceinline__ double phase_diffusion(const ampe_model_t& m,
+                                                  const ampe_mobility_t& mb, int p, double c,
+                                                  double T)
+{
+   const double c1 = 1.0 - c;
+   const double m0 = atomic_mobility(mb, 0, p, c, c1, T);
+   const double m1 = atomic_mobility(mb, 1, p, c, c1, T);
+   const double mm = c * m1 + c1 * m0;
+   const double mob = c * c1 * mm * 1.e12;
+   const ThermoCoef th = thermo_coef(m, T);
+   const double curv = th.RT / (c * (1.0 - c)) + dxi_of(th, c, p);
+   return mob * curv;
+}
+
 __device__ __forceinline__ double xlogx(double x)
 {
    return x > 0.0 ? x * log(x) : 0.0;
@@ -410,6 +454,7 @@ __device__ __forceinline__ double cvt<double, float>(float x)
 // ---------------------------------------------------------------------------
 namespace ampe {
 int check_model(const ampe_model_t* m);
+int check_mobility(const ampe_mobility_t* mob);
 extern long long g_launches;  // kernels launched through this library
 inline int launch_status()
 {

@@ -128,7 +128,7 @@ int kks_interior(const ampe_model_t& m, const Grid& g, const ThermoCoef* tab,
 // ---------------------------------------------------------------------------
 // fused right-hand side
 // ---------------------------------------------------------------------------
-template <bool HAS_Q>
+template <bool HAS_Q, bool MOB>
 __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
                             const double* quat, const double* tfield,
                             const ThermoCoef* tab, const double* cl,
@@ -193,7 +193,15 @@ __global__ void k_rhs_fused(ampe_model_t m, Grid g, const double* phi,
             const bool kksf = m.conc_form == AMPE_CONC_KKS;
             const double hphi = interp_func(vphi, kksf ? m.energy_interp : m.diff_interp);
             double dlq = m.D_liquid, dsq = m.D_solid;
-            if (tdep) {
+            if (MOB) {
+               // composition-dependent D_L, D_S from the atomic mobilities at
+               // the face means of the lagged cL, cS and of T
+               // (MobilityCompositionDiffusionStrategy.cc:83-611)
+               const double T = 0.5 * (temperature_at(m, g, tfield, a0, a1, a2) +
+                                       temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek));
+               dlq = phase_diffusion(m, m.mobility, 0, 0.5 * (cld[up] + cld[lo]), T);
+               dsq = phase_diffusion(m, m.mobility, 1, 0.5 * (csd[up] + csd[lo]), T);
+            } else if (tdep) {
                const double invT =
                    2.0 / (temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek) +
                           temperature_at(m, g, tfield, a0, a1, a2));
@@ -231,16 +239,25 @@ int rhs_fused(const ampe_model_t& m, const Grid& g, const double* phi,
               double* conc_rhs, cudaStream_t s)
 {
    if (m.conc_form == AMPE_CONC_KKS && (!conc || !cld || !csd)) return AMPE_ERR_INVALID;
+   const bool mob = m.conc_diffusion == AMPE_DIFF_MOBILITY;
+   if (mob && (m.conc_form != AMPE_CONC_EBS || !cld || !csd)) return AMPE_ERR_INVALID;
    long long b = (g.cells() + 255) / 256;
    if (b > max_blocks()) b = max_blocks();
-   if (quat)
-      k_rhs_fused<true><<<(unsigned)b, 256, 0, s>>>(
-          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, conc, cld, csd, phi_rhs,
-          conc_rhs);
-   else
-      k_rhs_fused<false><<<(unsigned)b, 256, 0, s>>>(
-          m, g, phi, quat, tfield, tab, cl, cs, dF, phid, ogm, conc, cld, csd, phi_rhs,
-          conc_rhs);
+#define AMPE_FUSED(Q, M)                                                                     \
+   k_rhs_fused<Q, M><<<(unsigned)b, 256, 0, s>>>(m, g, phi, quat, tfield, tab, cl, cs, dF,   \
+                                                 phid, ogm, conc, cld, csd, phi_rhs, conc_rhs)
+   if (quat) {
+      if (mob)
+         AMPE_FUSED(true, true);
+      else
+         AMPE_FUSED(true, false);
+   } else {
+      if (mob)
+         AMPE_FUSED(false, true);
+      else
+         AMPE_FUSED(false, false);
+   }
+#undef AMPE_FUSED
    return launch_status();
 }
 
@@ -259,7 +276,8 @@ extern "C" int ampe_rhs_phase_conc(const ampe_model_t* m, const double* phi,
    if (m->flux_type == AMPE_FLUX_ANISOTROPIC && !quat) return AMPE_ERR_INVALID;
    if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
    if (m->conc_form == AMPE_CONC_KKS) return AMPE_ERR_INVALID;  // needs c: ampe_conc_flux_kks
+   // the diffusivities (either model) at this phi, cL, cS
    return rhs_fused(*m, make_grid(*m), phi, quat, temp, nullptr, cl, cs,
-                    nullptr, phi, nullptr, nullptr, nullptr, nullptr, phi_rhs, conc_rhs,
+                    nullptr, phi, nullptr, nullptr, cl, cs, phi_rhs, conc_rhs,
                     (cudaStream_t)stream);
 }

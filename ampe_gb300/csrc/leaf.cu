@@ -55,6 +55,24 @@ int check_model(const ampe_model_t* m)
                            (e0 + 2 * s) * (e1 + 1 + 2 * s) * (e2 + 2 * sz) +
                            (e0 + 2 * s) * (e1 + 2 * s) * (e2 + 1 + 2 * sz);
    if (ghost > lim || faces > lim) return AMPE_ERR_TOO_LARGE;
+   if (m->conc_diffusion != AMPE_DIFF_ARRHENIUS && m->conc_diffusion != AMPE_DIFF_MOBILITY)
+      return AMPE_ERR_INVALID;
+   if (m->conc_diffusion == AMPE_DIFF_MOBILITY && check_mobility(&m->mobility))
+      return AMPE_ERR_INVALID;
+   return AMPE_OK;
+}
+
+// the logarithms of the mobility terms need a1 > 0
+int check_mobility(const ampe_mobility_t* mob)
+{
+   if (!mob) return AMPE_ERR_INVALID;
+   for (int s = 0; s < 2; s++)
+      for (int p = 0; p < 2; p++) {
+         for (int i = 0; i < 2; i++)
+            if (!(mob->q[s][p][i][1] > 0.0)) return AMPE_ERR_INVALID;  // ln(a1)
+         for (int n = 0; n < 4; n++)
+            if (!(mob->qq[s][p][n][1] > 0.0)) return AMPE_ERR_INVALID;
+      }
    return AMPE_OK;
 }
 
@@ -472,50 +490,6 @@ __global__ void k_kim_mobility(ampe_model_t m, Grid g, const double* tfield, con
    }
 }
 
-// Q_i(T) and the interaction terms of one species' mobility in one phase
-// (CALPHADMobility.h getQ, getQQ0..3)
-__device__ __forceinline__ double mob_q(const double* a, double T)
-{
-   return a[0] + kGasR * T * log(a[1]) + a[2] * T * log(T) + a[3] / T;
-}
-
-__device__ __forceinline__ double mob_qq(const double* a, double T)
-{
-   return a[0] + kGasR * T * log(a[1]);
-}
-
-// atomic mobility of species s in phase p at composition (c0, c1 = 1 - c0)
-// (CALPHADMobility::getAtomicMobility and getDeltaG, binary form)
-__device__ __forceinline__ double atomic_mobility(const ampe_mobility_t& mb, int s, int p,
-                                                  double c0, double c1, double T)
-{
-   const double dc = c0 - c1;
-   const double dG =
-       c0 * mob_q(mb.q[s][p][0], T) + c1 * mob_q(mb.q[s][p][1], T) +
-       c0 * c1 *
-           (mob_qq(mb.qq[s][p][0], T) +
-            dc * (mob_qq(mb.qq[s][p][1], T) +
-                  dc * (mob_qq(mb.qq[s][p][2], T) + dc * mob_qq(mb.qq[s][p][3], T))));
-   const double rtinv = 1.0 / (kGasR * T);
-   return exp(dG * rtinv) * rtinv;
-}
-
-// D_p = (mobility matrix) x (free-energy curvature), 1x1 for a binary
-// (computeLocalDiffusionMatrixL/A with computeDiffusionMobilityBinaryPhase)
-__device__ __forceinline__ double phase_diffusion(const ampe_model_t& m,
-                                                  const ampe_mobility_t& mb, int p, double c,
-                                                  double T)
-{
-   const double c1 = 1.0 - c;
-   const double m0 = atomic_mobility(mb, 0, p, c, c1, T);
-   const double m1 = atomic_mobility(mb, 1, p, c, c1, T);
-   const double mm = c * m1 + c1 * m0;
-   const double mob = c * c1 * mm * 1.e12;
-   const ThermoCoef th = thermo_coef(m, T);
-   const double d2f = th.RT / (c * (1.0 - c)) + dxi_of(th, c, p);
-   return mob * d2f;
-}
-
 __global__ void k_conc_diffusion_mobility(ampe_model_t m, ampe_mobility_t mb, Grid g,
                                           const double* phi, const double* temp,
                                           const double* cl, const double* cs, double* dl0,
@@ -725,13 +699,7 @@ int ampe_conc_diffusion_mobility(const ampe_model_t* m, const ampe_mobility_t* m
       return AMPE_ERR_INVALID;
    if (m->dim == 3 && (!dl2 || !ds2)) return AMPE_ERR_INVALID;
    if (m->temp_mode == AMPE_TEMP_FIELD && !temp) return AMPE_ERR_INVALID;
-   for (int s = 0; s < 2; s++)
-      for (int p = 0; p < 2; p++) {
-         for (int i = 0; i < 2; i++)
-            if (!(mob->q[s][p][i][1] > 0.0)) return AMPE_ERR_INVALID;  // ln(a1)
-         for (int n = 0; n < 4; n++)
-            if (!(mob->qq[s][p][n][1] > 0.0)) return AMPE_ERR_INVALID;
-      }
+   if (check_mobility(mob)) return AMPE_ERR_INVALID;
    Grid g = make_grid(*m);
    const long long tot = g.nfx() + g.nfy() + (g.dim == 3 ? g.nfz() : 0);
    k_conc_diffusion_mobility<<<blocks_for(tot), 256, 0, S(stream)>>>(

@@ -785,6 +785,28 @@ __device__ __forceinline__ void face_diff(const ampe_model_t& m,
    DS = hphi * dq.y;
 }
 
+// face weights with the composition-dependent D_L, D_S of the atomic
+// mobilities, evaluated in FP64 at the face means of the FP32 cL, cS of this
+// f(y) (MobilityCompositionDiffusionStrategy.cc:83-611) and rounded once
+template <int DIM, bool PB = false>
+__device__ __forceinline__ void face_diff_mob(const ampe_model_t& m, const Grid& g,
+                                              const double* tfield, const float* pf,
+                                              const float* cl, const float* cs,
+                                              long long lo, long long up, int a0,
+                                              int a1, int a2, int ei, int ej, int ek,
+                                              float& DL, float& DS)
+{
+   const Types<PB> ty(m);
+   const float vphi = average_func(pf[lo], pf[up], ty.avg);
+   const float hphi = interp_func(vphi, ty.diff);
+   const double T = 0.5 * (temperature_at(m, g, tfield, a0, a1, a2) +
+                           temperature_at(m, g, tfield, a0 - ei, a1 - ej, a2 - ek));
+   const double cL = 0.5 * ((double)cl[up] + (double)cl[lo]);
+   const double cS = 0.5 * ((double)cs[up] + (double)cs[lo]);
+   DL = (1.f - hphi) * d2f(phase_diffusion(m, m.mobility, 0, cL, T));
+   DS = hphi * d2f(phase_diffusion(m, m.mobility, 1, cS, T));
+}
+
 // temperature of cell (i,j,k) in FP32 (ghost cells take their periodic image)
 __device__ __forceinline__ float temp_f(const ampe_model_t& m, const MixParams& mp,
                                         const Grid& g, const double* tfield, int i,
@@ -906,6 +928,8 @@ __global__ void k_face_weights(ampe_model_t m, MixParams mp, Grid g, const doubl
          if (mp.kksc)
             kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, up, i, j, k, ei, ej, ek, a,
                                    b);
+         else if (m.conc_diffusion == AMPE_DIFF_MOBILITY)
+            face_diff_mob<DIM, PB>(m, g, tfield, pf, cl, cs, lo, up, i, j, k, ei, ej, ek, a, b);
          else
             face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, up, i, j, k, ei, ej, ek, a, b);
          const int f = dir == 0 ? g.fx(i, j, k) : (dir == 1 ? g.fy(i, j, k) : g.fz(i, j, k));

@@ -141,9 +141,11 @@ __global__ void k_coarsen_faces(Grid gf, Grid gc, int dir, const R* src,
 // EBSCompositionRHSStrategy.cc:330-420, then ConcFACOps.cc:28-60)
 template <class R>
 __global__ void k_conc_precond_faces(ampe_model_t m, Grid g, const double* phi,
+                                     const double* cld, const double* csd,
                                      const double* tfield, double gamma,
                                      R* D0, R* D1, R* D2)
 {
+   const bool mob = m.conc_diffusion == AMPE_DIFF_MOBILITY;
    const double qlR = m.Q_liquid / kGasR, qsR = m.Q_solid / kGasR;
    const bool tdep = m.Q_liquid != 0.0 || m.Q_solid != 0.0;
    const long long nz = g.dim == 3 ? g.nfz() : 0;
@@ -158,7 +160,13 @@ __global__ void k_conc_precond_faces(ampe_model_t m, Grid g, const double* phi,
       const double hphi = interp_func(
           vphi, m.conc_form == AMPE_CONC_KKS ? m.energy_interp : m.diff_interp);
       double dlq = m.D_liquid, dsq = m.D_solid;  // exp(0) = 1 exactly
-      if (tdep) {
+      if (mob) {
+         const long long up = g.c(i, j, k), lo = g.c(i - ei, j - ej, k - ek);
+         const double T = 0.5 * (temperature_at(m, g, tfield, i, j, k) +
+                                 temperature_at(m, g, tfield, i - ei, j - ej, k - ek));
+         dlq = phase_diffusion(m, m.mobility, 0, 0.5 * (cld[up] + cld[lo]), T);
+         dsq = phase_diffusion(m, m.mobility, 1, 0.5 * (csd[up] + csd[lo]), T);
+      } else if (tdep) {
          const double invT = 2.0 / (temperature_at(m, g, tfield, i - ei, j - ej, k - ek) +
                                     temperature_at(m, g, tfield, i, j, k));
          dlq = m.D_liquid * exp(-qlR * invT);
@@ -721,7 +729,7 @@ static void conc_precond_faces(Stepper& S, const double* tf, double gamma,
 {
    const long long nf = S.g.nfx() + S.g.nfy() + (S.g.dim == 3 ? S.g.nfz() : 0);
    k_conc_precond_faces<double><<<map_blocks(nf), 256, 0, S.s>>>(
-       S.m, S.g, S.phi_lag, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
+       S.m, S.g, S.phi_lag, S.cl_nf, S.cs_nf, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
    launch_status();
 }
 
@@ -1503,6 +1511,11 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
       if (p->precision == 1 && m->evolve_quat) return AMPE_ERR_INVALID;
    }
    if (m->evolve_quat && (m->quat_mobility_type != 'p' || !(m->quat_grad_floor > 0.0)))
+      return AMPE_ERR_INVALID;
+   // the mobility diffusivities belong to the "ebs" form and take the
+   // CALPHAD free-energy curvature
+   if (m->conc_diffusion == AMPE_DIFF_MOBILITY &&
+       (m->conc_form != AMPE_CONC_EBS || m->thermo != AMPE_THERMO_CALPHAD))
       return AMPE_ERR_INVALID;
    if (ampe_device_count() < 1) return AMPE_ERR_NO_DEVICE;
    Stepper* S = new (std::nothrow) Stepper;

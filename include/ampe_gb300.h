@@ -64,6 +64,9 @@ extern "C" {
 #define AMPE_CONC_EBS 0
 #define AMPE_CONC_KKS 1
 
+#define AMPE_DIFF_ARRHENIUS 0
+#define AMPE_DIFF_MOBILITY 1
+
 /* temperature sources */
 #define AMPE_TEMP_CONSTANT 0 /* T = T0 everywhere */
 #define AMPE_TEMP_GRADIENT 1 /* T = T0 + gradT * (i + 0.5) * dx[0], analytic */
@@ -82,6 +85,20 @@ typedef struct ampe_gterm {
    double d2[AMPE_MAX_TSEG], d3[AMPE_MAX_TSEG], d4[AMPE_MAX_TSEG];
    double d7[AMPE_MAX_TSEG], dm1[AMPE_MAX_TSEG], dm9[AMPE_MAX_TSEG];
 } ampe_gterm_t;
+
+/* CALPHAD atomic mobilities of a binary alloy, one set per species and phase
+ * (CALPHADMobility::initialize, CALPHADMobility.cc:17-150: the
+ * MobilityParameters block of a thermodynamic database).  For species s in
+ * phase p (0 liquid "PhaseL", 1 solid "PhaseA"):
+ *   q[s][p][i]  = (a0, a1, a2, a3) of qA (i = 0) and qB (i = 1):
+ *                 Q_i(T) = a0 + R T ln(a1) + a2 T ln(T) + a3 / T
+ *                 (a2 = a3 = 0 when the database gives two values);
+ *   qq[s][p][n] = (a0, a1) of q<n>AB, n = 0..3: a0 + R T ln(a1), (0, 1)
+ *                 when absent. */
+typedef struct ampe_mobility {
+   double q[2][2][2][4];
+   double qq[2][2][4][2];
+} ampe_mobility_t;
 
 typedef struct ampe_model {
    /* ---- grid: one uniform periodic patch level ---- */
@@ -144,6 +161,17 @@ typedef struct ampe_model {
     * default.  Only interior faces are read or written.  The stepper keeps
     * its own face arrays and ignores it. */
    int ng_side;
+
+   /* ---- composition diffusivities of the "ebs" form (diffusion_type,
+    * QuatModelParameters.cc:238-249; the strategy QuatModel.cc:375-395 and
+    * CompositionDiffusionStrategyFactory.h:36-95 build) ---- */
+   int conc_diffusion; /* AMPE_DIFF_ARRHENIUS: D_liquid, D_solid above
+                        * (temperature_dependent); AMPE_DIFF_MOBILITY: from
+                        * `mobility` at the face means of cL, cS and T
+                        * (composition_dependent, the reference's default for
+                        * "ebs"; see ampe_conc_diffusion_mobility) */
+   int pad2;
+   ampe_mobility_t mobility;
 } ampe_model_t;
 
 /* Integrator / preconditioner controls (QuatIntegrator.cc:278-301,
@@ -302,20 +330,6 @@ int ampe_kim_mobility(const ampe_model_t* m, const double* temp,
                       double Q0, double molar_volume, double* mobility,
                       void* stream);
 
-/* CALPHAD atomic mobilities of a binary alloy, one set per species and phase
- * (CALPHADMobility::initialize, CALPHADMobility.cc:17-150: the
- * MobilityParameters block of a thermodynamic database).  For species s in
- * phase p (0 liquid "PhaseL", 1 solid "PhaseA"):
- *   q[s][p][i]  = (a0, a1, a2, a3) of qA (i = 0) and qB (i = 1):
- *                 Q_i(T) = a0 + R T ln(a1) + a2 T ln(T) + a3 / T
- *                 (a2 = a3 = 0 when the database gives two values);
- *   qq[s][p][n] = (a0, a1) of q<n>AB, n = 0..3: a0 + R T ln(a1), (0, 1)
- *                 when absent. */
-typedef struct ampe_mobility {
-   double q[2][2][2][4];
-   double qq[2][2][4][2];
-} ampe_mobility_t;
-
 /* Composition-dependent diffusion from atomic mobilities, binary alloy
  * (MobilityCompositionDiffusionStrategy::setDiffusion,
  * MobilityCompositionDiffusionStrategy.cc:83-611, with
@@ -351,8 +365,10 @@ int ampe_computerhsconcentration(const ampe_model_t* m, const double* flux0,
 /* Whole phi+c right-hand side of QuatIntegrator::evaluateRHSFunction
  * (QuatIntegrator.cc:3134-3295) for given cL, cS (already computed on the
  * ghost box): phase flux + well + driving force times M_phi, and
- * composition M_c div(D_L grad cL + D_S grad cS).  phi, cl, cs, temp with
- * ghosts filled; outputs with ghost width 0. */
+ * composition M_c div(D_L grad cL + D_S grad cS), D_L and D_S of the
+ * model's conc_diffusion (AMPE_DIFF_MOBILITY: at the face means of these
+ * cL, cS).  phi, cl, cs, temp with ghosts filled; outputs with ghost
+ * width 0. */
 int ampe_rhs_phase_conc(const ampe_model_t* m, const double* phi,
                         const double* quat, const double* temp,
                         const double* cl, const double* cs, double* phi_rhs,

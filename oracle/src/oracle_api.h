@@ -66,6 +66,21 @@ void orc_rhs_phase_conc_q(const ampe_model_t* m, const double* phi,
                           const double* cl, const double* cs,
                           const double* phi_d, const double* ogm,
                           double* phi_rhs, double* conc_rhs);
+/* as orc_rhs_phase_conc_q with the face diffusivities at (phi_d, cl_d, cs_d)
+ * (the lagged fields of finite-difference Jacobian evaluations) */
+void orc_rhs_phase_conc_qd(const ampe_model_t* m, const double* phi,
+                           const double* quat, const double* temp,
+                           const double* cl, const double* cs,
+                           const double* phi_d, const double* cl_d,
+                           const double* cs_d, const double* ogm,
+                           double* phi_rhs, double* conc_rhs);
+/* the face diffusivities of the model's conc_diffusion: Arrhenius
+ * (orc_conc_diffusion) or the atomic mobilities at the face means of
+ * cl_d, cs_d (orc_conc_diffusion_mobility) */
+void orc_conc_diffusion_model(const ampe_model_t* m, const double* phi,
+                              const double* temp, const double* cl_d,
+                              const double* cs_d, double* dl0, double* dl1,
+                              double* dl2, double* ds0, double* ds1, double* ds2);
 /* quaternion kernels (quat.cc) */
 void orc_quat_grad_modulus(const ampe_model_t* m, const double* q, double* ogm);
 void orc_quat_mobility(const ampe_model_t* m, const double* phi, double* mq);

@@ -448,6 +448,32 @@ void orc_rhs_phase_conc_q(const ampe_model_t* m, const double* phi,
                           const double* phi_d, const double* ogm,
                           double* phi_rhs, double* conc_rhs)
 {
+   orc_rhs_phase_conc_qd(m, phi, quat, temp, cl, cs, phi_d, cl, cs, ogm, phi_rhs,
+                         conc_rhs);
+}
+
+// QuatModel.cc:375-395 / CompositionDiffusionStrategyFactory.h:36-95: the
+// "ebs" form's diffusivities, temperature_dependent or composition_dependent
+void orc_conc_diffusion_model(const ampe_model_t* m, const double* phi,
+                              const double* temp, const double* cl_d,
+                              const double* cs_d, double* dl0, double* dl1,
+                              double* dl2, double* ds0, double* ds1, double* ds2)
+{
+   if (m->conc_diffusion == AMPE_DIFF_MOBILITY)
+      orc_conc_diffusion_mobility(m, &m->mobility, phi, temp, cl_d, cs_d, dl0, dl1, dl2,
+                                  ds0, ds1, ds2, nullptr, nullptr, nullptr, nullptr,
+                                  nullptr, nullptr);
+   else
+      orc_conc_diffusion(m, phi, temp, dl0, dl1, dl2, ds0, ds1, ds2);
+}
+
+void orc_rhs_phase_conc_qd(const ampe_model_t* m, const double* phi,
+                           const double* quat, const double* temp,
+                           const double* cl, const double* cs,
+                           const double* phi_d, const double* cl_d,
+                           const double* cs_d, const double* ogm,
+                           double* phi_rhs, double* conc_rhs)
+{
    Layout L(*m);
    std::vector<double> f0(L.nfx()), f1(L.nfy()), f2(L.dim == 3 ? L.nfz() : 1);
    orc_phase_flux(m, phi, quat, f0.data(), f1.data(), f2.data());
@@ -459,8 +485,8 @@ void orc_rhs_phase_conc_q(const ampe_model_t* m, const double* phi,
 
    std::vector<double> dl0(L.nfx()), dl1(L.nfy()), dl2(f2.size());
    std::vector<double> ds0(L.nfx()), ds1(L.nfy()), ds2(f2.size());
-   orc_conc_diffusion(m, phi_d ? phi_d : phi, temp, dl0.data(), dl1.data(),
-                      dl2.data(), ds0.data(), ds1.data(), ds2.data());
+   orc_conc_diffusion_model(m, phi_d ? phi_d : phi, temp, cl_d, cs_d, dl0.data(),
+                            dl1.data(), dl2.data(), ds0.data(), ds1.data(), ds2.data());
    std::fill(f0.begin(), f0.end(), 0.0);
    std::fill(f1.begin(), f1.end(), 0.0);
    std::fill(f2.begin(), f2.end(), 0.0);
@@ -522,8 +548,8 @@ void orc_jv_analytic(const ampe_model_t* m, const double* phi,
    // composition part
    std::vector<double> l0(L.nfx()), l1(L.nfy()), l2(f2.size());
    std::vector<double> s0(L.nfx()), s1(L.nfy()), s2(f2.size());
-   orc_conc_diffusion(m, phi, nullptr, l0.data(), l1.data(), l2.data(),
-                      s0.data(), s1.data(), s2.data());
+   orc_conc_diffusion_model(m, phi, nullptr, cl, cs, l0.data(), l1.data(), l2.data(),
+                            s0.data(), s1.data(), s2.data());
    std::fill(f0.begin(), f0.end(), 0.0);
    std::fill(f1.begin(), f1.end(), 0.0);
    std::fill(f2.begin(), f2.end(), 0.0);

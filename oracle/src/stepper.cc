@@ -105,9 +105,9 @@ void eval_rhs(OStepper& s, const double* y, double* fy, int fd_flag)
    const double* qflux = nullptr;
    if (s.m.flux_type == AMPE_FLUX_ANISOTROPIC)
       qflux = quat ? s.q_g.data() : s.qorient.data();
-   orc_rhs_phase_conc_q(&s.m, s.phi_g.data(), qflux, temp_ptr(s),
-                        s.cl.data(), s.cs.data(), s.phi_lag.data(),
-                        quat ? s.ogm.data() : nullptr, fy, fy + s.N);
+   orc_rhs_phase_conc_qd(&s.m, s.phi_g.data(), qflux, temp_ptr(s), s.cl.data(),
+                         s.cs.data(), s.phi_lag.data(), s.cl_nf.data(), s.cs_nf.data(),
+                         quat ? s.ogm.data() : nullptr, fy, fy + s.N);
    if (s.m.conc_form == AMPE_CONC_KKS) {
       // "kks" composition form: coefficients from the lagged phi, cL, cS
       // (QuatIntegrator.cc:3266-3267), differences of the current phi and c
@@ -153,8 +153,9 @@ void precond_setup(OStepper& s, double gamma)
    std::vector<double> s0(L.nfx()), s1(L.nfy()), s2(l2.size());
    ampe_model_t mp = s.m;  // the "kks" form's D0 uses the energy interpolation
    if (s.m.conc_form == AMPE_CONC_KKS) mp.diff_interp = s.m.energy_interp;
-   orc_conc_diffusion(&mp, s.phi_lag.data(), temp_ptr(s), l0.data(),
-                      l1.data(), l2.data(), s0.data(), s1.data(), s2.data());
+   orc_conc_diffusion_model(&mp, s.phi_lag.data(), temp_ptr(s), s.cl_nf.data(),
+                            s.cs_nf.data(), l0.data(), l1.data(), l2.data(), s0.data(),
+                            s1.data(), s2.data());
    for (long f = 0; f < L.nfx(); f++) s.Dc[0][f] = -gamma * (l0[f] + s0[f]);
    for (long f = 0; f < L.nfy(); f++) s.Dc[1][f] = -gamma * (l1[f] + s1[f]);
    if (L.dim == 3)

@@ -143,17 +143,29 @@ def run(make_stepper, t_end=0.3, dt_max=2.0e-3, atol=1.0e-6, precision=0,
     return out
 
 
+def temperature(t):
+    """ScalarTemperatureStrategy::getCurrentTemperature
+    (ScalarTemperatureStrategy.cc:57-73) with the deck's 1450 K, -200 K per
+    unit time and target 1220 K."""
+    return max(1450.0 - 200.0 * t, 1220.0)
+
+
 def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
-                 interval=0.03, max_steps=100000):
+                 interval=0.03, max_steps=100000, case=None, mg_levels=4):
     """The deck's own integration: CVODE-style variable steps (orders 1-2,
     atol 1e-4 and rtol = atol / 100 as QuatIntegrator.cc:283-289 derives
     them from 3d.input:80-81, initial step h0), one accepted step per call
     (CV_ONE_STEP, QuatIntegrator.cc:1575) up to t_end, the temperature of
-    each step set from its start time (T = 1450 K - 200 K t, 3d.input:
-    20-25).  Returns the same record as run()."""
-    m = model()
-    phi, c = initial_state()
-    p = configs.step_params(dt=h0, precond=2, mg_levels=4, atol=atol, precision=precision)
+    each step set from its start time (temperature(t), 3d.input:20-25).
+    case = (model, (phi, c)) runs another case the same way.  Returns the
+    same record as run()."""
+    if case is None:
+        m = model()
+        phi, c = initial_state()
+    else:
+        m, (phi, c) = case
+    p = configs.step_params(dt=h0, precond=2, mg_levels=mg_levels, atol=atol,
+                            precision=precision)
     p.adaptive = 1
     s = make_stepper(m, p)
     s.set_state(phi, c)
@@ -163,7 +175,7 @@ def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
     next_out, t = interval, 0.0
     st = None
     while t < t_end - 1e-12 and out["steps"] < max_steps:
-        T = 1450.0 - 200.0 * t
+        T = temperature(t)
         s.set_temperature(T)
         r = s.advance_to(t_end, 1)
         rc, st = r if isinstance(r, tuple) else (0, r)

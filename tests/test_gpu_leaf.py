@@ -2,12 +2,15 @@
 the same seeded inputs (FP64: relative L2 <= 1e-12; differences are FMA
 contraction only)."""
 import ctypes as C
+import json
+import os
 
 import numpy as np
 import pytest
 
 import oracle as O
 from ampe_gb300 import abi, configs
+from ampe_gb300.calphad_db import mobility_struct
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -69,6 +72,14 @@ def models():
     m.aniso_eps = 0.05
     m.qlen = 4
     out.append(("calphad3d_aniso", m))
+    # composition-dependent diffusivities from the AuNi atomic mobilities
+    m = configs.calphad3d(10, seed=3, T_run=1450.0)
+    m.n[1], m.n[2] = 8, 6
+    m.conc_diffusion = abi.DIFF_MOBILITY
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                           "calphad_AuNi.json")) as f:
+        m.mobility = mobility_struct(json.load(f)["mobility"])
+    out.append(("calphad3d_mobility", m))
     return out
 
 

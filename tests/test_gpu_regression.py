@@ -11,7 +11,14 @@ sequence.  Checks:
   composition at every output time, and the final phi and c as 8^3-cell
   block means -- FP64 within 1e-8, mixed within 1e-5;
 * per-field parity with a live oracle run over the first start-up steps
-  (FP64 within 1e-10, mixed within 1e-6)."""
+  (FP64 within 1e-10, mixed within 1e-6).
+
+And tests/SingleGrainGrowthAuNi (tests/singlegrain.py), whose deck takes
+the composition-dependent diffusivities of the database's atomic
+mobilities, integrated with the deck's variable steps: the reference's
+acceptance values (solid fraction 0.32 +- 0.01 at t = 0.3, composition
+integral constant to 1e-4, test2d.py:38-64) and the oracle's run of it
+(tests/golden/singlegrain_oracle.json)."""
 import json
 import os
 
@@ -145,3 +152,70 @@ def test_kkscomposition_deck_tolerances(cuda, precision):
     assert abs(r["t"][-1] - 0.3) < 1e-9
     assert abs(solid - K.SOLID_TARGET) <= K.SOLID_TOL
     assert abs(drift) < K.DRIFT_TOL
+
+
+# ---------------------------------------------------------------------------
+# SingleGrainGrowthAuNi: the composition-dependent (atomic-mobility)
+# diffusivities, integrated as the deck integrates it
+# ---------------------------------------------------------------------------
+_SG_RUNS = {}
+SG_TOL = {0: 1e-7, 1: 2e-3}
+
+
+def _sg_run(precision):
+    import singlegrain as SG
+
+    if precision not in _SG_RUNS:
+        _SG_RUNS[precision] = SG.run(lambda m, p: _Gpu(m, p), precision=precision)
+    return _SG_RUNS[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_singlegrain_regression(cuda, precision):
+    """The reference's acceptance values (test2d.py:38-64): solid fraction
+    0.32 +- 0.01 at t = 0.3, composition integral constant to 1e-4."""
+    import singlegrain as SG
+
+    r = _sg_run(precision)
+    solid, drift = r["solid"][-1], r["drift"]
+    h = np.array(r["h"])
+    print("SingleGrainGrowthAuNi GPU precision %d: solid fraction %.5f at t = %.4f, drift "
+          "%.2e, %d steps (h %.2e .. %.2e), %d failures" % (precision, solid, r["t"][-1], drift,
+                                                          r["steps"], h.min(), h.max(),
+                                                          r["rejected"]))
+    assert abs(r["t"][-1] - 0.3) < 1e-9
+    assert abs(solid - SG.SOLID_TARGET) <= SG.SOLID_TOL
+    assert abs(drift) < SG.DRIFT_TOL
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_singlegrain_vs_oracle(cuda, precision):
+    """The GPU run against the oracle's run of the same case (the committed
+    fixture, tests/golden/make_singlegrain.py), at the oracle's output
+    times.  Rounding differences (FMA contraction; the oracle's own
+    unordered reductions) reach the variable-step controller, so FP64 takes
+    the oracle's step sequence to within a couple of steps (sizes within
+    1e-3 when the counts agree) and its trajectory within 1e-7; the mixed
+    path chooses its own steps."""
+    import singlegrain as SG
+
+    r = _sg_run(precision)
+    with open(SG.FIXTURE) as f:
+        gold = json.load(f)
+    if precision == 0:
+        assert abs(r["steps"] - gold["steps"]) <= 2
+        if r["steps"] == gold["steps"]:
+            assert np.allclose(r["h"], gold["h"], rtol=1e-3, atol=0)
+    else:
+        assert abs(r["steps"] - gold["steps"]) <= 0.1 * gold["steps"]
+    assert abs(r["t"][-1] - gold["t"][-1]) < 1e-12
+    solid = np.interp(gold["t"], r["t"], r["solid"])
+    cmean = np.interp(gold["t"], r["t"], r["cmean"])
+    ds = np.max(np.abs(solid - gold["solid"]))
+    dc = np.max(np.abs(cmean - gold["cmean"]))
+    eb = {f: O.rel_l2(SG.block_means(r[f], gold["block"]).ravel(), np.array(gold[f + "_blocks"]))
+          for f in ("phi", "c")}
+    print("  vs oracle: %d / %d steps, max |d solid| %.2e, max |d cmean| %.2e, block-mean rel "
+          "L2 phi %.2e c %.2e" % (r["steps"], gold["steps"], ds, dc, eb["phi"], eb["c"]))
+    assert ds <= SG_TOL[precision] and dc <= SG_TOL[precision]
+    assert eb["phi"] <= SG_TOL[precision] and eb["c"] <= SG_TOL[precision]

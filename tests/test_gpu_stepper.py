@@ -69,3 +69,81 @@ def test_deterministic_and_conservative(cuda):
         assert np.array_equal(a, b)
     assert abs(out[0][1].mean() - c.mean()) < 1e-9
     assert out[0][0].max() <= 1.05 and out[0][0].min() >= -0.05
+
+
+def _mobility_case():
+    """SingleGrainGrowthAuNi (tests/singlegrain.py) at a quarter of its
+    resolution: the composition-dependent diffusivities of the atomic
+    mobilities on the stepper's path."""
+    import singlegrain as SG
+
+    return SG.case(16)
+
+
+def test_mobility_rhs_parity(cuda):
+    m, (phi, c) = _mobility_case()
+    p = configs.step_params(precond=2, mg_levels=3)
+    o = O.OracleStepper(m, p)
+    o.set_state(phi, c)
+    g = ImplicitStepper(m, p)
+    g.set_state(phi, c)
+    fo, fg = o.eval_rhs(), g.eval_rhs()
+    assert O.rel_l2(fg[0], fo[0]) <= 1e-11
+    assert O.rel_l2(fg[1], fo[1]) <= 1e-11
+    # the mobility diffusivities differ from the (unused) Arrhenius constants
+    m2 = _mobility_case()[0]
+    m2.conc_diffusion = 0
+    a = O.OracleStepper(m2, p)
+    a.set_state(phi, c)
+    assert O.rel_l2(a.eval_rhs()[1], fo[1]) > 1e-3
+
+
+@pytest.mark.parametrize("precond", [1, 2])
+def test_mobility_steps_parity(cuda, precond):
+    m, (phi, c) = _mobility_case()
+    p = configs.step_params(dt=2e-4, precond=precond, mg_levels=3, atol=1e-5)
+    o = O.OracleStepper(m, p)
+    o.set_state(phi, c)
+    rc, so = o.advance(4)
+    assert rc == 0
+    g = ImplicitStepper(m, p)
+    g.set_state(phi, c)
+    sg = g.advance(4)
+    for k in ("steps", "newton_iters", "gmres_iters", "rhs_evals", "precond_solves", "fac_cycles"):
+        assert sg[k] == so[k], (k, sg[k], so[k])
+    for a, b in zip(g.get_state(), o.get_state()):
+        assert O.rel_l2(a, b) <= 1e-10
+
+
+def test_mobility_mixed_steps(cuda):
+    """The mixed path (FP32 kernels, face weights from the FP32 cL, cS with
+    the mobility diffusivities in FP64) against the FP64 oracle."""
+    m, (phi, c) = _mobility_case()
+    p = configs.step_params(dt=2e-4, precond=2, mg_levels=3, atol=1e-5)
+    o = O.OracleStepper(m, p)
+    o.set_state(phi, c)
+    assert o.advance(4)[0] == 0
+    p.precision = 1
+    g = ImplicitStepper(m, p)
+    g.set_state(phi, c)
+    g.advance(4)
+    xo = o.get_state()
+    xg = g.get_state()
+    for f in range(2):
+        err = O.rel_l2(xg[f], xo[f])
+        print("mobility mixed field %d rel L2 %.2e" % (f, err))
+        assert err <= 2e-6
+
+
+def test_mobility_refused_forms(cuda):
+    from ampe_gb300._native import AmpeError
+
+    m, _ = _mobility_case()
+    p = configs.step_params(dt=2e-4)
+    m.conc_form = 1  # "kks" form: its own diffusivities
+    with pytest.raises(AmpeError):
+        ImplicitStepper(m, p)
+    m, _ = _mobility_case()
+    m.mobility.q[0][0][0][1] = 0.0  # ln(0) of a mobility term
+    with pytest.raises(AmpeError):
+        ImplicitStepper(m, p)
