@@ -60,7 +60,12 @@ def initial_state(nh=32, radius=16.0, c_in=0.096, c_nominal=0.25):
     return mirror(ph), mirror(c)
 
 
-def model(nh=32):
+def model(nh=32, mobility=False):
+    """The deck's model with its D_L, D_S constants, or (mobility=True) with
+    the reference's actual diffusivities for it: "composition_dependent",
+    from the database's atomic mobilities, the default for "ebs" when the
+    deck names no diffusion_type (its D_L, D_S are then not read,
+    QuatModelParameters.cc:238-260)."""
     n = 2 * nh
     m = configs._blank_model(3, (n, n, n))
     with open(os.path.join(GOLD, "calphad_AuNi.json")) as f:
@@ -80,6 +85,8 @@ def model(nh=32):
     m.avg_type, m.well_type = b"a", b"d"
     m.newton_max_its = 50
     m.temp_mode = abi.TEMP_CONSTANT
+    if mobility:
+        m.conc_diffusion = abi.DIFF_MOBILITY
     return m
 
 
@@ -91,14 +98,15 @@ def block_means(a, b=4):
 
 
 def run(make_stepper, t_end=0.3, dt_max=2.0e-3, atol=1.0e-6, precision=0,
-        interval=0.03, t_stop=None):
+        interval=0.03, t_stop=None, mobility=False):
     """Advance the case to t_end with make_stepper(model, params) steppers.
 
     Returns a dict: per output time (every `interval`, as the deck's
     ScalarDiagnostics) the time, temperature, solid fraction and mean
     composition; the final phi and c; the number of accepted and rejected
-    steps.  t_stop < t_end ends the run early (same step sequence)."""
-    m = model()
+    steps.  t_stop < t_end ends the run early (same step sequence);
+    mobility selects model(mobility=True)."""
+    m = model(mobility=mobility)
     phi, c = initial_state()
     cl = cs = None
     p = configs.step_params(dt=dt_max, precond=2, mg_levels=4, atol=atol,

@@ -154,6 +154,37 @@ def test_kkscomposition_deck_tolerances(cuda, precision):
     assert abs(drift) < K.DRIFT_TOL
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kkscomposition_mobility_start_parity(cuda, precision):
+    """The deck with the reference's actual diffusivities for it (atomic
+    mobilities, kkscomposition.model(mobility=True)): the first start-up
+    steps against a live oracle run."""
+    ro = K.run(lambda m, p: O.OracleStepper(m, p), t_stop=3e-5, mobility=True)
+    rg = K.run(lambda m, p: _Gpu(m, p), precision=precision, t_stop=3e-5, mobility=True)
+    assert rg["steps"] == ro["steps"] >= 2
+    for f in ("phi", "c"):
+        err = O.rel_l2(rg[f], ro[f])
+        print("KKScomposition (mobility) start-up precision %d %s rel L2 %.3e"
+              % (precision, f, err))
+        assert err <= START_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kkscomposition_mobility_deck(cuda, precision):
+    """The deck as the reference runs it: atomic-mobility diffusivities and
+    the deck's variable steps.  The reference's acceptance values hold."""
+    m = K.model(mobility=True)
+    r = K.run_adaptive(lambda m, p: _Gpu(m, p), precision=precision,
+                       case=(m, K.initial_state()))
+    solid, drift = r["solid"][-1], r["drift"]
+    print("KKScomposition (mobility) adaptive precision %d: solid fraction %.5f at t = %.4f, "
+          "drift %.2e, %d steps, %d failures" % (precision, solid, r["t"][-1], drift,
+                                                 r["steps"], r["rejected"]))
+    assert abs(r["t"][-1] - 0.3) < 1e-9
+    assert abs(solid - K.SOLID_TARGET) <= K.SOLID_TOL
+    assert abs(drift) < K.DRIFT_TOL
+
+
 # ---------------------------------------------------------------------------
 # SingleGrainGrowthAuNi: the composition-dependent (atomic-mobility)
 # diffusivities, integrated as the deck integrates it
