@@ -905,8 +905,10 @@ __global__ void k_rhs_mixed(ampe_model_t m, MixParams mp, Grid g, AnisoF an, Fac
 // composition flux weights of every face (EBS: (1-h) D_L, h D_S with h =
 // diff_interp; "kks": D0, D_phi).  One thread per point (i, j, k) of the box
 // [0, n0] x [0, n1] x [0, n2] computes the lower x, y and z faces of cell
-// (i, j, k) that exist, sharing the cell's index math and loads.
-template <int DIM, bool PB>
+// (i, j, k) that exist, sharing the cell's index math and loads.  MOB: the
+// atomic-mobility diffusivities (their FP64 arithmetic in an instantiation
+// of its own, so the others keep their registers).
+template <int DIM, bool PB, bool MOB>
 __global__ void k_face_weights(ampe_model_t m, MixParams mp, Grid g, const double* tfield,
                                const float* __restrict__ pf, const float* __restrict__ cl,
                                const float* __restrict__ cs, FaceW fw)
@@ -928,7 +930,7 @@ __global__ void k_face_weights(ampe_model_t m, MixParams mp, Grid g, const doubl
          if (mp.kksc)
             kks_face_coef<DIM, PB>(m, mp, g, tfield, pf, cl, cs, lo, up, i, j, k, ei, ej, ek, a,
                                    b);
-         else if (m.conc_diffusion == AMPE_DIFF_MOBILITY)
+         else if (MOB)
             face_diff_mob<DIM, PB>(m, g, tfield, pf, cl, cs, lo, up, i, j, k, ei, ej, ek, a, b);
          else
             face_diff<DIM, PB>(m, mp, g, tfield, pf, lo, up, i, j, k, ei, ej, ek, a, b);
@@ -955,17 +957,26 @@ int rhs_mixed(const ampe_model_t& m, const MixParams& mp, const Grid& g,
           (long long)(g.n0 + 1) * (g.n1 + 1) * (g.dim == 3 ? g.n2 + 1 : 1);
       long long bf = (tot + 255) / 256;
       if (bf > max_blocks()) bf = max_blocks();
-      if (g.dim == 3) {
-         if (mp.pb)
-            k_face_weights<3, true><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+      const bool mob = !mp.kksc && m.conc_diffusion == AMPE_DIFF_MOBILITY;
+#define AMPE_FW(D, P, M) \
+   k_face_weights<D, P, M><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw)
+      if (mob) {
+         if (g.dim == 3)
+            AMPE_FW(3, false, true);
          else
-            k_face_weights<3, false><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+            AMPE_FW(2, false, true);
+      } else if (g.dim == 3) {
+         if (mp.pb)
+            AMPE_FW(3, true, false);
+         else
+            AMPE_FW(3, false, false);
       } else {
          if (mp.pb)
-            k_face_weights<2, true><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+            AMPE_FW(2, true, false);
          else
-            k_face_weights<2, false><<<(unsigned)bf, 256, 0, s>>>(m, mp, g, tfield, pf, cl, cs, fw);
+            AMPE_FW(2, false, false);
       }
+#undef AMPE_FW
       launch_status();
    }
    b = (g.cells() + 255) / 256;

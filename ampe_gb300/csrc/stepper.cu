@@ -139,13 +139,12 @@ __global__ void k_coarsen_faces(Grid gf, Grid gc, int dir, const R* src,
 // composition preconditioner faces: D = -gamma (D_L + D_S) at the faces
 // (EBSCompositionRHSStrategy::setDiffusionCoeffForPreconditioner,
 // EBSCompositionRHSStrategy.cc:330-420, then ConcFACOps.cc:28-60)
-template <class R>
+template <class R, bool MOB>
 __global__ void k_conc_precond_faces(ampe_model_t m, Grid g, const double* phi,
                                      const double* cld, const double* csd,
                                      const double* tfield, double gamma,
                                      R* D0, R* D1, R* D2)
 {
-   const bool mob = m.conc_diffusion == AMPE_DIFF_MOBILITY;
    const double qlR = m.Q_liquid / kGasR, qsR = m.Q_solid / kGasR;
    const bool tdep = m.Q_liquid != 0.0 || m.Q_solid != 0.0;
    const long long nz = g.dim == 3 ? g.nfz() : 0;
@@ -160,7 +159,7 @@ __global__ void k_conc_precond_faces(ampe_model_t m, Grid g, const double* phi,
       const double hphi = interp_func(
           vphi, m.conc_form == AMPE_CONC_KKS ? m.energy_interp : m.diff_interp);
       double dlq = m.D_liquid, dsq = m.D_solid;  // exp(0) = 1 exactly
-      if (mob) {
+      if (MOB) {
          const long long up = g.c(i, j, k), lo = g.c(i - ei, j - ej, k - ek);
          const double T = 0.5 * (temperature_at(m, g, tfield, i, j, k) +
                                  temperature_at(m, g, tfield, i - ei, j - ej, k - ek));
@@ -728,8 +727,12 @@ static void conc_precond_faces(Stepper& S, const double* tf, double gamma,
                                DevLevel<double>& C0)
 {
    const long long nf = S.g.nfx() + S.g.nfy() + (S.g.dim == 3 ? S.g.nfz() : 0);
-   k_conc_precond_faces<double><<<map_blocks(nf), 256, 0, S.s>>>(
-       S.m, S.g, S.phi_lag, S.cl_nf, S.cs_nf, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
+   if (S.m.conc_diffusion == AMPE_DIFF_MOBILITY)
+      k_conc_precond_faces<double, true><<<map_blocks(nf), 256, 0, S.s>>>(
+          S.m, S.g, S.phi_lag, S.cl_nf, S.cs_nf, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
+   else
+      k_conc_precond_faces<double, false><<<map_blocks(nf), 256, 0, S.s>>>(
+          S.m, S.g, S.phi_lag, S.cl_nf, S.cs_nf, tf, gamma, C0.D[0], C0.D[1], C0.D[2]);
    launch_status();
 }
 
