@@ -119,7 +119,8 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD && MODE != 2) ? 3 
    const int dxm = x == 0 ? n0 - 1 : -1;  // offsets of the periodic x neighbours
    const int dxp = x == n0 - 1 ? 1 - n0 : 1;
    const int j0 = blockIdx.x * TY;
-   const int k0 = blockIdx.y * kz, k1 = k0 + kz;
+   // the last chunk may be shorter (launches sized to one wave of blocks)
+   const int k0 = blockIdx.y * kz, k1 = min(k0 + kz, g.n2);
    // wrapped y index of ring row r (the block's rows and two halo rows on
    // each side) and its ghosted row offset, formed where they are used (a
    // few integer operations, no registers held and no load in front of the
@@ -348,6 +349,20 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && !HD && MODE != 2) ? 3 
    }
 }
 
+// planes per z chunk so that the launch's n1/ty x ceil(n2/kz) blocks fill the
+// SMs' resident slots (bps blocks per SM) in one wave: a second, partly
+// filled wave would leave most SMs idle for its whole duration.  Chunks of
+// at least 8 planes (each stages 4 planes and updates 2 red planes more
+// than it stores); the last chunk takes the remainder.
+static int wave_kz(const Grid& g, int ty, int bps)
+{
+   const long long by = g.n1 / ty;
+   const long long slots = (long long)device_sms() * std::max(1, bps);
+   long long nz = std::max(1LL, slots / by);
+   nz = std::min(nz, (long long)std::max(1, g.n2 / 8));
+   return (int)((g.n2 + nz - 1) / nz);
+}
+
 template <class R>
 static ZShape choose_zshape(const Grid& g)
 {
@@ -358,17 +373,9 @@ static ZShape choose_zshape(const Grid& g)
    // coefficients of 8 rows do not fit the register budget)
    zs.ty = sizeof(R) == 4 ? 8 : 4;
    if (zsweep_smem_bytes<R>(zs) > 74 * 1024) zs.ty = 4;
-   // planes per block: the most that still give every SM two blocks, at
-   // least 8 (each chunk stages 4 planes and updates 2 red planes twice)
-   const int by = g.n1 / zs.ty;
-   const int target = 2 * device_sms();
-   int best = g.n2;
-   for (int kz = g.n2; kz >= 8; kz--) {
-      if (g.n2 % kz) continue;
-      best = kz;
-      if ((long long)by * (g.n2 / kz) >= target) break;
-   }
-   zs.kz = best;
+   // planes per block: a default for two resident blocks per SM; each
+   // launch sizes its chunks to the blocks its kernel keeps resident
+   zs.kz = wave_kz(g, zs.ty, 2);
    return zs;
 }
 
@@ -379,7 +386,7 @@ bool sweep_z_ok(const Grid& g, ZShape* out)
    if (g.n0 % 32 || g.n0 > 256 || g.n1 % 2 || g.n2 % 2) return false;
    if (g.cells() < (1LL << 21)) return false;  // small levels: colour kernels
    const ZShape zs = choose_zshape<R>(g);
-   if (g.n1 % zs.ty || g.n2 % zs.kz || zs.kz < 8) return false;
+   if (g.n1 % zs.ty) return false;
    if (zsweep_smem_bytes<R>(zs) > 200 * 1024) return false;
    if (out) *out = zs;
    return true;
@@ -390,13 +397,27 @@ static int launch_ty(const FacOp<R>& op, const Grid& g, const ZShape& zs, const 
                      const R* uin, R* uout, const Grid& gc, const R* e, cudaStream_t s)
 {
    const int smem = (int)zsweep_smem_bytes<R>(zs);
+   auto* fn = k_sweep_z<R, HD, HC, HM, MODE, TY>;
    static std::atomic<unsigned long long> attr{0};
    if (first_on_device(attr))
-      cudaFuncSetAttribute(k_sweep_z<R, HD, HC, HM, MODE, TY>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-   const dim3 grid(g.n1 / TY, g.n2 / zs.kz);
-   k_sweep_z<R, HD, HC, HM, MODE, TY>
-       <<<grid, g.n0, smem, s>>>(op, g, zs.kz, f, uin, uout, gc, e);
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+   // resident blocks per SM of this instance at this block size (queried
+   // once per device and block size)
+   constexpr int kDevs = 64;
+   static std::atomic<int> bps_of[kDevs];
+   int dev = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevs) dev = 0;
+   int packed = bps_of[dev].load(std::memory_order_relaxed);
+   int bps = packed & 0xff;
+   if (!packed || (packed >> 8) != g.n0) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, g.n0, smem) != cudaSuccess ||
+          bps < 1)
+         bps = 1;
+      bps_of[dev].store((g.n0 << 8) | std::min(bps, 255), std::memory_order_relaxed);
+   }
+   const int kz = wave_kz(g, TY, bps);
+   const dim3 grid(g.n1 / TY, (g.n2 + kz - 1) / kz);
+   fn<<<grid, g.n0, smem, s>>>(op, g, kz, f, uin, uout, gc, e);
    return launch_status();
 }
 
