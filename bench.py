@@ -58,8 +58,8 @@ SMOOTH_BYTES_PER_CELL_FP64 = {3: 40, 2: 36}
 # 3D CALPHAD phi + c level, from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) of the z-marching sweep's four launch kinds (phase
 # and composition blocks, from zero and with the fused prolongation) at
-# 224^3, averaged: 206.9 MB per launch over 11,239,424 cells
-SMOOTH_DRAM_BYTES_PER_CELL_MEASURED = 18.4
+# 224^3, averaged: 205.8 MB per launch over 11,239,424 cells
+SMOOTH_DRAM_BYTES_PER_CELL_MEASURED = 18.3
 # MLP inference: 2 (3*64 + 64*64 + 64*64 + 64*2) multiply-adds per cell
 MLP_FLOPS_PER_CELL = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
 KERNEL_NAMES = {
