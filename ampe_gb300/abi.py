@@ -93,6 +93,8 @@ class Model(C.Structure):
         ("conc_diffusion", C.c_int),
         ("pad2", C.c_int),
         ("mobility", Mobility),
+        ("dTdt", C.c_double),
+        ("T_target", C.c_double),
     ]
 
     def cells(self):

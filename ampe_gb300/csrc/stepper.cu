@@ -510,6 +510,7 @@ struct Stepper {
    double h_next = 0.0, h1 = 0.0, h2 = 0.0, eta_max = 1.0e4;
    int q_next = 1, qwait = 2, nhist = 0;
    bool fn_valid = false;
+   double T_start = 0.0;  // T0 at t = 0 of a model with dTdt != 0
    double t = 0.0;
    ampe_step_stats_t st;
    // optional per-kernel CUDA-event timing on the stepper's stream
@@ -1080,6 +1081,47 @@ static int gmres32(Stepper& S, double gamma, const float* bf, double* x,
 // Newton iteration of one BDF step: y - gamma f(y) = a from the predictor
 // in S.y, convergence test del min(1, crate) <= newton_coef; result in
 // S.ynew.  0 = converged.
+// the temperature-dependent state after a change of S.m.T0 / gradT: the
+// FP32 constants, the per-x thermodynamic and diffusivity tables, the
+// network's copy of the model (launches on the stepper's stream, no wait)
+static int apply_temperature(Stepper& S)
+{
+   const float2* dq = S.mp.dq;
+   S.mp = make_mix_params(S.m);
+   S.mp.dq = dq;
+   const int nt = S.m.temp_mode == AMPE_TEMP_GRADIENT ? S.m.n[0] : 1;
+   int err = AMPE_OK;
+   if (S.tab) err = build_thermo_table(S.m, S.tab, nt, S.s);
+   if (!err && S.tabf) err = build_coef_f(S.tab, S.tabf, nt, S.s);
+   if (!err && S.dqtab) err = build_diff_table(S.m, S.mp, S.g, S.dqtab, S.s);
+   if (S.mlp) {  // the network sees the stepper's temperature field
+      S.mlp->m.T0 = S.m.T0;
+      S.mlp->m.gradT = S.m.gradT;
+   }
+   return err;
+}
+
+// QuatIntegrator::setTemperatureField before every f(t, y)
+// (QuatIntegrator.cc:3191): the model's T0(t)
+// (ScalarTemperatureStrategy::getCurrentTemperature,
+// ScalarTemperatureStrategy.cc:57-73; GradientTemperatureStrategy.cc:
+// 124-131 without a moving frame)
+static void at_time(Stepper& S, double t)
+{
+   const ampe_model_t& m = S.m;
+   if (m.dTdt == 0.0 || m.temp_mode == AMPE_TEMP_FIELD) return;
+   double T = S.T_start + m.dTdt * t;
+   if (m.temp_mode == AMPE_TEMP_CONSTANT) {
+      if (m.dTdt < 0.0 && T < m.T_target)
+         T = m.T_target;
+      else if (m.T_target > 0.0 && m.dTdt > 0.0 && T > m.T_target)
+         T = m.T_target;
+   }
+   if (T == m.T0) return;
+   S.m.T0 = T;
+   apply_temperature(S);
+}
+
 static int bdf_newton(Stepper& S, double gamma, double newton_coef)
 {
    const long long ny = S.NY;
@@ -1149,8 +1191,10 @@ static int bdf_newton(Stepper& S, double gamma, double newton_coef)
 
 // one fixed-size BDF step of size h, order q (constant-step coefficients,
 // linear-extrapolation predictor); result in S.ynew.  0 = converged.
-static int bdf_step(Stepper& S, double h, int q)
+// one BDF step of size h ending at t_end
+static int bdf_step(Stepper& S, double t_end, double h, int q)
 {
+   at_time(S, t_end);
    const long long ny = S.NY;
    double *a = S.a, *y = S.y, *yn = S.yn, *ynm1 = S.ynm1;
    double gamma;
@@ -1273,6 +1317,7 @@ static int adaptive_step(Stepper& S, double t_stop)
       double h = std::min(S.h_next, hmax);
       if (t_stop > S.t && S.t + h > t_stop - 1e-12 * std::fabs(t_stop)) h = t_stop - S.t;
       if (S.nhist == 0 && !S.fn_valid) {
+         at_time(S, S.t);
          eval_rhs(S, S.yn, nullptr, 0.0, S.fn, 0);
          S.fn_valid = true;
       }
@@ -1298,6 +1343,7 @@ static int adaptive_step(Stepper& S, double t_stop)
             a[t] = use2 ? a0 * yn[t] + a1 * y1[t] : yn[t];
          }, S.s);
       }
+      at_time(S, S.t + h);
       if (bdf_newton(S, gamma, 0.1 / P.c)) {
          ncf++;
          if (ncf >= 10 || h <= S.p.h_min) return 1;
@@ -1428,8 +1474,12 @@ static int finish_stats(Stepper& S, ampe_step_stats_t* stats)
 // accepted variable steps until t_stop (if > t) or max_steps
 static int advance_adaptive(Stepper& S, double t_stop, int max_steps)
 {
+   // a stop time not in the past (at t already: no step, as CVODE's
+   // CV_TSTOP_RETURN); anything earlier means none
+   const double eps = 1e-12 * std::fabs(t_stop);
+   const bool has_stop = t_stop >= S.t - eps;
    for (int n = 0; n < max_steps; n++) {
-      if (t_stop > S.t && S.t >= t_stop - 1e-12 * std::fabs(t_stop)) break;
+      if (has_stop && S.t >= t_stop - eps) break;
       if (adaptive_step(S, t_stop)) return AMPE_ERR_NOT_CONVERGED;
       step_accepted(S);
    }
@@ -1515,6 +1565,8 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    }
    if (m->evolve_quat && (m->quat_mobility_type != 'p' || !(m->quat_grad_floor > 0.0)))
       return AMPE_ERR_INVALID;
+   if (!std::isfinite(m->dTdt) || (m->dTdt != 0.0 && m->temp_mode == AMPE_TEMP_FIELD))
+      return AMPE_ERR_INVALID;
    // the mobility diffusivities belong to the "ebs" form and take the
    // CALPHAD free-energy curvature
    if (m->conc_diffusion == AMPE_DIFF_MOBILITY &&
@@ -1524,6 +1576,7 @@ int ampe_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p,
    Stepper* S = new (std::nothrow) Stepper;
    if (!S) return AMPE_ERR_INVALID;
    S->m = *m;
+   S->T_start = m->T0;
    S->m.ng_side = 0;  // the stepper's own face arrays carry no ghosts
    m = &S->m;
    S->p = *p;
@@ -1758,6 +1811,7 @@ int ampe_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs, int host)
 {
    Stepper* S = (Stepper*)h;
    if (!S || !phi_rhs || !conc_rhs) return AMPE_ERR_INVALID;
+   at_time(*S, S->t);
    eval_rhs(*S, S->yn, nullptr, 0.0, S->fy, 0);
    const cudaMemcpyKind kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
    const size_t bytes = sizeof(double) * (size_t)S->N;
@@ -1781,7 +1835,7 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
    for (int n = 0; n < nsteps; n++) {
       double hstep = S->p.dt;
       const int q = S->hist ? std::min(2, S->p.max_order) : 1;
-      int fail = bdf_step(*S, hstep, q);
+      int fail = bdf_step(*S, S->t + hstep, hstep, q);
       int retries = 0;
       if (fail) {
          // order-1 sub-steps: after each failure halve the sub-step and go
@@ -1797,7 +1851,7 @@ int ampe_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
             fail = 0;
             while (done < hstep * (1.0 - 1e-12)) {
                const double hh = std::min(hsub, hstep - done);
-               if (bdf_step(*S, hh, 1)) {
+               if (bdf_step(*S, S->t + done + hh, hh, 1)) {
                   fail = 1;
                   break;
                }
@@ -1843,20 +1897,10 @@ int ampe_stepper_set_temperature(void* h, double T0, double gradT)
    Stepper* S = (Stepper*)h;
    if (!S || !(T0 > 0.0) || S->m.temp_mode == AMPE_TEMP_FIELD) return AMPE_ERR_INVALID;
    if (S->m.temp_mode == AMPE_TEMP_CONSTANT && gradT != 0.0) return AMPE_ERR_INVALID;
+   if (S->m.dTdt != 0.0) return AMPE_ERR_INVALID;  // T follows the model's T0(t)
    S->m.T0 = T0;
    S->m.gradT = gradT;
-   const float2* dq = S->mp.dq;
-   S->mp = make_mix_params(S->m);
-   S->mp.dq = dq;
-   const int nt = S->m.temp_mode == AMPE_TEMP_GRADIENT ? S->m.n[0] : 1;
-   int err = AMPE_OK;
-   if (S->tab) err = build_thermo_table(S->m, S->tab, nt, S->s);
-   if (!err && S->tabf) err = build_coef_f(S->tab, S->tabf, nt, S->s);
-   if (!err && S->dqtab) err = build_diff_table(S->m, S->mp, S->g, S->dqtab, S->s);
-   if (S->mlp) {  // the network sees the stepper's temperature field
-      S->mlp->m.T0 = T0;
-      S->mlp->m.gradT = gradT;
-   }
+   int err = apply_temperature(*S);
    S->fn_valid = false;
    if (!err && cudaStreamSynchronize(S->s) != cudaSuccess) err = AMPE_ERR_CUDA;
    return err;
@@ -1945,6 +1989,7 @@ int ampe_stepper_jv(void* h, const double* v, double gamma, double* out,
       w[t] = 1.0 / e;
       wi[t] = e;
    }, S->s);
+   at_time(*S, S->t);
    eval_rhs(*S, S->yn, nullptr, 0.0, S->fy, 0);
    cudaMemcpyAsync(S->b, v, b2, in, S->s);
    if (S->p.precision == 1) {
@@ -2006,6 +2051,7 @@ int ampe_stepper_eval_rhs_full(void* h, double* out, int host)
 {
    Stepper* S = (Stepper*)h;
    if (!S || !out) return AMPE_ERR_INVALID;
+   at_time(*S, S->t);
    eval_rhs(*S, S->yn, nullptr, 0.0, S->fy, 0);
    const cudaMemcpyKind kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
    cudaMemcpyAsync(out, S->fy, sizeof(double) * (size_t)S->NY, kind, S->s);

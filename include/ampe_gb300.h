@@ -172,6 +172,19 @@ typedef struct ampe_model {
                         * "ebs"; see ampe_conc_diffusion_mobility) */
    int pad2;
    ampe_mobility_t mobility;
+
+   /* ---- temperature in time (ScalarTemperatureStrategy::
+    * getCurrentTemperature, ScalarTemperatureStrategy.cc:57-73;
+    * GradientTemperatureStrategy.cc:124-131), set at every f(t, y) as
+    * QuatIntegrator::evaluateRHSFunction does (QuatIntegrator.cc:3191):
+    * T0(t) = T0 + dTdt t with T0 the temperature at t = 0; in
+    * AMPE_TEMP_CONSTANT held at T_target once past it (dTdt < 0: below
+    * it; dTdt > 0 and T_target > 0: above it).  The stepper evaluates
+    * each BDF step's Newton iterations at the step's end time and f(y_n)
+    * at its start.  dTdt = 0: T0 fixed (ampe_stepper_set_temperature
+    * changes it; with dTdt != 0 that call is refused). */
+   double dTdt;
+   double T_target;
 } ampe_model_t;
 
 /* Integrator / preconditioner controls (QuatIntegrator.cc:278-301,
@@ -660,14 +673,17 @@ int ampe_stepper_advance(void* handle, int nsteps, ampe_step_stats_t* stats);
 /* p->adaptive: accepted steps until t reaches t_stop (the last step ends at
  * t_stop exactly) or max_steps steps were taken; max_steps = 1 is CVODE's
  * CV_ONE_STEP mode with a stop time, as QuatModel drives it (one internal
- * step per QuatIntegrator::Advance, QuatIntegrator.cc:2096-2104).  The
- * history (step sizes, order, back values) carries over between calls. */
+ * step per QuatIntegrator::Advance, QuatIntegrator.cc:2096-2104).  A
+ * t_stop the stepper has reached takes no step; one before the current t
+ * sets no stop time.  The history (step sizes, order, back values) carries
+ * over between calls. */
 int ampe_stepper_advance_to(void* handle, double t_stop, int max_steps,
                             ampe_step_stats_t* stats);
 /* Temperature of the following steps (TemperatureStrategy role: a scalar
- * T0 with an optional x gradient, e.g. T0 + dT/dt t set before each step);
- * the per-x thermodynamic tables are rebuilt, the BDF history is kept.
- * Models with temp_mode AMPE_TEMP_FIELD take their field via set_state. */
+ * T0 with an optional x gradient, set from the host between steps); the
+ * per-x thermodynamic tables are rebuilt, the BDF history is kept.  Models
+ * with temp_mode AMPE_TEMP_FIELD take their field via set_state; models
+ * with dTdt != 0 follow their T0(t) and refuse this call. */
 int ampe_stepper_set_temperature(void* handle, double T0, double gradT);
 /* Evaluate f(y) of the current state (fd_flag=0 path): outputs interior. */
 int ampe_stepper_eval_rhs(void* handle, double* phi_rhs, double* conc_rhs,

@@ -46,8 +46,26 @@ struct OStepper {
    double h_next = 0.0, h1 = 0.0, h2 = 0.0, eta_max = 1.0e4;
    int q_next = 1, qwait = 2, nhist = 0;
    double t = 0.0;
+   double T_start = 0.0;  // T0 at t = 0 of a model with dTdt != 0
    ampe_step_stats_t st{};
 };
+
+// QuatIntegrator::setTemperatureField before every f(t, y)
+// (QuatIntegrator.cc:3191): T0(t) of ScalarTemperatureStrategy::
+// getCurrentTemperature (ScalarTemperatureStrategy.cc:57-73), or T0 + dTdt t
+// of GradientTemperatureStrategy.cc:124-131 without a moving frame
+void at_time(OStepper& s, double t)
+{
+   if (s.m.dTdt == 0.0 || s.m.temp_mode == AMPE_TEMP_FIELD) return;
+   double T = s.T_start + s.m.dTdt * t;
+   if (s.m.temp_mode == AMPE_TEMP_CONSTANT) {
+      if (s.m.dTdt < 0.0 && T < s.m.T_target)
+         T = s.m.T_target;
+      else if (s.m.T_target > 0.0 && s.m.dTdt > 0.0 && T > s.m.T_target)
+         T = s.m.T_target;
+   }
+   s.m.T0 = T;
+}
 
 void to_ghosted(const OStepper& s, const double* src, std::vector<double>& g)
 {
@@ -327,8 +345,10 @@ int bdf_newton(OStepper& s, const std::vector<double>& a, std::vector<double>& y
 // One BDF step of size h and order q from yn (and ynm1 for q=2), constant-
 // step coefficients, linear-extrapolation predictor.
 // Returns 0 on convergence, 1 on Newton failure.
-int bdf_step(OStepper& s, double h, int q, std::vector<double>& ynew)
+// one BDF step of size h ending at t_end
+int bdf_step(OStepper& s, double t_end, double h, int q, std::vector<double>& ynew)
 {
+   at_time(s, t_end);
    const long n2 = s.NY;
    std::vector<double> a(n2), y(n2), w;
    double gamma;
@@ -423,6 +443,7 @@ int adaptive_step(OStepper& s, double t_stop)
    std::vector<double> fn;
    if (s.nhist == 0) {
       fn.resize(n2);
+      at_time(s, s.t);
       eval_rhs(s, s.yn.data(), fn.data(), 0);
    }
    std::vector<double> a(n2), y(n2), w, ynew;
@@ -448,6 +469,7 @@ int adaptive_step(OStepper& s, double t_stop)
          y[t] = pr;
          a[t] = q == 2 ? a0 * s.yn[t] + a1 * s.ynm1[t] : s.yn[t];
       }
+      at_time(s, s.t + h);
       if (bdf_newton(s, a, y, gamma, 0.1 / P.c, w, ynew)) {
          ncf++;
          if (ncf >= 10 || h <= s.p.h_min) return 1;
@@ -535,6 +557,7 @@ void* orc_stepper_create(const ampe_model_t* m, const ampe_step_params_t* p)
 {
    OStepper* s = new OStepper;
    s->m = *m;
+   s->T_start = m->T0;
    s->p = *p;
    Layout L(*m);
    s->N = L.cells();
@@ -651,6 +674,7 @@ void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs)
 {
    OStepper* s = (OStepper*)h;
    std::vector<double> fy(s->NY);
+   at_time(*s, s->t);
    eval_rhs(*s, s->yn.data(), fy.data(), 0);
    std::copy(fy.begin(), fy.begin() + s->N, phi_rhs);
    std::copy(fy.begin() + s->N, fy.begin() + 2 * s->N, conc_rhs);
@@ -660,6 +684,7 @@ void orc_stepper_eval_rhs(void* h, double* phi_rhs, double* conc_rhs)
 void orc_stepper_eval_rhs_full(void* h, double* out)
 {
    OStepper* s = (OStepper*)h;
+   at_time(*s, s->t);
    eval_rhs(*s, s->yn.data(), out, 0);
 }
 
@@ -670,8 +695,11 @@ long orc_stepper_size(void* h) { return ((OStepper*)h)->NY; }
 // variable steps until t_stop (if > t) or max_steps; 0 ok, 1 failed
 static int advance_adaptive(OStepper* s, double t_stop, int max_steps)
 {
+   // a stop time not in the past (at t already: no step); earlier: none
+   const double eps = 1e-12 * std::fabs(t_stop);
+   const bool has_stop = t_stop >= s->t - eps;
    for (int n = 0; n < max_steps; n++) {
-      if (t_stop > s->t && s->t >= t_stop - 1e-12 * std::fabs(t_stop)) break;
+      if (has_stop && s->t >= t_stop - eps) break;
       if (adaptive_step(*s, t_stop)) return 1;
       s->clr = s->cl_nf;  // QuatModel::resetRefPhaseConcentrations
       s->csr = s->cs_nf;
@@ -695,6 +723,7 @@ int orc_stepper_advance_to(void* h, double t_stop, int max_steps, ampe_step_stat
 void orc_stepper_set_temperature(void* h, double T0, double gradT)
 {
    OStepper* s = (OStepper*)h;
+   if (s->m.dTdt != 0.0) return;  // T follows the model's T0(t)
    s->m.T0 = T0;
    s->m.gradT = gradT;
 }
@@ -708,7 +737,7 @@ int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
    for (int n = 0; n < nsteps; n++) {
       double hstep = s->p.dt;
       int q = s->hist ? std::min(2, s->p.max_order) : 1;
-      int fail = bdf_step(*s, hstep, q, ynew);
+      int fail = bdf_step(*s, s->t + hstep, hstep, q, ynew);
       int retries = 0;
       if (fail) {
          // order-1 sub-steps: after each failure halve the sub-step and go
@@ -723,7 +752,7 @@ int orc_stepper_advance(void* h, int nsteps, ampe_step_stats_t* stats)
             fail = 0;
             while (done < hstep * (1.0 - 1e-12)) {
                const double hh = std::min(hsub, hstep - done);
-               if (bdf_step(*s, hh, 1, ynew)) {
+               if (bdf_step(*s, s->t + done + hh, hh, 1, ynew)) {
                   fail = 1;
                   break;
                }
@@ -769,6 +798,7 @@ void orc_stepper_jv(void* h, const double* v, double gamma, double* out,
    OStepper* s = (OStepper*)h;
    const long n2 = s->NY;
    std::vector<double> fy(n2), w(n2);
+   at_time(*s, s->t);
    eval_rhs(*s, s->yn.data(), fy.data(), 0);
    for (long c = 0; c < n2; c++)
       w[c] = 1.0 / (s->p.rtol * std::fabs(s->yn[c]) + s->p.atol);

@@ -151,11 +151,14 @@ def run(make_stepper, t_end=0.3, dt_max=2.0e-3, atol=1.0e-6, precision=0,
     return out
 
 
+T_START, DTDT, T_TARGET = 1450.0, -200.0, 1220.0  # 3d.input:20-25, 2d.input:24-29
+
+
 def temperature(t):
     """ScalarTemperatureStrategy::getCurrentTemperature
     (ScalarTemperatureStrategy.cc:57-73) with the deck's 1450 K, -200 K per
     unit time and target 1220 K."""
-    return max(1450.0 - 200.0 * t, 1220.0)
+    return max(T_START + DTDT * t, T_TARGET)
 
 
 def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
@@ -163,15 +166,17 @@ def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
     """The deck's own integration: CVODE-style variable steps (orders 1-2,
     atol 1e-4 and rtol = atol / 100 as QuatIntegrator.cc:283-289 derives
     them from 3d.input:80-81, initial step h0), one accepted step per call
-    (CV_ONE_STEP, QuatIntegrator.cc:1575) up to t_end, the temperature of
-    each step set from its start time (temperature(t), 3d.input:20-25).
-    case = (model, (phi, c)) runs another case the same way.  Returns the
-    same record as run()."""
+    (CV_ONE_STEP, QuatIntegrator.cc:1575) up to t_end, the temperature
+    following the deck's scalar history inside the stepper (model fields
+    T0, dTdt, T_target: every f(t, y) at temperature(t), as
+    QuatIntegrator.cc:3191 sets it).  case = (model, (phi, c)) runs another
+    case the same way.  Returns the same record as run()."""
     if case is None:
         m = model()
         phi, c = initial_state()
     else:
         m, (phi, c) = case
+    m.T0, m.dTdt, m.T_target = T_START, DTDT, T_TARGET
     p = configs.step_params(dt=h0, precond=2, mg_levels=mg_levels, atol=atol,
                             precision=precision)
     p.adaptive = 1
@@ -183,8 +188,6 @@ def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
     next_out, t = interval, 0.0
     st = None
     while t < t_end - 1e-12 and out["steps"] < max_steps:
-        T = temperature(t)
-        s.set_temperature(T)
         r = s.advance_to(t_end, 1)
         rc, st = r if isinstance(r, tuple) else (0, r)
         if rc != 0:
@@ -195,7 +198,7 @@ def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
         if t >= next_out - 1e-9 or t >= t_end - 1e-12:
             ph, cc = s.get_state()[:2]
             out["t"].append(t)
-            out["T"].append(T)
+            out["T"].append(temperature(t))
             out["solid"].append(float(ph.mean()))
             out["cmean"].append(float(cc.mean()))
             while next_out <= t + 1e-9:

@@ -92,7 +92,8 @@ def block_means(a, b=8):
 
 def run(make_stepper, precision=0, nh=64):
     """The deck's integration of the case (kkscomposition.run_adaptive:
-    variable steps at atol 1e-5, rtol 1e-7, T set per step) to t = 0.3."""
+    variable steps at atol 1e-5, rtol 1e-7, every f(t, y) at the deck's
+    T(t)) to t = 0.3."""
     import kkscomposition as K
 
     return K.run_adaptive(make_stepper, atol=ATOL, precision=precision, case=case(nh),

@@ -147,3 +147,54 @@ def test_mobility_refused_forms(cuda):
     m.mobility.q[0][0][0][1] = 0.0  # ln(0) of a mobility term
     with pytest.raises(AmpeError):
         ImplicitStepper(m, p)
+
+
+def _ramp_case():
+    """The reduced SingleGrainGrowthAuNi case with a steep temperature ramp
+    that reaches its target within the test's steps: T0(t) = 1450 K -
+    2e4 K t, held at 1440 K from t = 5e-4."""
+    m, state = _mobility_case()
+    m.T0, m.dTdt, m.T_target = 1450.0, -2.0e4, 1440.0
+    return m, state
+
+
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_temperature_ramp_parity(cuda, adaptive):
+    """Every f(t, y) at the model's T0(t) (QuatIntegrator.cc:3191,
+    ScalarTemperatureStrategy.cc:57-73), fixed and variable steps, against
+    the oracle: same counts, fields within 1e-10."""
+    m, (phi, c) = _ramp_case()
+    p = configs.step_params(dt=2e-4, precond=2, mg_levels=3, atol=1e-5)
+    p.adaptive = 1 if adaptive else 0
+    o = O.OracleStepper(m, p)
+    o.set_state(phi, c)
+    g = ImplicitStepper(m, p)
+    g.set_state(phi, c)
+    if adaptive:
+        rc, so = o.advance_to(8e-4, 100)
+        assert rc == 0
+        sg = g.advance_to(8e-4, 100)
+        assert abs(sg["t"] - 8e-4) < 1e-15
+    else:
+        rc, so = o.advance(4)
+        assert rc == 0
+        sg = g.advance(4)
+    for k in ("steps", "newton_iters", "gmres_iters", "rhs_evals", "fac_cycles"):
+        assert sg[k] == so[k], (k, sg[k], so[k])
+    xo, xg = o.get_state(), g.get_state()
+    for a, b in zip(xg, xo):
+        assert O.rel_l2(a, b) <= 1e-10
+    # the ramp changes the result: the same steps at a fixed 1450 K
+    m2, _ = _mobility_case()
+    f = ImplicitStepper(m2, p)
+    f.set_state(phi, c)
+    if adaptive:
+        f.advance_to(8e-4, 100)
+    else:
+        f.advance(4)
+    assert O.rel_l2(f.get_state()[0], xg[0]) > 1e-6
+    # the ramp owns the temperature
+    from ampe_gb300._native import AmpeError
+
+    with pytest.raises(AmpeError):
+        g.set_temperature(1400.0)

@@ -3,9 +3,9 @@
 tests/SingleGrainGrowthAuNi (test2d.py + 2d.input; the case itself is in
 tests/singlegrain.py), integrated as the deck integrates it.  The
 reference expects the solid volume fraction 0.32 +- 0.01 once t passes
-0.3 and the composition integral constant to 1e-4.  Measured: 0.3184 at
-t = 0.3, mean composition drift -4.8e-6, 576 steps (82 failed attempts),
-about 40 s on 8 cores (a default CPU test).  The same run, written by
+0.3 and the composition integral constant to 1e-4.  Measured: 0.3188 at
+t = 0.3, mean composition drift 2.4e-5 (the bound: 3.1e-5), 411 steps (1
+failed attempt), about 35 s on 8 cores (a default CPU test).  The same run, written by
 tests/golden/make_singlegrain.py, is the fixture the GPU regression test
 compares with."""
 import json
