@@ -162,21 +162,23 @@ def temperature(t):
 
 
 def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
-                 interval=0.03, max_steps=100000, case=None, mg_levels=4):
+                 interval=0.03, max_steps=100000, case=None, mg_levels=4, ramp=True):
     """The deck's own integration: CVODE-style variable steps (orders 1-2,
     atol 1e-4 and rtol = atol / 100 as QuatIntegrator.cc:283-289 derives
     them from 3d.input:80-81, initial step h0), one accepted step per call
     (CV_ONE_STEP, QuatIntegrator.cc:1575) up to t_end, the temperature
     following the deck's scalar history inside the stepper (model fields
     T0, dTdt, T_target: every f(t, y) at temperature(t), as
-    QuatIntegrator.cc:3191 sets it).  case = (model, (phi, c)) runs another
-    case the same way.  Returns the same record as run()."""
+    QuatIntegrator.cc:3191 sets it); ramp=False instead sets T from the
+    host before each step, at the step's start time, and holds it within
+    the step.  case = (model, (phi, c)) runs another case the same way.
+    Returns the same record as run()."""
     if case is None:
         m = model()
         phi, c = initial_state()
     else:
         m, (phi, c) = case
-    m.T0, m.dTdt, m.T_target = T_START, DTDT, T_TARGET
+    m.T0, m.dTdt, m.T_target = T_START, (DTDT if ramp else 0.0), T_TARGET
     p = configs.step_params(dt=h0, precond=2, mg_levels=mg_levels, atol=atol,
                             precision=precision)
     p.adaptive = 1
@@ -188,6 +190,8 @@ def run_adaptive(make_stepper, t_end=0.3, atol=1.0e-4, h0=1.0e-6, precision=0,
     next_out, t = interval, 0.0
     st = None
     while t < t_end - 1e-12 and out["steps"] < max_steps:
+        if not ramp:
+            s.set_temperature(temperature(t))
         r = s.advance_to(t_end, 1)
         rc, st = r if isinstance(r, tuple) else (0, r)
         if rc != 0:
