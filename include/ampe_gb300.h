@@ -9,10 +9,15 @@
  *   - the per-cell KKS phase-concentration Newton solve
  *     (PhaseConcentrationsStrategy::computePhaseConcentrationsOnPatch),
  *   - the composition right-hand side (EBSCompositionRHSStrategy fluxes with
- *     temperature dependent diffusion),
+ *     temperature dependent or atomic-mobility diffusivities; the "kks"
+ *     form),
+ *   - the quaternion orientation equation (gradients, mobility, face
+ *     coefficients, the symmetry-aware variants),
  *   - the Phase/Conc FAC operators (red-black Gauss-Seidel smoother,
  *     residual, within-level restrict/prolong),
- *   - a BDF Newton-GMRES stepper that plays the role of CVODE.
+ *   - a BDF Newton-GMRES stepper that plays the role of CVODE (fixed or
+ *     variable steps, the temperature history evaluated at every f(t, y)),
+ *   - a two-level composite FAC operator and solve (one refined box).
  *
  * Conventions shared by every entry point:
  *   - every array pointer is a DEVICE pointer unless the name says "host";
