@@ -58,9 +58,10 @@ int phase_set_c(const ampe_model_t& m, const Grid& g, const double* phi,
                 double gamma, R* ccell, cudaStream_t s);
 
 // One red-black sweep of a 3D level in a single z-marching pass (sweep_z.cu):
-// blocks of ty rows x the whole x extent (one thread per column) x kz
-// planes, u staged in a ring of kZRingPlanes shared-memory planes of
-// (ty + 4) rows of hs (= n0) elements.
+// blocks of ty rows x the whole x extent (one thread per column) x a chunk
+// of planes (kz here for two resident blocks per SM; each launch re-sizes
+// the chunks to its kernel's resident blocks, one wave), u staged in a ring
+// of kZRingPlanes shared-memory planes of (ty + 4) rows of hs elements.
 constexpr int kZRingPlanes = 6;
 constexpr int kZRowStride = 256;  // ring row stride (n0 <= 256)
 struct ZShape {
