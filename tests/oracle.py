@@ -60,6 +60,7 @@ def lib():
             "orc_kim_mobility": (None, [MP, P, P, P, D, D, D, D, P]),
             "orc_phase_diffusion_mobility": (D, [MP, C.POINTER(abi.Mobility), I, D, D]),
             "orc_conc_diffusion_mobility": (None, [MP, C.POINTER(abi.Mobility)] + [P] * 16),
+            "orc_conc_diffusion_model": (None, [MP] + [P] * 10),
             "orc_fac2_work_doubles": (C.c_longlong, [C.POINTER(abi.Fac2)]),
             "orc_fac2_composite_residual": (D, [C.POINTER(abi.Fac2), P, P] + [P] * 6),
             "orc_fac2_solve": (I, [C.POINTER(abi.Fac2), P, P, P, P, P, P, I, D, P]),

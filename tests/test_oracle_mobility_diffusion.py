@@ -130,3 +130,41 @@ def test_mobility_struct_defaults():
     assert list(mb.qq[1][1][1]) == [-42800.0, 1.0]
     assert list(mb.qq[0][0][3]) == [0.0, 1.0]
     assert list(mb.qq[0][1][0]) == [232300.0, 7.6881435e-08]
+
+
+def test_apply_database_fills_the_model():
+    """apply_database copies the MobilityParameters block into the model
+    and leaves the choice of diffusivities to conc_diffusion; the oracle's
+    right-hand side then takes the atomic-mobility diffusivities exactly
+    when conc_diffusion says so (orc_conc_diffusion_model)."""
+    m = _model(3, False)
+    ref = calphad_db.mobility_struct(_db()["mobility"])
+    assert bytes(m.mobility) == bytes(ref)
+    assert m.conc_diffusion == abi.DIFF_ARRHENIUS
+    orc = O.lib()
+    rng = np.random.default_rng(7)
+    phi = O.ghosted(m, rng.uniform(0, 1, m.interior_shape()))
+    cl = O.ghosted(m, rng.uniform(0.05, 0.3, m.interior_shape()))
+    cs = O.ghosted(m, rng.uniform(0.05, 0.3, m.interior_shape()))
+    fs = m.face_shapes()
+    out = {}
+    for kind in (abi.DIFF_ARRHENIUS, abi.DIFF_MOBILITY):
+        m.conc_diffusion = kind
+        dl = [np.zeros(s) for s in fs]
+        ds = [np.zeros(s) for s in fs]
+        orc.orc_conc_diffusion_model(C.byref(m), O.ptr(phi), None, O.ptr(cl), O.ptr(cs),
+                                     *[O.ptr(a) for a in dl], *[O.ptr(a) for a in ds])
+        out[kind] = (dl, ds)
+    dl = [np.zeros(s) for s in fs]
+    ds = [np.zeros(s) for s in fs]
+    orc.orc_conc_diffusion_mobility(C.byref(m), C.byref(m.mobility), O.ptr(phi), None,
+                                    O.ptr(cl), O.ptr(cs), *[O.ptr(a) for a in dl],
+                                    *[O.ptr(a) for a in ds], *([None] * 6))
+    for a, b in zip(out[abi.DIFF_MOBILITY][0] + out[abi.DIFF_MOBILITY][1], dl + ds):
+        assert np.array_equal(a, b)
+    dl = [np.zeros(s) for s in fs]
+    ds = [np.zeros(s) for s in fs]
+    orc.orc_conc_diffusion(C.byref(m), O.ptr(phi), None, *[O.ptr(a) for a in dl],
+                           *[O.ptr(a) for a in ds])
+    for a, b in zip(out[abi.DIFF_ARRHENIUS][0] + out[abi.DIFF_ARRHENIUS][1], dl + ds):
+        assert np.array_equal(a, b)
