@@ -1078,9 +1078,6 @@ static int gmres32(Stepper& S, double gamma, const float* bf, double* x,
    return k;
 }
 
-// Newton iteration of one BDF step: y - gamma f(y) = a from the predictor
-// in S.y, convergence test del min(1, crate) <= newton_coef; result in
-// S.ynew.  0 = converged.
 // the temperature-dependent state after a change of S.m.T0 / gradT: the
 // FP32 constants, the per-x thermodynamic and diffusivity tables, the
 // network's copy of the model (launches on the stepper's stream, no wait)
@@ -1122,6 +1119,9 @@ static void at_time(Stepper& S, double t)
    apply_temperature(S);
 }
 
+// Newton iteration of one BDF step: y - gamma f(y) = a from the predictor
+// in S.y, convergence test del min(1, crate) <= newton_coef; result in
+// S.ynew.  0 = converged.
 static int bdf_newton(Stepper& S, double gamma, double newton_coef)
 {
    const long long ny = S.NY;
@@ -1189,9 +1189,9 @@ static int bdf_newton(Stepper& S, double gamma, double newton_coef)
    return 1;
 }
 
-// one fixed-size BDF step of size h, order q (constant-step coefficients,
-// linear-extrapolation predictor); result in S.ynew.  0 = converged.
-// one BDF step of size h ending at t_end
+// one fixed-size BDF step of size h, order q, ending at t_end
+// (constant-step coefficients, linear-extrapolation predictor); result in
+// S.ynew.  0 = converged.
 static int bdf_step(Stepper& S, double t_end, double h, int q)
 {
    at_time(S, t_end);

@@ -342,10 +342,9 @@ int bdf_newton(OStepper& s, const std::vector<double>& a, std::vector<double>& y
    return 1;
 }
 
-// One BDF step of size h and order q from yn (and ynm1 for q=2), constant-
-// step coefficients, linear-extrapolation predictor.
+// One BDF step of size h and order q from yn (and ynm1 for q=2), ending at
+// t_end; constant-step coefficients, linear-extrapolation predictor.
 // Returns 0 on convergence, 1 on Newton failure.
-// one BDF step of size h ending at t_end
 int bdf_step(OStepper& s, double t_end, double h, int q, std::vector<double>& ynew)
 {
    at_time(s, t_end);
