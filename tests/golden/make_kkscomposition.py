@@ -7,6 +7,9 @@ test to compare its own run with.
 
 Run from the repository root (about 80 minutes on 8 cores):
     OMP_NUM_THREADS=8 python tests/golden/make_kkscomposition.py
+With --mobility: the same run with the atomic-mobility diffusivities the
+reference uses for this deck (kkscomposition.model(mobility=True)), written
+to tests/golden/kkscomposition_mobility_oracle.json.
 """
 import json
 import os
@@ -22,10 +25,12 @@ import oracle as O  # noqa: E402
 
 
 def main():
+    mobility = "--mobility" in sys.argv[1:]
     t0 = time.time()
-    r = K.run(lambda m, p: O.OracleStepper(m, p))
+    r = K.run(lambda m, p: O.OracleStepper(m, p), mobility=mobility)
     out = {
         "case": "tests/KKScomposition (64^3 periodic mirror of the 32^3 zero-slope box)",
+        "diffusivities": "atomic mobilities" if mobility else "the deck's D_L, D_S",
         "integrator": "fixed-step BDF1, dt <= 2e-3 after a geometric start-up, atol 1e-6",
         "t": r["t"], "T": r["T"], "solid": r["solid"], "cmean": r["cmean"],
         "steps": r["steps"], "rejected": r["rejected"], "drift": r["drift"],
@@ -34,7 +39,7 @@ def main():
         "c_blocks": K.block_means(r["c"], 8).ravel().tolist(),
         "cpu_seconds": time.time() - t0,
     }
-    with open(K.FIXTURE, "w") as f:
+    with open(K.FIXTURE_MOBILITY if mobility else K.FIXTURE, "w") as f:
         json.dump(out, f, indent=1)
     print("solid fraction %.4f at t = %.3f, drift %.2e, %d steps (%d rejected), %.0f s"
           % (out["solid"][-1], out["t"][-1], out["drift"], out["steps"], out["rejected"],

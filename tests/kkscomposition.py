@@ -36,6 +36,7 @@ from ampe_gb300.calphad_db import apply_database
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FIXTURE = os.path.join(GOLD, "kkscomposition_oracle.json")
+FIXTURE_MOBILITY = os.path.join(GOLD, "kkscomposition_mobility_oracle.json")
 
 # composition integral tolerance of test3d.py:44-46 (1e-4 on the integral
 # over the 0.9^3 um^3 box) as a tolerance on the mean composition
