@@ -86,40 +86,32 @@ def test_kkscomposition_start_parity(cuda, precision):
 _RUNS = {}
 
 
-def _gpu_run(precision, mobility=False):
-    key = (precision, mobility)
-    if key not in _RUNS:
-        _RUNS[key] = K.run(lambda m, p: _Gpu(m, p), precision=precision, mobility=mobility)
-    return _RUNS[key]
+def _gpu_run(precision):
+    if precision not in _RUNS:
+        _RUNS[precision] = K.run(lambda m, p: _Gpu(m, p), precision=precision)
+    return _RUNS[precision]
 
 
-@pytest.mark.parametrize("mobility", [False, True])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_kkscomposition_regression(cuda, precision, mobility):
-    """Fixed steps; the deck's D_L, D_S, or (mobility) the atomic-mobility
-    diffusivities the reference uses for the deck."""
-    if mobility and not os.path.exists(K.FIXTURE_MOBILITY):
-        pytest.skip("oracle trajectory fixture of the mobility run not generated")
-    r = _gpu_run(precision, mobility)
+def test_kkscomposition_regression(cuda, precision):
+    r = _gpu_run(precision)
     solid, drift = r["solid"][-1], r["drift"]
-    print("KKScomposition%s GPU precision %d: solid fraction %.5f at t = %.4f, drift %.2e, "
-          "%d steps, %d rejected" % (" (mobility)" if mobility else "", precision, solid,
-                                      r["t"][-1], drift, r["steps"], r["rejected"]))
+    print("KKScomposition GPU precision %d: solid fraction %.5f at t = %.4f, drift %.2e, "
+          "%d steps, %d rejected" % (precision, solid, r["t"][-1], drift, r["steps"],
+                                      r["rejected"]))
     assert abs(r["t"][-1] - 0.3) < 1e-9
     assert abs(solid - K.SOLID_TARGET) <= K.SOLID_TOL
     assert abs(drift) < K.DRIFT_TOL
 
 
-@pytest.mark.parametrize("mobility", [False, True])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_kkscomposition_trajectory_vs_oracle(cuda, precision, mobility):
+def test_kkscomposition_trajectory_vs_oracle(cuda, precision):
     """The GPU run against the oracle's run of the same case (the committed
-    trajectory fixtures, tests/golden/make_kkscomposition.py [--mobility])."""
-    path = K.FIXTURE_MOBILITY if mobility else K.FIXTURE
-    if not os.path.exists(path):
+    trajectory fixture, tests/golden/make_kkscomposition.py)."""
+    if not os.path.exists(K.FIXTURE):
         pytest.skip("oracle trajectory fixture not generated")
-    r = _gpu_run(precision, mobility)
-    with open(path) as f:
+    r = _gpu_run(precision)
+    with open(K.FIXTURE) as f:
         gold = json.load(f)
     if precision == 0:
         assert r["steps"] == gold["steps"] and r["rejected"] == gold["rejected"]
