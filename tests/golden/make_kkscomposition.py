@@ -9,7 +9,8 @@ Run from the repository root (about 80 minutes on 8 cores):
     OMP_NUM_THREADS=8 python tests/golden/make_kkscomposition.py
 With --mobility: the same run with the atomic-mobility diffusivities the
 reference uses for this deck (kkscomposition.model(mobility=True)), written
-to tests/golden/kkscomposition_mobility_oracle.json.
+to tests/golden/kkscomposition_mobility_oracle.json (about 140 minutes on
+8 cores).
 """
 import json
 import os
